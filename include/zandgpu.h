@@ -1,0 +1,141 @@
+/*
+ * zandgpu.h -- C ABI of libzandgpu.so, the GB300 (sm_103a) engine for the
+ * auxiliary-mode-expansion (AME) propagation of Zandpack's `zand` driver.
+ *
+ * Conventions
+ *   - complex numbers are interleaved (re, im) doubles, as numpy complex128;
+ *   - every function returns a zg_status; zg_last_error() gives the message of
+ *     the last failure on the calling thread;
+ *   - host pointers are plain host memory (pageable or pinned); device pointers
+ *     are CUDA device memory of the current device;
+ *   - no function throws across the ABI.
+ *
+ * Which reference interface each entry point replaces is cited per function
+ * (paths inside the Zandpack repository).
+ */
+#ifndef ZANDGPU_H
+#define ZANDGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  ZG_OK = 0,
+  ZG_EINVAL = 1,     /* bad argument or shape (the reference raises AssertionError) */
+  ZG_ENOMEM = 2,     /* device allocation failed */
+  ZG_ECUDA = 3,      /* CUDA runtime error */
+  ZG_ETIMEOUT = 4,   /* a bounded device-side wait gave up */
+  ZG_ENONFINITE = 5  /* the error norm is NaN or infinite */
+} zg_status;
+
+enum { ZG_PREC_F64 = 0, ZG_PREC_MIXED = 1 };
+enum { ZG_DH_NONE = 0, ZG_DH_MATRIX = 1, ZG_DH_HUBBARD = 2 };
+#define ZG_MAX_LEADS 16
+#define ZG_MAX_STAGES 13
+
+const char* zg_last_error(void);
+int zg_version(void);
+/* Number of kernels this library has launched since it was loaded. */
+long long zg_launch_count(void);
+
+/* ------------------------------------------------------------------------
+ * Compact layout of one propagation (host arrays, copied at creation).
+ * Built by zandpack_gb300.layout.CompactLayout from the reference's Arrays/
+ * (Zandpack/mpi/zand:113-124,568-664; Zandpack/Writer.py:61-151).
+ * Mode order: sourced modes by lead, then source-free modes by lead.
+ * ---------------------------------------------------------------------- */
+typedef struct {
+  int32_t n;           /* orbitals (NO) */
+  int32_t n_leads;     /* NL */
+  int32_t n_modes;     /* N: live auxiliary modes */
+  int32_t n_sourced;   /* Ns: modes with diff_GGP_GLP or diff_GGM_GLM nonzero */
+  int32_t nc;          /* coupling columns per lead (padded) */
+  double hbar;         /* eV fs */
+  const int32_t* mode_lead;   /* [N] */
+  const int64_t* s_start;     /* [NL+1] sourced rows of lead a: [s_start[a], s_start[a+1]) */
+  const int64_t* f_start;     /* [NL+1] free rows of lead a (absolute mode index) */
+  const int32_t* lead_cols;   /* [NL*nc] orbital of coupling column k of lead a */
+  const int32_t* colmap;      /* [NL*n] coupling column of orbital j in lead a, or -1 */
+  const double* H0;           /* [n*n] complex */
+  const double* Xp;           /* [N] complex: Xpp of the mode */
+  const double* Xm;           /* [N] complex: Xpm of the mode */
+  const double* GLP;          /* [N] complex */
+  const double* dGP;          /* [N] complex: diff_GGP_GLP */
+  const double* dGM;          /* [N] complex: diff_GGM_GLM */
+  const double* XI;           /* [N*nc] complex: xi on the lead's columns */
+  const double* IXI;          /* [N*nc] complex: Ixi on orbidx_alpha, else 0 */
+  const double* XIS;          /* [N*nc] complex: xi/hbar^2 on orbidx_Ixi_all_nonzero, else 0 */
+  const double* XIT2;         /* [N*nc] complex: xi on orbidx_xi_nonzero, else 0 */
+} zg_layout;
+
+typedef struct zg_traj zg_traj;
+
+/* One trajectory: constants, the RK_N+1 state slots (k_0..k_{RK_N-1}, y) and
+ * scratch on the device.  Replaces the per-rank arrays of SIGMA()/Worker()
+ * (Zandpack/mpi/zand:200-290,498-690).  precision: ZG_PREC_F64 or ZG_PREC_MIXED. */
+int zg_traj_create(int device, const zg_layout* layout, int precision, zg_traj** out);
+int zg_traj_destroy(zg_traj* t);
+/* out[0..7] = n, NL, N, Ns, Nf, nc, state size (complex elements), stages */
+int zg_traj_info(const zg_traj* t, int64_t* out);
+/* The cudaStream_t all work of the trajectory is issued on (for events). */
+void* zg_traj_stream(const zg_traj* t);
+
+/* Butcher tableau (Zandpack/mpi_RK4pars_dev.py:118-149 layout): A[s], B[s*(s+1)]
+ * (column s multiplies the stored y), CT[s], CH[s+1].  Entries of B outside
+ * idxholder[i] must be given as 0.  DOP54 is preloaded. */
+int zg_set_tableau(zg_traj* t, int stages, const double* A, const double* B,
+                   const double* CT, const double* CH);
+
+/* State slots: slot 0..stages-1 = k_i (the SIGS/PSIS/OMGS[i] arrays), slot
+ * `stages` = y (SIGS[-1] etc.).  Flat compact vector of `state size` complex. */
+int zg_set_state(zg_traj* t, int slot, const double* host);
+int zg_get_state(zg_traj* t, int slot, double* host);
+
+/* Stage input Y_i = sum_{j in idxholder[i]} B[i,j] Y_j (Y_stages = y); for
+ * i = 0 the input is y itself.  Replaces the MM / step_*_forward_nb stage
+ * combination (Zandpack/mpi/zand:306-313,722-735; Zandpack/func_step_forward.py:16-139). */
+int zg_stage_input(zg_traj* t, int stage);
+/* Download sigma of the current stage input (n*n complex), for a host dH(t, sigma). */
+int zg_get_stage_sigma(zg_traj* t, double* host);
+/* Upload the dH(t, sigma) matrix (n*n complex) that ZG_DH_MATRIX adds to H0. */
+int zg_set_dH(zg_traj* t, const double* host);
+
+/* k_stage = h f(ts, Y_stage): the stage body of zand (Zandpack/mpi/zand:318-387
+ * master, :713-809 worker).  delta[NL] = bias(ts, a); dH_mode selects
+ * H(t) = H0 (+ uploaded dH | + hubbard_U*diag(Re sigma_ii - 0.5)).  If
+ * currents != NULL, the lead currents Re Tr(PI_a)/hbar of this stage input
+ * are written there (:368-378). */
+int zg_rhs(zg_traj* t, int stage, double ts, double h, const double* delta,
+           int dH_mode, double hubbard_U, double* currents);
+
+/* err2[0..2] = TERR2_sig, TERR2_psi, TERR2_omg of the k slots
+ * (Zandpack/mpi_funcs.py:247-252; Zandpack/func_step_forward.py:39-53,75-91,141-159). */
+int zg_error_norm2(zg_traj* t, double* err2);
+
+/* y <- sum_j CH_j Y_j (step_fourth_*, Zandpack/mpi_funcs.py:254-259). */
+int zg_step_fourth(zg_traj* t);
+
+/* ------------------------------------------------------------------------
+ * Stateless array kernels on caller device buffers (complex128), the
+ * numba/numpy kernels of Zandpack/func_step_forward.py and mpi_funcs.py.
+ * Y holds `nslots` arrays of `count` complex elements, `slot_stride`
+ * complex elements apart.  stream: a cudaStream_t (NULL = default stream).
+ * ---------------------------------------------------------------------- */
+/* out = sum_{j in idx} b[j] Y[j]  (step_{sig,psi,omg}_forward_nb(Y, b, out, idx), :16-109) */
+int zg_combine_c128(const double* Y, int64_t slot_stride, int nslots, const double* b,
+                    const int32_t* idx, int nidx, double* out, int64_t count, void* stream);
+/* *result = sum_e |sum_j ct[j] Y[j][e]|^2  (TERR2_*_nb, :39-53; TERR2_*, mpi_funcs.py:247-252).
+ * Uses a device scratch buffer of partial sums that it allocates stream-ordered. */
+int zg_terr2_c128(const double* Y, int64_t slot_stride, int nslots, const double* ct,
+                  int64_t count, double* result, void* stream);
+/* Y[nslots-1] = sum_j ch[j] Y[j]  (step_fourth_*, mpi_funcs.py:254-259) */
+int zg_step_fourth_c128(double* Y, int64_t slot_stride, int nslots, const double* ch,
+                        int64_t count, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ZANDGPU_H */

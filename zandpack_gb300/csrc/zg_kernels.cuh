@@ -1,0 +1,83 @@
+// Kernel declarations and launch descriptors shared by the runtime and the
+// kernel translation units.
+#pragma once
+#include "zg_common.cuh"
+
+#include <atomic>
+
+namespace zg {
+
+// kernels launched by this library since load (all threads)
+extern std::atomic<long long> g_launches;
+
+// ------------------------------------------------------------ flat kernels
+// out[e] = sum_t c[t] * Y[idx[t]][e]   (Y slots `stride` complex apart)
+int launch_combine_c128(const double2* Y, int64_t stride, const CombineCoefs& cf, double2* out,
+                        int64_t count, cudaStream_t s);
+// Y[last][e] = sum_t c[t] * Y[idx[t]][e], in place (last is one of the idx)
+int launch_step_fourth_c128(double2* Y, int64_t stride, int last, const CombineCoefs& cf,
+                            int64_t count, cudaStream_t s);
+// partial[b] for b < nblocks: block sums of |sum_t c[t] Y[idx[t]][e]|^2 over e in [begin, end)
+int terr2_nblocks(int64_t count);
+int launch_terr2_partials_c128(const double2* Y, int64_t stride, const CombineCoefs& cf,
+                               int64_t begin, int64_t end, double* partial, int nblocks, cudaStream_t s);
+// out[j] = sum of partial[j*nblocks .. (j+1)*nblocks), j < nseg (fixed order)
+int launch_reduce_partials(const double* partial, int nblocks, int nseg, double* out, cudaStream_t s);
+
+// ------------------------------------------------------------ FP64 GEMM
+// C = alpha * opA(A) opB(B) + beta * C ; opA: 0 = A[m*lda+k], 1 = A[k*lda+m];
+// opB: 0 = B[k*ldb+n], 1 = B[n*ldb+k], 2 = conj(B[n*ldb+k]).  K = 0 writes beta*C.
+struct GemmProb {
+  const double2* A;
+  const double2* B;
+  double2* C;
+  int M, N, K;
+  int opA, opB;
+  int tile_begin, tiles_n;
+  int64_t lda, ldb, ldc;
+  double2 alpha, beta;
+};
+#define ZG_MAX_GEMM 32
+struct GemmBatch {
+  int nprob;
+  int total_tiles;
+  GemmProb p[ZG_MAX_GEMM];
+};
+// fills tile_begin/tiles_n/total_tiles and launches
+int launch_zgemm_batch(GemmBatch& b, cudaStream_t s);
+
+// ------------------------------------------------------------ RHS helpers
+struct StageParams {
+  double h, ts, hbar;
+  double delta[ZG_MAX_LEADS];
+};
+
+struct RhsDev {  // device pointers and sizes of one trajectory
+  int n, L, N, Ns, Nf, nc;
+  int64_t off_psi, off_omA, off_omB, S;
+  const int* mode_lead;
+  const int* lead_cols;
+  const int* colmap;
+  const double2 *H0, *Xp, *Xm, *GLP, *dGP, *XI, *U, *V;
+};
+
+struct OmTile {
+  int row0, nrows;      // absolute mode rows
+  int col0, ncols;      // local column within the block
+  int a, b;             // row lead, column lead
+  int blk;              // 0: OmA (columns are sourced modes), 1: OmB (free modes)
+  int term1, term2;     // which source products apply
+};
+
+int launch_build_ht(const RhsDev& d, const double2* sig, const double2* dH, int dH_mode, double U,
+                    double2* Ht, cudaStream_t s);
+int launch_gathers(const RhsDev& d, const double2* sig, const double2* psi, double2* sigC, double2* G,
+                   cudaStream_t s);
+int launch_sigma_finalize(const RhsDev& d, const StageParams& p, const double2* T, const double2* Pc,
+                          double2* ksig, double* currents, cudaStream_t s);
+int launch_psi_finalize(const RhsDev& d, const StageParams& p, const double2* psi, const double2* R2,
+                        const double2* ZA, const double2* ZB, double2* kpsi, cudaStream_t s);
+int launch_omega(const RhsDev& d, const StageParams& p, const OmTile* tiles, int ntiles, const double2* G,
+                 const double2* yin, double2* kout, cudaStream_t s);
+
+}  // namespace zg

@@ -1,0 +1,493 @@
+// Host runtime of libzandgpu: trajectory objects (device constants, the
+// Runge-Kutta state slots, scratch), the per-stage launch sequence of the AME
+// right-hand side, and the extern "C" entry points declared in zandgpu.h.
+#include <stdarg.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "zg_kernels.cuh"
+
+namespace zg {
+
+static thread_local char g_err[1024] = "";
+
+void set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+
+template <class T>
+static int dalloc(T** p, size_t count) {
+  *p = nullptr;
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+  if (e != cudaSuccess) {
+    set_error("cudaMalloc of %zu bytes failed: %s", count * sizeof(T), cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? ZG_ENOMEM : ZG_ECUDA;
+  }
+  return ZG_OK;
+}
+
+template <class T>
+static int upload(T* dst, const void* src, size_t count, cudaStream_t s) {
+  if (count == 0) return ZG_OK;
+  ZG_CHECK_CUDA(cudaMemcpyAsync(dst, src, count * sizeof(T), cudaMemcpyHostToDevice, s));
+  return ZG_OK;
+}
+
+}  // namespace zg
+
+using namespace zg;
+
+// DOP54 (Zandpack/mpi_RK4pars_dev.py:118-149): A, B (column 7 = stored y), CT = b5 - b4, CH = [b5, 1]
+static const double kDopA[7] = {0, 1. / 5, 3. / 10, 4. / 5, 8. / 9, 1, 1};
+static const double kDopB[7][8] = {
+    {0, 0, 0, 0, 0, 0, 0, 0},
+    {1. / 5, 0, 0, 0, 0, 0, 0, 1},
+    {3. / 40, 9. / 40, 0, 0, 0, 0, 0, 1},
+    {44. / 45, -56. / 15, 32. / 9, 0, 0, 0, 0, 1},
+    {19372. / 6561, -25360. / 2187, 64448. / 6561, -212. / 729, 0, 0, 0, 1},
+    {9017. / 3168, -355. / 33, 46732. / 5247, 49. / 176, -5103. / 18656, 0, 0, 1},
+    {35. / 384, 0, 500. / 1113, 125. / 192, -2187. / 6784, 11. / 84, 0, 1}};
+static const double kB5[7] = {35. / 384, 0, 500. / 1113, 125. / 192, -2187. / 6784, 11. / 84, 0};
+static const double kB4[7] = {5179. / 57600, 0, 7571. / 16695, 393. / 640, -92097. / 339200, 187. / 2100, 1. / 40};
+
+struct zg_traj {
+  int dev = 0;
+  int precision = ZG_PREC_F64;
+  cudaStream_t stream = nullptr;
+  int n = 0, L = 0, N = 0, Ns = 0, Nf = 0, nc = 0;
+  double hbar = 0;
+  int64_t off_psi = 0, off_omA = 0, off_omB = 0, S = 0;
+  std::vector<int64_t> s_start, f_start;
+  // tableau
+  int stages = 0;
+  std::vector<double> A, B, CT, CH;  // B: stages x (stages+1)
+  // device constants
+  double2 *H0 = nullptr, *Xp = nullptr, *Xm = nullptr, *GLP = nullptr, *dGP = nullptr, *XI = nullptr,
+          *IXI = nullptr, *XIS = nullptr, *U = nullptr, *V = nullptr;
+  int *mode_lead = nullptr, *lead_cols = nullptr, *colmap = nullptr;
+  OmTile* tiles = nullptr;
+  int ntiles = 0;
+  // state: (stages+1) slots of S complex; slot `stages` is y
+  double2* Y = nullptr;
+  int y_slots = 0;
+  double2* Ystage = nullptr;
+  const double2* cur_in = nullptr;
+  // scratch
+  double2 *Ht = nullptr, *dH = nullptr, *T = nullptr, *Pc = nullptr, *sigC = nullptr, *G = nullptr, *R2 = nullptr,
+          *ZA = nullptr, *ZB = nullptr;
+  double *J = nullptr, *partial = nullptr, *err = nullptr;
+  int nblk_err = 0;
+  bool dH_set = false;
+
+  RhsDev dev_view() const {
+    RhsDev d;
+    d.n = n; d.L = L; d.N = N; d.Ns = Ns; d.Nf = Nf; d.nc = nc;
+    d.off_psi = off_psi; d.off_omA = off_omA; d.off_omB = off_omB; d.S = S;
+    d.mode_lead = mode_lead; d.lead_cols = lead_cols; d.colmap = colmap;
+    d.H0 = H0; d.Xp = Xp; d.Xm = Xm; d.GLP = GLP; d.dGP = dGP; d.XI = XI; d.U = U; d.V = V;
+    return d;
+  }
+  double2* slot(int i) const { return Y + (int64_t)i * S; }
+};
+
+static void free_traj(zg_traj* t) {
+  if (!t) return;
+  void* ptrs[] = {t->H0, t->Xp, t->Xm, t->GLP, t->dGP, t->XI, t->IXI, t->XIS, t->U, t->V, t->mode_lead,
+                  t->lead_cols, t->colmap, t->tiles, t->Y, t->Ystage, t->Ht, t->dH, t->T, t->Pc, t->sigC,
+                  t->G, t->R2, t->ZA, t->ZB, t->J, t->partial, t->err};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (t->stream) cudaStreamDestroy(t->stream);
+  delete t;
+}
+
+static int alloc_state(zg_traj* t, int stages) {
+  if (t->Y && t->y_slots == stages + 1) return ZG_OK;
+  if (t->Y) cudaFree(t->Y);
+  t->Y = nullptr;
+  ZG_TRY(dalloc(&t->Y, (size_t)(stages + 1) * t->S));
+  t->y_slots = stages + 1;
+  ZG_CHECK_CUDA(cudaMemsetAsync(t->Y, 0, (size_t)(stages + 1) * t->S * sizeof(double2), t->stream));
+  return ZG_OK;
+}
+
+static int set_tableau_impl(zg_traj* t, int stages, const double* A, const double* B, const double* CT,
+                            const double* CH) {
+  ZG_REQUIRE(stages >= 1 && stages <= ZG_MAX_STAGES, "stages=%d out of range", stages);
+  t->stages = stages;
+  t->A.assign(A, A + stages);
+  t->B.assign(B, B + (size_t)stages * (stages + 1));
+  t->CT.assign(CT, CT + stages);
+  t->CH.assign(CH, CH + stages + 1);
+  return alloc_state(t, stages);
+}
+
+// Tiles of the Omega derivative: rows of one (class, lead) range against
+// columns of one lead's sourced (OmA) or free (OmB) modes.
+static void build_tiles(zg_traj* t, std::vector<OmTile>& out) {
+  const int TS = 64;
+  auto add = [&](int r0, int r1, int c0, int c1, int a, int b, int blk, int term1, int term2) {
+    for (int r = r0; r < r1; r += TS)
+      for (int c = c0; c < c1; c += TS) {
+        OmTile x;
+        x.row0 = r; x.nrows = std::min(TS, r1 - r);
+        x.col0 = c; x.ncols = std::min(TS, c1 - c);
+        x.a = a; x.b = b; x.blk = blk; x.term1 = term1; x.term2 = term2;
+        out.push_back(x);
+      }
+  };
+  for (int a = 0; a < t->L; ++a)
+    for (int b = 0; b < t->L; ++b) {
+      // OmA: columns = sourced modes of lead b (local column == mode index)
+      int c0 = (int)t->s_start[b], c1 = (int)t->s_start[b + 1];
+      add((int)t->s_start[a], (int)t->s_start[a + 1], c0, c1, a, b, 0, 1, 1);
+      add((int)t->f_start[a], (int)t->f_start[a + 1], c0, c1, a, b, 0, 1, 0);
+      // OmB: rows = sourced modes of lead a, columns = free modes of lead b
+      add((int)t->s_start[a], (int)t->s_start[a + 1], (int)(t->f_start[b] - t->Ns), (int)(t->f_start[b + 1] - t->Ns),
+          a, b, 1, 0, 1);
+    }
+}
+
+extern "C" {
+
+const char* zg_last_error(void) { return g_err; }
+int zg_version(void) { return 100; }
+long long zg_launch_count(void) { return g_launches.load(); }
+void* zg_traj_stream(const zg_traj* t) { return t ? (void*)t->stream : nullptr; }
+
+int zg_traj_create(int device, const zg_layout* Lo, int precision, zg_traj** out) {
+  ZG_REQUIRE(out && Lo, "null argument");
+  *out = nullptr;
+  ZG_REQUIRE(precision == ZG_PREC_F64, "precision mode %d not available in this build", precision);
+  ZG_REQUIRE(Lo->n > 0 && Lo->n_leads > 0 && Lo->n_leads <= ZG_MAX_LEADS && Lo->n_modes > 0 &&
+                 Lo->n_sourced >= 0 && Lo->n_sourced <= Lo->n_modes && Lo->nc > 0,
+             "bad layout sizes");
+  ZG_REQUIRE(Lo->hbar > 0, "hbar must be positive");
+  ZG_CHECK_CUDA(cudaSetDevice(device));
+  zg_traj* t = new zg_traj();
+  t->dev = device;
+  t->precision = precision;
+  t->n = Lo->n; t->L = Lo->n_leads; t->N = Lo->n_modes; t->Ns = Lo->n_sourced; t->Nf = t->N - t->Ns; t->nc = Lo->nc;
+  t->hbar = Lo->hbar;
+  const int64_t n = t->n, N = t->N, Ns = t->Ns, Nf = t->Nf, L = t->L, nc = t->nc;
+  t->off_psi = n * n;
+  t->off_omA = t->off_psi + N * n;
+  t->off_omB = t->off_omA + N * Ns;
+  t->S = t->off_omB + Ns * Nf;
+  t->s_start.assign(Lo->s_start, Lo->s_start + L + 1);
+  t->f_start.assign(Lo->f_start, Lo->f_start + L + 1);
+  int st = ZG_OK;
+#define ZG_STEP(x)  \
+  do {              \
+    st = (x);       \
+    if (st != ZG_OK) { free_traj(t); return st; } \
+  } while (0)
+  // validate row ranges
+  bool ok = t->s_start[0] == 0 && t->s_start[L] == Ns && t->f_start[0] == Ns && t->f_start[L] == N;
+  for (int a = 0; a < L && ok; ++a) ok = t->s_start[a] <= t->s_start[a + 1] && t->f_start[a] <= t->f_start[a + 1];
+  if (!ok) { free_traj(t); set_error("s_start/f_start do not partition the modes"); return ZG_EINVAL; }
+  for (int64_t m = 0; m < N; ++m) {
+    int a = Lo->mode_lead[m];
+    bool in = (m < Ns) ? (m >= t->s_start[a] && m < t->s_start[a + 1]) : (m >= t->f_start[a] && m < t->f_start[a + 1]);
+    if (a < 0 || a >= L || !in) { free_traj(t); set_error("mode_lead inconsistent with row ranges at mode %lld", (long long)m); return ZG_EINVAL; }
+  }
+  for (int64_t i = 0; i < L * nc; ++i)
+    if (Lo->lead_cols[i] < 0 || Lo->lead_cols[i] >= n) { free_traj(t); set_error("lead_cols out of range"); return ZG_EINVAL; }
+  for (int64_t i = 0; i < L * n; ++i)
+    if (Lo->colmap[i] < -1 || Lo->colmap[i] >= nc) { free_traj(t); set_error("colmap out of range"); return ZG_EINVAL; }
+  if (cudaStreamCreateWithFlags(&t->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    free_traj(t); set_error("cudaStreamCreate failed"); return ZG_ECUDA;
+  }
+  ZG_STEP(dalloc(&t->H0, n * n));
+  ZG_STEP(dalloc(&t->Xp, N)); ZG_STEP(dalloc(&t->Xm, N)); ZG_STEP(dalloc(&t->GLP, N)); ZG_STEP(dalloc(&t->dGP, N));
+  ZG_STEP(dalloc(&t->XI, N * nc)); ZG_STEP(dalloc(&t->IXI, N * nc)); ZG_STEP(dalloc(&t->XIS, N * nc));
+  ZG_STEP(dalloc(&t->U, N * nc)); ZG_STEP(dalloc(&t->V, N * nc));
+  ZG_STEP(dalloc(&t->mode_lead, N)); ZG_STEP(dalloc(&t->lead_cols, L * nc)); ZG_STEP(dalloc(&t->colmap, L * n));
+  ZG_STEP(upload<double2>(t->H0, Lo->H0, n * n, t->stream));
+  ZG_STEP(upload<double2>(t->Xp, Lo->Xp, N, t->stream));
+  ZG_STEP(upload<double2>(t->Xm, Lo->Xm, N, t->stream));
+  ZG_STEP(upload<double2>(t->GLP, Lo->GLP, N, t->stream));
+  ZG_STEP(upload<double2>(t->dGP, Lo->dGP, N, t->stream));
+  ZG_STEP(upload<double2>(t->XI, Lo->XI, N * nc, t->stream));
+  ZG_STEP(upload<double2>(t->IXI, Lo->IXI, N * nc, t->stream));
+  ZG_STEP(upload<double2>(t->XIS, Lo->XIS, N * nc, t->stream));
+  ZG_STEP(upload<int>(t->mode_lead, Lo->mode_lead, N, t->stream));
+  ZG_STEP(upload<int>(t->lead_cols, Lo->lead_cols, L * nc, t->stream));
+  ZG_STEP(upload<int>(t->colmap, Lo->colmap, L * n, t->stream));
+  {
+    // U = dGM * IXI (per column mode), V = dGP * XIT2 (per row mode)
+    std::vector<double2> U(N * nc), V(N * nc);
+    const double2* dGM = (const double2*)Lo->dGM;
+    const double2* dGP = (const double2*)Lo->dGP;
+    const double2* IXI = (const double2*)Lo->IXI;
+    const double2* XIT2 = (const double2*)Lo->XIT2;
+    for (int64_t m = 0; m < N; ++m)
+      for (int64_t k = 0; k < nc; ++k) {
+        U[m * nc + k] = cmul(dGM[m], IXI[m * nc + k]);
+        V[m * nc + k] = cmul(dGP[m], XIT2[m * nc + k]);
+      }
+    ZG_STEP(upload<double2>(t->U, U.data(), N * nc, t->stream));
+    ZG_STEP(upload<double2>(t->V, V.data(), N * nc, t->stream));
+    std::vector<OmTile> tiles;
+    build_tiles(t, tiles);
+    t->ntiles = (int)tiles.size();
+    ZG_STEP(dalloc(&t->tiles, tiles.size()));
+    ZG_STEP(upload<OmTile>(t->tiles, tiles.data(), tiles.size(), t->stream));
+    // keep host vectors alive until the copies finished
+    ZG_CHECK_CUDA(cudaStreamSynchronize(t->stream));
+  }
+  ZG_STEP(dalloc(&t->Ystage, t->S));
+  ZG_STEP(dalloc(&t->Ht, n * n)); ZG_STEP(dalloc(&t->dH, n * n)); ZG_STEP(dalloc(&t->T, n * n));
+  ZG_STEP(dalloc(&t->Pc, 2 * L * n * nc)); ZG_STEP(dalloc(&t->sigC, L * n * nc)); ZG_STEP(dalloc(&t->G, N * L * nc));
+  ZG_STEP(dalloc(&t->R2, std::max<int64_t>(Ns, 1) * n));
+  ZG_STEP(dalloc(&t->ZA, L * N * nc)); ZG_STEP(dalloc(&t->ZB, L * std::max<int64_t>(Ns, 1) * nc));
+  ZG_STEP(dalloc(&t->J, L));
+  t->nblk_err = terr2_nblocks(t->S);
+  ZG_STEP(dalloc(&t->partial, 3 * (size_t)t->nblk_err));
+  ZG_STEP(dalloc(&t->err, 3));
+  {
+    double B[7 * 8], CT[7], CH[8];
+    for (int i = 0; i < 7; ++i)
+      for (int j = 0; j < 8; ++j) B[i * 8 + j] = kDopB[i][j];
+    for (int j = 0; j < 7; ++j) { CT[j] = kB5[j] - kB4[j]; CH[j] = kB5[j]; }
+    CH[7] = 1.0;
+    ZG_STEP(set_tableau_impl(t, 7, kDopA, B, CT, CH));
+  }
+  t->cur_in = t->slot(t->stages);
+  ZG_CHECK_CUDA(cudaStreamSynchronize(t->stream));
+#undef ZG_STEP
+  *out = t;
+  return ZG_OK;
+}
+
+int zg_traj_destroy(zg_traj* t) {
+  if (!t) return ZG_OK;
+  cudaSetDevice(t->dev);
+  if (t->stream) cudaStreamSynchronize(t->stream);
+  free_traj(t);
+  return ZG_OK;
+}
+
+int zg_traj_info(const zg_traj* t, int64_t* out) {
+  ZG_REQUIRE(t && out, "null argument");
+  out[0] = t->n; out[1] = t->L; out[2] = t->N; out[3] = t->Ns; out[4] = t->Nf; out[5] = t->nc; out[6] = t->S;
+  out[7] = t->stages;
+  return ZG_OK;
+}
+
+int zg_set_tableau(zg_traj* t, int stages, const double* A, const double* B, const double* CT, const double* CH) {
+  ZG_REQUIRE(t && A && B && CT && CH, "null argument");
+  ZG_CHECK_CUDA(cudaSetDevice(t->dev));
+  ZG_TRY(set_tableau_impl(t, stages, A, B, CT, CH));
+  t->cur_in = t->slot(t->stages);
+  ZG_CHECK_CUDA(cudaStreamSynchronize(t->stream));
+  return ZG_OK;
+}
+
+int zg_set_state(zg_traj* t, int slot, const double* host) {
+  ZG_REQUIRE(t && host, "null argument");
+  ZG_REQUIRE(slot >= 0 && slot <= t->stages, "slot %d out of range", slot);
+  ZG_CHECK_CUDA(cudaSetDevice(t->dev));
+  ZG_CHECK_CUDA(cudaMemcpyAsync(t->slot(slot), host, t->S * sizeof(double2), cudaMemcpyHostToDevice, t->stream));
+  ZG_CHECK_CUDA(cudaStreamSynchronize(t->stream));
+  return ZG_OK;
+}
+
+int zg_get_state(zg_traj* t, int slot, double* host) {
+  ZG_REQUIRE(t && host, "null argument");
+  ZG_REQUIRE(slot >= 0 && slot <= t->stages, "slot %d out of range", slot);
+  ZG_CHECK_CUDA(cudaSetDevice(t->dev));
+  ZG_CHECK_CUDA(cudaMemcpyAsync(host, t->slot(slot), t->S * sizeof(double2), cudaMemcpyDeviceToHost, t->stream));
+  ZG_CHECK_CUDA(cudaStreamSynchronize(t->stream));
+  return ZG_OK;
+}
+
+int zg_stage_input(zg_traj* t, int stage) {
+  ZG_REQUIRE(t, "null argument");
+  ZG_REQUIRE(stage >= 0 && stage < t->stages, "stage %d out of range", stage);
+  ZG_CHECK_CUDA(cudaSetDevice(t->dev));
+  if (stage == 0) {
+    t->cur_in = t->slot(t->stages);
+    return ZG_OK;
+  }
+  CombineCoefs cf;
+  cf.n = 0;
+  for (int j = 0; j <= t->stages; ++j) {
+    double b = t->B[(size_t)stage * (t->stages + 1) + j];
+    if (b != 0.0) { cf.idx[cf.n] = j; cf.c[cf.n] = b; ++cf.n; }
+  }
+  ZG_TRY(launch_combine_c128(t->Y, t->S, cf, t->Ystage, t->S, t->stream));
+  t->cur_in = t->Ystage;
+  return ZG_OK;
+}
+
+int zg_get_stage_sigma(zg_traj* t, double* host) {
+  ZG_REQUIRE(t && host, "null argument");
+  ZG_CHECK_CUDA(cudaSetDevice(t->dev));
+  ZG_CHECK_CUDA(cudaMemcpyAsync(host, t->cur_in, (size_t)t->n * t->n * sizeof(double2), cudaMemcpyDeviceToHost,
+                                t->stream));
+  ZG_CHECK_CUDA(cudaStreamSynchronize(t->stream));
+  return ZG_OK;
+}
+
+int zg_set_dH(zg_traj* t, const double* host) {
+  ZG_REQUIRE(t && host, "null argument");
+  ZG_CHECK_CUDA(cudaSetDevice(t->dev));
+  ZG_CHECK_CUDA(cudaMemcpyAsync(t->dH, host, (size_t)t->n * t->n * sizeof(double2), cudaMemcpyHostToDevice,
+                                t->stream));
+  ZG_CHECK_CUDA(cudaStreamSynchronize(t->stream));
+  t->dH_set = true;
+  return ZG_OK;
+}
+
+int zg_rhs(zg_traj* t, int stage, double ts, double h, const double* delta, int dH_mode, double hubbard_U,
+           double* currents) {
+  ZG_REQUIRE(t && delta, "null argument");
+  ZG_REQUIRE(stage >= 0 && stage < t->stages, "stage %d out of range", stage);
+  ZG_REQUIRE(dH_mode == ZG_DH_NONE || dH_mode == ZG_DH_HUBBARD || (dH_mode == ZG_DH_MATRIX && t->dH_set),
+             "bad dH mode %d (ZG_DH_MATRIX needs zg_set_dH first)", dH_mode);
+  ZG_CHECK_CUDA(cudaSetDevice(t->dev));
+  const RhsDev d = t->dev_view();
+  StageParams p;
+  p.h = h; p.ts = ts; p.hbar = t->hbar;
+  for (int a = 0; a < ZG_MAX_LEADS; ++a) p.delta[a] = a < t->L ? delta[a] : 0.0;
+  const double2* in = t->cur_in;
+  const double2* sig = in;
+  const double2* psi = in + t->off_psi;
+  double2* out = t->slot(stage);
+  cudaStream_t s = t->stream;
+  const int64_t n = t->n, N = t->N, Ns = t->Ns, Nf = t->Nf, L = t->L, nc = t->nc;
+  ZG_TRY(launch_build_ht(d, sig, t->dH, dH_mode, hubbard_U, t->Ht, s));
+  ZG_TRY(launch_gathers(d, sig, psi, t->sigC, t->G, s));
+  std::vector<GemmProb> probs;
+  auto prob = [&](const double2* A, int64_t lda, int opA, const double2* B, int64_t ldb, int opB, double2* C,
+                  int64_t ldc, int M, int Nn, int K) {
+    GemmProb P;
+    P.A = A; P.B = B; P.C = C; P.M = M; P.N = Nn; P.K = K; P.opA = opA; P.opB = opB;
+    P.lda = lda; P.ldb = ldb; P.ldc = ldc;
+    P.alpha = make_double2(1.0, 0.0); P.beta = make_double2(0.0, 0.0);
+    P.tile_begin = 0; P.tiles_n = 1;
+    probs.push_back(P);
+  };
+  // T = H(t) sigma ; R1 = psi H(t)^T into k_psi
+  prob(t->Ht, n, 0, sig, n, 0, t->T, n, (int)n, (int)n, (int)n);
+  prob(psi, n, 0, t->Ht, n, 1, out + t->off_psi, n, (int)N, (int)n, (int)n);
+  for (int a = 0; a < L; ++a) {
+    // PI partials: Pc[cls][a] = psi[rows]^T IXI[rows]
+    int64_t r0 = t->s_start[a], r1 = t->s_start[a + 1];
+    prob(psi + r0 * n, n, 1, t->IXI + r0 * nc, nc, 0, t->Pc + ((0 * L + a) * n) * nc, nc, (int)n, (int)nc, (int)(r1 - r0));
+    r0 = t->f_start[a]; r1 = t->f_start[a + 1];
+    prob(psi + r0 * n, n, 1, t->IXI + r0 * nc, nc, 0, t->Pc + ((1 * L + a) * n) * nc, nc, (int)n, (int)nc, (int)(r1 - r0));
+    // R2 rows of lead a: XI[rows] sigC_a^T
+    r0 = t->s_start[a]; r1 = t->s_start[a + 1];
+    if (r1 > r0) prob(t->XI + r0 * nc, nc, 0, t->sigC + a * n * nc, nc, 1, t->R2 + r0 * n, n, (int)(r1 - r0), (int)n, (int)nc);
+    // Omega xi: ZA[a] = OmA[:, sourced of a] XIS[sourced of a]; ZB[a] = OmB[:, free of a] XIS[free of a]
+    r0 = t->s_start[a]; r1 = t->s_start[a + 1];
+    prob(in + t->off_omA + r0, Ns, 0, t->XIS + r0 * nc, nc, 0, t->ZA + a * N * nc, nc, (int)N, (int)nc, (int)(r1 - r0));
+    r0 = t->f_start[a]; r1 = t->f_start[a + 1];
+    if (Ns > 0)
+      prob(in + t->off_omB + (r0 - Ns), Nf, 0, t->XIS + r0 * nc, nc, 0, t->ZB + a * Ns * nc, nc, (int)Ns, (int)nc, (int)(r1 - r0));
+  }
+  for (size_t b0 = 0; b0 < probs.size(); b0 += ZG_MAX_GEMM) {
+    GemmBatch batch;
+    batch.nprob = (int)std::min<size_t>(ZG_MAX_GEMM, probs.size() - b0);
+    for (int i = 0; i < batch.nprob; ++i) batch.p[i] = probs[b0 + i];
+    ZG_TRY(launch_zgemm_batch(batch, s));
+  }
+  ZG_TRY(launch_sigma_finalize(d, p, t->T, t->Pc, out, currents ? t->J : nullptr, s));
+  ZG_TRY(launch_psi_finalize(d, p, psi, t->R2, t->ZA, t->ZB, out + t->off_psi, s));
+  ZG_TRY(launch_omega(d, p, t->tiles, t->ntiles, t->G, in, out, s));
+  if (currents) {
+    ZG_CHECK_CUDA(cudaMemcpyAsync(currents, t->J, L * sizeof(double), cudaMemcpyDeviceToHost, s));
+    ZG_CHECK_CUDA(cudaStreamSynchronize(s));
+  }
+  return ZG_OK;
+}
+
+int zg_error_norm2(zg_traj* t, double* err2) {
+  ZG_REQUIRE(t && err2, "null argument");
+  ZG_CHECK_CUDA(cudaSetDevice(t->dev));
+  CombineCoefs cf;
+  cf.n = 0;
+  for (int j = 0; j < t->stages; ++j)
+    if (t->CT[j] != 0.0) { cf.idx[cf.n] = j; cf.c[cf.n] = t->CT[j]; ++cf.n; }
+  const int64_t seg[4] = {0, t->off_psi, t->off_omA, t->S};
+  for (int k = 0; k < 3; ++k)
+    ZG_TRY(launch_terr2_partials_c128(t->Y, t->S, cf, seg[k], seg[k + 1], t->partial + (int64_t)k * t->nblk_err,
+                                      t->nblk_err, t->stream));
+  ZG_TRY(launch_reduce_partials(t->partial, t->nblk_err, 3, t->err, t->stream));
+  ZG_CHECK_CUDA(cudaMemcpyAsync(err2, t->err, 3 * sizeof(double), cudaMemcpyDeviceToHost, t->stream));
+  ZG_CHECK_CUDA(cudaStreamSynchronize(t->stream));
+  return ZG_OK;
+}
+
+int zg_step_fourth(zg_traj* t) {
+  ZG_REQUIRE(t, "null argument");
+  ZG_CHECK_CUDA(cudaSetDevice(t->dev));
+  CombineCoefs cf;
+  cf.n = 0;
+  for (int j = 0; j <= t->stages; ++j)
+    if (t->CH[j] != 0.0) { cf.idx[cf.n] = j; cf.c[cf.n] = t->CH[j]; ++cf.n; }
+  ZG_TRY(launch_step_fourth_c128(t->Y, t->S, t->stages, cf, t->S, t->stream));
+  ZG_CHECK_CUDA(cudaStreamSynchronize(t->stream));
+  return ZG_OK;
+}
+
+// ------------------------------------------------------------ array kernels
+static int coefs_from(CombineCoefs& cf, const double* c, const int32_t* idx, int nidx, int nslots) {
+  ZG_REQUIRE(nidx >= 0 && nidx <= ZG_MAX_STAGES + 1, "too many terms (%d)", nidx);
+  cf.n = 0;
+  for (int t = 0; t < nidx; ++t) {
+    int j = idx ? idx[t] : t;
+    ZG_REQUIRE(j >= 0 && j < nslots, "index %d out of range", j);
+    cf.idx[cf.n] = j;
+    cf.c[cf.n] = c[j];
+    ++cf.n;
+  }
+  return ZG_OK;
+}
+
+int zg_combine_c128(const double* Y, int64_t slot_stride, int nslots, const double* b, const int32_t* idx, int nidx,
+                    double* out, int64_t count, void* stream) {
+  ZG_REQUIRE(b && count >= 0 && slot_stride >= count && (count == 0 || (Y && out)), "bad arguments");
+  CombineCoefs cf;
+  ZG_TRY(coefs_from(cf, b, idx, nidx, nslots));
+  return launch_combine_c128((const double2*)Y, slot_stride, cf, (double2*)out, count, (cudaStream_t)stream);
+}
+
+int zg_terr2_c128(const double* Y, int64_t slot_stride, int nslots, const double* ct, int64_t count, double* result,
+                  void* stream) {
+  ZG_REQUIRE(ct && result && count >= 0 && slot_stride >= count && (count == 0 || Y), "bad arguments");
+  ZG_REQUIRE(nslots >= 1 && nslots <= ZG_MAX_STAGES + 1, "nslots %d out of range", nslots);
+  CombineCoefs cf;
+  ZG_TRY(coefs_from(cf, ct, nullptr, nslots, nslots));
+  cudaStream_t s = (cudaStream_t)stream;
+  const int nb = terr2_nblocks(count);
+  double* scratch = nullptr;  // nb partial sums + 1 result
+  ZG_CHECK_CUDA(cudaMallocAsync((void**)&scratch, (nb + 1) * sizeof(double), s));
+  int st = launch_terr2_partials_c128((const double2*)Y, slot_stride, cf, 0, count, scratch, nb, s);
+  if (st == ZG_OK) st = launch_reduce_partials(scratch, nb, 1, scratch + nb, s);
+  cudaError_t e = cudaSuccess;
+  if (st == ZG_OK) e = cudaMemcpyAsync(result, scratch + nb, sizeof(double), cudaMemcpyDeviceToHost, s);
+  cudaFreeAsync(scratch, s);
+  if (st != ZG_OK) return st;
+  if (e != cudaSuccess) { set_error("copy of the result failed: %s", cudaGetErrorString(e)); return ZG_ECUDA; }
+  ZG_CHECK_CUDA(cudaStreamSynchronize(s));
+  return ZG_OK;
+}
+
+int zg_step_fourth_c128(double* Y, int64_t slot_stride, int nslots, const double* ch, int64_t count, void* stream) {
+  ZG_REQUIRE(ch && count >= 0 && slot_stride >= count && (count == 0 || Y), "bad arguments");
+  ZG_REQUIRE(nslots >= 1 && nslots <= ZG_MAX_STAGES + 1, "nslots %d out of range", nslots);
+  CombineCoefs cf;
+  ZG_TRY(coefs_from(cf, ch, nullptr, nslots, nslots));
+  return launch_step_fourth_c128((double2*)Y, slot_stride, nslots - 1, cf, count, (cudaStream_t)stream);
+}
+
+}  // extern "C"

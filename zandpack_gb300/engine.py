@@ -1,0 +1,234 @@
+"""Device trajectory and the ``zand`` adaptive loop on top of libzandgpu.
+
+``Trajectory`` owns one propagation on the GPU: the compact-layout constants,
+the Runge-Kutta state slots and scratch (``zg_traj``).  ``Propagator`` drives it
+with the reference's Dormand-Prince 5(4) controller
+(Zandpack/mpi/zand:297-430): seven stages per attempt, stage inputs from the
+tableau rows, user callbacks ``bias(t, a)``, ``dH(t, sigma)`` and
+``dissipator(t, sigma)`` evaluated at every stage time, the unscaled absolute
+error test ``TE < eps``, ``h <- 0.9 h (eps/TE)^(1/5)`` after every attempt, and
+time advanced by the step size proposed for the next step, as the reference
+does (``t0 += h`` after ``h = hnew(h, TE)``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from typing import Callable, Optional
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, lib
+from .layout import CompactLayout
+from .tableau import DOP54, Tableau
+
+PREC = {"f64": _lib.ZG_PREC_F64, "mixed": _lib.ZG_PREC_MIXED}
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+class Trajectory:
+    """One AME propagation resident on the GPU."""
+
+    def __init__(self, arrays, hbar, precision="f64", device=0, psi0=None, omg0=None,
+                 dot_prod_zero_tol=1e-10, layout: Optional[CompactLayout] = None):
+        L = layout if layout is not None else CompactLayout(arrays, hbar, dot_prod_zero_tol, psi0=psi0, omg0=omg0)
+        self.layout = L
+        self.precision = precision
+        keep = dict(
+            mode_lead=np.ascontiguousarray(L.mode_lead, np.int32),
+            s_start=np.ascontiguousarray(L.s_start, np.int64),
+            f_start=np.ascontiguousarray(L.f_start, np.int64),
+            lead_cols=np.ascontiguousarray(L.lead_cols, np.int32),
+            colmap=np.ascontiguousarray(L.colmap, np.int32),
+            H0=np.ascontiguousarray(L.H0, np.complex128),
+            Xp=np.ascontiguousarray(L.Xp, np.complex128), Xm=np.ascontiguousarray(L.Xm, np.complex128),
+            GLP=np.ascontiguousarray(L.GLP, np.complex128), dGP=np.ascontiguousarray(L.dGP, np.complex128),
+            dGM=np.ascontiguousarray(L.dGM, np.complex128),
+            XI=np.ascontiguousarray(L.XI, np.complex128), IXI=np.ascontiguousarray(L.IXI, np.complex128),
+            XIS=np.ascontiguousarray(L.XIS, np.complex128), XIT2=np.ascontiguousarray(L.XIT2, np.complex128),
+        )
+        st = _lib.zg_layout(n=L.n, n_leads=L.NL, n_modes=L.N, n_sourced=L.Ns, nc=L.nc, hbar=L.hbar,
+                            **{k: _ptr(v) for k, v in keep.items()})
+        h = C.c_void_p()
+        check(lib().zg_traj_create(int(device), C.byref(st), PREC[precision], C.byref(h)))
+        self._h = h
+        info = np.zeros(8, np.int64)
+        check(lib().zg_traj_info(self._h, _ptr(info)))
+        self.size = int(info[6])
+        self.stages = int(info[7])
+        assert self.size == L.size
+        self._buf = np.empty(self.size, np.complex128)
+        self._sig = np.empty((L.n, L.n), np.complex128)
+        self._delta = np.zeros(_lib.ZG_MAX_LEADS, np.float64)
+        self._J = np.zeros(L.NL, np.float64)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().zg_traj_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ----------------------------------------------------------- tableau
+    def set_tableau(self, tab: Tableau):
+        B = np.nan_to_num(np.asarray(tab.B, np.float64), nan=0.0)
+        Bz = np.zeros_like(B)
+        for i in range(1, tab.RK_N):
+            ix = tab.idxholder[i]
+            Bz[i, ix] = B[i, ix]
+        args = [np.ascontiguousarray(x, np.float64) for x in (tab.A, Bz, tab.CT, tab.CH)]
+        check(lib().zg_set_tableau(self._h, tab.RK_N, *[_ptr(a) for a in args]))
+        self.stages = tab.RK_N
+
+    # ------------------------------------------------------------- state
+    def set_slot(self, slot, y):
+        y = np.ascontiguousarray(y, np.complex128)
+        assert y.size == self.size
+        check(lib().zg_set_state(self._h, int(slot), _ptr(y)))
+
+    def get_slot(self, slot):
+        out = np.empty(self.size, np.complex128)
+        check(lib().zg_get_state(self._h, int(slot), _ptr(out)))
+        return out
+
+    def set_y(self, sig, psi=None, omg=None):
+        L = self.layout
+        if psi is None or omg is None:
+            z = L.unpack(np.zeros(L.size, complex))
+            psi = z[1] if psi is None else psi
+            omg = z[2] if omg is None else omg
+        self.set_slot(self.stages, L.pack(sig, psi, omg))
+
+    def get_y(self):
+        return self.layout.unpack(self.get_slot(self.stages))
+
+    # -------------------------------------------------------------- stages
+    def stage_input(self, stage):
+        check(lib().zg_stage_input(self._h, int(stage)))
+
+    def stage_sigma(self):
+        check(lib().zg_get_stage_sigma(self._h, _ptr(self._sig)))
+        return self._sig
+
+    def set_dH(self, dH):
+        dH = np.ascontiguousarray(np.asarray(dH, np.complex128).reshape(self.layout.n, self.layout.n))
+        check(lib().zg_set_dH(self._h, _ptr(dH)))
+
+    def rhs(self, stage, ts, h, delta, dH_mode=_lib.ZG_DH_NONE, hubbard_U=0.0, currents=False):
+        d = self._delta
+        d[:] = 0.0
+        d[:len(delta)] = delta
+        Jp = _ptr(self._J) if currents else None
+        check(lib().zg_rhs(self._h, int(stage), float(ts), float(h), _ptr(d), int(dH_mode),
+                           float(hubbard_U), Jp))
+        return self._J.copy() if currents else None
+
+    def error_norm2(self):
+        e = np.zeros(3)
+        check(lib().zg_error_norm2(self._h, _ptr(e)))
+        return e
+
+    def step_fourth(self):
+        check(lib().zg_step_fourth(self._h))
+
+
+class Propagator:
+    """The ``zand`` time loop on the device (Zandpack/mpi/zand:297-430).
+
+    ``bias(t, a)`` and ``dH(t, sigma)`` are the reference's callbacks; ``dH``
+    receives sigma with the k axis, shape (1, n, n), and may return 0.0.
+    ``hubbard_U`` selects the built-in density-dependent term
+    U * diag(Re sigma_ii - 0.5) evaluated on the device instead of ``dH``.
+    """
+
+    def __init__(self, arrays, hbar, bias: Callable, dH: Optional[Callable] = None,
+                 dissipator: Optional[Callable] = None, hubbard_U: Optional[float] = None,
+                 precision="f64", device=0, tableau: Tableau = DOP54, psi0=None, omg0=None,
+                 dot_prod_zero_tol=1e-10, dH_depends_on_sigma=True):
+        self.traj = Trajectory(arrays, hbar, precision, device, psi0=psi0, omg0=omg0,
+                               dot_prod_zero_tol=dot_prod_zero_tol)
+        if tableau is not DOP54:
+            self.traj.set_tableau(tableau)
+        self.tab = tableau
+        self.bias = bias
+        self.dH = dH
+        self.dissipator = dissipator
+        self.hubbard_U = hubbard_U
+        self.dH_depends_on_sigma = dH_depends_on_sigma
+        self.NL = self.traj.layout.NL
+        self.n_rhs = 0
+
+    def set_state(self, sig, psi=None, omg=None):
+        self.traj.set_y(sig, psi, omg)
+
+    def _stage(self, i, t, h, want_J):
+        tr = self.traj
+        ts = t + self.tab.A[i] * h
+        tr.stage_input(i)
+        mode, U = _lib.ZG_DH_NONE, 0.0
+        if self.hubbard_U is not None:
+            mode, U = _lib.ZG_DH_HUBBARD, float(self.hubbard_U)
+        elif self.dH is not None:
+            sig = tr.stage_sigma()[None] if self.dH_depends_on_sigma else None
+            dh = self.dH(ts, sig)
+            if not (np.isscalar(dh) and dh == 0):
+                tr.set_dH(np.asarray(dh)[0] if np.ndim(dh) == 3 else dh)
+                mode = _lib.ZG_DH_MATRIX
+        if self.dissipator is not None:
+            dz = self.dissipator(ts, tr.stage_sigma()[None])
+            if not (np.isscalar(dz) and dz == 0):
+                raise NotImplementedError("a nonzero dissipator is not supported on the device path")
+        delta = [self.bias(ts, a) for a in range(self.NL)]
+        self.n_rhs += 1
+        return tr.rhs(i, ts, h, delta, mode, U, currents=want_J)
+
+    def attempt(self, t, h):
+        """One attempt of all stages from the stored y; returns (TE, J at stage 0, err2 parts)."""
+        J0 = None
+        for i in range(self.tab.RK_N):
+            J = self._stage(i, t, h, want_J=(i == 0))
+            if i == 0:
+                J0 = J
+        e = self.traj.error_norm2()
+        TE = math.sqrt(float(e.sum()))
+        return TE, J0, e
+
+    def run(self, t0, t1, h, eps, max_attempts=None, replay_h=None, record_sigma=True, on_step=None):
+        """Propagate from t0 until t >= t1 exactly as ``zand`` does; returns histories."""
+        t = float(t0)
+        out = dict(times=[t], sig=[], currents=[], h_hist=[], TE_hist=[], t_attempt=[], accepted=[])
+        if record_sigma:
+            out["sig"].append(self.traj.get_y()[0])
+        attempts = 0
+        while t < t1:
+            accepted = False
+            while not accepted:
+                if max_attempts is not None and attempts >= max_attempts:
+                    return out
+                if replay_h is not None:
+                    h = float(replay_h[attempts])
+                TE, J0, _ = self.attempt(t, h)
+                out["h_hist"].append(h)
+                out["TE_hist"].append(TE)
+                out["t_attempt"].append(t)
+                attempts += 1
+                accepted = TE < eps
+                out["accepted"].append(accepted)
+                h = self.tab.hnew(h, TE, eps)
+            out["currents"].append(J0)
+            self.traj.step_fourth()
+            t += h
+            out["times"].append(t)
+            if record_sigma:
+                out["sig"].append(self.traj.get_y()[0])
+            if on_step is not None:
+                on_step(t, h)
+        return out
