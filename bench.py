@@ -1,0 +1,360 @@
+"""Throughput of the AME propagation: simulated femtoseconds per wall second.
+
+Workload (default ``--config c3``): the n = 1024 case -- a 32 x 32 square
+lattice (hopping -1 eV), two leads on opposite edges with 32 coupling orbitals
+each, 40 rank-8 Lorentzians and 30 Pade poles per lead, the mean-field Hubbard
+term U = 2 eV * (Re diag sigma - 0.5) rebuilt at every stage, sinusoidal bias
+0.2 V sin(2 pi 0.05 t) split +-V/2.  Inputs are seeded synthetic ``Arrays``
+(``zandpack_gb300.workloads``); the state starts from the isolated-device
+Fermi density matrix with psi = Omega = 0.
+
+A step is one Dormand-Prince 5(4) attempt of the reference controller (seven
+right-hand sides, the embedded error norm, the accept test and, on
+acceptance, the update).  ``value`` = simulated fs advanced over the K timed
+steps / their wall time measured with CUDA events on the trajectory's stream.
+``e2e`` repeats it through the public API with the initial state uploaded from
+pinned host memory and sigma plus the lead currents read back after every
+accepted step, as ``zand`` records them.
+
+``--impl reference`` times the CPU restatement of the reference (the oracle,
+NumPy/BLAS on all host cores) on the same workload; its step is one stage of
+the attempt (stage combination + right-hand side), its simulated time is the
+attempt's advance shared evenly over the attempt's stages.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "simulated fs/s at n=1024"
+WORKLOAD_DESC = {
+    "c3": "n=1024 32x32 square lattice, 2 leads x 32 orbitals, 40 rank-8 Lorentzians + 30 Pade poles per lead, "
+          "Hubbard dH(sigma) U=2 eV every stage, bias 0.2 V sin(2pi 0.05 t); eps=1e-6",
+    "c2": "n=256 honeycomb ribbon, 2 leads x 16 orbitals, 32 rank-4 Lorentzians + 40 Pade poles, Gaussian pulse",
+    "c1": "n=20 chain, 2 leads x 1 orbital, 16 Lorentzians + 20 Pade poles, exponential ramp",
+    "c5": "n=2048 random sparse, 4 leads x 72 orbitals, 24 rank-8 Lorentzians + 40 Pade poles, step bias lead 0",
+}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    return ws, rank
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.p = None
+        self.path = os.path.join(HERE, "gpurun_out", "bench_clocks.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p is not None:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except Exception:
+                self.p.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, fl in rows for i, v in enumerate(fl) if v.lower() == "active"})
+        return {"sm_mhz": float(np.median([r[0] for r in rows])), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+def rhs_flops(L):
+    """Algorithmic real flops of one right-hand side (structurally nonzero work)."""
+    n, N, Ns, Nf, nc = L.n, L.N, L.Ns, L.Nf, L.nc
+    gemm = 8 * n ** 3 + 8 * N * n * n + 8 * n * N * nc + 8 * Ns * nc * n + 8 * N * Ns * nc + 8 * Ns * Nf * nc
+    omega = 8 * N * Ns * nc + 8 * Ns * Ns * nc + 8 * Ns * Nf * nc + 10 * (N * Ns + Ns * Nf)
+    return gemm, omega
+
+
+def run_ours(args):
+    import torch
+    from zandpack_gb300 import _lib
+    from zandpack_gb300.engine import Propagator
+    from zandpack_gb300.workloads import make_workload
+    ws, rank = _dist()
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    w = make_workload(args.config)
+    pr = Propagator(w.arrays, w.hbar, w.bias_fn(), hubbard_U=w.hubbard_U, precision=args.precision, device=dev)
+    tr = pr.traj
+    L = tr.layout
+    stream = torch.cuda.ExternalStream(_lib.lib().zg_traj_stream(tr._h), device=dev)
+    eps = w.eps
+
+    def attempts(state, k):
+        t, h = state
+        adv = 0.0
+        for _ in range(k):
+            TE, J0, _ = pr.attempt(t, h)
+            hn = pr.tab.hnew(h, TE, eps)
+            if TE < eps:
+                tr.step_fourth()
+                t += hn
+                adv += hn
+            h = hn
+        return (t, h), adv
+
+    pr.set_state(w.arrays["DM_Ortho"])
+    state = (w.t0, w.stepsize)
+    state, _ = attempts(state, args.warmup)
+    peaks = np.zeros(2)
+    _lib.check(_lib.lib().zg_measure_peaks(dev, peaks.ctypes.data_as(__import__("ctypes").c_void_p)))
+    import ctypes
+    _lib.check(_lib.lib().zg_profile(tr._h, 1))
+    n0 = _lib.lib().zg_launch_count()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(dev) as clk:
+        e0.record(stream)
+        state, adv = attempts(state, args.steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    launches = _lib.lib().zg_launch_count() - n0
+    pms = np.zeros(len(_lib.PROF_REGIONS))
+    pcnt = np.zeros(len(_lib.PROF_REGIONS), np.int64)
+    _lib.check(_lib.lib().zg_profile_read(tr._h, pms.ctypes.data_as(ctypes.c_void_p), pcnt.ctypes.data_as(ctypes.c_void_p)))
+    _lib.check(_lib.lib().zg_profile(tr._h, 0))
+    if ws > 1:
+        t = torch.tensor([ms, adv], device="cuda", dtype=torch.float64)
+        tmax = t.clone()
+        torch.distributed.all_reduce(tmax, op=torch.distributed.ReduceOp.MAX)
+        tsum = t.clone()
+        torch.distributed.all_reduce(tsum)
+        ms, adv_total = float(tmax[0]), float(tsum[1])
+    else:
+        adv_total = adv
+    value = adv_total / (ms / 1e3)
+    # ---- e2e through the public API: pinned upload + per-step sigma/current readback
+    e2e = run_e2e(pr, w, args, state, stream)
+    reg = dict(zip(_lib.PROF_REGIONS, zip(pms.tolist(), pcnt.tolist())))
+    gemm_f, omega_f = rhs_flops(L)
+    g_ms, g_n = reg["gemm"]
+    achieved = gemm_f / (g_ms / g_n / 1e3) / 1e12 if g_n else None
+    fp64_peak = peaks[0] / 1e3
+    out = {
+        "metric": METRIC, "value": value, "unit": "fs/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "c128" if args.precision == "f64" else "mixed", "data": "synthetic",
+        "config": {"workload": "%s: %s" % (args.config, WORKLOAD_DESC.get(args.config, "")),
+                   "precision": args.precision, "layout": L.summary(),
+                   "l2": "inputs larger than L2: %d state slots x %.0f MB" % (tr.stages + 1, L.size * 16 / 1e6),
+                   "parallelism": "replicas" if ws > 1 else "single"},
+        "rhs_evals_per_s": tr.stages * args.steps * ws / (ms / 1e3),
+        "simulated_fs": adv_total,
+        "t_h_after": list(state),
+        "roofline": {"bound": "fp64", "kernel": "k_zgemm (batched FP64 complex GEMMs of one RHS)",
+                     "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                     "frac": (achieved / fp64_peak) if achieved else None, "traffic": None,
+                     "peak_source": "live DFMA probe zg_measure_peaks (FP64 is not in MEASURED_PEAKS.json)",
+                     "algorithmic_flops_per_launch": gemm_f,
+                     "regions_ms_per_call": {k: (v[0] / v[1] if v[1] else None) for k, v in reg.items()}},
+        "e2e": e2e,
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+        "peaks_live_gflops": {"fp64": peaks[0], "fp32": peaks[1]},
+    }
+    if rank == 0:
+        out["cpu_baseline"] = cpu_baseline(args, w, adv_total / (args.steps * ws))
+        print(json.dumps(out))
+    tr.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def run_e2e(pr, w, args, state, stream):
+    import torch
+    tr = pr.traj
+    L = tr.layout
+    y0 = L.pack(w.arrays["DM_Ortho"], *L.unpack(np.zeros(L.size, complex))[1:])
+    pinned = torch.from_numpy(y0.view(np.float64)).pin_memory()
+    sig_host = torch.empty((L.n, L.n * 2), dtype=torch.float64).pin_memory()
+    import ctypes
+    from zandpack_gb300._lib import check, lib
+    eps = w.eps
+    t, h = w.t0, state[1]
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    check(lib().zg_set_state(tr._h, tr.stages, ctypes.c_void_p(pinned.data_ptr())))
+    adv = 0.0
+    d2h = 0
+    for _ in range(args.steps):
+        TE, J0, _ = pr.attempt(t, h)
+        hn = pr.tab.hnew(h, TE, eps)
+        d2h += 3 * 8 + L.NL * 8
+        if TE < eps:
+            tr.step_fourth()
+            check(lib().zg_get_sigma(tr._h, tr.stages, ctypes.c_void_p(sig_host.data_ptr())))
+            d2h += L.n * L.n * 16
+            t += hn
+            adv += hn
+        h = hn
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    return {"value": adv / (ms / 1e3), "unit": "fs/s", "h2d_bytes_per_step": int(L.size * 16 / args.steps),
+            "d2h_bytes_per_step": int(d2h / args.steps),
+            "note": "initial state uploaded once from pinned memory (bytes amortised over the steps); "
+                    "sigma and currents read back after every accepted step"}
+
+
+def _oracle_stages(w, nstages, warm_stages=0):
+    """Run the oracle's controller stage by stage; returns (wall s, simulated fs
+    attributed to the timed stages, stages timed)."""
+    from oracle import zand_np as zo
+    prob = zo.Problem(w.arrays, w.hbar)
+    bias, dH = w.bias_fn(), w.dH_fn()
+    s0, p0, o0 = prob.zero_state()
+    SIGS = np.zeros((8,) + s0.shape, complex)
+    PSIS = np.zeros((8,) + p0.shape, complex)
+    OMGS = np.zeros((8,) + o0.shape, complex)
+    SIGS[-1] = w.arrays["DM_Ortho"]
+    t, h = w.t0, w.stepsize
+    wall, sim = 0.0, 0.0
+    timed_in_attempt = 0
+    for k in range(warm_stages + nstages):
+        i = k % 7
+        if i == 0:
+            timed_in_attempt = 0
+        t_start = time.perf_counter()
+        if i == 0:
+            ys, yp, yo = SIGS[-1], PSIS[-1], OMGS[-1]
+        else:
+            ix = zo.idxholder[i]
+            ys, yp, yo = (zo.stage_combine(Y, zo.B[i], ix) for Y in (SIGS, PSIS, OMGS))
+        ts = t + zo.A[i] * h
+        ks, kp, ko, _, _ = prob.rhs(h, ys, yp, yo, prob.H0 + dH(ts, ys), [bias(ts, a) for a in range(prob.NL)])
+        SIGS[i], PSIS[i], OMGS[i] = ks, kp, ko
+        adv = None
+        if i == 6:
+            TE = math.sqrt(sum(zo.terr2(Y[:7], zo.CT) for Y in (SIGS, PSIS, OMGS)))
+            hn = float(zo.hnew_func(h, TE, w.eps))
+            adv = 0.0
+            if TE < w.eps:
+                for Y in (SIGS, PSIS, OMGS):
+                    zo.step_fourth(Y, zo.CH)
+                t += hn
+                adv = hn
+            h_used, h = h, hn
+        dt = time.perf_counter() - t_start
+        if k >= warm_stages:
+            wall += dt
+            timed_in_attempt += 1
+        if adv is not None:
+            # the attempt's advance is shared evenly over its seven stages
+            sim += adv * timed_in_attempt / 7
+            timed_in_attempt = 0
+    # an attempt cut off by the end of the sample counts at the step it uses
+    sim += h * timed_in_attempt / 7
+    return wall, sim, nstages
+
+
+def cpu_baseline(args, w, adv_per_attempt):
+    """Oracle (NumPy restatement of the reference) on a bounded sample: two
+    stages of the same workload; simulated time uses the GPU run's mean advance
+    per attempt so both arms follow the same controller trajectory."""
+    nst = 2
+    try:
+        wall, _, done = _oracle_stages(w, nst, 0)
+    except MemoryError:
+        return {"value": None, "unit": "fs/s", "cores": os.cpu_count(), "kind": "port",
+                "sample": "oracle out of host memory"}
+    per_stage = wall / done
+    return {"value": adv_per_attempt / (7 * per_stage), "unit": "fs/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": "%d stages (combination + RHS) of %s from the initial state, NumPy/BLAS default threads; "
+                      "fs per attempt taken from the GPU run (%.4g fs)" % (done, args.config, adv_per_attempt),
+            "s_per_rhs": per_stage}
+
+
+def run_reference(args):
+    ws, rank = _dist()
+    if rank != 0:
+        return
+    from zandpack_gb300.workloads import make_workload
+    w = make_workload(args.config)
+    # warm-up stages then timed stages; each "step" is one stage of an attempt
+    wall, sim, done = _oracle_stages(w, args.steps, args.warmup)
+    value = sim / wall if wall > 0 else None
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": "fs/s", "n_gpus": ws,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall / done * 1e3,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+           "config": {"workload": "%s: %s" % (args.config, WORKLOAD_DESC.get(args.config, "")),
+                      "precision": "f64", "layout": "reference padded (NL, NX, NOT)"},
+           "cpu_baseline": {"value": value, "unit": "fs/s", "cores": os.cpu_count(), "kind": "port",
+                            "sample": "%d stages of the reference controller (oracle restatement, NumPy/BLAS)" % done},
+           "e2e": {"value": value, "unit": "fs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="c3")
+    ap.add_argument("--precision", default="f64", choices=["f64", "mixed"])
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -117,6 +117,19 @@ int zg_error_norm2(zg_traj* t, double* err2);
 
 /* y <- sum_j CH_j Y_j (step_fourth_*, Zandpack/mpi_funcs.py:254-259). */
 int zg_step_fourth(zg_traj* t);
+/* Download sigma (n*n complex) of a state slot; the DM the reference records
+ * after every accepted step (Zandpack/mpi/zand:428-430). */
+int zg_get_sigma(zg_traj* t, int slot, double* host);
+
+/* Measurement.  With profiling on, CUDA events on the trajectory's stream
+ * bracket each region; zg_profile_read returns accumulated milliseconds and
+ * counts per region (indices ZG_PROF_*).  zg_profile(t, 1) also resets them. */
+enum { ZG_PROF_GEMM = 0, ZG_PROF_OMEGA = 1, ZG_PROF_FINAL = 2, ZG_PROF_COMBINE = 3, ZG_PROF_ERROR = 4,
+       ZG_PROF_UPDATE = 5, ZG_PROF_RHS = 6, ZG_PROF_PREP = 7, ZG_PROF_REGIONS = 8 };
+int zg_profile(zg_traj* t, int enable);
+int zg_profile_read(zg_traj* t, double* ms, long long* count);
+/* Live FP64 and FP32 FMA throughput of `device` in GFLOP/s (out[0], out[1]). */
+int zg_measure_peaks(int device, double* out);
 
 /* ------------------------------------------------------------------------
  * Stateless array kernels on caller device buffers (complex128), the

@@ -16,6 +16,7 @@ ZG_PREC_F64, ZG_PREC_MIXED = 0, 1
 ZG_DH_NONE, ZG_DH_MATRIX, ZG_DH_HUBBARD = 0, 1, 2
 ZG_MAX_LEADS = 16
 ZG_MAX_STAGES = 13
+PROF_REGIONS = ["gemm", "omega", "final", "combine", "error", "update", "rhs", "prep"]
 
 _NAMES = {ZG_EINVAL: "EINVAL", ZG_ENOMEM: "ENOMEM", ZG_ECUDA: "ECUDA", ZG_ETIMEOUT: "ETIMEOUT",
           ZG_ENONFINITE: "ENONFINITE"}
@@ -59,6 +60,10 @@ _SIGS = {
     "zg_rhs": ([_P, C.c_int, C.c_double, C.c_double, _P, C.c_int, C.c_double, _P], C.c_int),
     "zg_error_norm2": ([_P, _P], C.c_int),
     "zg_step_fourth": ([_P], C.c_int),
+    "zg_get_sigma": ([_P, C.c_int, _P], C.c_int),
+    "zg_profile": ([_P, C.c_int], C.c_int),
+    "zg_profile_read": ([_P, _P, _P], C.c_int),
+    "zg_measure_peaks": ([C.c_int, _P], C.c_int),
     "zg_combine_c128": ([_P, C.c_int64, C.c_int, _P, _P, C.c_int, _P, C.c_int64, _P], C.c_int),
     "zg_terr2_c128": ([_P, C.c_int64, C.c_int, _P, C.c_int64, _P, _P], C.c_int),
     "zg_step_fourth_c128": ([_P, C.c_int64, C.c_int, _P, C.c_int64, _P], C.c_int),

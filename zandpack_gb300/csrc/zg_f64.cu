@@ -464,3 +464,56 @@ int launch_omega(const RhsDev& d, const StageParams& p, const OmTile* tiles, int
 }
 
 }  // namespace zg
+
+namespace zg {
+
+// ------------------------------------------------------------ peak probes
+// Independent FMA chains per thread; the result store is never taken but keeps
+// the chains live.
+template <typename T>
+__global__ void __launch_bounds__(256) k_fma_peak(T* out, T a, T b, int iters) {
+  T x0 = (T)threadIdx.x * (T)1e-9, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6,
+    x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+    x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+  }
+  T s = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+  if (s == (T)1.2345) out[0] = s;
+}
+
+int measure_peaks(double* out) {
+  int dev = 0, sms = 0;
+  ZG_CHECK_CUDA(cudaGetDevice(&dev));
+  ZG_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  double* d = nullptr;
+  ZG_CHECK_CUDA(cudaMalloc(&d, 16));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const int blocks = sms * 8, thr = 256;
+  for (int which = 0; which < 2; ++which) {
+    const int iters = which == 0 ? 2048 : 65536;
+    double best = 0.0;
+    for (int rep = 0; rep < 3; ++rep) {
+      cudaEventRecord(e0);
+      if (which == 0) k_fma_peak<double><<<blocks, thr>>>(d, 0.999, 1e-3, iters);
+      else k_fma_peak<float><<<blocks, thr>>>((float*)d, 0.999f, 1e-3f, iters);
+      cudaEventRecord(e1);
+      cudaError_t err = cudaEventSynchronize(e1);
+      if (err != cudaSuccess) { cudaFree(d); set_error("peak probe: %s", cudaGetErrorString(err)); return ZG_ECUDA; }
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      double gf = 2.0 * 8.0 * iters * (double)blocks * thr / (ms * 1e6);
+      best = gf > best ? gf : best;
+    }
+    out[which] = best;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(d);
+  ZG_CHECK_LAUNCH();
+  return ZG_OK;
+}
+
+}  // namespace zg

@@ -77,6 +77,9 @@ int launch_sigma_finalize(const RhsDev& d, const StageParams& p, const double2* 
                           double2* ksig, double* currents, cudaStream_t s);
 int launch_psi_finalize(const RhsDev& d, const StageParams& p, const double2* psi, const double2* R2,
                         const double2* ZA, const double2* ZB, double2* kpsi, cudaStream_t s);
+// out[0] = FP64 FMA rate, out[1] = FP32 FMA rate, GFLOP/s (2 flops per FMA)
+int measure_peaks(double* out);
+
 int launch_omega(const RhsDev& d, const StageParams& p, const OmTile* tiles, int ntiles, const double2* G,
                  const double2* yin, double2* kout, cudaStream_t s);
 

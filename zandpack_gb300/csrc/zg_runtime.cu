@@ -84,6 +84,16 @@ struct zg_traj {
   double *J = nullptr, *partial = nullptr, *err = nullptr;
   int nblk_err = 0;
   bool dH_set = false;
+  // profiling: CUDA event pairs on `stream` around each region, collected at host syncs
+  struct Prof {
+    bool on = false;
+    static const int RING = 64;
+    cudaEvent_t b[ZG_PROF_REGIONS][RING], e[ZG_PROF_REGIONS][RING];
+    int pending[ZG_PROF_REGIONS] = {};
+    double ms[ZG_PROF_REGIONS] = {};
+    long long cnt[ZG_PROF_REGIONS] = {};
+    bool created = false;
+  } prof;
 
   RhsDev dev_view() const {
     RhsDev d;
@@ -96,8 +106,42 @@ struct zg_traj {
   double2* slot(int i) const { return Y + (int64_t)i * S; }
 };
 
+// ---------------------------------------------------------------- profiling
+static void prof_collect(zg_traj* t) {
+  auto& P = t->prof;
+  if (!P.created) return;
+  for (int r = 0; r < ZG_PROF_REGIONS; ++r) {
+    for (int i = 0; i < P.pending[r]; ++i) {
+      float ms = 0.f;
+      if (cudaEventSynchronize(P.e[r][i]) == cudaSuccess && cudaEventElapsedTime(&ms, P.b[r][i], P.e[r][i]) == cudaSuccess) {
+        P.ms[r] += ms;
+        P.cnt[r] += 1;
+      }
+    }
+    P.pending[r] = 0;
+  }
+}
+static void prof_begin(zg_traj* t, int r) {
+  auto& P = t->prof;
+  if (!P.on) return;
+  if (P.pending[r] == P.RING) prof_collect(t);
+  cudaEventRecord(P.b[r][P.pending[r]], t->stream);
+}
+static void prof_end(zg_traj* t, int r) {
+  auto& P = t->prof;
+  if (!P.on) return;
+  cudaEventRecord(P.e[r][P.pending[r]], t->stream);
+  P.pending[r] += 1;
+}
+
 static void free_traj(zg_traj* t) {
   if (!t) return;
+  if (t->prof.created)
+    for (int r = 0; r < ZG_PROF_REGIONS; ++r)
+      for (int i = 0; i < t->prof.RING; ++i) {
+        cudaEventDestroy(t->prof.b[r][i]);
+        cudaEventDestroy(t->prof.e[r][i]);
+      }
   void* ptrs[] = {t->H0, t->Xp, t->Xm, t->GLP, t->dGP, t->XI, t->IXI, t->XIS, t->U, t->V, t->mode_lead,
                   t->lead_cols, t->colmap, t->tiles, t->Y, t->Ystage, t->Ht, t->dH, t->T, t->Pc, t->sigC,
                   t->G, t->R2, t->ZA, t->ZB, t->J, t->partial, t->err};
@@ -322,7 +366,9 @@ int zg_stage_input(zg_traj* t, int stage) {
     double b = t->B[(size_t)stage * (t->stages + 1) + j];
     if (b != 0.0) { cf.idx[cf.n] = j; cf.c[cf.n] = b; ++cf.n; }
   }
+  prof_begin(t, ZG_PROF_COMBINE);
   ZG_TRY(launch_combine_c128(t->Y, t->S, cf, t->Ystage, t->S, t->stream));
+  prof_end(t, ZG_PROF_COMBINE);
   t->cur_in = t->Ystage;
   return ZG_OK;
 }
@@ -363,8 +409,11 @@ int zg_rhs(zg_traj* t, int stage, double ts, double h, const double* delta, int 
   double2* out = t->slot(stage);
   cudaStream_t s = t->stream;
   const int64_t n = t->n, N = t->N, Ns = t->Ns, Nf = t->Nf, L = t->L, nc = t->nc;
+  prof_begin(t, ZG_PROF_RHS);
+  prof_begin(t, ZG_PROF_PREP);
   ZG_TRY(launch_build_ht(d, sig, t->dH, dH_mode, hubbard_U, t->Ht, s));
   ZG_TRY(launch_gathers(d, sig, psi, t->sigC, t->G, s));
+  prof_end(t, ZG_PROF_PREP);
   std::vector<GemmProb> probs;
   auto prob = [&](const double2* A, int64_t lda, int opA, const double2* B, int64_t ldb, int opB, double2* C,
                   int64_t ldc, int M, int Nn, int K) {
@@ -398,11 +447,18 @@ int zg_rhs(zg_traj* t, int stage, double ts, double h, const double* delta, int 
     GemmBatch batch;
     batch.nprob = (int)std::min<size_t>(ZG_MAX_GEMM, probs.size() - b0);
     for (int i = 0; i < batch.nprob; ++i) batch.p[i] = probs[b0 + i];
+    prof_begin(t, ZG_PROF_GEMM);
     ZG_TRY(launch_zgemm_batch(batch, s));
+    prof_end(t, ZG_PROF_GEMM);
   }
+  prof_begin(t, ZG_PROF_FINAL);
   ZG_TRY(launch_sigma_finalize(d, p, t->T, t->Pc, out, currents ? t->J : nullptr, s));
   ZG_TRY(launch_psi_finalize(d, p, psi, t->R2, t->ZA, t->ZB, out + t->off_psi, s));
+  prof_end(t, ZG_PROF_FINAL);
+  prof_begin(t, ZG_PROF_OMEGA);
   ZG_TRY(launch_omega(d, p, t->tiles, t->ntiles, t->G, in, out, s));
+  prof_end(t, ZG_PROF_OMEGA);
+  prof_end(t, ZG_PROF_RHS);
   if (currents) {
     ZG_CHECK_CUDA(cudaMemcpyAsync(currents, t->J, L * sizeof(double), cudaMemcpyDeviceToHost, s));
     ZG_CHECK_CUDA(cudaStreamSynchronize(s));
@@ -417,13 +473,16 @@ int zg_error_norm2(zg_traj* t, double* err2) {
   cf.n = 0;
   for (int j = 0; j < t->stages; ++j)
     if (t->CT[j] != 0.0) { cf.idx[cf.n] = j; cf.c[cf.n] = t->CT[j]; ++cf.n; }
+  prof_begin(t, ZG_PROF_ERROR);
   const int64_t seg[4] = {0, t->off_psi, t->off_omA, t->S};
   for (int k = 0; k < 3; ++k)
     ZG_TRY(launch_terr2_partials_c128(t->Y, t->S, cf, seg[k], seg[k + 1], t->partial + (int64_t)k * t->nblk_err,
                                       t->nblk_err, t->stream));
   ZG_TRY(launch_reduce_partials(t->partial, t->nblk_err, 3, t->err, t->stream));
+  prof_end(t, ZG_PROF_ERROR);
   ZG_CHECK_CUDA(cudaMemcpyAsync(err2, t->err, 3 * sizeof(double), cudaMemcpyDeviceToHost, t->stream));
   ZG_CHECK_CUDA(cudaStreamSynchronize(t->stream));
+  prof_collect(t);
   return ZG_OK;
 }
 
@@ -434,9 +493,55 @@ int zg_step_fourth(zg_traj* t) {
   cf.n = 0;
   for (int j = 0; j <= t->stages; ++j)
     if (t->CH[j] != 0.0) { cf.idx[cf.n] = j; cf.c[cf.n] = t->CH[j]; ++cf.n; }
+  prof_begin(t, ZG_PROF_UPDATE);
   ZG_TRY(launch_step_fourth_c128(t->Y, t->S, t->stages, cf, t->S, t->stream));
+  prof_end(t, ZG_PROF_UPDATE);
   ZG_CHECK_CUDA(cudaStreamSynchronize(t->stream));
   return ZG_OK;
+}
+
+int zg_get_sigma(zg_traj* t, int slot, double* host) {
+  ZG_REQUIRE(t && host, "null argument");
+  ZG_REQUIRE(slot >= 0 && slot <= t->stages, "slot %d out of range", slot);
+  ZG_CHECK_CUDA(cudaSetDevice(t->dev));
+  ZG_CHECK_CUDA(cudaMemcpyAsync(host, t->slot(slot), (size_t)t->n * t->n * sizeof(double2), cudaMemcpyDeviceToHost,
+                                t->stream));
+  ZG_CHECK_CUDA(cudaStreamSynchronize(t->stream));
+  return ZG_OK;
+}
+
+int zg_profile(zg_traj* t, int enable) {
+  ZG_REQUIRE(t, "null argument");
+  ZG_CHECK_CUDA(cudaSetDevice(t->dev));
+  auto& P = t->prof;
+  if (enable && !P.created) {
+    for (int r = 0; r < ZG_PROF_REGIONS; ++r)
+      for (int i = 0; i < P.RING; ++i) {
+        ZG_CHECK_CUDA(cudaEventCreate(&P.b[r][i]));
+        ZG_CHECK_CUDA(cudaEventCreate(&P.e[r][i]));
+      }
+    P.created = true;
+  }
+  ZG_CHECK_CUDA(cudaStreamSynchronize(t->stream));
+  prof_collect(t);
+  P.on = enable != 0;
+  for (int r = 0; r < ZG_PROF_REGIONS; ++r) { P.ms[r] = 0; P.cnt[r] = 0; }
+  return ZG_OK;
+}
+
+int zg_profile_read(zg_traj* t, double* ms, long long* count) {
+  ZG_REQUIRE(t && ms && count, "null argument");
+  ZG_CHECK_CUDA(cudaSetDevice(t->dev));
+  ZG_CHECK_CUDA(cudaStreamSynchronize(t->stream));
+  prof_collect(t);
+  for (int r = 0; r < ZG_PROF_REGIONS; ++r) { ms[r] = t->prof.ms[r]; count[r] = t->prof.cnt[r]; }
+  return ZG_OK;
+}
+
+int zg_measure_peaks(int device, double* out) {
+  ZG_REQUIRE(out, "null argument");
+  ZG_CHECK_CUDA(cudaSetDevice(device));
+  return measure_peaks(out);
 }
 
 // ------------------------------------------------------------ array kernels
