@@ -144,6 +144,18 @@ int zg_combine_c128(const double* Y, int64_t slot_stride, int nslots, const doub
  * Uses a device scratch buffer of partial sums that it allocates stream-ordered. */
 int zg_terr2_c128(const double* Y, int64_t slot_stride, int nslots, const double* ct,
                   int64_t count, double* result, void* stream);
+/* Same result as zg_terr2_c128, for callers that must not allocate device
+ * memory while they run (for example a serving loop that reserved all of HBM
+ * up front, or a host whose device memory is owned by another allocator).
+ * No counterpart in the reference.  The partial sums live in a static 8 KiB
+ * device array (1024 doubles) inside the library; every count is accepted, a
+ * request needing more scratch than that is refused with ZG_EINVAL.  Calls
+ * share the array: calls that overlap on the GPU race and must be serialised.
+ * The first call on a device looks up the array's device address (with that
+ * device current) and caches it; make that first call before any stream
+ * capture. */
+int zg_terr2_c128_noalloc(const double* Y, int64_t slot_stride, int nslots, const double* ct,
+                          int64_t count, double* result, void* stream);
 /* Y[nslots-1] = sum_j ch[j] Y[j]  (step_fourth_*, mpi_funcs.py:254-259) */
 int zg_step_fourth_c128(double* Y, int64_t slot_stride, int nslots, const double* ch,
                         int64_t count, void* stream);
