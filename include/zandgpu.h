@@ -132,6 +132,18 @@ int zg_profile_read(zg_traj* t, double* ms, long long* count);
 int zg_measure_peaks(int device, double* out);
 
 /* ------------------------------------------------------------------------
+ * Tensor-core building blocks of the mixed-precision path (device pointers).
+ * ---------------------------------------------------------------------- */
+/* hi = x rounded to TF32 (nearest, ties away), lo = (x - hi) rounded to TF32. */
+int zg_split_tf32(const float* x, float* hi, float* lo, int64_t n, void* stream);
+/* D (M x N, row-major fp32) = (Ah + Al)(Bh + Bl)^T minus the Al.Bl^T term, on
+ * tcgen05 tensor cores; A is M x K, B is N x K, row-major, TF32-exact values;
+ * K % 4 == 0, N % 32 == 0.  Synchronises the stream; ZG_ETIMEOUT if a bounded
+ * device-side wait gave up. */
+int zg_gemm_tf32x3(const float* Ah, const float* Al, const float* Bh, const float* Bl, float* D,
+                   int M, int N, int K, void* stream);
+
+/* ------------------------------------------------------------------------
  * Stateless array kernels on caller device buffers (complex128), the
  * numba/numpy kernels of Zandpack/func_step_forward.py and mpi_funcs.py.
  * Y holds `nslots` arrays of `count` complex elements, `slot_stride`

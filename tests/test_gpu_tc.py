@@ -1,0 +1,63 @@
+"""tcgen05 3xTF32 GEMM and the TF32 split against float64 references."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _p(t):
+    return C.c_void_p(t.data_ptr())
+
+
+def _split(x):
+    import torch
+    from zandpack_gb300._lib import check, lib
+    hi = torch.empty_like(x)
+    lo = torch.empty_like(x)
+    check(lib().zg_split_tf32(_p(x), _p(hi), _p(lo), x.numel(), None))
+    return hi, lo
+
+
+def test_split_tf32():
+    import torch
+    x = torch.randn(100003, device="cuda", dtype=torch.float32) * 1e3
+    hi, lo = _split(x)
+    torch.cuda.synchronize()
+    hb = hi.view(torch.int32).cpu().numpy()
+    lb = lo.view(torch.int32).cpu().numpy()
+    assert (hb & 0x1FFF == 0).all() and (lb & 0x1FFF == 0).all()
+    xd = x.double().cpu().numpy()
+    err = np.abs(hi.double().cpu().numpy() + lo.double().cpu().numpy() - xd) / np.abs(xd).max()
+    assert err.max() < 2.0 ** -21
+
+
+@pytest.mark.parametrize("M,N,K", [(128, 256, 32), (128, 128, 64), (200, 96, 100), (1024, 2048, 2048),
+                                   (4480, 2048, 2048)])
+def test_gemm_tf32x3(M, N, K):
+    import torch
+    from zandpack_gb300._lib import check, lib
+    g = torch.Generator(device="cuda").manual_seed(M * 7 + N + K)
+    A = torch.randn(M, K, device="cuda", generator=g)
+    B = torch.randn(N, K, device="cuda", generator=g)
+    Ah, Al = _split(A)
+    Bh, Bl = _split(B)
+    D = torch.full((M, N), float("nan"), device="cuda")
+    check(lib().zg_gemm_tf32x3(_p(Ah), _p(Al), _p(Bh), _p(Bl), _p(D), M, N, K, None))
+    ref = (Ah.double() + Al.double()) @ (Bh.double() + Bl.double()).T
+    err = (D.double() - ref).abs().max().item() / ref.abs().max().item()
+    assert err < 2e-6, err
+    if M * N * K >= 1 << 32:
+        # rough timing, printed for the log
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        for _ in range(2):
+            check(lib().zg_gemm_tf32x3(_p(Ah), _p(Al), _p(Bh), _p(Bl), _p(D), M, N, K, None))
+        e0.record()
+        for _ in range(5):
+            check(lib().zg_gemm_tf32x3(_p(Ah), _p(Al), _p(Bh), _p(Bl), _p(D), M, N, K, None))
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / 5
+        print("\nGEMM %dx%dx%d 3xTF32: %.3f ms, %.1f TFLOP/s (tensor flops %.1f)" % (
+            M, N, K, ms, 2 * M * N * K / ms / 1e9, 6 * M * N * K / ms / 1e9))

@@ -3,12 +3,31 @@
 #pragma once
 #include "zg_common.cuh"
 
+#include <cuda.h>
+
 #include <atomic>
 
 namespace zg {
 
 // kernels launched by this library since load (all threads)
 extern std::atomic<long long> g_launches;
+
+// ------------------------------------------------ tensor-core GEMM (3xTF32)
+// D (M x N, fp32, row stride ldd) = (Ah + Al)(Bh + Bl)^T without Al.Bl^T;
+// A is M x K, B is N x K, row-major; values are exact TF32 numbers.
+struct TcGemm {
+  CUtensorMap Ah, Al, Bh, Bl;
+  float* D;
+  long long ldd;
+  int M, N, K, BN;
+  int* err;  // device int, nonzero after a timed-out wait
+};
+int make_tmap_f32(CUtensorMap* map, const float* base, int64_t rows, int64_t cols, int64_t ld, int box_rows);
+int tc_gemm_prepare(TcGemm& g, const float* Ah, const float* Al, const float* Bh, const float* Bl, int64_t lda,
+                    int64_t ldb, float* D, int64_t ldd, int M, int N, int K, int* err);
+int tc_gemm_launch(const TcGemm& g, cudaStream_t s);
+// hi = rna_tf32(x), lo = rna_tf32(x - hi)
+int launch_split_tf32(const float* x, float* hi, float* lo, int64_t n, cudaStream_t s);
 
 // ------------------------------------------------------------ flat kernels
 // out[e] = sum_t c[t] * Y[idx[t]][e]   (Y slots `stride` complex apart)

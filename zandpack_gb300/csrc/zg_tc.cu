@@ -1,0 +1,407 @@
+// Tensor-core GEMM for the mixed-precision path: D = A * B^T in FP32 from
+// split-TF32 operands on the 5th-generation tensor cores (tcgen05).
+//
+//   D[m][n] = sum_k (Ahi + Alo)[m][k] (Bhi + Blo)[n][k]
+//           ~ Ahi.Bhi^T + Ahi.Blo^T + Alo.Bhi^T          ("3xTF32")
+//
+// A is M x K and B is N x K, both row-major with K contiguous (K-major), FP32
+// arrays whose values are exact TF32 numbers (zg_split_tf32 produces them).
+// Complex products use the real embedding of the complex operand (see
+// zg_mixed.cu), so this kernel only sees real matrices.
+//
+// One CTA computes a BM x BN tile (BM = 128 lanes of TMEM, BN fp32 columns):
+//   * one elected thread of warp 4 streams K-blocks of 32 elements (one
+//     128-byte swizzle row) of Ahi, Alo, Bhi, Blo into a STAGES-deep ring of
+//     shared-memory buffers with TMA (cp.async.bulk.tensor, SWIZZLE_128B);
+//   * one elected thread of warp 5 issues tcgen05.mma (kind::tf32, M=128,
+//     N=BN, K=8) for the three products of a K-block into one of two TMEM
+//     accumulator buffers and commits to the smem buffer's "empty" barrier
+//     and to the TMEM buffer's "full" barrier;
+//   * warps 0-3 read each K-block's partial sum from TMEM (tcgen05.ld
+//     32x32b), add it into FP32 registers and release the TMEM buffer.
+// The tensor core truncates inside its accumulation, so a single accumulator
+// over K = 2048 drifts by ~1e-5 relative; per-K-block partials summed with
+// round-to-nearest keep the product at ~1e-7.
+// Every wait on an mbarrier is bounded by a clock64 budget; on timeout the
+// thread records an error code in *err and stops issuing, the MMA thread
+// waits for its own MMAs, the producer for its copies in flight, and TMEM is
+// freed before the CTA exits.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include "zg_kernels.cuh"
+
+namespace zg {
+
+#define TC_BM 128
+#define TC_BK 32
+#define TC_WAIT_CYCLES (4LL * 1000 * 1000 * 1000)  // ~2 s at 2 GHz
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// bounded wait: true when the phase with `parity` completed, false on timeout
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err, int code) {
+  if (mbar_try(bar, parity)) return true;
+  const long long t0 = clock64();
+  while (!mbar_try(bar, parity)) {
+    if (clock64() - t0 > TC_WAIT_CYCLES) {
+      atomicCAS(err, 0, code);
+      return false;
+    }
+  }
+  return true;
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, uint32_t bar, int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
+          dst),
+      "l"((uint64_t)map), "r"(bar), "r"(x), "r"(y)
+      : "memory");
+}
+
+// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row core groups 1024 B apart
+__device__ __forceinline__ uint64_t umma_desc_sw128(uint32_t addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr & 0x3FFFF) >> 4);        // start address
+  d |= (uint64_t)(16 >> 4) << 16;                // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;              // stride byte offset
+  d |= (uint64_t)1 << 46;                        // descriptor version (sm_100 family)
+  d |= (uint64_t)2 << 61;                        // SWIZZLE_128B
+  return d;
+}
+
+// instruction descriptor: D f32, A/B tf32, both K-major, M x N
+__host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_tf32(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accum) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+          tmem_d),
+      "l"(a), "l"(b), "r"(idesc), "r"(accum));
+}
+
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+template <int BN, int STAGES>
+struct TcCfg {
+  static constexpr int A_BYTES = TC_BM * TC_BK * 4;   // 16 KB
+  static constexpr int B_BYTES = BN * TC_BK * 4;      // 16 KB at BN = 128
+  static constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
+  static constexpr int BAR_OFF = STAGES * STAGE_BYTES;
+  static constexpr int SMEM = BAR_OFF + 256 + 1024;  // barriers, TMEM slot, alignment slack
+  static constexpr uint32_t TMEM_COLS = 2 * BN;      // two accumulator buffers
+};
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+#define TC_LD32(r, taddr)                                                                                         \
+  asm volatile(                                                                                                   \
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"              \
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"                                  \
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), \
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),     \
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),    \
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])                  \
+      : "r"(taddr))
+
+// Warp roles (192 threads): warps 0-3 drain the accumulator (TMEM lane
+// quarter = warp), warp 4 lane 0 loads with TMA, warp 5 lane 0 issues MMAs
+// and owns the TMEM allocation.  Each K-block of 32 is accumulated alone in
+// one of two TMEM buffers and added into FP32 registers (round to nearest),
+// so the tensor core's truncating accumulation never spans more than 12
+// instructions.
+template <int BN, int STAGES>
+__global__ void __launch_bounds__(192, 1)
+    k_gemm_tf32x3(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtensorMap mAl,
+                  const __grid_constant__ CUtensorMap mBh, const __grid_constant__ CUtensorMap mBl, float* __restrict__ D,
+                  int M, int N, int K, long long ldd, int* err) {
+  using C = TcCfg<BN, STAGES>;
+  extern __shared__ uint8_t smem_raw[];
+  const uint32_t raw = smem_u32(smem_raw);
+  const uint32_t pad = (1024u - (raw & 1023u)) & 1023u;
+  uint8_t* smem = smem_raw + pad;
+  const uint32_t sbase = raw + pad;
+  const uint32_t bar_full = sbase + C::BAR_OFF;        // STAGES x 8 B
+  const uint32_t bar_empty = bar_full + 8 * STAGES;    // STAGES x 8 B
+  const uint32_t bar_tfull = bar_empty + 8 * STAGES;   // 2 x 8 B
+  const uint32_t bar_tempty = bar_tfull + 16;          // 2 x 8 B
+  const uint32_t bar_done = bar_tempty + 16;           // 8 B
+  uint32_t* tmem_slot = (uint32_t*)(smem + C::BAR_OFF + 16 * STAGES + 40);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * BN;
+  const int nk = (K + TC_BK - 1) / TC_BK;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(bar_full + 8 * s, 1);
+      mbar_init(bar_empty + 8 * s, 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(bar_tfull + 8 * b, 1);
+      mbar_init(bar_tempty + 8 * b, 128);
+    }
+    mbar_init(bar_done, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 5) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(C::TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 4) {
+    if (lane == 0) {
+      // ---------------- TMA producer
+      int issued[STAGES];
+      for (int s = 0; s < STAGES; ++s) issued[s] = 0;
+      bool ok = true;
+      for (int kb = 0; kb < nk && ok; ++kb) {
+        const int s = kb % STAGES;
+        const uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
+        ok = mbar_wait(bar_empty + 8 * s, ph ^ 1u, err, 1);
+        if (!ok) break;
+        const uint32_t st = sbase + s * C::STAGE_BYTES;
+        mbar_expect_tx(bar_full + 8 * s, C::STAGE_BYTES);
+        const int kx = kb * TC_BK;
+        tma_load_2d(st, &mAh, bar_full + 8 * s, kx, m0);
+        tma_load_2d(st + C::A_BYTES, &mAl, bar_full + 8 * s, kx, m0);
+        tma_load_2d(st + 2 * C::A_BYTES, &mBh, bar_full + 8 * s, kx, n0);
+        tma_load_2d(st + 2 * C::A_BYTES + C::B_BYTES, &mBl, bar_full + 8 * s, kx, n0);
+        issued[s] = kb / STAGES + 1;
+      }
+      if (!ok) {
+        // wait (bounded) for the copies already in flight before leaving
+        for (int s = 0; s < STAGES; ++s)
+          if (issued[s] > 0) mbar_wait(bar_full + 8 * s, (uint32_t)(issued[s] - 1) & 1u, err, 4);
+      }
+    }
+  } else if (warp == 5) {
+    if (lane == 0) {
+      // ---------------- MMA issuer
+      constexpr uint32_t idesc = idesc_tf32(TC_BM, BN);
+      for (int kb = 0; kb < nk; ++kb) {
+        const int s = kb % STAGES;
+        const uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
+        const int b = kb & 1;
+        if (!mbar_wait(bar_full + 8 * s, ph, err, 2)) break;
+        if (!mbar_wait(bar_tempty + 8 * b, ((uint32_t)(kb >> 1) & 1u) ^ 1u, err, 5)) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t st = sbase + s * C::STAGE_BYTES;
+        const uint32_t aH = st, aL = st + C::A_BYTES, bH = st + 2 * C::A_BYTES, bL = bH + C::B_BYTES;
+        const uint32_t d = tmem + (uint32_t)(b * BN);
+#pragma unroll
+        for (int j = 0; j < TC_BK / 8; ++j) {
+          const uint32_t off = j * 32;  // 8 tf32 = 32 bytes along K inside the swizzle row
+          umma_tf32(d, umma_desc_sw128(aH + off), umma_desc_sw128(bH + off), idesc, j > 0 ? 1u : 0u);
+          umma_tf32(d, umma_desc_sw128(aH + off), umma_desc_sw128(bL + off), idesc, 1u);
+          umma_tf32(d, umma_desc_sw128(aL + off), umma_desc_sw128(bH + off), idesc, 1u);
+        }
+        umma_commit(bar_empty + 8 * s);  // frees the smem buffer once these MMAs have read it
+        umma_commit(bar_tfull + 8 * b);  // hands the K-block sum to the drain warps
+      }
+      umma_commit(bar_done);
+      mbar_wait(bar_done, 0, err, 6);  // every MMA issued above has completed
+    }
+  } else {
+    // ---------------- drain warps 0-3: row m0 + 32*warp + lane
+    float acc[BN];
+#pragma unroll
+    for (int i = 0; i < BN; ++i) acc[i] = 0.f;
+    const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+    bool ok = true;
+    for (int kb = 0; kb < nk; ++kb) {
+      const int b = kb & 1;
+      ok = __all_sync(0xffffffffu, mbar_wait(bar_tfull + 8 * b, (uint32_t)(kb >> 1) & 1u, err, 3));
+      if (!ok) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t t0 = tmem + lane_base + (uint32_t)(b * BN);
+#pragma unroll
+      for (int c = 0; c < BN; c += 64) {
+        uint32_t r0[32], r1[32];
+        TC_LD32(r0, t0 + c);
+        TC_LD32(r1, t0 + c + 32);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int i = 0; i < 32; ++i) {
+          acc[c + i] += __uint_as_float(r0[i]);
+          acc[c + 32 + i] += __uint_as_float(r1[i]);
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      mbar_arrive(bar_tempty + 8 * b);
+    }
+    const int row = m0 + warp * 32 + lane;
+    if (ok && row < M) {
+      float* dst = D + (long long)row * ldd + n0;
+      if (n0 + BN <= N && (((uintptr_t)dst) & 15) == 0) {
+#pragma unroll
+        for (int i = 0; i < BN; i += 4) *(float4*)(dst + i) = make_float4(acc[i], acc[i + 1], acc[i + 2], acc[i + 3]);
+      } else {
+#pragma unroll
+        for (int i = 0; i < BN; ++i)
+          if (n0 + i < N) dst[i] = acc[i];
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 5) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(C::TMEM_COLS) : "memory");
+  }
+}
+
+// ---------------------------------------------------------------- host side
+static PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+
+static int tmap_encode_fn() {
+  if (g_encode) return ZG_OK;
+  void* fn = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  ZG_CHECK_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q));
+  if (fn == nullptr || q != cudaDriverEntryPointSuccess) {
+    set_error("cuTensorMapEncodeTiled is not available from the driver");
+    return ZG_ECUDA;
+  }
+  g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+  return ZG_OK;
+}
+
+// rows x cols fp32 row-major (cols contiguous, row stride ld elements), box = 32 x box_rows
+int make_tmap_f32(CUtensorMap* map, const float* base, int64_t rows, int64_t cols, int64_t ld, int box_rows) {
+  ZG_TRY(tmap_encode_fn());
+  ZG_REQUIRE(((uintptr_t)base & 15) == 0, "TMA base address must be 16-byte aligned");
+  ZG_REQUIRE((ld * 4) % 16 == 0, "TMA row stride must be a multiple of 16 bytes");
+  ZG_REQUIRE(rows > 0 && cols > 0, "empty TMA tensor");
+  cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)(ld * 4)};
+  cuuint32_t box[2] = {TC_BK, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)base, dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    set_error("cuTensorMapEncodeTiled failed (%d) for %lld x %lld, ld %lld", (int)r, (long long)rows,
+              (long long)cols, (long long)ld);
+    return ZG_ECUDA;
+  }
+  return ZG_OK;
+}
+
+template <int BN, int STAGES>
+static int launch_tc(const TcGemm& g, cudaStream_t s) {
+  using C = TcCfg<BN, STAGES>;
+  static bool configured[64] = {};
+  int dev = 0;
+  ZG_CHECK_CUDA(cudaGetDevice(&dev));
+  if (dev < 64 && !configured[dev]) {
+    ZG_CHECK_CUDA(cudaFuncSetAttribute(k_gemm_tf32x3<BN, STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
+    configured[dev] = true;
+  }
+  dim3 grid((g.N + BN - 1) / BN, (g.M + TC_BM - 1) / TC_BM);
+  k_gemm_tf32x3<BN, STAGES><<<grid, 192, C::SMEM, s>>>(g.Ah, g.Al, g.Bh, g.Bl, g.D, g.M, g.N, g.K, g.ldd, g.err);
+  ZG_CHECK_LAUNCH();
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  return ZG_OK;
+}
+
+int tc_gemm_prepare(TcGemm& g, const float* Ah, const float* Al, const float* Bh, const float* Bl, int64_t lda,
+                    int64_t ldb, float* D, int64_t ldd, int M, int N, int K, int* err) {
+  ZG_REQUIRE(M > 0 && N > 0 && K > 0, "empty tensor-core GEMM");
+  ZG_REQUIRE(N % 32 == 0, "tensor-core GEMM needs N a multiple of 32 (got %d)", N);
+  g.BN = 128;
+  ZG_TRY(make_tmap_f32(&g.Ah, Ah, M, K, lda, TC_BM));
+  ZG_TRY(make_tmap_f32(&g.Al, Al, M, K, lda, TC_BM));
+  ZG_TRY(make_tmap_f32(&g.Bh, Bh, N, K, ldb, g.BN));
+  ZG_TRY(make_tmap_f32(&g.Bl, Bl, N, K, ldb, g.BN));
+  g.D = D; g.ldd = ldd; g.M = M; g.N = N; g.K = K; g.err = err;
+  return ZG_OK;
+}
+
+int tc_gemm_launch(const TcGemm& g, cudaStream_t s) { return launch_tc<128, 3>(g, s); }
+
+// hi = rna_tf32(x), lo = rna_tf32(x - hi)
+__global__ void k_split_tf32(const float* __restrict__ x, float* __restrict__ hi, float* __restrict__ lo, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float v = x[i];
+    uint32_t h, l;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
+    const float r = v - __uint_as_float(h);
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l) : "f"(r));
+    hi[i] = __uint_as_float(h);
+    lo[i] = __uint_as_float(l);
+  }
+}
+
+int launch_split_tf32(const float* x, float* hi, float* lo, int64_t n, cudaStream_t s) {
+  if (n <= 0) return ZG_OK;
+  k_split_tf32<<<grid_for(n, 256, 152 * 8), 256, 0, s>>>(x, hi, lo, n);
+  ZG_CHECK_LAUNCH();
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  return ZG_OK;
+}
+
+}  // namespace zg
+
+using namespace zg;
+
+extern "C" int zg_split_tf32(const float* x, float* hi, float* lo, int64_t n, void* stream) {
+  ZG_REQUIRE(n >= 0 && (n == 0 || (x && hi && lo)), "bad arguments");
+  return launch_split_tf32(x, hi, lo, n, (cudaStream_t)stream);
+}
+
+extern "C" int zg_gemm_tf32x3(const float* Ah, const float* Al, const float* Bh, const float* Bl, float* D, int M,
+                              int N, int K, void* stream) {
+  ZG_REQUIRE(Ah && Al && Bh && Bl && D, "null argument");
+  ZG_REQUIRE(K % 4 == 0, "K must be a multiple of 4 (16-byte rows for TMA)");
+  cudaStream_t s = (cudaStream_t)stream;
+  int* err = nullptr;
+  ZG_CHECK_CUDA(cudaMallocAsync((void**)&err, sizeof(int), s));
+  ZG_CHECK_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
+  TcGemm g;
+  int st = tc_gemm_prepare(g, Ah, Al, Bh, Bl, K, K, D, N, M, N, K, err);
+  if (st == ZG_OK) st = tc_gemm_launch(g, s);
+  int herr = 0;
+  cudaError_t e = cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s);
+  cudaFreeAsync(err, s);
+  if (st != ZG_OK) return st;
+  if (e != cudaSuccess) { set_error("%s", cudaGetErrorString(e)); return ZG_ECUDA; }
+  ZG_CHECK_CUDA(cudaStreamSynchronize(s));
+  if (herr != 0) {
+    set_error("tensor-core GEMM wait timed out (code %d)", herr);
+    return ZG_ETIMEOUT;
+  }
+  return ZG_OK;
+}
