@@ -181,12 +181,35 @@ def run_ours(args):
     reg = dict(zip(_lib.PROF_REGIONS, zip(pms.tolist(), pcnt.tolist())))
     gemm_f, omega_f = rhs_flops(L)
     g_ms, g_n = reg["gemm"]
-    achieved = gemm_f / (g_ms / g_n / 1e3) / 1e12 if g_n else None
-    fp64_peak = peaks[0] / 1e3
+    if args.precision == "f64":
+        fp64_peak = peaks[0] / 1e3
+        achieved = gemm_f / (g_ms / g_n / 1e3) / 1e12 if g_n else None
+        roof = {"bound": "fp64", "kernel": "k_zgemm (batched FP64 complex GEMMs of one RHS)",
+                "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                "frac": (achieved / fp64_peak) if achieved else None, "traffic": None,
+                "peak_source": "live DFMA probe zg_measure_peaks (FP64 is not in MEASURED_PEAKS.json)",
+                "algorithmic_flops_per_launch": gemm_f}
+    else:
+        # psi H(t)^T on tcgen05: real-embedded complex GEMM M x 2np x 2np, three TF32 products
+        np_ = (L.n + 15) // 16 * 16
+        tc_flops = 3 * 2 * L.N * (2 * np_) * (2 * np_)
+        alg_flops = 8 * L.N * L.n * L.n
+        t_launch = g_ms / g_n / 1e3 if g_n else None
+        tf32 = measure_tf32_peak()
+        achieved = tc_flops / t_launch / 1e12 if t_launch else None
+        roof = {"bound": "tensor", "kernel": "k_gemm_tf32x3<128,3> (psi H(t)^T, tcgen05 kind::tf32, 3xTF32)",
+                "achieved": achieved, "peak": tf32, "unit": "TFLOP/s",
+                "frac": (achieved / tf32) if achieved and tf32 else None, "traffic": None,
+                "peak_source": "live cuBLAS TF32 GEMM 8192^3 (torch.matmul, allow_tf32); TF32 is not in "
+                               "MEASURED_PEAKS.json (bf16 there: %s TFLOP/s)" % _peaks_file().get("bf16_tflops"),
+                "tensor_flops_per_launch": tc_flops, "algorithmic_flops_per_launch": alg_flops,
+                "algorithmic_tflops": alg_flops / t_launch / 1e12 if t_launch else None,
+                "ms_per_launch": t_launch * 1e3 if t_launch else None}
+    roof["regions_ms_per_call"] = {k: (v[0] / v[1] if v[1] else None) for k, v in reg.items()}
     out = {
         "metric": METRIC, "value": value, "unit": "fs/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "c128" if args.precision == "f64" else "mixed", "data": "synthetic",
+        "dtype": "c128" if args.precision == "f64" else "c64 tf32x3 compute, c128 state", "data": "synthetic",
         "config": {"workload": "%s: %s" % (args.config, WORKLOAD_DESC.get(args.config, "")),
                    "precision": args.precision, "layout": L.summary(),
                    "l2": "inputs larger than L2: %d state slots x %.0f MB" % (tr.stages + 1, L.size * 16 / 1e6),
@@ -194,23 +217,78 @@ def run_ours(args):
         "rhs_evals_per_s": tr.stages * args.steps * ws / (ms / 1e3),
         "simulated_fs": adv_total,
         "t_h_after": list(state),
-        "roofline": {"bound": "fp64", "kernel": "k_zgemm (batched FP64 complex GEMMs of one RHS)",
-                     "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-                     "frac": (achieved / fp64_peak) if achieved else None, "traffic": None,
-                     "peak_source": "live DFMA probe zg_measure_peaks (FP64 is not in MEASURED_PEAKS.json)",
-                     "algorithmic_flops_per_launch": gemm_f,
-                     "regions_ms_per_call": {k: (v[0] / v[1] if v[1] else None) for k, v in reg.items()}},
+        "roofline": roof,
         "e2e": e2e,
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
         "peaks_live_gflops": {"fp64": peaks[0], "fp32": peaks[1]},
     }
+    tr.close()
+    if args.precision == "mixed" and not args.no_f64_ref:
+        out["f64_path"] = f64_reference_timing(w, dev, state, value, ms / args.steps)
     if rank == 0:
         out["cpu_baseline"] = cpu_baseline(args, w, adv_total / (args.steps * ws))
         print(json.dumps(out))
-    tr.close()
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def _peaks_file():
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def measure_tf32_peak():
+    """cuBLAS TF32 throughput (TFLOP/s) of an 8192^3 GEMM, best of 5."""
+    import torch
+    old = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = True
+    try:
+        a = torch.randn(8192, 8192, device="cuda")
+        b = torch.randn(8192, 8192, device="cuda")
+        for _ in range(2):
+            torch.matmul(a, b)
+        best = 0.0
+        for _ in range(5):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            torch.matmul(a, b)
+            e1.record()
+            torch.cuda.synchronize()
+            best = max(best, 2 * 8192 ** 3 / (e0.elapsed_time(e1) / 1e3) / 1e12)
+        del a, b
+        return best
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = old
+
+
+def f64_reference_timing(w, dev, state, mixed_value, mixed_ms):
+    """The plain FP64 device path on the same workload and controller state:
+    one warm-up and two timed attempts (the same step size), for the
+    mixed/FP64 ratio of the target specification."""
+    import torch
+    from zandpack_gb300 import _lib
+    from zandpack_gb300.engine import Propagator
+    pr = Propagator(w.arrays, w.hbar, w.bias_fn(), hubbard_U=w.hubbard_U, precision="f64", device=dev)
+    pr.set_state(w.arrays["DM_Ortho"])
+    t, h = state
+    stream = torch.cuda.ExternalStream(_lib.lib().zg_traj_stream(pr.traj._h), device=dev)
+    pr.attempt(t, h)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(2):
+        pr.attempt(t, h)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / 2
+    pr.traj.close()
+    return {"ms_per_step": ms, "value_same_h": mixed_value * mixed_ms / ms, "unit": "fs/s",
+            "mixed_over_f64": ms / mixed_ms,
+            "note": "FP64 attempt time at the mixed run's step size; value_same_h = mixed value x time ratio"}
 
 
 def run_e2e(pr, w, args, state, stream):
@@ -346,7 +424,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="c3")
-    ap.add_argument("--precision", default="f64", choices=["f64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["f64", "mixed"])
+    ap.add_argument("--no-f64-ref", action="store_true", help="skip timing the FP64 path beside the mixed one")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

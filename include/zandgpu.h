@@ -125,7 +125,8 @@ int zg_get_sigma(zg_traj* t, int slot, double* host);
  * bracket each region; zg_profile_read returns accumulated milliseconds and
  * counts per region (indices ZG_PROF_*).  zg_profile(t, 1) also resets them. */
 enum { ZG_PROF_GEMM = 0, ZG_PROF_OMEGA = 1, ZG_PROF_FINAL = 2, ZG_PROF_COMBINE = 3, ZG_PROF_ERROR = 4,
-       ZG_PROF_UPDATE = 5, ZG_PROF_RHS = 6, ZG_PROF_PREP = 7, ZG_PROF_REGIONS = 8 };
+       ZG_PROF_UPDATE = 5, ZG_PROF_RHS = 6, ZG_PROF_PREP = 7, ZG_PROF_SMALL = 8, ZG_PROF_GEMM2 = 9,
+       ZG_PROF_REGIONS = 10 };
 int zg_profile(zg_traj* t, int enable);
 int zg_profile_read(zg_traj* t, double* ms, long long* count);
 /* Live FP64 and FP32 FMA throughput of `device` in GFLOP/s (out[0], out[1]). */

@@ -16,7 +16,7 @@ ZG_PREC_F64, ZG_PREC_MIXED = 0, 1
 ZG_DH_NONE, ZG_DH_MATRIX, ZG_DH_HUBBARD = 0, 1, 2
 ZG_MAX_LEADS = 16
 ZG_MAX_STAGES = 13
-PROF_REGIONS = ["gemm", "omega", "final", "combine", "error", "update", "rhs", "prep"]
+PROF_REGIONS = ["gemm", "omega", "final", "combine", "error", "update", "rhs", "prep", "small", "gemm2"]
 
 _NAMES = {ZG_EINVAL: "EINVAL", ZG_ENOMEM: "ENOMEM", ZG_ECUDA: "ECUDA", ZG_ETIMEOUT: "ETIMEOUT",
           ZG_ENONFINITE: "ENONFINITE"}

@@ -51,15 +51,30 @@ __host__ __device__ __forceinline__ void cfma(double2& acc, double2 a, double2 b
   acc.y = fma(a.x, b.y, acc.y);
   acc.y = fma(a.y, b.x, acc.y);
 }
-__host__ __device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
+__host__ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
-__host__ __device__ __forceinline__ void cfmaf(float2& acc, float2 a, float2 b) {
+__host__ __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__host__ __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__host__ __device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+__host__ __device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+__host__ __device__ __forceinline__ void cfma(float2& acc, float2 a, float2 b) {
   acc.x = fmaf(a.x, b.x, acc.x);
   acc.x = fmaf(-a.y, b.y, acc.x);
   acc.y = fmaf(a.x, b.y, acc.y);
   acc.y = fmaf(a.y, b.x, acc.y);
 }
+
+// complex type of a real type
+template <typename T> struct cx;
+template <> struct cx<double> {
+  using t = double2;
+  __host__ __device__ static double2 make(double a, double b) { return make_double2(a, b); }
+};
+template <> struct cx<float> {
+  using t = float2;
+  __host__ __device__ static float2 make(float a, float b) { return make_float2(a, b); }
+};
 
 // ------------------------------------------------------- launch helpers
 inline int grid_for(int64_t n, int threads, int max_blocks) {

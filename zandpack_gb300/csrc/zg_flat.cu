@@ -1,0 +1,300 @@
+// Streaming kernels over the flat Runge-Kutta state: stage combination,
+// embedded error norm and final update, in the FP64 and the mixed-precision
+// forms, plus type conversions and the FMA peak probes.
+//
+// FP64 form: state slots are complex128; every operation is IEEE double.
+// Mixed form: y is complex128, a complex64 shadow y32 = fl32(y) feeds the
+// stage inputs, stage derivatives k are complex64; sums over k run in FP32,
+// the error norm accumulates its squares in FP64 and the update adds the
+// FP32 increment to y in FP64.  On GB300 the FP64 pipe runs ~70x slower
+// than FP32, so the mixed form keeps FP64 arithmetic to the update alone.
+#include "zg_kernels.cuh"
+
+namespace zg {
+
+std::atomic<long long> g_launches{0};
+
+#define GRID_STRIDE(e, count) \
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < (count); e += (int64_t)gridDim.x * blockDim.x)
+
+// =================================================================== FP64
+__global__ void __launch_bounds__(256) k_combine(const double2* __restrict__ Y, int64_t stride, CombineCoefs cf,
+                                                 double2* __restrict__ out, int64_t count) {
+  GRID_STRIDE(e, count) {
+    double2 acc = make_double2(0.0, 0.0);
+    for (int t = 0; t < cf.n; ++t) {
+      double2 v = Y[cf.idx[t] * stride + e];
+      acc.x = fma(cf.c[t], v.x, acc.x);
+      acc.y = fma(cf.c[t], v.y, acc.y);
+    }
+    out[e] = acc;
+  }
+}
+
+int launch_combine_c128(const double2* Y, int64_t stride, const CombineCoefs& cf, double2* out, int64_t count,
+                        cudaStream_t s) {
+  if (count <= 0) return ZG_OK;
+  k_combine<<<grid_for(count, 256, 152 * 16), 256, 0, s>>>(Y, stride, cf, out, count);
+  ZG_CHECK_LAUNCH();
+  count_launch();
+  return ZG_OK;
+}
+
+__global__ void __launch_bounds__(256) k_step_fourth(double2* Y, int64_t stride, int last, CombineCoefs cf,
+                                                     int64_t count) {
+  GRID_STRIDE(e, count) {
+    double2 acc = make_double2(0.0, 0.0);
+    for (int t = 0; t < cf.n; ++t) {
+      double2 v = Y[cf.idx[t] * stride + e];
+      acc.x = fma(cf.c[t], v.x, acc.x);
+      acc.y = fma(cf.c[t], v.y, acc.y);
+    }
+    Y[last * stride + e] = acc;  // every read of element e happened above
+  }
+}
+
+int launch_step_fourth_c128(double2* Y, int64_t stride, int last, const CombineCoefs& cf, int64_t count,
+                            cudaStream_t s) {
+  if (count <= 0) return ZG_OK;
+  k_step_fourth<<<grid_for(count, 256, 152 * 16), 256, 0, s>>>(Y, stride, last, cf, count);
+  ZG_CHECK_LAUNCH();
+  count_launch();
+  return ZG_OK;
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// block sum of 256 threads; result valid in thread 0
+__device__ __forceinline__ double block_sum256(double v) {
+  __shared__ double red[8];
+  v = warp_sum(v);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (threadIdx.x < 32) {
+    r = threadIdx.x < 8 ? red[threadIdx.x] : 0.0;
+    r = warp_sum(r);
+  }
+  __syncthreads();
+  return r;
+}
+
+__global__ void __launch_bounds__(256) k_terr2(const double2* __restrict__ Y, int64_t stride, CombineCoefs cf,
+                                               int64_t begin, int64_t end, double* __restrict__ partial) {
+  double s = 0.0;
+  for (int64_t e = begin + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < end;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    double2 acc = make_double2(0.0, 0.0);
+    for (int t = 0; t < cf.n; ++t) {
+      double2 v = Y[cf.idx[t] * stride + e];
+      acc.x = fma(cf.c[t], v.x, acc.x);
+      acc.y = fma(cf.c[t], v.y, acc.y);
+    }
+    s = fma(acc.x, acc.x, s);
+    s = fma(acc.y, acc.y, s);
+  }
+  s = block_sum256(s);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+
+int terr2_nblocks(int64_t count) { return grid_for(count, 256, 152 * 4); }
+
+int launch_terr2_partials_c128(const double2* Y, int64_t stride, const CombineCoefs& cf, int64_t begin, int64_t end,
+                               double* partial, int nblocks, cudaStream_t s) {
+  k_terr2<<<nblocks, 256, 0, s>>>(Y, stride, cf, begin, end, partial);
+  ZG_CHECK_LAUNCH();
+  count_launch();
+  return ZG_OK;
+}
+
+__global__ void __launch_bounds__(256) k_reduce_partials(const double* __restrict__ partial, int nblocks,
+                                                         double* __restrict__ out) {
+  const double* p = partial + (int64_t)blockIdx.x * nblocks;
+  double s = 0.0;
+  for (int i = threadIdx.x; i < nblocks; i += blockDim.x) s += p[i];
+  s = block_sum256(s);
+  if (threadIdx.x == 0) out[blockIdx.x] = s;
+}
+
+int launch_reduce_partials(const double* partial, int nblocks, int nseg, double* out, cudaStream_t s) {
+  k_reduce_partials<<<nseg, 256, 0, s>>>(partial, nblocks, out);
+  ZG_CHECK_LAUNCH();
+  count_launch();
+  return ZG_OK;
+}
+
+// ================================================================== mixed
+__device__ __forceinline__ void split_tf32(float v, float& hi, float& lo) {
+  uint32_t h, l;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
+  const float r = v - __uint_as_float(h);
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l) : "f"(r));
+  hi = __uint_as_float(h);
+  lo = __uint_as_float(l);
+}
+
+__global__ void __launch_bounds__(256) k_stage_input_mixed(const float2* __restrict__ y32, const float2* __restrict__ K,
+                                                           int64_t stride, CombineCoefs cf, MixedLayout ml,
+                                                           float2* __restrict__ stage) {
+  GRID_STRIDE(e, ml.S) {
+    float2 v = y32[e];
+    for (int t = 0; t < cf.n; ++t) {
+      const float c = (float)cf.c[t];
+      const float2 k = K[cf.idx[t] * stride + e];
+      v.x = fmaf(c, k.x, v.x);
+      v.y = fmaf(c, k.y, v.y);
+    }
+    if (e < ml.off_psi) {
+      stage[e] = v;
+    } else if (e < ml.off_omA) {
+      const int64_t r = e - ml.off_psi;
+      const int64_t m = r / ml.n, i = r % ml.n;
+      float2 hi, lo;
+      split_tf32(v.x, hi.x, lo.x);
+      split_tf32(v.y, hi.y, lo.y);
+      stage[ml.st_psih + m * ml.np + i] = hi;
+      stage[ml.st_psil + m * ml.np + i] = lo;
+    } else {
+      stage[ml.st_om + (e - ml.off_omA)] = v;
+    }
+  }
+}
+
+int launch_stage_input_mixed(const float2* y32, const float2* K, int64_t stride, const CombineCoefs& cf,
+                             const MixedLayout& ml, float2* stage, cudaStream_t s) {
+  k_stage_input_mixed<<<grid_for(ml.S, 256, 152 * 16), 256, 0, s>>>(y32, K, stride, cf, ml, stage);
+  ZG_CHECK_LAUNCH();
+  count_launch();
+  return ZG_OK;
+}
+
+__global__ void __launch_bounds__(256) k_terr2_mixed(const float2* __restrict__ K, int64_t stride, CombineCoefs cf,
+                                                     int64_t begin, int64_t end, double* __restrict__ partial) {
+  double s = 0.0;
+  for (int64_t e = begin + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < end;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    float2 acc = make_float2(0.f, 0.f);
+    for (int t = 0; t < cf.n; ++t) {
+      const float c = (float)cf.c[t];
+      const float2 v = K[cf.idx[t] * stride + e];
+      acc.x = fmaf(c, v.x, acc.x);
+      acc.y = fmaf(c, v.y, acc.y);
+    }
+    s += (double)fmaf(acc.x, acc.x, acc.y * acc.y);
+  }
+  s = block_sum256(s);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+
+int launch_terr2_partials_mixed(const float2* K, int64_t stride, const CombineCoefs& cf, int64_t begin, int64_t end,
+                                double* partial, int nblocks, cudaStream_t s) {
+  k_terr2_mixed<<<nblocks, 256, 0, s>>>(K, stride, cf, begin, end, partial);
+  ZG_CHECK_LAUNCH();
+  count_launch();
+  return ZG_OK;
+}
+
+__global__ void __launch_bounds__(256) k_update_mixed(double2* __restrict__ y64, float2* __restrict__ y32,
+                                                      const float2* __restrict__ K, int64_t stride, CombineCoefs cf,
+                                                      int64_t count) {
+  GRID_STRIDE(e, count) {
+    float2 d = make_float2(0.f, 0.f);
+    for (int t = 0; t < cf.n; ++t) {
+      const float c = (float)cf.c[t];
+      const float2 v = K[cf.idx[t] * stride + e];
+      d.x = fmaf(c, v.x, d.x);
+      d.y = fmaf(c, v.y, d.y);
+    }
+    double2 y = y64[e];
+    y.x += (double)d.x;
+    y.y += (double)d.y;
+    y64[e] = y;
+    y32[e] = make_float2((float)y.x, (float)y.y);
+  }
+}
+
+int launch_update_mixed(double2* y64, float2* y32, const float2* K, int64_t stride, const CombineCoefs& cf,
+                        int64_t count, cudaStream_t s) {
+  if (count <= 0) return ZG_OK;
+  k_update_mixed<<<grid_for(count, 256, 152 * 16), 256, 0, s>>>(y64, y32, K, stride, cf, count);
+  ZG_CHECK_LAUNCH();
+  count_launch();
+  return ZG_OK;
+}
+
+__global__ void k_f64_to_f32(const double2* __restrict__ a, float2* __restrict__ b, int64_t count) {
+  GRID_STRIDE(e, count) b[e] = make_float2((float)a[e].x, (float)a[e].y);
+}
+__global__ void k_f32_to_f64(const float2* __restrict__ a, double2* __restrict__ b, int64_t count) {
+  GRID_STRIDE(e, count) b[e] = make_double2((double)a[e].x, (double)a[e].y);
+}
+
+int launch_f64_to_f32(const double2* a, float2* b, int64_t count, cudaStream_t s) {
+  if (count <= 0) return ZG_OK;
+  k_f64_to_f32<<<grid_for(count, 256, 152 * 16), 256, 0, s>>>(a, b, count);
+  ZG_CHECK_LAUNCH();
+  count_launch();
+  return ZG_OK;
+}
+int launch_f32_to_f64(const float2* a, double2* b, int64_t count, cudaStream_t s) {
+  if (count <= 0) return ZG_OK;
+  k_f32_to_f64<<<grid_for(count, 256, 152 * 16), 256, 0, s>>>(a, b, count);
+  ZG_CHECK_LAUNCH();
+  count_launch();
+  return ZG_OK;
+}
+
+// ============================================================ peak probes
+// Independent FMA chains per thread; the result store is never taken but keeps
+// the chains live.
+template <typename T>
+__global__ void __launch_bounds__(256) k_fma_peak(T* out, T a, T b, int iters) {
+  T x0 = (T)threadIdx.x * (T)1e-9, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6,
+    x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+    x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+  }
+  T s = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+  if (s == (T)1.2345) out[0] = s;
+}
+
+int measure_peaks(double* out) {
+  int dev = 0, sms = 0;
+  ZG_CHECK_CUDA(cudaGetDevice(&dev));
+  ZG_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  double* d = nullptr;
+  ZG_CHECK_CUDA(cudaMalloc(&d, 16));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const int blocks = sms * 8, thr = 256;
+  for (int which = 0; which < 2; ++which) {
+    const int iters = which == 0 ? 2048 : 65536;
+    double best = 0.0;
+    for (int rep = 0; rep < 3; ++rep) {
+      cudaEventRecord(e0);
+      if (which == 0) k_fma_peak<double><<<blocks, thr>>>(d, 0.999, 1e-3, iters);
+      else k_fma_peak<float><<<blocks, thr>>>((float*)d, 0.999f, 1e-3f, iters);
+      cudaEventRecord(e1);
+      cudaError_t err = cudaEventSynchronize(e1);
+      if (err != cudaSuccess) { cudaFree(d); set_error("peak probe: %s", cudaGetErrorString(err)); return ZG_ECUDA; }
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      double gf = 2.0 * 8.0 * iters * (double)blocks * thr / (ms * 1e6);
+      best = gf > best ? gf : best;
+    }
+    out[which] = best;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(d);
+  ZG_CHECK_LAUNCH();
+  return ZG_OK;
+}
+
+}  // namespace zg

@@ -11,6 +11,7 @@ namespace zg {
 
 // kernels launched by this library since load (all threads)
 extern std::atomic<long long> g_launches;
+inline void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 // ------------------------------------------------ tensor-core GEMM (3xTF32)
 // D (M x N, fp32, row stride ldd) = (Ah + Al)(Bh + Bl)^T without Al.Bl^T;
@@ -29,7 +30,7 @@ int tc_gemm_launch(const TcGemm& g, cudaStream_t s);
 // hi = rna_tf32(x), lo = rna_tf32(x - hi)
 int launch_split_tf32(const float* x, float* hi, float* lo, int64_t n, cudaStream_t s);
 
-// ------------------------------------------------------------ flat kernels
+// ------------------------------------------------------ flat kernels (FP64)
 // out[e] = sum_t c[t] * Y[idx[t]][e]   (Y slots `stride` complex apart)
 int launch_combine_c128(const double2* Y, int64_t stride, const CombineCoefs& cf, double2* out,
                         int64_t count, cudaStream_t s);
@@ -43,27 +44,60 @@ int launch_terr2_partials_c128(const double2* Y, int64_t stride, const CombineCo
 // out[j] = sum of partial[j*nblocks .. (j+1)*nblocks), j < nseg (fixed order)
 int launch_reduce_partials(const double* partial, int nblocks, int nseg, double* out, cudaStream_t s);
 
-// ------------------------------------------------------------ FP64 GEMM
-// C = alpha * opA(A) opB(B) + beta * C ; opA: 0 = A[m*lda+k], 1 = A[k*lda+m];
+// --------------------------------------------------- flat kernels (mixed)
+// Offsets of the mixed-precision stage buffer (complex64 units): sigma (n x n),
+// psi hi and lo parts (N x np each, zero beyond column n), Omega (OmA | OmB).
+struct MixedLayout {
+  int64_t n, N, np;
+  int64_t off_psi, off_omA, S;            // flat state offsets
+  int64_t st_psih, st_psil, st_om, st_S;  // stage buffer offsets / size
+};
+// stage = y32 + sum_t c[t] K[idx[t]] in FP32, psi written as TF32 hi/lo parts
+int launch_stage_input_mixed(const float2* y32, const float2* K, int64_t stride, const CombineCoefs& cf,
+                             const MixedLayout& ml, float2* stage, cudaStream_t s);
+// FP64 block sums of |sum_t c[t] K[idx[t]][e]|^2 (inner sum in FP32)
+int launch_terr2_partials_mixed(const float2* K, int64_t stride, const CombineCoefs& cf, int64_t begin, int64_t end,
+                                double* partial, int nblocks, cudaStream_t s);
+// y64 += sum_t c[t] K[idx[t]] (increment in FP32, addition in FP64); y32 = fl32(y64)
+int launch_update_mixed(double2* y64, float2* y32, const float2* K, int64_t stride, const CombineCoefs& cf,
+                        int64_t count, cudaStream_t s);
+int launch_f64_to_f32(const double2* a, float2* b, int64_t count, cudaStream_t s);
+int launch_f32_to_f64(const float2* a, double2* b, int64_t count, cudaStream_t s);
+
+// ------------------------------------------------ SIMT complex GEMM batch
+// C = alpha * opA(A [+ A2]) opB(B) + beta * C ; opA: 0 = A[m*lda+k], 1 = A[k*lda+m];
 // opB: 0 = B[k*ldb+n], 1 = B[n*ldb+k], 2 = conj(B[n*ldb+k]).  K = 0 writes beta*C.
+template <typename T>
 struct GemmProb {
-  const double2* A;
-  const double2* B;
-  double2* C;
+  using C = typename cx<T>::t;
+  const C* A;
+  const C* A2;  // optional second part of A (hi/lo split operands), same layout
+  const C* B;
+  C* Cm;
   int M, N, K;
   int opA, opB;
-  int tile_begin, tiles_n;
+  int tile_begin, tiles_n, tiles_mn;
+  int ksplit, kchunk;  // split-K: ksplit partial products of kchunk, summed in a fixed order
+  int64_t ws_off;      // offset of this problem's partials in the workspace
   int64_t lda, ldb, ldc;
-  double2 alpha, beta;
+  C alpha, beta;
 };
 #define ZG_MAX_GEMM 32
+template <typename T>
 struct GemmBatch {
   int nprob;
   int total_tiles;
-  GemmProb p[ZG_MAX_GEMM];
+  typename cx<T>::t* ws;  // split-K workspace
+  GemmProb<T> p[ZG_MAX_GEMM];
 };
-// fills tile_begin/tiles_n/total_tiles and launches
-int launch_zgemm_batch(GemmBatch& b, cudaStream_t s);
+// Chooses split-K factors (enough CTAs for the device) and workspace offsets;
+// returns the workspace size in complex elements.
+template <typename T>
+int64_t plan_zgemm_batch(GemmBatch<T>& b);
+// Launches the batch (after planning with the same shapes); problems with
+// ksplit > 1 need beta == 0 and a workspace of plan_zgemm_batch() elements.
+template <typename T>
+int launch_zgemm_batch(GemmBatch<T>& b, int64_t ws_capacity, cudaStream_t s);
 
 // ------------------------------------------------------------ RHS helpers
 struct StageParams {
@@ -71,13 +105,14 @@ struct StageParams {
   double delta[ZG_MAX_LEADS];
 };
 
+template <typename T>
 struct RhsDev {  // device pointers and sizes of one trajectory
+  using C = typename cx<T>::t;
   int n, L, N, Ns, Nf, nc;
-  int64_t off_psi, off_omA, off_omB, S;
   const int* mode_lead;
   const int* lead_cols;
   const int* colmap;
-  const double2 *H0, *Xp, *Xm, *GLP, *dGP, *XI, *U, *V;
+  const C *Xp, *Xm, *GLP, *dGP, *XI, *U, *V;
 };
 
 struct OmTile {
@@ -88,18 +123,41 @@ struct OmTile {
   int term1, term2;     // which source products apply
 };
 
-int launch_build_ht(const RhsDev& d, const double2* sig, const double2* dH, int dH_mode, double U,
-                    double2* Ht, cudaStream_t s);
-int launch_gathers(const RhsDev& d, const double2* sig, const double2* psi, double2* sigC, double2* G,
+// sigC[a][i][k] = sig[i][C_a[k]], G[m][a][k] = (psi + psi_lo)[m][C_a[k]]
+template <typename T>
+int launch_gathers(const RhsDev<T>& d, const typename cx<T>::t* sig, const typename cx<T>::t* psi,
+                   const typename cx<T>::t* psi_lo, int64_t ldpsi, typename cx<T>::t* sigC, typename cx<T>::t* G,
                    cudaStream_t s);
-int launch_sigma_finalize(const RhsDev& d, const StageParams& p, const double2* T, const double2* Pc,
-                          double2* ksig, double* currents, cudaStream_t s);
-int launch_psi_finalize(const RhsDev& d, const StageParams& p, const double2* psi, const double2* R2,
-                        const double2* ZA, const double2* ZB, double2* kpsi, cudaStream_t s);
+template <typename T>
+int launch_sigma_finalize(const RhsDev<T>& d, const StageParams& p, const typename cx<T>::t* Tm, int64_t ldT,
+                          const typename cx<T>::t* Pc, typename cx<T>::t* ksig, cudaStream_t s);
+template <typename T>
+int launch_currents(const RhsDev<T>& d, const StageParams& p, const typename cx<T>::t* Pc, double* J, cudaStream_t s);
+template <typename T>
+int launch_psi_finalize(const RhsDev<T>& d, const StageParams& p, const typename cx<T>::t* psi,
+                        const typename cx<T>::t* psi_lo, int64_t ldpsi, const typename cx<T>::t* R1, int64_t ldR1,
+                        const typename cx<T>::t* R2, const typename cx<T>::t* ZA, const typename cx<T>::t* ZB,
+                        typename cx<T>::t* kpsi, cudaStream_t s);
+template <typename T>
+int launch_omega(const RhsDev<T>& d, const StageParams& p, const OmTile* tiles, int ntiles, const typename cx<T>::t* G,
+                 const typename cx<T>::t* omA_in, const typename cx<T>::t* omB_in, typename cx<T>::t* omA_out,
+                 typename cx<T>::t* omB_out, cudaStream_t s);
+
+// H(t) = H0 + dH (FP64 path)
+int launch_build_ht(int n, const double2* H0, const double2* sig, const double2* dH, int dH_mode, double U,
+                    double2* Ht, cudaStream_t s);
+// Mixed path operands of the two tensor-core GEMMs, TF32 hi/lo parts:
+//   Ht (n x np complex = n x 2np real)             A of  T = H(t) sigma
+//   BH (2np x 2np real embedding of H(t)^T form)    B of  R1 = psi H(t)^T
+//   BS (2np x 2np real embedding of sigma)          B of  T
+int launch_build_operands_mixed(int n, int np, const double2* H0, const float2* sig32, const double2* dH, int dH_mode,
+                                double U, float* Hth, float* Htl, float* BHh, float* BHl, float* BSh, float* BSl,
+                                cudaStream_t s);
+// Lead currents in FP64 from the FP64 state: J_a = 2 Re sum_{m in a} sum_k psi[m][C_a[k]] IXI[m][k] / hbar^2
+int launch_currents64(int n, int L, int N, int nc, const int* mode_lead, const int* lead_cols, const double2* psi,
+                      const double2* IXI, double hbar, double* J, cudaStream_t s);
+
 // out[0] = FP64 FMA rate, out[1] = FP32 FMA rate, GFLOP/s (2 flops per FMA)
 int measure_peaks(double* out);
-
-int launch_omega(const RhsDev& d, const StageParams& p, const OmTile* tiles, int ntiles, const double2* G,
-                 const double2* yin, double2* kout, cudaStream_t s);
 
 }  // namespace zg

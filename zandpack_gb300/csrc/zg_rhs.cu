@@ -1,0 +1,585 @@
+// Right-hand-side kernels of the AME equations (Zandpack/mpi/zand:318-387
+// sigma, :745-778 psi, :782-809 Omega), templated on the real type: double
+// for the FP64 path, float for the mixed-precision path (whose two large
+// products run on the tensor cores, zg_tc.cu).
+#include "zg_kernels.cuh"
+
+namespace zg {
+
+#define GRID_STRIDE(e, count) \
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < (count); e += (int64_t)gridDim.x * blockDim.x)
+
+template <typename T>
+__device__ __forceinline__ typename cx<T>::t czero() {
+  return cx<T>::make((T)0, (T)0);
+}
+
+// =================================================================== GEMM
+// 64x64 output tile per 256-thread block, K staged 8 at a time in shared
+// memory; thread (tx, ty) owns rows ty+16i and columns tx+16j (i, j < 4).
+#define ZT 64
+#define ZK 8
+
+template <typename T>
+__device__ __forceinline__ typename cx<T>::t load_opA(const GemmProb<T>& P, int m, int k) {
+  using C = typename cx<T>::t;
+  if (m >= P.M || k >= P.K) return czero<T>();
+  const int64_t o = P.opA == 0 ? (int64_t)m * P.lda + k : (int64_t)k * P.lda + m;
+  C v = P.A[o];
+  if (P.A2) v = cadd(v, P.A2[o]);
+  return v;
+}
+template <typename T>
+__device__ __forceinline__ typename cx<T>::t load_opB(const GemmProb<T>& P, int k, int n) {
+  if (n >= P.N || k >= P.K) return czero<T>();
+  if (P.opB == 0) return P.B[(int64_t)k * P.ldb + n];
+  const typename cx<T>::t v = P.B[(int64_t)n * P.ldb + k];
+  return P.opB == 2 ? cconj(v) : v;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_zgemm(const __grid_constant__ GemmBatch<T> batch) {
+  using C = typename cx<T>::t;
+  const int tile = blockIdx.x;
+  int pi = 0;
+  while (pi + 1 < batch.nprob && tile >= batch.p[pi + 1].tile_begin) ++pi;
+  const GemmProb<T>& P = batch.p[pi];
+  const int ltk = tile - P.tile_begin;
+  const int split = ltk / P.tiles_mn, lt = ltk % P.tiles_mn;
+  const int m0 = (lt / P.tiles_n) * ZT, n0 = (lt % P.tiles_n) * ZT;
+  const int kb0 = split * P.kchunk;
+  const int kb1 = min(P.K, kb0 + P.kchunk);
+  __shared__ C As[ZK][ZT];
+  __shared__ C Bs[ZK][ZT];
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  C acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = czero<T>();
+  for (int k0 = kb0; k0 < kb1; k0 += ZK) {
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+      const int idx = tid + 256 * r;
+      int m, k, n;
+      if (P.opA == 0) { m = idx >> 3; k = idx & 7; } else { m = idx & 63; k = idx >> 6; }
+      As[k][m] = k0 + k < kb1 ? load_opA(P, m0 + m, k0 + k) : czero<T>();
+      if (P.opB == 0) { n = idx & 63; k = idx >> 6; } else { n = idx >> 3; k = idx & 7; }
+      Bs[k][n] = k0 + k < kb1 ? load_opB(P, k0 + k, n0 + n) : czero<T>();
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < ZK; ++kk) {
+      C a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) cfma(acc[i][j], a[i], b[j]);
+    }
+    __syncthreads();
+  }
+  const bool use_beta = (P.beta.x != (T)0 || P.beta.y != (T)0);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int m = m0 + ty + 16 * i;
+    if (m >= P.M) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int n = n0 + tx + 16 * j;
+      if (n >= P.N) continue;
+      if (P.ksplit > 1) {  // partial product of this K chunk, reduced later in split order
+        batch.ws[P.ws_off + ((int64_t)split * P.M + m) * P.N + n] = acc[i][j];
+        continue;
+      }
+      C* c = P.Cm + (int64_t)m * P.ldc + n;
+      C v = cmul(P.alpha, acc[i][j]);
+      if (use_beta) v = cadd(v, cmul(P.beta, *c));
+      *c = v;
+    }
+  }
+}
+
+// C = alpha * sum over splits of the partials, splits added in order
+template <typename T>
+__global__ void k_zgemm_reduce(const __grid_constant__ GemmBatch<T> batch) {
+  using C = typename cx<T>::t;
+  for (int pi = 0; pi < batch.nprob; ++pi) {
+    const GemmProb<T>& P = batch.p[pi];
+    if (P.ksplit <= 1) continue;
+    const int64_t mn = (int64_t)P.M * P.N;
+    GRID_STRIDE(e, mn) {
+      C v = czero<T>();
+      for (int sp = 0; sp < P.ksplit; ++sp) v = cadd(v, batch.ws[P.ws_off + sp * mn + e]);
+      P.Cm[(e / P.N) * P.ldc + (e % P.N)] = cmul(P.alpha, v);
+    }
+  }
+}
+
+template <typename T>
+int64_t plan_zgemm_batch(GemmBatch<T>& b) {
+  // A problem with few output tiles and a long K would serialise on a handful
+  // of CTAs: split its K into chunks of >= 256 until it has ~2 CTAs per SM.
+  const int64_t target = 2 * 152;
+  int tiles = 0;
+  int64_t ws = 0;
+  for (int i = 0; i < b.nprob; ++i) {
+    GemmProb<T>& P = b.p[i];
+    const int tm = (P.M + ZT - 1) / ZT, tn = (P.N + ZT - 1) / ZT;
+    P.tiles_n = tn > 0 ? tn : 1;
+    P.tiles_mn = tm * tn > 0 ? tm * tn : 1;
+    P.ksplit = 1;
+    P.kchunk = P.K > 0 ? P.K : 1;
+    P.ws_off = 0;
+    const bool plain_beta = P.beta.x == (T)0 && P.beta.y == (T)0;
+    if (plain_beta && P.K >= 512 && tm * tn > 0 && tm * tn < 152) {
+      int want = (int)((target + tm * tn - 1) / (tm * tn));
+      int maxs = P.K / 256;  // at least 256 of K per split
+      int ks = want < maxs ? want : maxs;
+      if (ks > 1) {
+        int chunk = (P.K + ks - 1) / ks;
+        chunk = (chunk + ZK - 1) / ZK * ZK;
+        P.kchunk = chunk;
+        P.ksplit = (P.K + chunk - 1) / chunk;
+        P.ws_off = ws;
+        ws += (int64_t)P.ksplit * P.M * P.N;
+      }
+    }
+    P.tile_begin = tiles;
+    tiles += (tm * tn) * P.ksplit;
+  }
+  b.total_tiles = tiles;
+  return ws;
+}
+
+template <typename T>
+int launch_zgemm_batch(GemmBatch<T>& b, int64_t ws_capacity, cudaStream_t s) {
+  ZG_REQUIRE(b.nprob > 0 && b.nprob <= ZG_MAX_GEMM, "gemm batch size %d out of range", b.nprob);
+  for (int i = 0; i < b.nprob; ++i)
+    ZG_REQUIRE(b.p[i].M >= 0 && b.p[i].N >= 0 && b.p[i].K >= 0, "negative gemm extent");
+  const int64_t need = plan_zgemm_batch<T>(b);
+  ZG_REQUIRE(need <= ws_capacity && (need == 0 || b.ws), "split-K workspace too small (%lld > %lld)",
+             (long long)need, (long long)ws_capacity);
+  if (b.total_tiles == 0) return ZG_OK;
+  k_zgemm<T><<<b.total_tiles, 256, 0, s>>>(b);
+  ZG_CHECK_LAUNCH();
+  count_launch();
+  if (need > 0) {
+    k_zgemm_reduce<T><<<152 * 4, 256, 0, s>>>(b);
+    ZG_CHECK_LAUNCH();
+    count_launch();
+  }
+  return ZG_OK;
+}
+
+// ============================================================ RHS helpers
+template <typename T>
+__global__ void k_gathers(const RhsDev<T> d, const typename cx<T>::t* __restrict__ sig,
+                          const typename cx<T>::t* __restrict__ psi, const typename cx<T>::t* __restrict__ psi_lo,
+                          int64_t ldpsi, typename cx<T>::t* __restrict__ sigC, typename cx<T>::t* __restrict__ G) {
+  const int64_t ns = (int64_t)d.L * d.n * d.nc;
+  const int64_t ng = (int64_t)d.N * d.L * d.nc;
+  GRID_STRIDE(e, ns + ng) {
+    if (e < ns) {
+      const int k = (int)(e % d.nc);
+      const int64_t r = e / d.nc;
+      const int i = (int)(r % d.n), a = (int)(r / d.n);
+      sigC[e] = sig[(int64_t)i * d.n + d.lead_cols[a * d.nc + k]];
+    } else {
+      const int64_t g = e - ns;
+      const int k = (int)(g % d.nc);
+      const int64_t r = g / d.nc;
+      const int a = (int)(r % d.L);
+      const int64_t m = r / d.L;
+      const int64_t o = m * ldpsi + d.lead_cols[a * d.nc + k];
+      typename cx<T>::t v = psi[o];
+      if (psi_lo) v = cadd(v, psi_lo[o]);
+      G[g] = v;
+    }
+  }
+}
+
+template <typename T>
+int launch_gathers(const RhsDev<T>& d, const typename cx<T>::t* sig, const typename cx<T>::t* psi,
+                   const typename cx<T>::t* psi_lo, int64_t ldpsi, typename cx<T>::t* sigC, typename cx<T>::t* G,
+                   cudaStream_t s) {
+  int64_t tot = (int64_t)d.L * d.n * d.nc + (int64_t)d.N * d.L * d.nc;
+  k_gathers<T><<<grid_for(tot, 256, 152 * 8), 256, 0, s>>>(d, sig, psi, psi_lo, ldpsi, sigC, G);
+  ZG_CHECK_LAUNCH();
+  count_launch();
+  return ZG_OK;
+}
+
+// P_full[i][j] = sum over (class, lead a) of Pc[class][a][i][colmap[a][j]]
+template <typename T>
+__device__ __forceinline__ typename cx<T>::t p_full(const RhsDev<T>& d, const typename cx<T>::t* Pc, int i, int j) {
+  typename cx<T>::t v = czero<T>();
+  for (int a = 0; a < d.L; ++a) {
+    const int k = d.colmap[a * d.n + j];
+    if (k < 0) continue;
+#pragma unroll
+    for (int cls = 0; cls < 2; ++cls) v = cadd(v, Pc[((int64_t)(cls * d.L + a) * d.n + i) * d.nc + k]);
+  }
+  return v;
+}
+
+// k_sig = (h/hbar) (-i (T - T^H) + (P + P^H)/hbar), T = H(t) sigma  (Zandpack/mpi/zand:340-387)
+template <typename T>
+__global__ void k_sigma_finalize(const RhsDev<T> d, const StageParams p, const typename cx<T>::t* __restrict__ Tm,
+                                 int64_t ldT, const typename cx<T>::t* __restrict__ Pc,
+                                 typename cx<T>::t* __restrict__ ksig) {
+  const int64_t nn = (int64_t)d.n * d.n;
+  const T ih = (T)(1.0 / p.hbar);
+  const T sc = (T)(p.h / p.hbar);
+  GRID_STRIDE(e, nn) {
+    const int i = (int)(e / d.n), j = (int)(e % d.n);
+    const typename cx<T>::t tij = Tm[(int64_t)i * ldT + j], tji = Tm[(int64_t)j * ldT + i];
+    const typename cx<T>::t pij = p_full(d, Pc, i, j), pji = p_full(d, Pc, j, i);
+    // -i (tij - conj(tji)) = (tij.y + tji.y, -(tij.x - tji.x))
+    typename cx<T>::t v = cx<T>::make(tij.y + tji.y, -(tij.x - tji.x));
+    v.x += (pij.x + pji.x) * ih;
+    v.y += (pij.y - pji.y) * ih;
+    ksig[e] = cscale(v, sc);
+  }
+}
+
+template <typename T>
+int launch_sigma_finalize(const RhsDev<T>& d, const StageParams& p, const typename cx<T>::t* Tm, int64_t ldT,
+                          const typename cx<T>::t* Pc, typename cx<T>::t* ksig, cudaStream_t s) {
+  int64_t nn = (int64_t)d.n * d.n;
+  k_sigma_finalize<T><<<grid_for(nn, 256, 152 * 8), 256, 0, s>>>(d, p, Tm, ldT, Pc, ksig);
+  ZG_CHECK_LAUNCH();
+  count_launch();
+  return ZG_OK;
+}
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double block_sum256_d(double v) {
+  __shared__ double red[8];
+  v = warp_sum_d(v);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (threadIdx.x < 32) {
+    r = threadIdx.x < 8 ? red[threadIdx.x] : 0.0;
+    r = warp_sum_d(r);
+  }
+  __syncthreads();
+  return r;
+}
+
+// J_a = 2 Re Tr(P_a) / hbar^2 = Re Tr(PI_a)/hbar  (Zandpack/mpi/zand:368-378)
+template <typename T>
+__global__ void k_currents(const RhsDev<T> d, const StageParams p, const typename cx<T>::t* __restrict__ Pc,
+                           double* __restrict__ J) {
+  const int a = blockIdx.x;
+  double s = 0.0;
+  for (int k = threadIdx.x; k < d.nc; k += blockDim.x) {
+    const int i = d.lead_cols[a * d.nc + k];
+#pragma unroll
+    for (int cls = 0; cls < 2; ++cls) s += (double)Pc[((int64_t)(cls * d.L + a) * d.n + i) * d.nc + k].x;
+  }
+  s = block_sum256_d(s);
+  if (threadIdx.x == 0) J[a] = 2.0 * s / (p.hbar * p.hbar);
+}
+
+template <typename T>
+int launch_currents(const RhsDev<T>& d, const StageParams& p, const typename cx<T>::t* Pc, double* J, cudaStream_t s) {
+  k_currents<T><<<d.L, 256, 0, s>>>(d, p, Pc, J);
+  ZG_CHECK_LAUNCH();
+  count_launch();
+  return ZG_OK;
+}
+
+// J_a from the FP64 state: 2 Re sum_{m in lead a} sum_k psi[m][C_a[k]] IXI[m][k] / hbar^2
+__global__ void k_currents64(int n, int N, int nc, const int* __restrict__ mode_lead, const int* __restrict__ lead_cols,
+                             const double2* __restrict__ psi, const double2* __restrict__ IXI, double hbar,
+                             double* __restrict__ J) {
+  const int a = blockIdx.x;
+  double s = 0.0;
+  for (int64_t e = threadIdx.x; e < (int64_t)N * nc; e += blockDim.x) {
+    const int64_t m = e / nc;
+    const int k = (int)(e % nc);
+    if (mode_lead[m] != a) continue;
+    const double2 ps = psi[m * n + lead_cols[a * nc + k]];
+    const double2 ix = IXI[e];
+    s += ps.x * ix.x - ps.y * ix.y;
+  }
+  s = block_sum256_d(s);
+  if (threadIdx.x == 0) J[a] = 2.0 * s / (hbar * hbar);
+}
+
+int launch_currents64(int n, int L, int N, int nc, const int* mode_lead, const int* lead_cols, const double2* psi,
+                      const double2* IXI, double hbar, double* J, cudaStream_t s) {
+  k_currents64<<<L, 256, 0, s>>>(n, N, nc, mode_lead, lead_cols, psi, IXI, hbar, J);
+  ZG_CHECK_LAUNCH();
+  count_launch();
+  return ZG_OK;
+}
+
+// k_psi = -i h [ R1/hbar - (X+ + Delta)/hbar psi + dGP R2 + Z(Omega xi) + GL_P xi ]
+// with R1 = psi H^T  (Zandpack/mpi/zand:745-778)
+template <typename T>
+__global__ void k_psi_finalize(const RhsDev<T> d, const StageParams p, const typename cx<T>::t* __restrict__ psi,
+                               const typename cx<T>::t* __restrict__ psi_lo, int64_t ldpsi,
+                               const typename cx<T>::t* R1, int64_t ldR1, const typename cx<T>::t* __restrict__ R2,
+                               const typename cx<T>::t* __restrict__ ZA, const typename cx<T>::t* __restrict__ ZB,
+                               typename cx<T>::t* kpsi) {
+  using C = typename cx<T>::t;
+  const int64_t tot = (int64_t)d.N * d.n;
+  const T ih = (T)(1.0 / p.hbar);
+  const T h = (T)p.h;
+  GRID_STRIDE(e, tot) {
+    const int64_t m = e / d.n;
+    const int i = (int)(e % d.n);
+    const int a = d.mode_lead[m];
+    C xp = d.Xp[m];
+    xp.x += (T)p.delta[a];
+    C ps = psi[m * ldpsi + i];
+    if (psi_lo) ps = cadd(ps, psi_lo[m * ldpsi + i]);
+    C v = cscale(R1[m * ldR1 + i], ih);
+    v = csub(v, cscale(cmul(xp, ps), ih));
+    if (m < d.Ns) v = cadd(v, cmul(d.dGP[m], R2[m * d.n + i]));
+    for (int b = 0; b < d.L; ++b) {
+      const int k = d.colmap[b * d.n + i];
+      if (k < 0) continue;
+      v = cadd(v, ZA[((int64_t)b * d.N + m) * d.nc + k]);
+      if (m < d.Ns) v = cadd(v, ZB[((int64_t)b * d.Ns + m) * d.nc + k]);
+    }
+    const int ka = d.colmap[a * d.n + i];
+    if (ka >= 0) v = cadd(v, cmul(d.GLP[m], d.XI[m * d.nc + ka]));
+    // (-i h) v = (h v.y, -h v.x)
+    kpsi[e] = cx<T>::make(h * v.y, -h * v.x);
+  }
+}
+
+template <typename T>
+int launch_psi_finalize(const RhsDev<T>& d, const StageParams& p, const typename cx<T>::t* psi,
+                        const typename cx<T>::t* psi_lo, int64_t ldpsi, const typename cx<T>::t* R1, int64_t ldR1,
+                        const typename cx<T>::t* R2, const typename cx<T>::t* ZA, const typename cx<T>::t* ZB,
+                        typename cx<T>::t* kpsi, cudaStream_t s) {
+  int64_t tot = (int64_t)d.N * d.n;
+  k_psi_finalize<T><<<grid_for(tot, 256, 152 * 16), 256, 0, s>>>(d, p, psi, psi_lo, ldpsi, R1, ldR1, R2, ZA, ZB, kpsi);
+  ZG_CHECK_LAUNCH();
+  count_launch();
+  return ZG_OK;
+}
+
+// Omega stage derivative on one 64x64 tile whose rows belong to lead a and
+// columns to lead b (Zandpack/mpi/zand:782-809):
+//   k[m,l] = h sum_k G[m][b][k] U[l][k]              (term1, U = dGM * IXI)
+//          + h sum_k V[m][k] conj(G[l][a][k])        (term2, V = dGP * XIT2)
+//          + (i h/hbar)(X+_m + D_a - X-_l - D_b) Omega[m,l]
+template <typename T>
+__global__ void __launch_bounds__(256) k_omega(const RhsDev<T> d, const StageParams p, const OmTile* __restrict__ tiles,
+                                               const typename cx<T>::t* __restrict__ G,
+                                               const typename cx<T>::t* __restrict__ omA_in,
+                                               const typename cx<T>::t* __restrict__ omB_in,
+                                               typename cx<T>::t* __restrict__ omA_out,
+                                               typename cx<T>::t* __restrict__ omB_out) {
+  using C = typename cx<T>::t;
+  const OmTile t = tiles[blockIdx.x];
+  __shared__ C As[ZK][ZT];
+  __shared__ C Bs[ZK][ZT];
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const int nc = d.nc;
+  const int colmode0 = (t.blk == 0 ? 0 : d.Ns) + t.col0;  // absolute mode of local column col0
+  C acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = czero<T>();
+  const int kbeg = t.term1 ? 0 : nc, kend = t.term2 ? 2 * nc : nc;
+  for (int k0 = kbeg; k0 < kend; k0 += ZK) {
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+      const int idx = tid + 256 * r;
+      const int rr = idx >> 3, kk = idx & 7;
+      const int k = k0 + kk;
+      C av = czero<T>(), bv = czero<T>();
+      if (k < kend) {
+        if (rr < t.nrows) {
+          const int64_t m = t.row0 + rr;
+          av = k < nc ? G[(m * d.L + t.b) * nc + k] : d.V[m * nc + (k - nc)];
+        }
+        if (rr < t.ncols) {
+          const int64_t l = colmode0 + rr;
+          bv = k < nc ? d.U[l * nc + k] : cconj(G[(l * d.L + t.a) * nc + (k - nc)]);
+        }
+      }
+      As[kk][rr] = av;
+      Bs[kk][rr] = bv;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < ZK; ++kk) {
+      C a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) cfma(acc[i][j], a[i], b[j]);
+    }
+    __syncthreads();
+  }
+  const T sc = (T)(p.h / p.hbar);
+  const T h = (T)p.h;
+  const int64_t ld = t.blk == 0 ? d.Ns : d.Nf;
+  const C* in = t.blk == 0 ? omA_in : omB_in;
+  C* out = t.blk == 0 ? omA_out : omB_out;
+  const T da = (T)p.delta[t.a], db = (T)p.delta[t.b];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int r = ty + 16 * i;
+    if (r >= t.nrows) continue;
+    const int64_t m = t.row0 + r;
+    C xp = d.Xp[m];
+    xp.x += da;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int c = tx + 16 * j;
+      if (c >= t.ncols) continue;
+      const int64_t l = colmode0 + c;
+      C xm = d.Xm[l];
+      xm.x += db;
+      const int64_t e = m * ld + (t.col0 + c);
+      const C dd = cmul(csub(xp, xm), in[e]);  // (X+ - X-) Omega
+      // (i h/hbar) dd = sc * (-dd.y, dd.x)
+      C v = cscale(acc[i][j], h);
+      v.x -= sc * dd.y;
+      v.y += sc * dd.x;
+      out[e] = v;
+    }
+  }
+}
+
+template <typename T>
+int launch_omega(const RhsDev<T>& d, const StageParams& p, const OmTile* tiles, int ntiles, const typename cx<T>::t* G,
+                 const typename cx<T>::t* omA_in, const typename cx<T>::t* omB_in, typename cx<T>::t* omA_out,
+                 typename cx<T>::t* omB_out, cudaStream_t s) {
+  if (ntiles == 0) return ZG_OK;
+  k_omega<T><<<ntiles, 256, 0, s>>>(d, p, tiles, G, omA_in, omB_in, omA_out, omB_out);
+  ZG_CHECK_LAUNCH();
+  count_launch();
+  return ZG_OK;
+}
+
+// ========================================================= H(t), operands
+// Ht = H0 + dH, dH = uploaded matrix or U*diag(Re sigma_ii - 0.5)
+__global__ void k_build_ht(int n, const double2* __restrict__ H0, const double2* __restrict__ sig,
+                           const double2* __restrict__ dH, int dH_mode, double U, double2* __restrict__ Ht) {
+  const int64_t nn = (int64_t)n * n;
+  GRID_STRIDE(e, nn) {
+    double2 v = H0[e];
+    if (dH_mode == ZG_DH_MATRIX) v = cadd(v, dH[e]);
+    const int i = (int)(e / n), j = (int)(e % n);
+    if (dH_mode == ZG_DH_HUBBARD && i == j) v.x += U * (sig[e].x - 0.5);
+    Ht[e] = v;
+  }
+}
+
+int launch_build_ht(int n, const double2* H0, const double2* sig, const double2* dH, int dH_mode, double U,
+                    double2* Ht, cudaStream_t s) {
+  int64_t nn = (int64_t)n * n;
+  k_build_ht<<<grid_for(nn, 256, 152 * 8), 256, 0, s>>>(n, H0, sig, dH, dH_mode, U, Ht);
+  ZG_CHECK_LAUNCH();
+  count_launch();
+  return ZG_OK;
+}
+
+__device__ __forceinline__ void split_tf32_r(float v, float& hi, float& lo) {
+  uint32_t h, l;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
+  const float r = v - __uint_as_float(h);
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l) : "f"(r));
+  hi = __uint_as_float(h);
+  lo = __uint_as_float(l);
+}
+
+// One thread per complex element (r, c) of the np x np padded grid:
+//   Ht[r][c]                      -> Hth/Htl at row r, real columns 2c, 2c+1
+//   BH rows 2r, 2r+1, cols 2c, 2c+1 = [[Hr, -Hi], [Hi, Hr]] of H(t)[r][c]
+//   BS rows 2r, 2r+1, cols 2c, 2c+1 = [[Sr, -Si], [Si, Sr]] of sigma[c][r]
+// Padding (r or c >= n) is written as zero.
+__global__ void k_build_operands_mixed(int n, int np, const double2* __restrict__ H0, const float2* __restrict__ sig32,
+                                       const double2* __restrict__ dH, int dH_mode, double U, float* __restrict__ Hth,
+                                       float* __restrict__ Htl, float* __restrict__ BHh, float* __restrict__ BHl,
+                                       float* __restrict__ BSh, float* __restrict__ BSl) {
+  const int64_t tot = (int64_t)np * np;
+  const int64_t ld = 2 * (int64_t)np;
+  GRID_STRIDE(e, tot) {
+    const int r = (int)(e / np), c = (int)(e % np);
+    float hr = 0.f, hi = 0.f, sr = 0.f, si = 0.f;
+    if (r < n && c < n) {
+      double2 v = H0[(int64_t)r * n + c];
+      if (dH_mode == ZG_DH_MATRIX) v = cadd(v, dH[(int64_t)r * n + c]);
+      if (dH_mode == ZG_DH_HUBBARD && r == c) v.x += U * ((double)sig32[(int64_t)r * n + r].x - 0.5);
+      hr = (float)v.x;
+      hi = (float)v.y;
+      const float2 sv = sig32[(int64_t)c * n + r];
+      sr = sv.x;
+      si = sv.y;
+    }
+    float a, b;
+    if (r < n) {
+      split_tf32_r(hr, a, b);
+      Hth[(int64_t)r * ld + 2 * c] = a;
+      Htl[(int64_t)r * ld + 2 * c] = b;
+      split_tf32_r(hi, a, b);
+      Hth[(int64_t)r * ld + 2 * c + 1] = a;
+      Htl[(int64_t)r * ld + 2 * c + 1] = b;
+    }
+    const int64_t o0 = (int64_t)(2 * r) * ld + 2 * c, o1 = o0 + ld;
+    float xr_h, xr_l, xi_h, xi_l, mi_h, mi_l;
+    split_tf32_r(hr, xr_h, xr_l);
+    split_tf32_r(hi, xi_h, xi_l);
+    split_tf32_r(-hi, mi_h, mi_l);
+    BHh[o0] = xr_h; BHl[o0] = xr_l; BHh[o0 + 1] = mi_h; BHl[o0 + 1] = mi_l;
+    BHh[o1] = xi_h; BHl[o1] = xi_l; BHh[o1 + 1] = xr_h; BHl[o1 + 1] = xr_l;
+    split_tf32_r(sr, xr_h, xr_l);
+    split_tf32_r(si, xi_h, xi_l);
+    split_tf32_r(-si, mi_h, mi_l);
+    BSh[o0] = xr_h; BSl[o0] = xr_l; BSh[o0 + 1] = mi_h; BSl[o0 + 1] = mi_l;
+    BSh[o1] = xi_h; BSl[o1] = xi_l; BSh[o1 + 1] = xr_h; BSl[o1 + 1] = xr_l;
+  }
+}
+
+int launch_build_operands_mixed(int n, int np, const double2* H0, const float2* sig32, const double2* dH, int dH_mode,
+                                double U, float* Hth, float* Htl, float* BHh, float* BHl, float* BSh, float* BSl,
+                                cudaStream_t s) {
+  int64_t tot = (int64_t)np * np;
+  k_build_operands_mixed<<<grid_for(tot, 256, 152 * 16), 256, 0, s>>>(n, np, H0, sig32, dH, dH_mode, U, Hth, Htl, BHh,
+                                                                      BHl, BSh, BSl);
+  ZG_CHECK_LAUNCH();
+  count_launch();
+  return ZG_OK;
+}
+
+// ----------------------------------------------------------- instantiate
+#define ZG_INST(T)                                                                                                   \
+  template int64_t plan_zgemm_batch<T>(GemmBatch<T>&);                                                               \
+  template int launch_zgemm_batch<T>(GemmBatch<T>&, int64_t, cudaStream_t);                                         \
+  template int launch_gathers<T>(const RhsDev<T>&, const cx<T>::t*, const cx<T>::t*, const cx<T>::t*, int64_t,      \
+                                 cx<T>::t*, cx<T>::t*, cudaStream_t);                                                 \
+  template int launch_sigma_finalize<T>(const RhsDev<T>&, const StageParams&, const cx<T>::t*, int64_t,              \
+                                        const cx<T>::t*, cx<T>::t*, cudaStream_t);                                    \
+  template int launch_currents<T>(const RhsDev<T>&, const StageParams&, const cx<T>::t*, double*, cudaStream_t);     \
+  template int launch_psi_finalize<T>(const RhsDev<T>&, const StageParams&, const cx<T>::t*, const cx<T>::t*,        \
+                                      int64_t, const cx<T>::t*, int64_t, const cx<T>::t*, const cx<T>::t*,           \
+                                      const cx<T>::t*, cx<T>::t*, cudaStream_t);                                     \
+  template int launch_omega<T>(const RhsDev<T>&, const StageParams&, const OmTile*, int, const cx<T>::t*,            \
+                               const cx<T>::t*, const cx<T>::t*, cx<T>::t*, cx<T>::t*, cudaStream_t);
+ZG_INST(double)
+ZG_INST(float)
+
+}  // namespace zg

@@ -1,6 +1,7 @@
 // Host runtime of libzandgpu: trajectory objects (device constants, the
 // Runge-Kutta state slots, scratch), the per-stage launch sequence of the AME
-// right-hand side, and the extern "C" entry points declared in zandgpu.h.
+// right-hand side in the FP64 and the mixed-precision form, and the
+// extern "C" entry points declared in zandgpu.h.
 #include <stdarg.h>
 #include <string.h>
 
@@ -67,23 +68,40 @@ struct zg_traj {
   // tableau
   int stages = 0;
   std::vector<double> A, B, CT, CH;  // B: stages x (stages+1)
-  // device constants
+  // device constants (FP64)
   double2 *H0 = nullptr, *Xp = nullptr, *Xm = nullptr, *GLP = nullptr, *dGP = nullptr, *XI = nullptr,
           *IXI = nullptr, *XIS = nullptr, *U = nullptr, *V = nullptr;
   int *mode_lead = nullptr, *lead_cols = nullptr, *colmap = nullptr;
   OmTile* tiles = nullptr;
   int ntiles = 0;
-  // state: (stages+1) slots of S complex; slot `stages` is y
+  // FP64 path: (stages+1) slots of S complex128, slot `stages` is y.
+  // Mixed path: one FP64 slot (y) here, k slots in K32.
   double2* Y = nullptr;
   int y_slots = 0;
   double2* Ystage = nullptr;
   const double2* cur_in = nullptr;
-  // scratch
+  // FP64 scratch
   double2 *Ht = nullptr, *dH = nullptr, *T = nullptr, *Pc = nullptr, *sigC = nullptr, *G = nullptr, *R2 = nullptr,
           *ZA = nullptr, *ZB = nullptr;
   double *J = nullptr, *partial = nullptr, *err = nullptr;
   int nblk_err = 0;
   bool dH_set = false;
+  // ---- mixed path
+  int np = 0;  // n padded to a multiple of 16
+  MixedLayout ml;
+  float2 *Xp32 = nullptr, *Xm32 = nullptr, *GLP32 = nullptr, *dGP32 = nullptr, *XI32 = nullptr, *XIS32 = nullptr,
+         *IXI32 = nullptr, *U32 = nullptr, *V32 = nullptr;
+  float2 *y32 = nullptr, *K32 = nullptr, *stage32 = nullptr;
+  int k_slots = 0;
+  float *Hth = nullptr, *Htl = nullptr, *BHh = nullptr, *BHl = nullptr, *BSh = nullptr, *BSl = nullptr;
+  float2 *T32 = nullptr, *R1p = nullptr, *Pc32 = nullptr, *sigC32 = nullptr, *G32 = nullptr, *R2_32 = nullptr,
+         *ZA32 = nullptr, *ZB32 = nullptr;
+  double2 *conv64 = nullptr, *sig64 = nullptr;
+  int* tc_err = nullptr;
+  double2* ws64 = nullptr;
+  float2* ws32 = nullptr;
+  int64_t ws64_cap = 0, ws32_cap = 0;
+  TcGemm gT, gR1;
   // profiling: CUDA event pairs on `stream` around each region, collected at host syncs
   struct Prof {
     bool on = false;
@@ -95,16 +113,28 @@ struct zg_traj {
     bool created = false;
   } prof;
 
-  RhsDev dev_view() const {
-    RhsDev d;
-    d.n = n; d.L = L; d.N = N; d.Ns = Ns; d.Nf = Nf; d.nc = nc;
-    d.off_psi = off_psi; d.off_omA = off_omA; d.off_omB = off_omB; d.S = S;
-    d.mode_lead = mode_lead; d.lead_cols = lead_cols; d.colmap = colmap;
-    d.H0 = H0; d.Xp = Xp; d.Xm = Xm; d.GLP = GLP; d.dGP = dGP; d.XI = XI; d.U = U; d.V = V;
-    return d;
-  }
+  template <typename R>
+  RhsDev<R> dev_view() const;
   double2* slot(int i) const { return Y + (int64_t)i * S; }
+  float2* kslot(int i) const { return K32 + (int64_t)i * S; }
 };
+
+template <>
+RhsDev<double> zg_traj::dev_view<double>() const {
+  RhsDev<double> d;
+  d.n = n; d.L = L; d.N = N; d.Ns = Ns; d.Nf = Nf; d.nc = nc;
+  d.mode_lead = mode_lead; d.lead_cols = lead_cols; d.colmap = colmap;
+  d.Xp = Xp; d.Xm = Xm; d.GLP = GLP; d.dGP = dGP; d.XI = XI; d.U = U; d.V = V;
+  return d;
+}
+template <>
+RhsDev<float> zg_traj::dev_view<float>() const {
+  RhsDev<float> d;
+  d.n = n; d.L = L; d.N = N; d.Ns = Ns; d.Nf = Nf; d.nc = nc;
+  d.mode_lead = mode_lead; d.lead_cols = lead_cols; d.colmap = colmap;
+  d.Xp = Xp32; d.Xm = Xm32; d.GLP = GLP32; d.dGP = dGP32; d.XI = XI32; d.U = U32; d.V = V32;
+  return d;
+}
 
 // ---------------------------------------------------------------- profiling
 static void prof_collect(zg_traj* t) {
@@ -144,7 +174,10 @@ static void free_traj(zg_traj* t) {
       }
   void* ptrs[] = {t->H0, t->Xp, t->Xm, t->GLP, t->dGP, t->XI, t->IXI, t->XIS, t->U, t->V, t->mode_lead,
                   t->lead_cols, t->colmap, t->tiles, t->Y, t->Ystage, t->Ht, t->dH, t->T, t->Pc, t->sigC,
-                  t->G, t->R2, t->ZA, t->ZB, t->J, t->partial, t->err};
+                  t->G, t->R2, t->ZA, t->ZB, t->J, t->partial, t->err, t->Xp32, t->Xm32, t->GLP32, t->dGP32,
+                  t->XI32, t->XIS32, t->IXI32, t->U32, t->V32, t->y32, t->K32, t->stage32, t->Hth, t->Htl, t->BHh,
+                  t->BHl, t->BSh, t->BSl, t->T32, t->R1p, t->Pc32, t->sigC32, t->G32, t->R2_32, t->ZA32, t->ZB32,
+                  t->conv64, t->sig64, t->tc_err, t->ws64, t->ws32};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (t->stream) cudaStreamDestroy(t->stream);
@@ -152,18 +185,36 @@ static void free_traj(zg_traj* t) {
 }
 
 static int alloc_state(zg_traj* t, int stages) {
-  if (t->Y && t->y_slots == stages + 1) return ZG_OK;
-  if (t->Y) cudaFree(t->Y);
-  t->Y = nullptr;
-  ZG_TRY(dalloc(&t->Y, (size_t)(stages + 1) * t->S));
-  t->y_slots = stages + 1;
-  ZG_CHECK_CUDA(cudaMemsetAsync(t->Y, 0, (size_t)(stages + 1) * t->S * sizeof(double2), t->stream));
+  const bool mixed = t->precision == ZG_PREC_MIXED;
+  const int yslots = mixed ? 1 : stages + 1;
+  if (!t->Y || t->y_slots != yslots) {
+    if (t->Y) cudaFree(t->Y);
+    t->Y = nullptr;
+    ZG_TRY(dalloc(&t->Y, (size_t)yslots * t->S));
+    t->y_slots = yslots;
+    ZG_CHECK_CUDA(cudaMemsetAsync(t->Y, 0, (size_t)yslots * t->S * sizeof(double2), t->stream));
+  }
+  if (mixed && (!t->K32 || t->k_slots != stages)) {
+    if (t->K32) cudaFree(t->K32);
+    t->K32 = nullptr;
+    ZG_TRY(dalloc(&t->K32, (size_t)stages * t->S));
+    t->k_slots = stages;
+    ZG_CHECK_CUDA(cudaMemsetAsync(t->K32, 0, (size_t)stages * t->S * sizeof(float2), t->stream));
+  }
   return ZG_OK;
 }
+
+// y slot index inside Y: FP64 path keeps it after the k slots, mixed keeps only y
+static double2* y64(const zg_traj* t) { return t->precision == ZG_PREC_MIXED ? t->Y : t->slot(t->stages); }
 
 static int set_tableau_impl(zg_traj* t, int stages, const double* A, const double* B, const double* CT,
                             const double* CH) {
   ZG_REQUIRE(stages >= 1 && stages <= ZG_MAX_STAGES, "stages=%d out of range", stages);
+  if (t->precision == ZG_PREC_MIXED) {
+    // the mixed path applies y with weight 1 implicitly
+    ZG_REQUIRE(CH[stages] == 1.0, "mixed precision needs CH[stages] == 1");
+    for (int i = 1; i < stages; ++i) ZG_REQUIRE(B[(size_t)i * (stages + 1) + stages] == 1.0, "mixed precision needs B[i][stages] == 1");
+  }
   t->stages = stages;
   t->A.assign(A, A + stages);
   t->B.assign(B, B + (size_t)stages * (stages + 1));
@@ -198,17 +249,73 @@ static void build_tiles(zg_traj* t, std::vector<OmTile>& out) {
     }
 }
 
+static void to_f32(const double2* a, float2* b, size_t n) {
+  for (size_t i = 0; i < n; ++i) b[i] = make_float2((float)a[i].x, (float)a[i].y);
+}
+
+static int create_mixed(zg_traj* t, const zg_layout* Lo, const std::vector<double2>& U, const std::vector<double2>& V) {
+  const int64_t n = t->n, N = t->N, Ns = t->Ns, Nf = t->Nf, L = t->L, nc = t->nc;
+  const int64_t np = (n + 15) / 16 * 16;
+  t->np = (int)np;
+  MixedLayout& ml = t->ml;
+  ml.n = n; ml.N = N; ml.np = np;
+  ml.off_psi = t->off_psi; ml.off_omA = t->off_omA; ml.S = t->S;
+  ml.st_psih = n * n;
+  ml.st_psil = ml.st_psih + N * np;
+  ml.st_om = ml.st_psil + N * np;
+  ml.st_S = ml.st_om + N * Ns + Ns * Nf;
+  cudaStream_t s = t->stream;
+  std::vector<float2> tmp;
+  auto up32 = [&](float2** dst, const double* src, size_t cnt) -> int {
+    tmp.resize(cnt);
+    to_f32((const double2*)src, tmp.data(), cnt);
+    ZG_TRY(dalloc(dst, cnt));
+    ZG_CHECK_CUDA(cudaMemcpy(*dst, tmp.data(), cnt * sizeof(float2), cudaMemcpyHostToDevice));
+    return ZG_OK;
+  };
+  ZG_TRY(up32(&t->Xp32, Lo->Xp, N));
+  ZG_TRY(up32(&t->Xm32, Lo->Xm, N));
+  ZG_TRY(up32(&t->GLP32, Lo->GLP, N));
+  ZG_TRY(up32(&t->dGP32, Lo->dGP, N));
+  ZG_TRY(up32(&t->XI32, Lo->XI, N * nc));
+  ZG_TRY(up32(&t->XIS32, Lo->XIS, N * nc));
+  ZG_TRY(up32(&t->IXI32, Lo->IXI, N * nc));
+  ZG_TRY(up32(&t->U32, (const double*)U.data(), N * nc));
+  ZG_TRY(up32(&t->V32, (const double*)V.data(), N * nc));
+  ZG_TRY(dalloc(&t->y32, t->S));
+  ZG_TRY(dalloc(&t->stage32, ml.st_S));
+  ZG_CHECK_CUDA(cudaMemsetAsync(t->stage32, 0, ml.st_S * sizeof(float2), s));  // psi padding columns stay zero
+  ZG_TRY(dalloc(&t->Hth, n * 2 * np)); ZG_TRY(dalloc(&t->Htl, n * 2 * np));
+  ZG_TRY(dalloc(&t->BHh, 4 * np * np)); ZG_TRY(dalloc(&t->BHl, 4 * np * np));
+  ZG_TRY(dalloc(&t->BSh, 4 * np * np)); ZG_TRY(dalloc(&t->BSl, 4 * np * np));
+  ZG_TRY(dalloc(&t->T32, n * np)); ZG_TRY(dalloc(&t->R1p, N * np));
+  ZG_TRY(dalloc(&t->Pc32, 2 * L * n * nc)); ZG_TRY(dalloc(&t->sigC32, L * n * nc)); ZG_TRY(dalloc(&t->G32, N * L * nc));
+  ZG_TRY(dalloc(&t->R2_32, std::max<int64_t>(Ns, 1) * n));
+  ZG_TRY(dalloc(&t->ZA32, L * N * nc)); ZG_TRY(dalloc(&t->ZB32, L * std::max<int64_t>(Ns, 1) * nc));
+  ZG_TRY(dalloc(&t->sig64, n * n));
+  ZG_TRY(dalloc(&t->tc_err, 1));
+  ZG_CHECK_CUDA(cudaMemsetAsync(t->tc_err, 0, sizeof(int), s));
+  // tensor maps of the two tensor-core GEMMs (fixed buffers)
+  const float* psih = (const float*)(t->stage32 + ml.st_psih);
+  const float* psil = (const float*)(t->stage32 + ml.st_psil);
+  ZG_TRY(tc_gemm_prepare(t->gT, t->Hth, t->Htl, t->BSh, t->BSl, 2 * np, 2 * np, (float*)t->T32, 2 * np, (int)n,
+                         (int)(2 * np), (int)(2 * np), t->tc_err));
+  ZG_TRY(tc_gemm_prepare(t->gR1, psih, psil, t->BHh, t->BHl, 2 * np, 2 * np, (float*)t->R1p, 2 * np, (int)N,
+                         (int)(2 * np), (int)(2 * np), t->tc_err));
+  return ZG_OK;
+}
+
 extern "C" {
 
 const char* zg_last_error(void) { return g_err; }
-int zg_version(void) { return 100; }
+int zg_version(void) { return 101; }
 long long zg_launch_count(void) { return g_launches.load(); }
 void* zg_traj_stream(const zg_traj* t) { return t ? (void*)t->stream : nullptr; }
 
 int zg_traj_create(int device, const zg_layout* Lo, int precision, zg_traj** out) {
   ZG_REQUIRE(out && Lo, "null argument");
   *out = nullptr;
-  ZG_REQUIRE(precision == ZG_PREC_F64, "precision mode %d not available in this build", precision);
+  ZG_REQUIRE(precision == ZG_PREC_F64 || precision == ZG_PREC_MIXED, "unknown precision mode %d", precision);
   ZG_REQUIRE(Lo->n > 0 && Lo->n_leads > 0 && Lo->n_leads <= ZG_MAX_LEADS && Lo->n_modes > 0 &&
                  Lo->n_sourced >= 0 && Lo->n_sourced <= Lo->n_modes && Lo->nc > 0,
              "bad layout sizes");
@@ -219,11 +326,11 @@ int zg_traj_create(int device, const zg_layout* Lo, int precision, zg_traj** out
   t->precision = precision;
   t->n = Lo->n; t->L = Lo->n_leads; t->N = Lo->n_modes; t->Ns = Lo->n_sourced; t->Nf = t->N - t->Ns; t->nc = Lo->nc;
   t->hbar = Lo->hbar;
-  const int64_t n = t->n, N = t->N, Ns = t->Ns, Nf = t->Nf, L = t->L, nc = t->nc;
+  const int64_t n = t->n, N = t->N, Ns = t->Ns, L = t->L, nc = t->nc;
   t->off_psi = n * n;
   t->off_omA = t->off_psi + N * n;
   t->off_omB = t->off_omA + N * Ns;
-  t->S = t->off_omB + Ns * Nf;
+  t->S = t->off_omB + Ns * t->Nf;
   t->s_start.assign(Lo->s_start, Lo->s_start + L + 1);
   t->f_start.assign(Lo->f_start, Lo->f_start + L + 1);
   int st = ZG_OK;
@@ -238,8 +345,9 @@ int zg_traj_create(int device, const zg_layout* Lo, int precision, zg_traj** out
   if (!ok) { free_traj(t); set_error("s_start/f_start do not partition the modes"); return ZG_EINVAL; }
   for (int64_t m = 0; m < N; ++m) {
     int a = Lo->mode_lead[m];
-    bool in = (m < Ns) ? (m >= t->s_start[a] && m < t->s_start[a + 1]) : (m >= t->f_start[a] && m < t->f_start[a + 1]);
-    if (a < 0 || a >= L || !in) { free_traj(t); set_error("mode_lead inconsistent with row ranges at mode %lld", (long long)m); return ZG_EINVAL; }
+    bool in = a >= 0 && a < L &&
+              ((m < Ns) ? (m >= t->s_start[a] && m < t->s_start[a + 1]) : (m >= t->f_start[a] && m < t->f_start[a + 1]));
+    if (!in) { free_traj(t); set_error("mode_lead inconsistent with row ranges at mode %lld", (long long)m); return ZG_EINVAL; }
   }
   for (int64_t i = 0; i < L * nc; ++i)
     if (Lo->lead_cols[i] < 0 || Lo->lead_cols[i] >= n) { free_traj(t); set_error("lead_cols out of range"); return ZG_EINVAL; }
@@ -264,9 +372,9 @@ int zg_traj_create(int device, const zg_layout* Lo, int precision, zg_traj** out
   ZG_STEP(upload<int>(t->mode_lead, Lo->mode_lead, N, t->stream));
   ZG_STEP(upload<int>(t->lead_cols, Lo->lead_cols, L * nc, t->stream));
   ZG_STEP(upload<int>(t->colmap, Lo->colmap, L * n, t->stream));
+  // U = dGM * IXI (per column mode), V = dGP * XIT2 (per row mode)
+  std::vector<double2> U(N * nc), V(N * nc);
   {
-    // U = dGM * IXI (per column mode), V = dGP * XIT2 (per row mode)
-    std::vector<double2> U(N * nc), V(N * nc);
     const double2* dGM = (const double2*)Lo->dGM;
     const double2* dGP = (const double2*)Lo->dGP;
     const double2* IXI = (const double2*)Lo->IXI;
@@ -276,25 +384,28 @@ int zg_traj_create(int device, const zg_layout* Lo, int precision, zg_traj** out
         U[m * nc + k] = cmul(dGM[m], IXI[m * nc + k]);
         V[m * nc + k] = cmul(dGP[m], XIT2[m * nc + k]);
       }
-    ZG_STEP(upload<double2>(t->U, U.data(), N * nc, t->stream));
-    ZG_STEP(upload<double2>(t->V, V.data(), N * nc, t->stream));
-    std::vector<OmTile> tiles;
-    build_tiles(t, tiles);
-    t->ntiles = (int)tiles.size();
-    ZG_STEP(dalloc(&t->tiles, tiles.size()));
-    ZG_STEP(upload<OmTile>(t->tiles, tiles.data(), tiles.size(), t->stream));
-    // keep host vectors alive until the copies finished
-    ZG_CHECK_CUDA(cudaStreamSynchronize(t->stream));
   }
-  ZG_STEP(dalloc(&t->Ystage, t->S));
-  ZG_STEP(dalloc(&t->Ht, n * n)); ZG_STEP(dalloc(&t->dH, n * n)); ZG_STEP(dalloc(&t->T, n * n));
-  ZG_STEP(dalloc(&t->Pc, 2 * L * n * nc)); ZG_STEP(dalloc(&t->sigC, L * n * nc)); ZG_STEP(dalloc(&t->G, N * L * nc));
-  ZG_STEP(dalloc(&t->R2, std::max<int64_t>(Ns, 1) * n));
-  ZG_STEP(dalloc(&t->ZA, L * N * nc)); ZG_STEP(dalloc(&t->ZB, L * std::max<int64_t>(Ns, 1) * nc));
+  ZG_STEP(upload<double2>(t->U, U.data(), N * nc, t->stream));
+  ZG_STEP(upload<double2>(t->V, V.data(), N * nc, t->stream));
+  std::vector<OmTile> tiles;
+  build_tiles(t, tiles);
+  t->ntiles = (int)tiles.size();
+  ZG_STEP(dalloc(&t->tiles, tiles.size()));
+  ZG_STEP(upload<OmTile>(t->tiles, tiles.data(), tiles.size(), t->stream));
+  ZG_STEP(dalloc(&t->dH, n * n));
   ZG_STEP(dalloc(&t->J, L));
   t->nblk_err = terr2_nblocks(t->S);
   ZG_STEP(dalloc(&t->partial, 3 * (size_t)t->nblk_err));
   ZG_STEP(dalloc(&t->err, 3));
+  if (precision == ZG_PREC_F64) {
+    ZG_STEP(dalloc(&t->Ystage, t->S));
+    ZG_STEP(dalloc(&t->Ht, n * n)); ZG_STEP(dalloc(&t->T, n * n));
+    ZG_STEP(dalloc(&t->Pc, 2 * L * n * nc)); ZG_STEP(dalloc(&t->sigC, L * n * nc)); ZG_STEP(dalloc(&t->G, N * L * nc));
+    ZG_STEP(dalloc(&t->R2, std::max<int64_t>(Ns, 1) * n));
+    ZG_STEP(dalloc(&t->ZA, L * N * nc)); ZG_STEP(dalloc(&t->ZB, L * std::max<int64_t>(Ns, 1) * nc));
+  } else {
+    ZG_STEP(create_mixed(t, Lo, U, V));
+  }
   {
     double B[7 * 8], CT[7], CH[8];
     for (int i = 0; i < 7; ++i)
@@ -303,7 +414,9 @@ int zg_traj_create(int device, const zg_layout* Lo, int precision, zg_traj** out
     CH[7] = 1.0;
     ZG_STEP(set_tableau_impl(t, 7, kDopA, B, CT, CH));
   }
-  t->cur_in = t->slot(t->stages);
+  t->cur_in = y64(t);
+  if (precision == ZG_PREC_MIXED) ZG_STEP(launch_f64_to_f32(t->Y, t->y32, t->S, t->stream));
+  // host vectors above must outlive their asynchronous copies
   ZG_CHECK_CUDA(cudaStreamSynchronize(t->stream));
 #undef ZG_STEP
   *out = t;
@@ -329,8 +442,13 @@ int zg_set_tableau(zg_traj* t, int stages, const double* A, const double* B, con
   ZG_REQUIRE(t && A && B && CT && CH, "null argument");
   ZG_CHECK_CUDA(cudaSetDevice(t->dev));
   ZG_TRY(set_tableau_impl(t, stages, A, B, CT, CH));
-  t->cur_in = t->slot(t->stages);
+  t->cur_in = y64(t);
   ZG_CHECK_CUDA(cudaStreamSynchronize(t->stream));
+  return ZG_OK;
+}
+
+static int ensure_conv64(zg_traj* t) {
+  if (!t->conv64) ZG_TRY(dalloc(&t->conv64, t->S));
   return ZG_OK;
 }
 
@@ -338,7 +456,17 @@ int zg_set_state(zg_traj* t, int slot, const double* host) {
   ZG_REQUIRE(t && host, "null argument");
   ZG_REQUIRE(slot >= 0 && slot <= t->stages, "slot %d out of range", slot);
   ZG_CHECK_CUDA(cudaSetDevice(t->dev));
-  ZG_CHECK_CUDA(cudaMemcpyAsync(t->slot(slot), host, t->S * sizeof(double2), cudaMemcpyHostToDevice, t->stream));
+  const size_t bytes = t->S * sizeof(double2);
+  if (t->precision == ZG_PREC_F64) {
+    ZG_CHECK_CUDA(cudaMemcpyAsync(t->slot(slot), host, bytes, cudaMemcpyHostToDevice, t->stream));
+  } else if (slot == t->stages) {
+    ZG_CHECK_CUDA(cudaMemcpyAsync(t->Y, host, bytes, cudaMemcpyHostToDevice, t->stream));
+    ZG_TRY(launch_f64_to_f32(t->Y, t->y32, t->S, t->stream));
+  } else {
+    ZG_TRY(ensure_conv64(t));
+    ZG_CHECK_CUDA(cudaMemcpyAsync(t->conv64, host, bytes, cudaMemcpyHostToDevice, t->stream));
+    ZG_TRY(launch_f64_to_f32(t->conv64, t->kslot(slot), t->S, t->stream));
+  }
   ZG_CHECK_CUDA(cudaStreamSynchronize(t->stream));
   return ZG_OK;
 }
@@ -347,7 +475,18 @@ int zg_get_state(zg_traj* t, int slot, double* host) {
   ZG_REQUIRE(t && host, "null argument");
   ZG_REQUIRE(slot >= 0 && slot <= t->stages, "slot %d out of range", slot);
   ZG_CHECK_CUDA(cudaSetDevice(t->dev));
-  ZG_CHECK_CUDA(cudaMemcpyAsync(host, t->slot(slot), t->S * sizeof(double2), cudaMemcpyDeviceToHost, t->stream));
+  const size_t bytes = t->S * sizeof(double2);
+  const double2* src;
+  if (t->precision == ZG_PREC_F64) {
+    src = t->slot(slot);
+  } else if (slot == t->stages) {
+    src = t->Y;
+  } else {
+    ZG_TRY(ensure_conv64(t));
+    ZG_TRY(launch_f32_to_f64(t->kslot(slot), t->conv64, t->S, t->stream));
+    src = t->conv64;
+  }
+  ZG_CHECK_CUDA(cudaMemcpyAsync(host, src, bytes, cudaMemcpyDeviceToHost, t->stream));
   ZG_CHECK_CUDA(cudaStreamSynchronize(t->stream));
   return ZG_OK;
 }
@@ -356,28 +495,45 @@ int zg_stage_input(zg_traj* t, int stage) {
   ZG_REQUIRE(t, "null argument");
   ZG_REQUIRE(stage >= 0 && stage < t->stages, "stage %d out of range", stage);
   ZG_CHECK_CUDA(cudaSetDevice(t->dev));
-  if (stage == 0) {
-    t->cur_in = t->slot(t->stages);
-    return ZG_OK;
-  }
   CombineCoefs cf;
   cf.n = 0;
-  for (int j = 0; j <= t->stages; ++j) {
-    double b = t->B[(size_t)stage * (t->stages + 1) + j];
-    if (b != 0.0) { cf.idx[cf.n] = j; cf.c[cf.n] = b; ++cf.n; }
+  if (t->precision == ZG_PREC_F64) {
+    if (stage == 0) {
+      t->cur_in = t->slot(t->stages);
+      return ZG_OK;
+    }
+    for (int j = 0; j <= t->stages; ++j) {
+      double b = t->B[(size_t)stage * (t->stages + 1) + j];
+      if (b != 0.0) { cf.idx[cf.n] = j; cf.c[cf.n] = b; ++cf.n; }
+    }
+    prof_begin(t, ZG_PROF_COMBINE);
+    ZG_TRY(launch_combine_c128(t->Y, t->S, cf, t->Ystage, t->S, t->stream));
+    prof_end(t, ZG_PROF_COMBINE);
+    t->cur_in = t->Ystage;
+    return ZG_OK;
   }
+  // mixed: y32 + sum over k slots (y enters with weight B[i][stages] == 1)
+  if (stage > 0)
+    for (int j = 0; j < t->stages; ++j) {
+      double b = t->B[(size_t)stage * (t->stages + 1) + j];
+      if (b != 0.0) { cf.idx[cf.n] = j; cf.c[cf.n] = b; ++cf.n; }
+    }
   prof_begin(t, ZG_PROF_COMBINE);
-  ZG_TRY(launch_combine_c128(t->Y, t->S, cf, t->Ystage, t->S, t->stream));
+  ZG_TRY(launch_stage_input_mixed(t->y32, t->K32, t->S, cf, t->ml, t->stage32, t->stream));
   prof_end(t, ZG_PROF_COMBINE);
-  t->cur_in = t->Ystage;
+  t->cur_in = nullptr;
   return ZG_OK;
 }
 
 int zg_get_stage_sigma(zg_traj* t, double* host) {
   ZG_REQUIRE(t && host, "null argument");
   ZG_CHECK_CUDA(cudaSetDevice(t->dev));
-  ZG_CHECK_CUDA(cudaMemcpyAsync(host, t->cur_in, (size_t)t->n * t->n * sizeof(double2), cudaMemcpyDeviceToHost,
-                                t->stream));
+  const double2* src = t->cur_in;
+  if (t->precision == ZG_PREC_MIXED) {
+    ZG_TRY(launch_f32_to_f64(t->stage32, t->sig64, (int64_t)t->n * t->n, t->stream));
+    src = t->sig64;
+  }
+  ZG_CHECK_CUDA(cudaMemcpyAsync(host, src, (size_t)t->n * t->n * sizeof(double2), cudaMemcpyDeviceToHost, t->stream));
   ZG_CHECK_CUDA(cudaStreamSynchronize(t->stream));
   return ZG_OK;
 }
@@ -392,76 +548,190 @@ int zg_set_dH(zg_traj* t, const double* host) {
   return ZG_OK;
 }
 
-int zg_rhs(zg_traj* t, int stage, double ts, double h, const double* delta, int dH_mode, double hubbard_U,
-           double* currents) {
-  ZG_REQUIRE(t && delta, "null argument");
-  ZG_REQUIRE(stage >= 0 && stage < t->stages, "stage %d out of range", stage);
-  ZG_REQUIRE(dH_mode == ZG_DH_NONE || dH_mode == ZG_DH_HUBBARD || (dH_mode == ZG_DH_MATRIX && t->dH_set),
-             "bad dH mode %d (ZG_DH_MATRIX needs zg_set_dH first)", dH_mode);
-  ZG_CHECK_CUDA(cudaSetDevice(t->dev));
-  const RhsDev d = t->dev_view();
-  StageParams p;
-  p.h = h; p.ts = ts; p.hbar = t->hbar;
-  for (int a = 0; a < ZG_MAX_LEADS; ++a) p.delta[a] = a < t->L ? delta[a] : 0.0;
+static void gemm_prob_f64(std::vector<GemmProb<double>>& v, const double2* A, int64_t lda, int opA, const double2* B,
+                          int64_t ldb, int opB, double2* C, int64_t ldc, int M, int N, int K) {
+  GemmProb<double> P;
+  P.A = A; P.A2 = nullptr; P.B = B; P.Cm = C; P.M = M; P.N = N; P.K = K; P.opA = opA; P.opB = opB;
+  P.lda = lda; P.ldb = ldb; P.ldc = ldc;
+  P.alpha = make_double2(1.0, 0.0); P.beta = make_double2(0.0, 0.0);
+  P.tile_begin = 0; P.tiles_n = 1;
+  v.push_back(P);
+}
+static void gemm_prob_f32(std::vector<GemmProb<float>>& v, const float2* A, const float2* A2, int64_t lda, int opA,
+                          const float2* B, int64_t ldb, int opB, float2* C, int64_t ldc, int M, int N, int K) {
+  GemmProb<float> P;
+  P.A = A; P.A2 = A2; P.B = B; P.Cm = C; P.M = M; P.N = N; P.K = K; P.opA = opA; P.opB = opB;
+  P.lda = lda; P.ldb = ldb; P.ldc = ldc;
+  P.alpha = make_float2(1.f, 0.f); P.beta = make_float2(0.f, 0.f);
+  P.tile_begin = 0; P.tiles_n = 1;
+  v.push_back(P);
+}
+
+}  // extern "C"
+
+// split-K workspace of one precision, grown on first use (the first right-hand
+// side of a trajectory sizes it; later calls never allocate)
+template <typename R>
+static int run_batches(zg_traj* t, std::vector<GemmProb<R>>& probs, typename cx<R>::t** ws, int64_t* cap,
+                       cudaStream_t s) {
+  for (size_t b0 = 0; b0 < probs.size(); b0 += ZG_MAX_GEMM) {
+    GemmBatch<R> batch;
+    batch.nprob = (int)std::min<size_t>(ZG_MAX_GEMM, probs.size() - b0);
+    for (int i = 0; i < batch.nprob; ++i) batch.p[i] = probs[b0 + i];
+    const int64_t need = plan_zgemm_batch<R>(batch);
+    if (need > *cap) {
+      ZG_CHECK_CUDA(cudaStreamSynchronize(s));
+      if (*ws) cudaFree(*ws);
+      *ws = nullptr;
+      *cap = 0;
+      ZG_TRY(dalloc(ws, need));
+      *cap = need;
+    }
+    batch.ws = *ws;
+    ZG_TRY(launch_zgemm_batch<R>(batch, *cap, s));
+  }
+  return ZG_OK;
+}
+
+extern "C" {
+
+static int rhs_f64(zg_traj* t, int stage, const StageParams& p, int dH_mode, double hubbard_U, bool want_J) {
+  const RhsDev<double> d = t->dev_view<double>();
   const double2* in = t->cur_in;
   const double2* sig = in;
   const double2* psi = in + t->off_psi;
   double2* out = t->slot(stage);
   cudaStream_t s = t->stream;
   const int64_t n = t->n, N = t->N, Ns = t->Ns, Nf = t->Nf, L = t->L, nc = t->nc;
-  prof_begin(t, ZG_PROF_RHS);
   prof_begin(t, ZG_PROF_PREP);
-  ZG_TRY(launch_build_ht(d, sig, t->dH, dH_mode, hubbard_U, t->Ht, s));
-  ZG_TRY(launch_gathers(d, sig, psi, t->sigC, t->G, s));
+  ZG_TRY(launch_build_ht((int)n, t->H0, sig, t->dH, dH_mode, hubbard_U, t->Ht, s));
+  ZG_TRY(launch_gathers<double>(d, sig, psi, nullptr, n, t->sigC, t->G, s));
   prof_end(t, ZG_PROF_PREP);
-  std::vector<GemmProb> probs;
-  auto prob = [&](const double2* A, int64_t lda, int opA, const double2* B, int64_t ldb, int opB, double2* C,
-                  int64_t ldc, int M, int Nn, int K) {
-    GemmProb P;
-    P.A = A; P.B = B; P.C = C; P.M = M; P.N = Nn; P.K = K; P.opA = opA; P.opB = opB;
-    P.lda = lda; P.ldb = ldb; P.ldc = ldc;
-    P.alpha = make_double2(1.0, 0.0); P.beta = make_double2(0.0, 0.0);
-    P.tile_begin = 0; P.tiles_n = 1;
-    probs.push_back(P);
-  };
+  std::vector<GemmProb<double>> probs;
   // T = H(t) sigma ; R1 = psi H(t)^T into k_psi
-  prob(t->Ht, n, 0, sig, n, 0, t->T, n, (int)n, (int)n, (int)n);
-  prob(psi, n, 0, t->Ht, n, 1, out + t->off_psi, n, (int)N, (int)n, (int)n);
+  gemm_prob_f64(probs, t->Ht, n, 0, sig, n, 0, t->T, n, (int)n, (int)n, (int)n);
+  gemm_prob_f64(probs, psi, n, 0, t->Ht, n, 1, out + t->off_psi, n, (int)N, (int)n, (int)n);
   for (int a = 0; a < L; ++a) {
     // PI partials: Pc[cls][a] = psi[rows]^T IXI[rows]
     int64_t r0 = t->s_start[a], r1 = t->s_start[a + 1];
-    prob(psi + r0 * n, n, 1, t->IXI + r0 * nc, nc, 0, t->Pc + ((0 * L + a) * n) * nc, nc, (int)n, (int)nc, (int)(r1 - r0));
+    gemm_prob_f64(probs, psi + r0 * n, n, 1, t->IXI + r0 * nc, nc, 0, t->Pc + ((0 * L + a) * n) * nc, nc, (int)n,
+                  (int)nc, (int)(r1 - r0));
     r0 = t->f_start[a]; r1 = t->f_start[a + 1];
-    prob(psi + r0 * n, n, 1, t->IXI + r0 * nc, nc, 0, t->Pc + ((1 * L + a) * n) * nc, nc, (int)n, (int)nc, (int)(r1 - r0));
+    gemm_prob_f64(probs, psi + r0 * n, n, 1, t->IXI + r0 * nc, nc, 0, t->Pc + ((1 * L + a) * n) * nc, nc, (int)n,
+                  (int)nc, (int)(r1 - r0));
     // R2 rows of lead a: XI[rows] sigC_a^T
     r0 = t->s_start[a]; r1 = t->s_start[a + 1];
-    if (r1 > r0) prob(t->XI + r0 * nc, nc, 0, t->sigC + a * n * nc, nc, 1, t->R2 + r0 * n, n, (int)(r1 - r0), (int)n, (int)nc);
+    if (r1 > r0)
+      gemm_prob_f64(probs, t->XI + r0 * nc, nc, 0, t->sigC + a * n * nc, nc, 1, t->R2 + r0 * n, n, (int)(r1 - r0),
+                    (int)n, (int)nc);
     // Omega xi: ZA[a] = OmA[:, sourced of a] XIS[sourced of a]; ZB[a] = OmB[:, free of a] XIS[free of a]
-    r0 = t->s_start[a]; r1 = t->s_start[a + 1];
-    prob(in + t->off_omA + r0, Ns, 0, t->XIS + r0 * nc, nc, 0, t->ZA + a * N * nc, nc, (int)N, (int)nc, (int)(r1 - r0));
+    gemm_prob_f64(probs, in + t->off_omA + r0, Ns, 0, t->XIS + r0 * nc, nc, 0, t->ZA + a * N * nc, nc, (int)N,
+                  (int)nc, (int)(r1 - r0));
     r0 = t->f_start[a]; r1 = t->f_start[a + 1];
     if (Ns > 0)
-      prob(in + t->off_omB + (r0 - Ns), Nf, 0, t->XIS + r0 * nc, nc, 0, t->ZB + a * Ns * nc, nc, (int)Ns, (int)nc, (int)(r1 - r0));
+      gemm_prob_f64(probs, in + t->off_omB + (r0 - Ns), Nf, 0, t->XIS + r0 * nc, nc, 0, t->ZB + a * Ns * nc, nc,
+                    (int)Ns, (int)nc, (int)(r1 - r0));
   }
-  for (size_t b0 = 0; b0 < probs.size(); b0 += ZG_MAX_GEMM) {
-    GemmBatch batch;
-    batch.nprob = (int)std::min<size_t>(ZG_MAX_GEMM, probs.size() - b0);
-    for (int i = 0; i < batch.nprob; ++i) batch.p[i] = probs[b0 + i];
-    prof_begin(t, ZG_PROF_GEMM);
-    ZG_TRY(launch_zgemm_batch(batch, s));
-    prof_end(t, ZG_PROF_GEMM);
-  }
+  prof_begin(t, ZG_PROF_GEMM);
+  ZG_TRY(run_batches<double>(t, probs, &t->ws64, &t->ws64_cap, s));
+  prof_end(t, ZG_PROF_GEMM);
   prof_begin(t, ZG_PROF_FINAL);
-  ZG_TRY(launch_sigma_finalize(d, p, t->T, t->Pc, out, currents ? t->J : nullptr, s));
-  ZG_TRY(launch_psi_finalize(d, p, psi, t->R2, t->ZA, t->ZB, out + t->off_psi, s));
+  ZG_TRY(launch_sigma_finalize<double>(d, p, t->T, n, t->Pc, out, s));
+  if (want_J) ZG_TRY(launch_currents<double>(d, p, t->Pc, t->J, s));
+  ZG_TRY(launch_psi_finalize<double>(d, p, psi, nullptr, n, out + t->off_psi, n, t->R2, t->ZA, t->ZB,
+                                     out + t->off_psi, s));
   prof_end(t, ZG_PROF_FINAL);
   prof_begin(t, ZG_PROF_OMEGA);
-  ZG_TRY(launch_omega(d, p, t->tiles, t->ntiles, t->G, in, out, s));
+  ZG_TRY(launch_omega<double>(d, p, t->tiles, t->ntiles, t->G, in + t->off_omA, in + t->off_omB, out + t->off_omA,
+                              out + t->off_omB, s));
   prof_end(t, ZG_PROF_OMEGA);
+  return ZG_OK;
+}
+
+static int rhs_mixed(zg_traj* t, int stage, const StageParams& p, int dH_mode, double hubbard_U, bool want_J) {
+  const RhsDev<float> d = t->dev_view<float>();
+  const MixedLayout& ml = t->ml;
+  const float2* sig = t->stage32;
+  const float2* psih = t->stage32 + ml.st_psih;
+  const float2* psil = t->stage32 + ml.st_psil;
+  const float2* omA = t->stage32 + ml.st_om;
+  const float2* omB = omA + (int64_t)t->N * t->Ns;
+  float2* out = t->kslot(stage);
+  cudaStream_t s = t->stream;
+  const int64_t n = t->n, N = t->N, Ns = t->Ns, Nf = t->Nf, L = t->L, nc = t->nc, np = t->np;
+  prof_begin(t, ZG_PROF_PREP);
+  ZG_TRY(launch_build_operands_mixed((int)n, (int)np, t->H0, sig, t->dH, dH_mode, hubbard_U, t->Hth, t->Htl, t->BHh,
+                                     t->BHl, t->BSh, t->BSl, s));
+  ZG_TRY(launch_gathers<float>(d, sig, psih, psil, np, t->sigC32, t->G32, s));
+  prof_end(t, ZG_PROF_PREP);
+  // tensor cores: R1 = psi H(t)^T and T = H(t) sigma
+  prof_begin(t, ZG_PROF_GEMM);
+  ZG_TRY(tc_gemm_launch(t->gR1, s));
+  prof_end(t, ZG_PROF_GEMM);
+  prof_begin(t, ZG_PROF_GEMM2);
+  ZG_TRY(tc_gemm_launch(t->gT, s));
+  prof_end(t, ZG_PROF_GEMM2);
+  // SIMT FP32: PI partials, xi sigma^T rows, Omega xi
+  std::vector<GemmProb<float>> probs;
+  for (int a = 0; a < L; ++a) {
+    int64_t r0 = t->s_start[a], r1 = t->s_start[a + 1];
+    gemm_prob_f32(probs, psih + r0 * np, psil + r0 * np, np, 1, t->IXI32 + r0 * nc, nc, 0,
+                  t->Pc32 + ((0 * L + a) * n) * nc, nc, (int)n, (int)nc, (int)(r1 - r0));
+    r0 = t->f_start[a]; r1 = t->f_start[a + 1];
+    gemm_prob_f32(probs, psih + r0 * np, psil + r0 * np, np, 1, t->IXI32 + r0 * nc, nc, 0,
+                  t->Pc32 + ((1 * L + a) * n) * nc, nc, (int)n, (int)nc, (int)(r1 - r0));
+    r0 = t->s_start[a]; r1 = t->s_start[a + 1];
+    if (r1 > r0)
+      gemm_prob_f32(probs, t->XI32 + r0 * nc, nullptr, nc, 0, t->sigC32 + a * n * nc, nc, 1, t->R2_32 + r0 * n, n,
+                    (int)(r1 - r0), (int)n, (int)nc);
+    gemm_prob_f32(probs, omA + r0, nullptr, Ns, 0, t->XIS32 + r0 * nc, nc, 0, t->ZA32 + a * N * nc, nc, (int)N,
+                  (int)nc, (int)(r1 - r0));
+    r0 = t->f_start[a]; r1 = t->f_start[a + 1];
+    if (Ns > 0)
+      gemm_prob_f32(probs, omB + (r0 - Ns), nullptr, Nf, 0, t->XIS32 + r0 * nc, nc, 0, t->ZB32 + a * Ns * nc, nc,
+                    (int)Ns, (int)nc, (int)(r1 - r0));
+  }
+  prof_begin(t, ZG_PROF_SMALL);
+  ZG_TRY(run_batches<float>(t, probs, &t->ws32, &t->ws32_cap, s));
+  prof_end(t, ZG_PROF_SMALL);
+  prof_begin(t, ZG_PROF_FINAL);
+  ZG_TRY(launch_sigma_finalize<float>(d, p, t->T32, np, t->Pc32, out, s));
+  if (want_J) {
+    if (stage == 0)  // the stage-0 input is y itself: currents from the FP64 state
+      ZG_TRY(launch_currents64((int)n, (int)L, (int)N, (int)nc, t->mode_lead, t->lead_cols, t->Y + t->off_psi, t->IXI,
+                               t->hbar, t->J, s));
+    else
+      ZG_TRY(launch_currents<float>(d, p, t->Pc32, t->J, s));
+  }
+  ZG_TRY(launch_psi_finalize<float>(d, p, psih, psil, np, t->R1p, np, t->R2_32, t->ZA32, t->ZB32, out + t->off_psi,
+                                    s));
+  prof_end(t, ZG_PROF_FINAL);
+  prof_begin(t, ZG_PROF_OMEGA);
+  ZG_TRY(launch_omega<float>(d, p, t->tiles, t->ntiles, t->G32, omA, omB, out + t->off_omA, out + t->off_omB, s));
+  prof_end(t, ZG_PROF_OMEGA);
+  return ZG_OK;
+}
+
+int zg_rhs(zg_traj* t, int stage, double ts, double h, const double* delta, int dH_mode, double hubbard_U,
+           double* currents) {
+  ZG_REQUIRE(t && delta, "null argument");
+  ZG_REQUIRE(stage >= 0 && stage < t->stages, "stage %d out of range", stage);
+  ZG_REQUIRE(dH_mode == ZG_DH_NONE || dH_mode == ZG_DH_HUBBARD || (dH_mode == ZG_DH_MATRIX && t->dH_set),
+             "bad dH mode %d (ZG_DH_MATRIX needs zg_set_dH first)", dH_mode);
+  ZG_REQUIRE(t->precision == ZG_PREC_F64 || t->cur_in == nullptr, "zg_stage_input must precede zg_rhs");
+  ZG_CHECK_CUDA(cudaSetDevice(t->dev));
+  StageParams p;
+  p.h = h; p.ts = ts; p.hbar = t->hbar;
+  for (int a = 0; a < ZG_MAX_LEADS; ++a) p.delta[a] = a < t->L ? delta[a] : 0.0;
+  prof_begin(t, ZG_PROF_RHS);
+  if (t->precision == ZG_PREC_F64)
+    ZG_TRY(rhs_f64(t, stage, p, dH_mode, hubbard_U, currents != nullptr));
+  else
+    ZG_TRY(rhs_mixed(t, stage, p, dH_mode, hubbard_U, currents != nullptr));
   prof_end(t, ZG_PROF_RHS);
   if (currents) {
-    ZG_CHECK_CUDA(cudaMemcpyAsync(currents, t->J, L * sizeof(double), cudaMemcpyDeviceToHost, s));
-    ZG_CHECK_CUDA(cudaStreamSynchronize(s));
+    ZG_CHECK_CUDA(cudaMemcpyAsync(currents, t->J, t->L * sizeof(double), cudaMemcpyDeviceToHost, t->stream));
+    ZG_CHECK_CUDA(cudaStreamSynchronize(t->stream));
   }
   return ZG_OK;
 }
@@ -473,16 +743,26 @@ int zg_error_norm2(zg_traj* t, double* err2) {
   cf.n = 0;
   for (int j = 0; j < t->stages; ++j)
     if (t->CT[j] != 0.0) { cf.idx[cf.n] = j; cf.c[cf.n] = t->CT[j]; ++cf.n; }
-  prof_begin(t, ZG_PROF_ERROR);
   const int64_t seg[4] = {0, t->off_psi, t->off_omA, t->S};
-  for (int k = 0; k < 3; ++k)
-    ZG_TRY(launch_terr2_partials_c128(t->Y, t->S, cf, seg[k], seg[k + 1], t->partial + (int64_t)k * t->nblk_err,
-                                      t->nblk_err, t->stream));
+  prof_begin(t, ZG_PROF_ERROR);
+  for (int k = 0; k < 3; ++k) {
+    double* part = t->partial + (int64_t)k * t->nblk_err;
+    if (t->precision == ZG_PREC_F64)
+      ZG_TRY(launch_terr2_partials_c128(t->Y, t->S, cf, seg[k], seg[k + 1], part, t->nblk_err, t->stream));
+    else
+      ZG_TRY(launch_terr2_partials_mixed(t->K32, t->S, cf, seg[k], seg[k + 1], part, t->nblk_err, t->stream));
+  }
   ZG_TRY(launch_reduce_partials(t->partial, t->nblk_err, 3, t->err, t->stream));
   prof_end(t, ZG_PROF_ERROR);
   ZG_CHECK_CUDA(cudaMemcpyAsync(err2, t->err, 3 * sizeof(double), cudaMemcpyDeviceToHost, t->stream));
+  int herr = 0;
+  if (t->tc_err) ZG_CHECK_CUDA(cudaMemcpyAsync(&herr, t->tc_err, sizeof(int), cudaMemcpyDeviceToHost, t->stream));
   ZG_CHECK_CUDA(cudaStreamSynchronize(t->stream));
   prof_collect(t);
+  if (herr != 0) {
+    set_error("a bounded wait in the tensor-core GEMM gave up (code %d)", herr);
+    return ZG_ETIMEOUT;
+  }
   return ZG_OK;
 }
 
@@ -491,10 +771,16 @@ int zg_step_fourth(zg_traj* t) {
   ZG_CHECK_CUDA(cudaSetDevice(t->dev));
   CombineCoefs cf;
   cf.n = 0;
-  for (int j = 0; j <= t->stages; ++j)
-    if (t->CH[j] != 0.0) { cf.idx[cf.n] = j; cf.c[cf.n] = t->CH[j]; ++cf.n; }
   prof_begin(t, ZG_PROF_UPDATE);
-  ZG_TRY(launch_step_fourth_c128(t->Y, t->S, t->stages, cf, t->S, t->stream));
+  if (t->precision == ZG_PREC_F64) {
+    for (int j = 0; j <= t->stages; ++j)
+      if (t->CH[j] != 0.0) { cf.idx[cf.n] = j; cf.c[cf.n] = t->CH[j]; ++cf.n; }
+    ZG_TRY(launch_step_fourth_c128(t->Y, t->S, t->stages, cf, t->S, t->stream));
+  } else {
+    for (int j = 0; j < t->stages; ++j)
+      if (t->CH[j] != 0.0) { cf.idx[cf.n] = j; cf.c[cf.n] = t->CH[j]; ++cf.n; }
+    ZG_TRY(launch_update_mixed(t->Y, t->y32, t->K32, t->S, cf, t->S, t->stream));
+  }
   prof_end(t, ZG_PROF_UPDATE);
   ZG_CHECK_CUDA(cudaStreamSynchronize(t->stream));
   return ZG_OK;
@@ -504,8 +790,17 @@ int zg_get_sigma(zg_traj* t, int slot, double* host) {
   ZG_REQUIRE(t && host, "null argument");
   ZG_REQUIRE(slot >= 0 && slot <= t->stages, "slot %d out of range", slot);
   ZG_CHECK_CUDA(cudaSetDevice(t->dev));
-  ZG_CHECK_CUDA(cudaMemcpyAsync(host, t->slot(slot), (size_t)t->n * t->n * sizeof(double2), cudaMemcpyDeviceToHost,
-                                t->stream));
+  const int64_t nn = (int64_t)t->n * t->n;
+  const double2* src;
+  if (t->precision == ZG_PREC_F64) {
+    src = t->slot(slot);
+  } else if (slot == t->stages) {
+    src = t->Y;
+  } else {
+    ZG_TRY(launch_f32_to_f64(t->kslot(slot), t->sig64, nn, t->stream));
+    src = t->sig64;
+  }
+  ZG_CHECK_CUDA(cudaMemcpyAsync(host, src, nn * sizeof(double2), cudaMemcpyDeviceToHost, t->stream));
   ZG_CHECK_CUDA(cudaStreamSynchronize(t->stream));
   return ZG_OK;
 }

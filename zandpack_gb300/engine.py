@@ -201,8 +201,14 @@ class Propagator:
         TE = math.sqrt(float(e.sum()))
         return TE, J0, e
 
-    def run(self, t0, t1, h, eps, max_attempts=None, replay_h=None, record_sigma=True, on_step=None):
-        """Propagate from t0 until t >= t1 exactly as ``zand`` does; returns histories."""
+    def run(self, t0, t1, h, eps, max_attempts=None, replay_h=None, force_accept=None, record_sigma=True,
+            on_step=None):
+        """Propagate from t0 until t >= t1 exactly as ``zand`` does; returns histories.
+
+        Replay mode (for comparisons on a fixed time grid): ``replay_h[i]`` is
+        the step size of attempt i and, after the last attempt, the final
+        advance; ``force_accept[i]`` overrides the accept decision of attempt i.
+        """
         t = float(t0)
         out = dict(times=[t], sig=[], currents=[], h_hist=[], TE_hist=[], t_attempt=[], accepted=[])
         if record_sigma:
@@ -220,9 +226,11 @@ class Propagator:
                 out["TE_hist"].append(TE)
                 out["t_attempt"].append(t)
                 attempts += 1
-                accepted = TE < eps
+                accepted = TE < eps if force_accept is None else bool(force_accept[attempts - 1])
                 out["accepted"].append(accepted)
                 h = self.tab.hnew(h, TE, eps)
+                if replay_h is not None and attempts < len(replay_h):
+                    h = float(replay_h[attempts])
             out["currents"].append(J0)
             self.traj.step_fourth()
             t += h

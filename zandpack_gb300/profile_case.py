@@ -1,0 +1,40 @@
+"""Run a few Dormand-Prince attempts of a synthetic workload, for profilers.
+
+    python -m zandpack_gb300.profile_case --config c3 --precision mixed --attempts 2
+
+Builds the workload, uploads the initial state, runs ``--warmup`` attempts and
+then ``--attempts`` attempts, and exits; nothing else runs on the GPU.
+"""
+from __future__ import annotations
+
+import argparse
+import time
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--config", default="c3")
+    ap.add_argument("--precision", default="mixed", choices=["f64", "mixed"])
+    ap.add_argument("--attempts", type=int, default=2)
+    ap.add_argument("--warmup", type=int, default=1)
+    args = ap.parse_args()
+    from .engine import Propagator
+    from .workloads import make_workload
+    w = make_workload(args.config)
+    pr = Propagator(w.arrays, w.hbar, w.bias_fn(), hubbard_U=w.hubbard_U, precision=args.precision)
+    pr.set_state(w.arrays["DM_Ortho"])
+    t, h = w.t0, w.stepsize
+    for i in range(args.warmup + args.attempts):
+        t0 = time.perf_counter()
+        TE, _, _ = pr.attempt(t, h)
+        hn = pr.tab.hnew(h, TE, w.eps)
+        if TE < w.eps:
+            pr.traj.step_fourth()
+            t += hn
+        h = hn
+        print("attempt %d: TE=%.3e h=%.4g t=%.4g (%.2f ms host wall)" % (i, TE, h, t, (time.perf_counter() - t0) * 1e3))
+    pr.traj.close()
+
+
+if __name__ == "__main__":
+    main()
