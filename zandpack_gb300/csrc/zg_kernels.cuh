@@ -87,6 +87,7 @@ template <typename T>
 struct GemmBatch {
   int nprob;
   int total_tiles;
+  int bn;                 // tile width chosen by the planner (32 or 64)
   typename cx<T>::t* ws;  // split-K workspace
   GemmProb<T> p[ZG_MAX_GEMM];
 };
@@ -154,8 +155,14 @@ int launch_build_operands_mixed(int n, int np, const double2* H0, const float2* 
                                 double U, float* Hth, float* Htl, float* BHh, float* BHl, float* BSh, float* BSl,
                                 cudaStream_t s);
 // Lead currents in FP64 from the FP64 state: J_a = 2 Re sum_{m in a} sum_k psi[m][C_a[k]] IXI[m][k] / hbar^2
-int launch_currents64(int n, int L, int N, int nc, const int* mode_lead, const int* lead_cols, const double2* psi,
-                      const double2* IXI, double hbar, double* J, cudaStream_t s);
+// row ranges per lead: sourced rows [s[a], s[a+1]), free rows [f[a], f[a+1])
+struct CurRows {
+  int64_t s[ZG_MAX_LEADS + 1];
+  int64_t f[ZG_MAX_LEADS + 1];
+};
+// part: L x 64 doubles of scratch
+int launch_currents64(int n, int L, int nc, const CurRows& rows, const int* lead_cols, const double2* psi,
+                      const double2* IXI, double hbar, double* part, double* J, cudaStream_t s);
 
 // out[0] = FP64 FMA rate, out[1] = FP32 FMA rate, GFLOP/s (2 flops per FMA)
 int measure_peaks(double* out);

@@ -15,9 +15,11 @@ __device__ __forceinline__ typename cx<T>::t czero() {
 }
 
 // =================================================================== GEMM
-// 64x64 output tile per 256-thread block, K staged 8 at a time in shared
-// memory; thread (tx, ty) owns rows ty+16i and columns tx+16j (i, j < 4).
-#define ZT 64
+// Output tile of BM x BN complex per 256-thread block, K staged 8 at a time
+// in shared memory; TX = BN/4 threads along N, TY = 256/TX along M, thread
+// (tx, ty) owns rows ty+TY*i and columns tx+TX*j (i, j < 4).  BN = 64 gives
+// 64x64 tiles; BN = 32 gives 128x32 tiles for the products whose N is the
+// coupling width (n_c <= 32), which would leave half of a 64-wide tile idle.
 #define ZK 8
 
 template <typename T>
@@ -37,21 +39,22 @@ __device__ __forceinline__ typename cx<T>::t load_opB(const GemmProb<T>& P, int 
   return P.opB == 2 ? cconj(v) : v;
 }
 
-template <typename T>
+template <typename T, int BN>
 __global__ void __launch_bounds__(256) k_zgemm(const __grid_constant__ GemmBatch<T> batch) {
   using C = typename cx<T>::t;
+  constexpr int TX = BN / 4, TY = 256 / TX, BM = 4 * TY;
   const int tile = blockIdx.x;
   int pi = 0;
   while (pi + 1 < batch.nprob && tile >= batch.p[pi + 1].tile_begin) ++pi;
   const GemmProb<T>& P = batch.p[pi];
   const int ltk = tile - P.tile_begin;
   const int split = ltk / P.tiles_mn, lt = ltk % P.tiles_mn;
-  const int m0 = (lt / P.tiles_n) * ZT, n0 = (lt % P.tiles_n) * ZT;
+  const int m0 = (lt / P.tiles_n) * BM, n0 = (lt % P.tiles_n) * BN;
   const int kb0 = split * P.kchunk;
   const int kb1 = min(P.K, kb0 + P.kchunk);
-  __shared__ C As[ZK][ZT];
-  __shared__ C Bs[ZK][ZT];
-  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  __shared__ C As[ZK][BM];
+  __shared__ C Bs[ZK][BN];
+  const int tid = threadIdx.x, tx = tid % TX, ty = tid / TX;
   C acc[4][4];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
@@ -59,12 +62,17 @@ __global__ void __launch_bounds__(256) k_zgemm(const __grid_constant__ GemmBatch
     for (int j = 0; j < 4; ++j) acc[i][j] = czero<T>();
   for (int k0 = kb0; k0 < kb1; k0 += ZK) {
 #pragma unroll
-    for (int r = 0; r < 2; ++r) {
+    for (int r = 0; r < BM / 32; ++r) {
       const int idx = tid + 256 * r;
-      int m, k, n;
-      if (P.opA == 0) { m = idx >> 3; k = idx & 7; } else { m = idx & 63; k = idx >> 6; }
+      int m, k;
+      if (P.opA == 0) { m = idx >> 3; k = idx & 7; } else { m = idx % BM; k = idx / BM; }
       As[k][m] = k0 + k < kb1 ? load_opA(P, m0 + m, k0 + k) : czero<T>();
-      if (P.opB == 0) { n = idx & 63; k = idx >> 6; } else { n = idx >> 3; k = idx & 7; }
+    }
+#pragma unroll
+    for (int r = 0; r < BN / 32; ++r) {
+      const int idx = tid + 256 * r;
+      int n, k;
+      if (P.opB == 0) { n = idx % BN; k = idx / BN; } else { n = idx >> 3; k = idx & 7; }
       Bs[k][n] = k0 + k < kb1 ? load_opB(P, k0 + k, n0 + n) : czero<T>();
     }
     __syncthreads();
@@ -72,9 +80,9 @@ __global__ void __launch_bounds__(256) k_zgemm(const __grid_constant__ GemmBatch
     for (int kk = 0; kk < ZK; ++kk) {
       C a[4], b[4];
 #pragma unroll
-      for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
+      for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + TY * i];
 #pragma unroll
-      for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx + 16 * j];
+      for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx + TX * j];
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
@@ -85,11 +93,11 @@ __global__ void __launch_bounds__(256) k_zgemm(const __grid_constant__ GemmBatch
   const bool use_beta = (P.beta.x != (T)0 || P.beta.y != (T)0);
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
-    const int m = m0 + ty + 16 * i;
+    const int m = m0 + ty + TY * i;
     if (m >= P.M) continue;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      const int n = n0 + tx + 16 * j;
+      const int n = n0 + tx + TX * j;
       if (n >= P.N) continue;
       if (P.ksplit > 1) {  // partial product of this K chunk, reduced later in split order
         batch.ws[P.ws_off + ((int64_t)split * P.M + m) * P.N + n] = acc[i][j];
@@ -121,6 +129,11 @@ __global__ void k_zgemm_reduce(const __grid_constant__ GemmBatch<T> batch) {
 
 template <typename T>
 int64_t plan_zgemm_batch(GemmBatch<T>& b) {
+  // tile width: 32 when every problem is at most 32 wide
+  int maxN = 0;
+  for (int i = 0; i < b.nprob; ++i) maxN = b.p[i].N > maxN ? b.p[i].N : maxN;
+  b.bn = maxN <= 32 ? 32 : 64;
+  const int BN = b.bn, BM = 4 * (256 / (BN / 4));
   // A problem with few output tiles and a long K would serialise on a handful
   // of CTAs: split its K into chunks of >= 256 until it has ~2 CTAs per SM.
   const int64_t target = 2 * 152;
@@ -128,7 +141,7 @@ int64_t plan_zgemm_batch(GemmBatch<T>& b) {
   int64_t ws = 0;
   for (int i = 0; i < b.nprob; ++i) {
     GemmProb<T>& P = b.p[i];
-    const int tm = (P.M + ZT - 1) / ZT, tn = (P.N + ZT - 1) / ZT;
+    const int tm = (P.M + BM - 1) / BM, tn = (P.N + BN - 1) / BN;
     P.tiles_n = tn > 0 ? tn : 1;
     P.tiles_mn = tm * tn > 0 ? tm * tn : 1;
     P.ksplit = 1;
@@ -164,7 +177,10 @@ int launch_zgemm_batch(GemmBatch<T>& b, int64_t ws_capacity, cudaStream_t s) {
   ZG_REQUIRE(need <= ws_capacity && (need == 0 || b.ws), "split-K workspace too small (%lld > %lld)",
              (long long)need, (long long)ws_capacity);
   if (b.total_tiles == 0) return ZG_OK;
-  k_zgemm<T><<<b.total_tiles, 256, 0, s>>>(b);
+  if (b.bn == 32)
+    k_zgemm<T, 32><<<b.total_tiles, 256, 0, s>>>(b);
+  else
+    k_zgemm<T, 64><<<b.total_tiles, 256, 0, s>>>(b);
   ZG_CHECK_LAUNCH();
   count_launch();
   if (need > 0) {
@@ -298,27 +314,45 @@ int launch_currents(const RhsDev<T>& d, const StageParams& p, const typename cx<
   return ZG_OK;
 }
 
-// J_a from the FP64 state: 2 Re sum_{m in lead a} sum_k psi[m][C_a[k]] IXI[m][k] / hbar^2
-__global__ void k_currents64(int n, int N, int nc, const int* __restrict__ mode_lead, const int* __restrict__ lead_cols,
-                             const double2* __restrict__ psi, const double2* __restrict__ IXI, double hbar,
-                             double* __restrict__ J) {
-  const int a = blockIdx.x;
+// J_a from the FP64 state: 2 Re sum_{m in lead a} sum_k psi[m][C_a[k]] IXI[m][k] / hbar^2.
+// Grid (CUR_CHUNKS, L): chunk c of lead a sums a strided share of the lead's
+// (row, k) pairs; the chunks of a lead are then added in a fixed order.
+#define CUR_CHUNKS 64
+__global__ void __launch_bounds__(256) k_currents64_part(int n, int nc, CurRows rows,
+                                                         const int* __restrict__ lead_cols,
+                                                         const double2* __restrict__ psi,
+                                                         const double2* __restrict__ IXI, double* __restrict__ part) {
+  const int a = blockIdx.y;
+  const int64_t s0 = rows.s[a], ns = rows.s[a + 1] - s0;
+  const int64_t f0 = rows.f[a], nf = rows.f[a + 1] - f0;
+  const int64_t tot = (ns + nf) * nc;
   double s = 0.0;
-  for (int64_t e = threadIdx.x; e < (int64_t)N * nc; e += blockDim.x) {
-    const int64_t m = e / nc;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = e / nc;
     const int k = (int)(e % nc);
-    if (mode_lead[m] != a) continue;
+    const int64_t m = r < ns ? s0 + r : f0 + (r - ns);
     const double2 ps = psi[m * n + lead_cols[a * nc + k]];
-    const double2 ix = IXI[e];
+    const double2 ix = IXI[m * nc + k];
     s += ps.x * ix.x - ps.y * ix.y;
   }
   s = block_sum256_d(s);
-  if (threadIdx.x == 0) J[a] = 2.0 * s / (hbar * hbar);
+  if (threadIdx.x == 0) part[a * CUR_CHUNKS + blockIdx.x] = s;
 }
 
-int launch_currents64(int n, int L, int N, int nc, const int* mode_lead, const int* lead_cols, const double2* psi,
-                      const double2* IXI, double hbar, double* J, cudaStream_t s) {
-  k_currents64<<<L, 256, 0, s>>>(n, N, nc, mode_lead, lead_cols, psi, IXI, hbar, J);
+__global__ void k_currents64_final(const double* __restrict__ part, double hbar, double* __restrict__ J) {
+  if (threadIdx.x != 0) return;
+  const int a = blockIdx.x;
+  double s = 0.0;
+  for (int c = 0; c < CUR_CHUNKS; ++c) s += part[a * CUR_CHUNKS + c];
+  J[a] = 2.0 * s / (hbar * hbar);
+}
+
+int launch_currents64(int n, int L, int nc, const CurRows& rows, const int* lead_cols, const double2* psi,
+                      const double2* IXI, double hbar, double* part, double* J, cudaStream_t s) {
+  k_currents64_part<<<dim3(CUR_CHUNKS, L), 256, 0, s>>>(n, nc, rows, lead_cols, psi, IXI, part);
+  ZG_CHECK_LAUNCH();
+  count_launch();
+  k_currents64_final<<<L, 32, 0, s>>>(part, hbar, J);
   ZG_CHECK_LAUNCH();
   count_launch();
   return ZG_OK;
@@ -386,8 +420,8 @@ __global__ void __launch_bounds__(256) k_omega(const RhsDev<T> d, const StagePar
                                                typename cx<T>::t* __restrict__ omB_out) {
   using C = typename cx<T>::t;
   const OmTile t = tiles[blockIdx.x];
-  __shared__ C As[ZK][ZT];
-  __shared__ C Bs[ZK][ZT];
+  __shared__ C As[ZK][64];
+  __shared__ C Bs[ZK][64];
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   const int nc = d.nc;
   const int colmode0 = (t.blk == 0 ? 0 : d.Ns) + t.col0;  // absolute mode of local column col0

@@ -83,7 +83,7 @@ struct zg_traj {
   // FP64 scratch
   double2 *Ht = nullptr, *dH = nullptr, *T = nullptr, *Pc = nullptr, *sigC = nullptr, *G = nullptr, *R2 = nullptr,
           *ZA = nullptr, *ZB = nullptr;
-  double *J = nullptr, *partial = nullptr, *err = nullptr;
+  double *J = nullptr, *Jpart = nullptr, *partial = nullptr, *err = nullptr;
   int nblk_err = 0;
   bool dH_set = false;
   // ---- mixed path
@@ -174,7 +174,8 @@ static void free_traj(zg_traj* t) {
       }
   void* ptrs[] = {t->H0, t->Xp, t->Xm, t->GLP, t->dGP, t->XI, t->IXI, t->XIS, t->U, t->V, t->mode_lead,
                   t->lead_cols, t->colmap, t->tiles, t->Y, t->Ystage, t->Ht, t->dH, t->T, t->Pc, t->sigC,
-                  t->G, t->R2, t->ZA, t->ZB, t->J, t->partial, t->err, t->Xp32, t->Xm32, t->GLP32, t->dGP32,
+                  t->G, t->R2, t->ZA, t->ZB, t->J, t->Jpart, t->partial, t->err, t->Xp32, t->Xm32, t->GLP32,
+                  t->dGP32,
                   t->XI32, t->XIS32, t->IXI32, t->U32, t->V32, t->y32, t->K32, t->stage32, t->Hth, t->Htl, t->BHh,
                   t->BHl, t->BSh, t->BSl, t->T32, t->R1p, t->Pc32, t->sigC32, t->G32, t->R2_32, t->ZA32, t->ZB32,
                   t->conv64, t->sig64, t->tc_err, t->ws64, t->ws32};
@@ -394,6 +395,7 @@ int zg_traj_create(int device, const zg_layout* Lo, int precision, zg_traj** out
   ZG_STEP(upload<OmTile>(t->tiles, tiles.data(), tiles.size(), t->stream));
   ZG_STEP(dalloc(&t->dH, n * n));
   ZG_STEP(dalloc(&t->J, L));
+  ZG_STEP(dalloc(&t->Jpart, L * 64));
   t->nblk_err = terr2_nblocks(t->S);
   ZG_STEP(dalloc(&t->partial, 3 * (size_t)t->nblk_err));
   ZG_STEP(dalloc(&t->err, 3));
@@ -572,12 +574,21 @@ static void gemm_prob_f32(std::vector<GemmProb<float>>& v, const float2* A, cons
 // split-K workspace of one precision, grown on first use (the first right-hand
 // side of a trajectory sizes it; later calls never allocate)
 template <typename R>
-static int run_batches(zg_traj* t, std::vector<GemmProb<R>>& probs, typename cx<R>::t** ws, int64_t* cap,
+static int run_batches(zg_traj* t, std::vector<GemmProb<R>>& all, typename cx<R>::t** ws, int64_t* cap,
                        cudaStream_t s) {
-  for (size_t b0 = 0; b0 < probs.size(); b0 += ZG_MAX_GEMM) {
+  // problems at most 32 wide (the n_c-wide products) run with 128x32 tiles
+  std::vector<GemmProb<R>> probs;
+  for (int pass = 0; pass < 2; ++pass)
+    for (const auto& P : all)
+      if ((P.N <= 32) == (pass == 0)) probs.push_back(P);
+  size_t narrow = 0;
+  for (const auto& P : all) narrow += P.N <= 32;
+  for (size_t b0 = 0; b0 < probs.size();) {
     GemmBatch<R> batch;
-    batch.nprob = (int)std::min<size_t>(ZG_MAX_GEMM, probs.size() - b0);
+    const size_t end = b0 < narrow ? narrow : probs.size();
+    batch.nprob = (int)std::min<size_t>(ZG_MAX_GEMM, end - b0);
     for (int i = 0; i < batch.nprob; ++i) batch.p[i] = probs[b0 + i];
+    b0 += batch.nprob;
     const int64_t need = plan_zgemm_batch<R>(batch);
     if (need > *cap) {
       ZG_CHECK_CUDA(cudaStreamSynchronize(s));
@@ -698,8 +709,12 @@ static int rhs_mixed(zg_traj* t, int stage, const StageParams& p, int dH_mode, d
   ZG_TRY(launch_sigma_finalize<float>(d, p, t->T32, np, t->Pc32, out, s));
   if (want_J) {
     if (stage == 0)  // the stage-0 input is y itself: currents from the FP64 state
-      ZG_TRY(launch_currents64((int)n, (int)L, (int)N, (int)nc, t->mode_lead, t->lead_cols, t->Y + t->off_psi, t->IXI,
-                               t->hbar, t->J, s));
+    {
+      CurRows rows;
+      for (int a = 0; a <= L; ++a) { rows.s[a] = t->s_start[a]; rows.f[a] = t->f_start[a]; }
+      ZG_TRY(launch_currents64((int)n, (int)L, (int)nc, rows, t->lead_cols, t->Y + t->off_psi, t->IXI, t->hbar,
+                               t->Jpart, t->J, s));
+    }
     else
       ZG_TRY(launch_currents<float>(d, p, t->Pc32, t->J, s));
   }
