@@ -52,32 +52,51 @@ __global__ void __launch_bounds__(256) k_zgemm(const __grid_constant__ GemmBatch
   const int m0 = (lt / P.tiles_n) * BM, n0 = (lt % P.tiles_n) * BN;
   const int kb0 = split * P.kchunk;
   const int kb1 = min(P.K, kb0 + P.kchunk);
-  __shared__ C As[ZK][BM];
-  __shared__ C Bs[ZK][BN];
+  // K staged ZKG at a time; the next stage's global loads are issued into
+  // registers before the current stage is computed, hiding their latency
+  constexpr int ZKG = 16, RA = BM * ZKG / 256, RB = BN * ZKG / 256;
+  // rows padded by one element: K-contiguous operands are stored column-wise
+  // (16 threads with consecutive k, same m), which without padding would hit
+  // one bank 16 times
+  __shared__ C As[ZKG][BM + 1];
+  __shared__ C Bs[ZKG][BN + 1];
   const int tid = threadIdx.x, tx = tid % TX, ty = tid / TX;
   C acc[4][4];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
     for (int j = 0; j < 4; ++j) acc[i][j] = czero<T>();
-  for (int k0 = kb0; k0 < kb1; k0 += ZK) {
+  int am[RA], ak[RA], bn_[RB], bk[RB];
 #pragma unroll
-    for (int r = 0; r < BM / 32; ++r) {
-      const int idx = tid + 256 * r;
-      int m, k;
-      if (P.opA == 0) { m = idx >> 3; k = idx & 7; } else { m = idx % BM; k = idx / BM; }
-      As[k][m] = k0 + k < kb1 ? load_opA(P, m0 + m, k0 + k) : czero<T>();
-    }
+  for (int r = 0; r < RA; ++r) {
+    const int idx = tid + 256 * r;
+    if (P.opA == 0) { am[r] = idx >> 4; ak[r] = idx & 15; } else { am[r] = idx % BM; ak[r] = idx / BM; }
+  }
 #pragma unroll
-    for (int r = 0; r < BN / 32; ++r) {
-      const int idx = tid + 256 * r;
-      int n, k;
-      if (P.opB == 0) { n = idx % BN; k = idx / BN; } else { n = idx >> 3; k = idx & 7; }
-      Bs[k][n] = k0 + k < kb1 ? load_opB(P, k0 + k, n0 + n) : czero<T>();
-    }
+  for (int r = 0; r < RB; ++r) {
+    const int idx = tid + 256 * r;
+    if (P.opB == 0) { bn_[r] = idx % BN; bk[r] = idx / BN; } else { bn_[r] = idx >> 4; bk[r] = idx & 15; }
+  }
+  C ra[RA], rb[RB];
+#pragma unroll
+  for (int r = 0; r < RA; ++r) ra[r] = kb0 + ak[r] < kb1 ? load_opA(P, m0 + am[r], kb0 + ak[r]) : czero<T>();
+#pragma unroll
+  for (int r = 0; r < RB; ++r) rb[r] = kb0 + bk[r] < kb1 ? load_opB(P, kb0 + bk[r], n0 + bn_[r]) : czero<T>();
+  for (int k0 = kb0; k0 < kb1; k0 += ZKG) {
+#pragma unroll
+    for (int r = 0; r < RA; ++r) As[ak[r]][am[r]] = ra[r];
+#pragma unroll
+    for (int r = 0; r < RB; ++r) Bs[bk[r]][bn_[r]] = rb[r];
     __syncthreads();
+    const int k1 = k0 + ZKG;
+    if (k1 < kb1) {
 #pragma unroll
-    for (int kk = 0; kk < ZK; ++kk) {
+      for (int r = 0; r < RA; ++r) ra[r] = k1 + ak[r] < kb1 ? load_opA(P, m0 + am[r], k1 + ak[r]) : czero<T>();
+#pragma unroll
+      for (int r = 0; r < RB; ++r) rb[r] = k1 + bk[r] < kb1 ? load_opB(P, k1 + bk[r], n0 + bn_[r]) : czero<T>();
+    }
+#pragma unroll
+    for (int kk = 0; kk < ZKG; ++kk) {
       C a[4], b[4];
 #pragma unroll
       for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + TY * i];
@@ -420,8 +439,11 @@ __global__ void __launch_bounds__(256) k_omega(const RhsDev<T> d, const StagePar
                                                typename cx<T>::t* __restrict__ omB_out) {
   using C = typename cx<T>::t;
   const OmTile t = tiles[blockIdx.x];
-  __shared__ C As[ZK][64];
-  __shared__ C Bs[ZK][64];
+  // K (the 2 n_c source terms) staged ZKO at a time, next stage prefetched into registers
+  constexpr int ZKO = sizeof(T) == 4 ? 32 : 16, RO = 64 * ZKO / 256;
+  // padded rows: stores run along k (column-wise), which would otherwise hit one bank
+  __shared__ C As[ZKO][64 + 1];
+  __shared__ C Bs[ZKO][64 + 1];
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   const int nc = d.nc;
   const int colmode0 = (t.blk == 0 ? 0 : d.Ns) + t.col0;  // absolute mode of local column col0
@@ -431,12 +453,12 @@ __global__ void __launch_bounds__(256) k_omega(const RhsDev<T> d, const StagePar
 #pragma unroll
     for (int j = 0; j < 4; ++j) acc[i][j] = czero<T>();
   const int kbeg = t.term1 ? 0 : nc, kend = t.term2 ? 2 * nc : nc;
-  for (int k0 = kbeg; k0 < kend; k0 += ZK) {
+  C ra[RO], rb[RO];
+  auto fetch = [&](int k0) {
 #pragma unroll
-    for (int r = 0; r < 2; ++r) {
+    for (int r = 0; r < RO; ++r) {
       const int idx = tid + 256 * r;
-      const int rr = idx >> 3, kk = idx & 7;
-      const int k = k0 + kk;
+      const int rr = idx / ZKO, k = k0 + idx % ZKO;
       C av = czero<T>(), bv = czero<T>();
       if (k < kend) {
         if (rr < t.nrows) {
@@ -448,12 +470,22 @@ __global__ void __launch_bounds__(256) k_omega(const RhsDev<T> d, const StagePar
           bv = k < nc ? d.U[l * nc + k] : cconj(G[(l * d.L + t.a) * nc + (k - nc)]);
         }
       }
-      As[kk][rr] = av;
-      Bs[kk][rr] = bv;
+      ra[r] = av;
+      rb[r] = bv;
+    }
+  };
+  fetch(kbeg);
+  for (int k0 = kbeg; k0 < kend; k0 += ZKO) {
+#pragma unroll
+    for (int r = 0; r < RO; ++r) {
+      const int idx = tid + 256 * r;
+      As[idx % ZKO][idx / ZKO] = ra[r];
+      Bs[idx % ZKO][idx / ZKO] = rb[r];
     }
     __syncthreads();
+    if (k0 + ZKO < kend) fetch(k0 + ZKO);
 #pragma unroll
-    for (int kk = 0; kk < ZK; ++kk) {
+    for (int kk = 0; kk < ZKO; ++kk) {
       C a[4], b[4];
 #pragma unroll
       for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
