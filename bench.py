@@ -232,6 +232,8 @@ def run_ours(args):
     if args.precision == "mixed" and not args.no_f64_ref:
         out["f64_path"] = f64_reference_timing(w, dev, state, value, ms / args.steps)
     if rank == 0:
+        if args.ensemble > 0:
+            out["ensemble"] = run_ensemble(args)
         out["cpu_baseline"] = cpu_baseline(args, w, adv_total / (args.steps * ws))
         print(json.dumps(out))
     if ws > 1:
@@ -404,6 +406,21 @@ def cpu_baseline(args, w, adv_per_attempt):
             "s_per_rhs": per_stage}
 
 
+def run_ensemble(args):
+    """The serving ensemble (512 independent trajectories, Poisson arrivals at
+    50/s, sizes n in {64..512}, 2-3 leads, each with its own step size), served
+    with continuous batching; p50/p99 latency from arrival to completion."""
+    from zandpack_gb300.serve import Server, c4_estimate
+    from zandpack_gb300.workloads import c4_requests, c4_workload
+    reqs = c4_requests(args.ensemble, rate=50.0, seed=1004, t_span=args.ensemble_fs)
+    srv = Server(c4_workload, c4_estimate, max_slots=args.slots, precision=args.precision, keep_sigma=False)
+    res, stats = srv.run(reqs)
+    stats["t_span_fs"] = args.ensemble_fs
+    stats["rate_per_s"] = 50.0
+    stats["errors"] = sorted({r.error for r in res if r.error})[:3]
+    return stats
+
+
 def run_reference(args):
     ws, rank = _dist()
     if rank != 0:
@@ -433,6 +450,9 @@ def main():
     ap.add_argument("--config", default="c3")
     ap.add_argument("--precision", default="mixed", choices=["f64", "mixed"])
     ap.add_argument("--no-f64-ref", action="store_true", help="skip timing the FP64 path beside the mixed one")
+    ap.add_argument("--ensemble", type=int, default=512, help="requests of the serving ensemble (0: skip)")
+    ap.add_argument("--ensemble-fs", type=float, default=1.0, help="simulated fs per ensemble trajectory")
+    ap.add_argument("--slots", type=int, default=32, help="concurrent trajectories of the ensemble")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -117,6 +117,29 @@ int zg_error_norm2(zg_traj* t, double* err2);
 
 /* y <- sum_j CH_j Y_j (step_fourth_*, Zandpack/mpi_funcs.py:254-259). */
 int zg_step_fourth(zg_traj* t);
+
+/* Analytic lead biases evaluated inside the library: Delta_a(t) = w[a] V(t) with
+ *   ZG_BIAS_ZERO: V = 0;  ZG_BIAS_EXP_RAMP: V0 (1 - exp(-t/tau));
+ *   ZG_BIAS_GAUSS: V0 exp(-(t-tc)^2 / (2 sigma^2));  ZG_BIAS_SIN: V0 sin(2 pi f t);
+ *   ZG_BIAS_STEP: V0 for t > 0, else 0;  ZG_BIAS_BOX: V0 (tanh(t/tau) - tanh((t-tc)/tau))/2.
+ * The +V/2, -V/2 split of make_constant_bias (Zandpack/Pulses.py:81-88) is
+ * w = {0.5, -0.5, 0, ...}; box_pulse is Zandpack/Pulses.py:72-74. */
+enum { ZG_BIAS_ZERO = 0, ZG_BIAS_EXP_RAMP = 1, ZG_BIAS_GAUSS = 2, ZG_BIAS_SIN = 3, ZG_BIAS_STEP = 4,
+       ZG_BIAS_BOX = 5 };
+typedef struct {
+  int32_t kind;
+  double V0, tau, tc, sigma, f;
+  double w[ZG_MAX_LEADS];
+} zg_bias;
+
+/* One attempt of the zand controller (Zandpack/mpi/zand:301-430) with
+ * library-evaluated bias and dH (dH_mode ZG_DH_NONE or ZG_DH_HUBBARD):
+ * all stages from the stored y at time *t with step *h, the error norm,
+ * accept iff TE < eps; on acceptance y is updated and *t advances by the new
+ * step size; *h becomes 0.9 h (eps/TE)^(1/5) either way.  currents (may be
+ * NULL) receives the stage-0 lead currents.  One host call per attempt. */
+int zg_attempt(zg_traj* t, double* time, double* h, double eps, const zg_bias* bias, int dH_mode,
+               double hubbard_U, double* TE, int* accepted, double* currents);
 /* Download sigma (n*n complex) of a state slot; the DM the reference records
  * after every accepted step (Zandpack/mpi/zand:428-430). */
 int zg_get_sigma(zg_traj* t, int slot, double* host);

@@ -42,8 +42,18 @@ class zg_layout(C.Structure):
                 ("XIT2", C.c_void_p)]
 
 
+ZG_BIAS = {"zero": 0, "exp_ramp": 1, "gauss": 2, "sin": 3, "step": 4, "box": 5}
+
+
+class zg_bias(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("V0", C.c_double), ("tau", C.c_double), ("tc", C.c_double),
+                ("sigma", C.c_double), ("f", C.c_double), ("w", C.c_double * ZG_MAX_LEADS)]
+
+
 _P = C.c_void_p
 _SIGS = {
+    "zg_attempt": ([_P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_double, C.POINTER(zg_bias), C.c_int,
+                    C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_int), _P], C.c_int),
     "zg_last_error": ([], C.c_char_p),
     "zg_version": ([], C.c_int),
     "zg_launch_count": ([], C.c_longlong),

@@ -5,7 +5,10 @@
 #include <stdarg.h>
 #include <string.h>
 
+#include <math.h>
+
 #include <algorithm>
+#include <cmath>
 #include <vector>
 
 #include "zg_kernels.cuh"
@@ -798,6 +801,57 @@ int zg_step_fourth(zg_traj* t) {
   }
   prof_end(t, ZG_PROF_UPDATE);
   ZG_CHECK_CUDA(cudaStreamSynchronize(t->stream));
+  return ZG_OK;
+}
+
+}  // extern "C"
+
+static double bias_value(const zg_bias& b, double t, int a) {
+  double V = 0.0;
+  switch (b.kind) {
+    case ZG_BIAS_ZERO: V = 0.0; break;
+    case ZG_BIAS_EXP_RAMP: V = b.V0 * (1.0 - exp(-t / b.tau)); break;
+    case ZG_BIAS_GAUSS: V = b.V0 * exp(-(t - b.tc) * (t - b.tc) / (2.0 * b.sigma * b.sigma)); break;
+    case ZG_BIAS_SIN: V = b.V0 * sin(2.0 * M_PI * b.f * t); break;
+    case ZG_BIAS_STEP: V = t > 0.0 ? b.V0 : 0.0; break;
+    case ZG_BIAS_BOX: V = b.V0 * (tanh(t / b.tau) - tanh((t - b.tc) / b.tau)) / 2.0; break;
+    default: V = 0.0;
+  }
+  return b.w[a] * V;
+}
+
+extern "C" {
+
+int zg_attempt(zg_traj* t, double* time, double* h, double eps, const zg_bias* bias, int dH_mode, double hubbard_U,
+               double* TE, int* accepted, double* currents) {
+  ZG_REQUIRE(t && time && h && bias && TE && accepted, "null argument");
+  ZG_REQUIRE(dH_mode == ZG_DH_NONE || dH_mode == ZG_DH_HUBBARD, "zg_attempt needs dH_mode NONE or HUBBARD");
+  ZG_REQUIRE(bias->kind >= ZG_BIAS_ZERO && bias->kind <= ZG_BIAS_BOX, "unknown bias kind %d", bias->kind);
+  const double t0 = *time, h0 = *h;
+  double delta[ZG_MAX_LEADS];
+  for (int i = 0; i < t->stages; ++i) {
+    ZG_TRY(zg_stage_input(t, i));
+    const double ts = t0 + t->A[i] * h0;
+    for (int a = 0; a < ZG_MAX_LEADS; ++a) delta[a] = a < t->L ? bias_value(*bias, ts, a) : 0.0;
+    ZG_TRY(zg_rhs(t, i, ts, h0, delta, dH_mode, hubbard_U, (i == 0 && currents) ? currents : nullptr));
+  }
+  double e2[3];
+  ZG_TRY(zg_error_norm2(t, e2));
+  const double te = sqrt(e2[0] + e2[1] + e2[2]);
+  *TE = te;
+  if (!std::isfinite(te)) {
+    set_error("error norm is not finite (%g)", te);
+    return ZG_ENONFINITE;
+  }
+  const int acc = te < eps;
+  *accepted = acc;
+  // h <- 0.9 h (eps/TE)^(1/5) (Zandpack/mpi_RK4pars_dev.py:148-149), after every attempt
+  const double hn = te > 0.0 ? 0.9 * h0 * pow(eps / te, 0.2) : INFINITY;
+  if (acc) {
+    ZG_TRY(zg_step_fourth(t));
+    *time = t0 + hn;  // the reference advances by the step size proposed next
+  }
+  *h = hn;
   return ZG_OK;
 }
 

@@ -136,8 +136,47 @@ class Trajectory:
         check(lib().zg_error_norm2(self._h, _ptr(e)))
         return e
 
+    def attempt_native(self, t, h, eps, bias, hubbard_U=None, currents=True):
+        """One controller attempt inside the library (``zg_attempt``): bias is
+        a ``zg_bias`` (see ``native_bias``), dH the device Hubbard term or none.
+        Returns (TE, accepted, t_new, h_new, stage-0 currents)."""
+        tt, hh = C.c_double(t), C.c_double(h)
+        TE, acc = C.c_double(), C.c_int()
+        mode = _lib.ZG_DH_HUBBARD if hubbard_U is not None else _lib.ZG_DH_NONE
+        Jp = _ptr(self._J) if currents else None
+        check(lib().zg_attempt(self._h, C.byref(tt), C.byref(hh), float(eps), C.byref(bias), mode,
+                               float(hubbard_U or 0.0), C.byref(TE), C.byref(acc), Jp))
+        return TE.value, bool(acc.value), tt.value, hh.value, (self._J.copy() if currents else None)
+
+    def get_sigma(self):
+        buf = np.empty((self.layout.n, self.layout.n), np.complex128)
+        check(lib().zg_get_sigma(self._h, self.stages, _ptr(buf)))
+        return buf
+
     def step_fourth(self):
         check(lib().zg_step_fourth(self._h))
+
+
+def native_bias(spec, n_leads):
+    """``zg_bias`` for the analytic bias specifications of ``workloads``
+    (exp_ramp, gauss, sin: +V/2 on lead 0, -V/2 on lead 1; step_lead0: V on
+    lead 0; zero)."""
+    b = _lib.zg_bias()
+    k = spec["kind"]
+    w = [0.0] * _lib.ZG_MAX_LEADS
+    if k in ("exp_ramp", "gauss", "sin"):
+        w[0], w[1] = 0.5, -0.5
+    elif k == "step_lead0":
+        w[0] = 1.0
+    for i in range(_lib.ZG_MAX_LEADS):
+        b.w[i] = w[i] if i < n_leads else 0.0
+    b.kind = _lib.ZG_BIAS["step" if k == "step_lead0" else k]
+    b.V0 = float(spec.get("V0", 0.0))
+    b.tau = float(spec.get("tau", 1.0))
+    b.tc = float(spec.get("tc", 0.0))
+    b.sigma = float(spec.get("sigma", 1.0))
+    b.f = float(spec.get("f", 0.0))
+    return b
 
 
 class Propagator:

@@ -1,0 +1,178 @@
+"""Serving many independent propagations on one GPU (continuous batching).
+
+Requests arrive as a stream (their ``arrival`` times, seconds).  The server
+admits a request as soon as a slot is free and its estimated device footprint
+fits the HBM budget; an admitted request is built (host input preparation),
+given its own trajectory on the device -- its own CUDA stream, state and step
+size -- and propagated by a worker thread that calls one ``zg_attempt`` per
+Dormand-Prince attempt (the library releases the Python GIL during each
+call).  Trajectories therefore overlap on the GPU while requests that arrive
+later wait for memory or a slot.  Each result is the final sigma, the last
+lead currents, the number of attempts and the latency (completion minus
+arrival).
+
+Results do not depend on what else runs: trajectories share no device buffers
+and every kernel is deterministic, so a trajectory computed in the mix is
+identical to the same trajectory computed alone.
+"""
+from __future__ import annotations
+
+import dataclasses
+import queue
+import threading
+import time
+from typing import Callable, List, Optional
+
+import numpy as np
+
+from .engine import Trajectory, native_bias
+from .layout import CompactLayout
+
+
+def footprint_bytes(n, N, Ns, nc, L, precision="mixed"):
+    """Device bytes of one trajectory (state slots, stage buffers, operands and
+    scratch) as zg_traj_create allocates them."""
+    Nf = N - Ns
+    S = n * n + N * n + N * Ns + Ns * Nf
+    np_ = (n + 15) // 16 * 16
+    const = 16 * (n * n + N * (5 + 5 * nc))
+    if precision == "f64":
+        state = 16 * S * 8 + 16 * S
+        scratch = 16 * (3 * n * n + 3 * L * n * nc + N * L * nc + Ns * n + L * (N + Ns) * nc)
+    else:
+        state = 16 * S + 8 * S + 8 * S * 7 + 8 * (n * n + 2 * N * np_ + N * Ns + Ns * Nf)
+        scratch = (4 * (2 * n * 2 * np_ + 4 * 4 * np_ * np_) + 8 * (n * np_ + N * np_)
+                   + 8 * (3 * L * n * nc + N * L * nc + Ns * n + L * (N + Ns) * nc) + 16 * n * n)
+    return int(1.15 * (const + state + scratch)) + (64 << 20)
+
+
+@dataclasses.dataclass
+class Result:
+    id: int
+    arrival: float
+    admitted: float
+    finished: float
+    attempts: int
+    accepted: int
+    t_end: float
+    sigma: Optional[np.ndarray]
+    currents: Optional[np.ndarray]
+    n: int
+    modes: int
+    error: Optional[str] = None
+
+    @property
+    def latency(self):
+        return self.finished - self.arrival
+
+
+class Server:
+    def __init__(self, build: Callable, estimate: Callable, device=0, max_slots=16, hbm_budget=None,
+                 precision="mixed", keep_sigma=True):
+        self.build, self.estimate = build, estimate
+        self.device, self.max_slots = device, max_slots
+        self.precision = precision
+        self.keep_sigma = keep_sigma
+        if hbm_budget is None:
+            import torch
+            free, _ = torch.cuda.mem_get_info(device)
+            hbm_budget = int(0.8 * free)
+        self.hbm_budget = hbm_budget
+        self.lock = threading.Lock()
+        self.in_use = 0
+        self.peak_in_use = 0
+        self.peak_slots = 0
+
+    def _run_one(self, req, t_admit, fp, out: List[Result], done: threading.Semaphore):
+        res = Result(id=req["id"], arrival=req["arrival"], admitted=t_admit, finished=0.0, attempts=0, accepted=0,
+                     t_end=0.0, sigma=None, currents=None, n=req.get("n", 0), modes=0)
+        tr = None
+        try:
+            w = self.build(req)
+            L = CompactLayout(w.arrays, w.hbar)
+            res.modes = L.N
+            tr = Trajectory(w.arrays, w.hbar, precision=self.precision, device=self.device, layout=L)
+            tr.set_y(w.arrays["DM_Ortho"])
+            b = native_bias(w.bias, L.NL)
+            t, h = w.t0, w.stepsize
+            J = None
+            while t < w.t1:
+                TE, acc, t, h, J0 = tr.attempt_native(t, h, w.eps, b, w.hubbard_U)
+                res.attempts += 1
+                if acc:
+                    res.accepted += 1
+                    J = J0
+            res.t_end = t
+            res.currents = J
+            if self.keep_sigma:
+                res.sigma = tr.get_sigma()
+        except Exception as e:  # reported per request, the server keeps going
+            res.error = repr(e)
+        finally:
+            if tr is not None:
+                tr.close()
+            res.finished = time.perf_counter() - self.t_start
+            with self.lock:
+                self.in_use -= fp
+                out.append(res)
+            done.release()
+
+    def run(self, requests, time_scale=1.0):
+        """Serve ``requests`` (dicts with ``id``, ``arrival``); arrivals are
+        replayed in wall time scaled by ``time_scale``.  Returns the results
+        in completion order and summary statistics."""
+        reqs = sorted(requests, key=lambda r: r["arrival"])
+        self.t_start = time.perf_counter()
+        out: List[Result] = []
+        slots = threading.Semaphore(self.max_slots)
+        threads = []
+        pending = list(reqs)
+        while pending:
+            req = pending[0]
+            due = req["arrival"] * time_scale
+            now = time.perf_counter() - self.t_start
+            if now < due:
+                time.sleep(min(due - now, 0.01))
+                continue
+            fp = self.estimate(req, self.precision)
+            if fp > self.hbm_budget:
+                pending.pop(0)
+                out.append(Result(id=req["id"], arrival=due, admitted=now, finished=now, attempts=0, accepted=0,
+                                  t_end=0.0, sigma=None, currents=None, n=req.get("n", 0), modes=0,
+                                  error="footprint %d B exceeds the HBM budget" % fp))
+                continue
+            slots.acquire()
+            while True:
+                with self.lock:
+                    if self.in_use + fp <= self.hbm_budget:
+                        self.in_use += fp
+                        self.peak_in_use = max(self.peak_in_use, self.in_use)
+                        break
+                time.sleep(0.002)
+            pending.pop(0)
+            r = dict(req)
+            r["arrival"] = due
+            th = threading.Thread(target=self._run_one,
+                                  args=(r, time.perf_counter() - self.t_start, fp, out, slots), daemon=True)
+            th.start()
+            threads.append(th)
+            self.peak_slots = max(self.peak_slots, sum(t.is_alive() for t in threads))
+        for th in threads:
+            th.join()
+        wall = time.perf_counter() - self.t_start
+        ok = [r for r in out if r.error is None]
+        lat = np.array([r.latency for r in ok]) if ok else np.zeros(1)
+        stats = dict(requests=len(reqs), completed=len(ok), failed=len(out) - len(ok), wall_s=wall,
+                     throughput_traj_per_s=len(ok) / wall, simulated_fs=float(sum(r.t_end for r in ok)),
+                     p50_latency_s=float(np.percentile(lat, 50)), p99_latency_s=float(np.percentile(lat, 99)),
+                     mean_latency_s=float(lat.mean()), attempts=int(sum(r.attempts for r in ok)),
+                     peak_hbm_reserved=int(self.peak_in_use), hbm_budget=int(self.hbm_budget),
+                     max_slots=self.max_slots)
+        stats["simulated_fs_per_s"] = stats["simulated_fs"] / wall
+        return out, stats
+
+
+def c4_estimate(req, precision):
+    from .workloads import c4_mode_estimate
+    N, Ns, nc = c4_mode_estimate(req)
+    return footprint_bytes(req["n"], N, Ns, nc, req["leads"], precision)

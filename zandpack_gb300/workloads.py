@@ -386,6 +386,64 @@ CONFIGS = {
 }
 
 
+# ------------------------------------------------------------ ensemble (c4)
+C4_SIZES = [(64, (8, 8)), (128, (16, 8)), (256, (16, 16)), (384, (24, 16)), (512, (32, 16))]
+
+
+def c4_requests(count=512, rate=50.0, seed=1004, t_span=2.0):
+    """Requests of the serving ensemble: Poisson arrivals at ``rate`` per
+    second, device sizes n in {64,128,256,384,512} as 1D chains (n_c = 1) or
+    2D lattices (8x8, 16x8, 16x16, 24x16, 32x16, n_c = W), 2-3 leads, 16-32
+    Lorentzians of rank min(4, n_c), 20-40 Pade poles, Gaussian pulses with
+    amplitude U[0.1, 1] V and width U[2, 20] fs, propagated over ``t_span`` fs."""
+    rng = np.random.default_rng(seed)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, count))
+    out = []
+    for i in range(count):
+        n, shape = C4_SIZES[int(rng.integers(len(C4_SIZES)))]
+        out.append(dict(id=i, arrival=float(arrivals[i]), n=n, shape=shape,
+                        geom="1d" if rng.random() < 0.5 else "2d", leads=int(rng.integers(2, 4)),
+                        n_l=int(rng.integers(16, 33)), n_f=int(rng.integers(20, 41)),
+                        amp=float(rng.uniform(0.1, 1.0)), width=float(rng.uniform(2.0, 20.0)),
+                        seed=int(rng.integers(2 ** 31)), t1=float(t_span)))
+    return out
+
+
+def c4_coupling(req):
+    n = req["n"]
+    if req["geom"] == "1d":
+        c = [[0], [n - 1], [n // 2]]
+    else:
+        lx, ly = req["shape"]
+        c = [list(range(ly)), list(range((lx - 1) * ly, lx * ly)),
+             [i * ly + (ly - 1) for i in range(1, lx - 1)][:ly]]
+    return c[:req["leads"]]
+
+
+def c4_workload(req) -> Workload:
+    rng = np.random.default_rng(req["seed"])
+    n = req["n"]
+    if req["geom"] == "1d":
+        H = chain(n, -2.7)
+    else:
+        H = square_lattice(req["shape"][0], req["shape"][1], -1.0)
+    coupling = c4_coupling(req)
+    lor = [_lorentzians(rng, req["n_l"], len(c), min(4, len(c))) for c in coupling]
+    A = build_arrays(H, coupling, lor, req["n_f"])
+    bias = {"kind": "gauss", "V0": req["amp"], "tc": req["width"], "sigma": req["width"]}
+    return Workload(name="c4-%d" % req["id"], arrays=A, t0=0.0, t1=req["t1"], eps=1e-6, stepsize=0.02,
+                    hbar=HBAR, bias=bias, hubbard_U=None, kT=0.025, coupling=coupling)
+
+
+def c4_mode_estimate(req):
+    """(N, Ns, nc) of a request without building it: live modes are the
+    Lorentzian ranks plus the Fermi-pole modes (rank n_c each)."""
+    cs = [len(c) for c in c4_coupling(req)]
+    Ns = sum(req["n_l"] * min(4, c) for c in cs)
+    N = Ns + sum(2 * req["n_f"] * c for c in cs)
+    return N, Ns, max(cs)
+
+
 def make_workload(name: str) -> Workload:
     k, fn = CONFIGS[name]
     rng = np.random.default_rng(1000 + k)
