@@ -144,6 +144,36 @@ int zg_attempt(zg_traj* t, double* time, double* h, double eps, const zg_bias* b
  * after every accepted step (Zandpack/mpi/zand:428-430). */
 int zg_get_sigma(zg_traj* t, int slot, double* host);
 
+/* Graph-launched attempts.  The same attempt as zg_attempt, with the
+ * controller (t, h, TE, accept, next step size) kept on the device and the
+ * whole attempt captured once as a CUDA graph, so that a run of attempts needs
+ * one graph launch each and one host synchronisation per batch of attempts.
+ * Once t >= t1 (or a non-finite error norm) the trajectory is done and further
+ * launched attempts change nothing.  Replaces the host loop of
+ * Zandpack/mpi/zand:301-430 for analytic biases. */
+#define ZG_GRAPH_MAX_BATCH 256
+typedef struct {
+  double t;       /* time at the start of the attempt */
+  double h;       /* step size of the attempt */
+  double TE;      /* error norm */
+  double h_next;  /* 0.9 h (eps/TE)^(1/5) */
+  int32_t accepted;
+  int32_t status; /* ZG_OK or ZG_ENONFINITE */
+  double J[ZG_MAX_LEADS]; /* stage-0 lead currents */
+} zg_attempt_rec;
+/* Capture the attempt graph for this bias and dH mode (ZG_DH_NONE or
+ * ZG_DH_HUBBARD).  zg_set_tableau and a change of zg_profile drop the graph;
+ * the next zg_graph_run captures it again.  With profiling on, the regions of
+ * the last attempt of each batch are accumulated. */
+int zg_graph_prepare(zg_traj* t, const zg_bias* bias, int dH_mode, double hubbard_U);
+/* Set the device controller: time, step size, tolerance and end time. */
+int zg_graph_set(zg_traj* t, double time, double h, double eps, double t1);
+/* Launch `count` (<= ZG_GRAPH_MAX_BATCH) attempts back to back, then
+ * synchronise once.  recs (may be NULL) receives one record per attempt that
+ * ran before the trajectory was done, *nrec their number; time, h and done
+ * (each may be NULL) the controller after the batch. */
+int zg_graph_run(zg_traj* t, int count, zg_attempt_rec* recs, int* nrec, double* time, double* h, int* done);
+
 /* Measurement.  With profiling on, CUDA events on the trajectory's stream
  * bracket each region; zg_profile_read returns accumulated milliseconds and
  * counts per region (indices ZG_PROF_*).  zg_profile(t, 1) also resets them. */

@@ -40,3 +40,23 @@ def test_admission_by_footprint():
     res, stats = srv.run(reqs)
     assert stats["completed"] == len(reqs)
     assert stats["peak_hbm_reserved"] <= budget
+
+
+def test_graph_mode_matches_host_mode():
+    """Graph-launched attempts (controller on the device) serve the same
+    results as one zg_attempt call per attempt: same attempt counts, sigma and
+    currents to 1e-10 (device and host libm may differ in the last place of
+    the bias and the step-size update)."""
+    from zandpack_gb300.serve import Server, c4_estimate
+    from zandpack_gb300.workloads import c4_requests, c4_workload
+    reqs = c4_requests(8, rate=400.0, seed=79, t_span=0.3)
+    g, gs = Server(c4_workload, c4_estimate, max_slots=4, attempt_mode="graph").run(reqs, time_scale=0.0)
+    h, hs = Server(c4_workload, c4_estimate, max_slots=4, attempt_mode="host").run(reqs, time_scale=0.0)
+    assert gs["completed"] == hs["completed"] == len(reqs), [r.error for r in g + h if r.error]
+    hm = {r.id: r for r in h}
+    for r in g:
+        s = hm[r.id]
+        assert r.attempts == s.attempts and r.accepted == s.accepted
+        assert abs(r.t_end - s.t_end) <= 1e-9 * abs(s.t_end)
+        assert np.abs(r.sigma - s.sigma).max() <= 1e-10
+        assert np.abs(r.currents - s.currents).max() <= 1e-10

@@ -50,8 +50,20 @@ class zg_bias(C.Structure):
                 ("sigma", C.c_double), ("f", C.c_double), ("w", C.c_double * ZG_MAX_LEADS)]
 
 
+ZG_GRAPH_MAX_BATCH = 256
+
+
+class zg_attempt_rec(C.Structure):
+    _fields_ = [("t", C.c_double), ("h", C.c_double), ("TE", C.c_double), ("h_next", C.c_double),
+                ("accepted", C.c_int32), ("status", C.c_int32), ("J", C.c_double * ZG_MAX_LEADS)]
+
+
 _P = C.c_void_p
 _SIGS = {
+    "zg_graph_prepare": ([_P, C.POINTER(zg_bias), C.c_int, C.c_double], C.c_int),
+    "zg_graph_set": ([_P, C.c_double, C.c_double, C.c_double, C.c_double], C.c_int),
+    "zg_graph_run": ([_P, C.c_int, _P, C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_double),
+                      C.POINTER(C.c_int)], C.c_int),
     "zg_attempt": ([_P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_double, C.POINTER(zg_bias), C.c_int,
                     C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_int), _P], C.c_int),
     "zg_last_error": ([], C.c_char_p),

@@ -13,6 +13,7 @@
 namespace zg {
 
 std::atomic<long long> g_launches{0};
+thread_local long long t_launches = 0;
 
 #define GRID_STRIDE(e, count) \
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < (count); e += (int64_t)gridDim.x * blockDim.x)
@@ -41,7 +42,8 @@ int launch_combine_c128(const double2* Y, int64_t stride, const CombineCoefs& cf
 }
 
 __global__ void __launch_bounds__(256) k_step_fourth(double2* Y, int64_t stride, int last, CombineCoefs cf,
-                                                     int64_t count) {
+                                                     int64_t count, const int* gate) {
+  if (gate && *gate == 0) return;
   GRID_STRIDE(e, count) {
     double2 acc = make_double2(0.0, 0.0);
     for (int t = 0; t < cf.n; ++t) {
@@ -54,9 +56,9 @@ __global__ void __launch_bounds__(256) k_step_fourth(double2* Y, int64_t stride,
 }
 
 int launch_step_fourth_c128(double2* Y, int64_t stride, int last, const CombineCoefs& cf, int64_t count,
-                            cudaStream_t s) {
+                            cudaStream_t s, const int* gate) {
   if (count <= 0) return ZG_OK;
-  k_step_fourth<<<grid_for(count, 256, 152 * 16), 256, 0, s>>>(Y, stride, last, cf, count);
+  k_step_fourth<<<grid_for(count, 256, 152 * 16), 256, 0, s>>>(Y, stride, last, cf, count, gate);
   ZG_CHECK_LAUNCH();
   count_launch();
   return ZG_OK;
@@ -200,7 +202,8 @@ int launch_terr2_partials_mixed(const float2* K, int64_t stride, const CombineCo
 
 __global__ void __launch_bounds__(256) k_update_mixed(double2* __restrict__ y64, float2* __restrict__ y32,
                                                       const float2* __restrict__ K, int64_t stride, CombineCoefs cf,
-                                                      int64_t count) {
+                                                      int64_t count, const int* gate) {
+  if (gate && *gate == 0) return;
   GRID_STRIDE(e, count) {
     float2 d = make_float2(0.f, 0.f);
     for (int t = 0; t < cf.n; ++t) {
@@ -218,9 +221,9 @@ __global__ void __launch_bounds__(256) k_update_mixed(double2* __restrict__ y64,
 }
 
 int launch_update_mixed(double2* y64, float2* y32, const float2* K, int64_t stride, const CombineCoefs& cf,
-                        int64_t count, cudaStream_t s) {
+                        int64_t count, cudaStream_t s, const int* gate) {
   if (count <= 0) return ZG_OK;
-  k_update_mixed<<<grid_for(count, 256, 152 * 16), 256, 0, s>>>(y64, y32, K, stride, cf, count);
+  k_update_mixed<<<grid_for(count, 256, 152 * 16), 256, 0, s>>>(y64, y32, K, stride, cf, count, gate);
   ZG_CHECK_LAUNCH();
   count_launch();
   return ZG_OK;
@@ -243,6 +246,102 @@ int launch_f64_to_f32(const double2* a, float2* b, int64_t count, cudaStream_t s
 int launch_f32_to_f64(const float2* a, double2* b, int64_t count, cudaStream_t s) {
   if (count <= 0) return ZG_OK;
   k_f32_to_f64<<<grid_for(count, 256, 152 * 16), 256, 0, s>>>(a, b, count);
+  ZG_CHECK_LAUNCH();
+  count_launch();
+  return ZG_OK;
+}
+
+// ============================================================ controller
+__global__ void k_set_params(StageParams p, StageParams* out) {
+  if (threadIdx.x == 0) *out = p;
+}
+
+int launch_set_params(const StageParams& p, StageParams* out, cudaStream_t s) {
+  k_set_params<<<1, 32, 0, s>>>(p, out);
+  ZG_CHECK_LAUNCH();
+  count_launch();
+  return ZG_OK;
+}
+
+__global__ void k_stage_prologue(const DevCtl* __restrict__ ctl, zg_bias b, double A_i, double hbar,
+                                 StageParams* __restrict__ out) {
+  const double t = ctl->t, h = ctl->h;
+  const double ts = t + A_i * h;
+  const int a = threadIdx.x;
+  if (a < ZG_MAX_LEADS) out->delta[a] = zg_bias_value(b, ts, a);
+  if (a == 0) {
+    out->h = h;
+    out->ts = ts;
+    out->hbar = hbar;
+  }
+}
+
+int launch_stage_prologue(const DevCtl* ctl, const zg_bias& b, double A_i, double hbar, StageParams* out,
+                          cudaStream_t s) {
+  k_stage_prologue<<<1, 32, 0, s>>>(ctl, b, A_i, hbar, out);
+  ZG_CHECK_LAUNCH();
+  count_launch();
+  return ZG_OK;
+}
+
+// accept iff TE < eps; h <- 0.9 h (eps/TE)^(1/5) (Zandpack/mpi_RK4pars_dev.py:148-149)
+__global__ void k_control(const double* __restrict__ err3, DevCtl* __restrict__ ctl) {
+  if (threadIdx.x != 0) return;
+  ctl->skip = ctl->done;
+  if (ctl->done) {
+    ctl->accepted = 0;
+    return;
+  }
+  const double te = sqrt(err3[0] + err3[1] + err3[2]);
+  ctl->TE = te;
+  if (!isfinite(te)) {
+    ctl->status = ZG_ENONFINITE;
+    ctl->accepted = 0;
+    ctl->hnew = ctl->h;
+    return;
+  }
+  ctl->accepted = te < ctl->eps ? 1 : 0;
+  ctl->hnew = te > 0.0 ? 0.9 * ctl->h * pow(ctl->eps / te, 0.2) : INFINITY;
+}
+
+int launch_control(const double* err3, DevCtl* ctl, cudaStream_t s) {
+  k_control<<<1, 32, 0, s>>>(err3, ctl);
+  ZG_CHECK_LAUNCH();
+  count_launch();
+  return ZG_OK;
+}
+
+// the reference advances time by the step size proposed for the next step
+__global__ void k_advance(DevCtl* __restrict__ ctl, const double* __restrict__ J, int L,
+                          zg_attempt_rec* __restrict__ recs, int cap) {
+  if (ctl->skip) return;
+  const int r = ctl->rec_n;
+  if (r < cap) {
+    zg_attempt_rec* o = recs + r;
+    if (threadIdx.x < ZG_MAX_LEADS) o->J[threadIdx.x] = threadIdx.x < L ? J[threadIdx.x] : 0.0;
+    if (threadIdx.x == 0) {
+      o->t = ctl->t;
+      o->h = ctl->h;
+      o->TE = ctl->TE;
+      o->h_next = ctl->hnew;
+      o->accepted = ctl->accepted;
+      o->status = ctl->status;
+    }
+  }
+  __syncwarp();
+  if (threadIdx.x != 0) return;
+  ctl->rec_n = r + 1;
+  ctl->attempts += 1;
+  if (ctl->accepted) {
+    ctl->t += ctl->hnew;
+    ctl->naccepted += 1;
+  }
+  ctl->h = ctl->hnew;
+  ctl->done = (ctl->t >= ctl->t1 || ctl->status != 0) ? 1 : 0;
+}
+
+int launch_advance(DevCtl* ctl, const double* J, int L, zg_attempt_rec* recs, int cap, cudaStream_t s) {
+  k_advance<<<1, 32, 0, s>>>(ctl, J, L, recs, cap);
   ZG_CHECK_LAUNCH();
   count_launch();
   return ZG_OK;

@@ -11,7 +11,12 @@ namespace zg {
 
 // kernels launched by this library since load (all threads)
 extern std::atomic<long long> g_launches;
-inline void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+// kernels launched (or captured into a graph) by the calling thread
+extern thread_local long long t_launches;
+inline void count_launch() {
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  ++t_launches;
+}
 
 // ------------------------------------------------ tensor-core GEMM (3xTF32)
 // D (M x N, fp32, row stride ldd) = (Ah + Al)(Bh + Bl)^T without Al.Bl^T;
@@ -35,8 +40,9 @@ int launch_split_tf32(const float* x, float* hi, float* lo, int64_t n, cudaStrea
 int launch_combine_c128(const double2* Y, int64_t stride, const CombineCoefs& cf, double2* out,
                         int64_t count, cudaStream_t s);
 // Y[last][e] = sum_t c[t] * Y[idx[t]][e], in place (last is one of the idx)
+// gate (device int, may be null): the update is skipped when *gate == 0
 int launch_step_fourth_c128(double2* Y, int64_t stride, int last, const CombineCoefs& cf,
-                            int64_t count, cudaStream_t s);
+                            int64_t count, cudaStream_t s, const int* gate = nullptr);
 // partial[b] for b < nblocks: block sums of |sum_t c[t] Y[idx[t]][e]|^2 over e in [begin, end)
 int terr2_nblocks(int64_t count);
 int launch_terr2_partials_c128(const double2* Y, int64_t stride, const CombineCoefs& cf,
@@ -60,7 +66,7 @@ int launch_terr2_partials_mixed(const float2* K, int64_t stride, const CombineCo
                                 double* partial, int nblocks, cudaStream_t s);
 // y64 += sum_t c[t] K[idx[t]] (increment in FP32, addition in FP64); y32 = fl32(y64)
 int launch_update_mixed(double2* y64, float2* y32, const float2* K, int64_t stride, const CombineCoefs& cf,
-                        int64_t count, cudaStream_t s);
+                        int64_t count, cudaStream_t s, const int* gate = nullptr);
 int launch_f64_to_f32(const double2* a, float2* b, int64_t count, cudaStream_t s);
 int launch_f32_to_f64(const float2* a, double2* b, int64_t count, cudaStream_t s);
 
@@ -106,6 +112,42 @@ struct StageParams {
   double delta[ZG_MAX_LEADS];
 };
 
+// ------------------------------------------------ device-side controller
+// State of the zand controller kept on the device, so that one attempt runs
+// as one CUDA graph without host round trips.
+struct DevCtl {
+  double t, h, eps, t1;
+  double TE, hnew;
+  int accepted, done, status, attempts, naccepted;
+  int skip;   // this attempt started after the trajectory was done: changes nothing
+  int rec_n;  // records written since the batch began
+  int pad;
+};
+// Delta_a(t) of an analytic bias (zg_bias), host and device
+__host__ __device__ inline double zg_bias_value(const zg_bias& b, double t, int a) {
+  double V = 0.0;
+  switch (b.kind) {
+    case ZG_BIAS_EXP_RAMP: V = b.V0 * (1.0 - exp(-t / b.tau)); break;
+    case ZG_BIAS_GAUSS: V = b.V0 * exp(-(t - b.tc) * (t - b.tc) / (2.0 * b.sigma * b.sigma)); break;
+    case ZG_BIAS_SIN: V = b.V0 * sin(2.0 * 3.14159265358979323846 * b.f * t); break;
+    case ZG_BIAS_STEP: V = t > 0.0 ? b.V0 : 0.0; break;
+    case ZG_BIAS_BOX: V = b.V0 * (tanh(t / b.tau) - tanh((t - b.tc) / b.tau)) / 2.0; break;
+    default: V = 0.0;
+  }
+  return b.w[a] * V;
+}
+// *out = p (stage parameters given by the host)
+int launch_set_params(const StageParams& p, StageParams* out, cudaStream_t s);
+// *out = h, ts = t + A_i h, hbar, delta[a] = bias(ts, a) from the device controller
+int launch_stage_prologue(const DevCtl* ctl, const zg_bias& b, double A_i, double hbar, StageParams* out,
+                          cudaStream_t s);
+// TE = sqrt(err[0]+err[1]+err[2]); accepted = TE < eps; hnew = 0.9 h (eps/TE)^(1/5);
+// an attempt that starts after done is skipped (accepted = 0)
+int launch_control(const double* err3, DevCtl* ctl, cudaStream_t s);
+// after the (gated) update: records the attempt (recs[rec_n], stage-0 currents
+// J[0..L)), then on acceptance t += hnew; always h = hnew; done = t >= t1
+int launch_advance(DevCtl* ctl, const double* J, int L, zg_attempt_rec* recs, int cap, cudaStream_t s);
+
 template <typename T>
 struct RhsDev {  // device pointers and sizes of one trajectory
   using C = typename cx<T>::t;
@@ -130,17 +172,17 @@ int launch_gathers(const RhsDev<T>& d, const typename cx<T>::t* sig, const typen
                    const typename cx<T>::t* psi_lo, int64_t ldpsi, typename cx<T>::t* sigC, typename cx<T>::t* G,
                    cudaStream_t s);
 template <typename T>
-int launch_sigma_finalize(const RhsDev<T>& d, const StageParams& p, const typename cx<T>::t* Tm, int64_t ldT,
+int launch_sigma_finalize(const RhsDev<T>& d, const StageParams* p, const typename cx<T>::t* Tm, int64_t ldT,
                           const typename cx<T>::t* Pc, typename cx<T>::t* ksig, cudaStream_t s);
 template <typename T>
-int launch_currents(const RhsDev<T>& d, const StageParams& p, const typename cx<T>::t* Pc, double* J, cudaStream_t s);
+int launch_currents(const RhsDev<T>& d, const StageParams* p, const typename cx<T>::t* Pc, double* J, cudaStream_t s);
 template <typename T>
-int launch_psi_finalize(const RhsDev<T>& d, const StageParams& p, const typename cx<T>::t* psi,
+int launch_psi_finalize(const RhsDev<T>& d, const StageParams* p, const typename cx<T>::t* psi,
                         const typename cx<T>::t* psi_lo, int64_t ldpsi, const typename cx<T>::t* R1, int64_t ldR1,
                         const typename cx<T>::t* R2, const typename cx<T>::t* ZA, const typename cx<T>::t* ZB,
                         typename cx<T>::t* kpsi, cudaStream_t s);
 template <typename T>
-int launch_omega(const RhsDev<T>& d, const StageParams& p, const OmTile* tiles, int ntiles, const typename cx<T>::t* G,
+int launch_omega(const RhsDev<T>& d, const StageParams* p, const OmTile* tiles, int ntiles, const typename cx<T>::t* G,
                  const typename cx<T>::t* omA_in, const typename cx<T>::t* omB_in, typename cx<T>::t* omA_out,
                  typename cx<T>::t* omB_out, cudaStream_t s);
 

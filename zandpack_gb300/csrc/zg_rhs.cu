@@ -263,9 +263,10 @@ __device__ __forceinline__ typename cx<T>::t p_full(const RhsDev<T>& d, const ty
 
 // k_sig = (h/hbar) (-i (T - T^H) + (P + P^H)/hbar), T = H(t) sigma  (Zandpack/mpi/zand:340-387)
 template <typename T>
-__global__ void k_sigma_finalize(const RhsDev<T> d, const StageParams p, const typename cx<T>::t* __restrict__ Tm,
+__global__ void k_sigma_finalize(const RhsDev<T> d, const StageParams* __restrict__ pp, const typename cx<T>::t* __restrict__ Tm,
                                  int64_t ldT, const typename cx<T>::t* __restrict__ Pc,
                                  typename cx<T>::t* __restrict__ ksig) {
+  const StageParams p = *pp;
   const int64_t nn = (int64_t)d.n * d.n;
   const T ih = (T)(1.0 / p.hbar);
   const T sc = (T)(p.h / p.hbar);
@@ -282,7 +283,7 @@ __global__ void k_sigma_finalize(const RhsDev<T> d, const StageParams p, const t
 }
 
 template <typename T>
-int launch_sigma_finalize(const RhsDev<T>& d, const StageParams& p, const typename cx<T>::t* Tm, int64_t ldT,
+int launch_sigma_finalize(const RhsDev<T>& d, const StageParams* p, const typename cx<T>::t* Tm, int64_t ldT,
                           const typename cx<T>::t* Pc, typename cx<T>::t* ksig, cudaStream_t s) {
   int64_t nn = (int64_t)d.n * d.n;
   k_sigma_finalize<T><<<grid_for(nn, 256, 152 * 8), 256, 0, s>>>(d, p, Tm, ldT, Pc, ksig);
@@ -312,8 +313,9 @@ __device__ __forceinline__ double block_sum256_d(double v) {
 
 // J_a = 2 Re Tr(P_a) / hbar^2 = Re Tr(PI_a)/hbar  (Zandpack/mpi/zand:368-378)
 template <typename T>
-__global__ void k_currents(const RhsDev<T> d, const StageParams p, const typename cx<T>::t* __restrict__ Pc,
+__global__ void k_currents(const RhsDev<T> d, const StageParams* __restrict__ pp, const typename cx<T>::t* __restrict__ Pc,
                            double* __restrict__ J) {
+  const StageParams p = *pp;
   const int a = blockIdx.x;
   double s = 0.0;
   for (int k = threadIdx.x; k < d.nc; k += blockDim.x) {
@@ -326,7 +328,7 @@ __global__ void k_currents(const RhsDev<T> d, const StageParams p, const typenam
 }
 
 template <typename T>
-int launch_currents(const RhsDev<T>& d, const StageParams& p, const typename cx<T>::t* Pc, double* J, cudaStream_t s) {
+int launch_currents(const RhsDev<T>& d, const StageParams* p, const typename cx<T>::t* Pc, double* J, cudaStream_t s) {
   k_currents<T><<<d.L, 256, 0, s>>>(d, p, Pc, J);
   ZG_CHECK_LAUNCH();
   count_launch();
@@ -380,11 +382,12 @@ int launch_currents64(int n, int L, int nc, const CurRows& rows, const int* lead
 // k_psi = -i h [ R1/hbar - (X+ + Delta)/hbar psi + dGP R2 + Z(Omega xi) + GL_P xi ]
 // with R1 = psi H^T  (Zandpack/mpi/zand:745-778)
 template <typename T>
-__global__ void k_psi_finalize(const RhsDev<T> d, const StageParams p, const typename cx<T>::t* __restrict__ psi,
+__global__ void k_psi_finalize(const RhsDev<T> d, const StageParams* __restrict__ pp, const typename cx<T>::t* __restrict__ psi,
                                const typename cx<T>::t* __restrict__ psi_lo, int64_t ldpsi,
                                const typename cx<T>::t* R1, int64_t ldR1, const typename cx<T>::t* __restrict__ R2,
                                const typename cx<T>::t* __restrict__ ZA, const typename cx<T>::t* __restrict__ ZB,
                                typename cx<T>::t* kpsi) {
+  const StageParams p = *pp;
   using C = typename cx<T>::t;
   const int64_t tot = (int64_t)d.N * d.n;
   const T ih = (T)(1.0 / p.hbar);
@@ -414,7 +417,7 @@ __global__ void k_psi_finalize(const RhsDev<T> d, const StageParams p, const typ
 }
 
 template <typename T>
-int launch_psi_finalize(const RhsDev<T>& d, const StageParams& p, const typename cx<T>::t* psi,
+int launch_psi_finalize(const RhsDev<T>& d, const StageParams* p, const typename cx<T>::t* psi,
                         const typename cx<T>::t* psi_lo, int64_t ldpsi, const typename cx<T>::t* R1, int64_t ldR1,
                         const typename cx<T>::t* R2, const typename cx<T>::t* ZA, const typename cx<T>::t* ZB,
                         typename cx<T>::t* kpsi, cudaStream_t s) {
@@ -431,12 +434,13 @@ int launch_psi_finalize(const RhsDev<T>& d, const StageParams& p, const typename
 //          + h sum_k V[m][k] conj(G[l][a][k])        (term2, V = dGP * XIT2)
 //          + (i h/hbar)(X+_m + D_a - X-_l - D_b) Omega[m,l]
 template <typename T>
-__global__ void __launch_bounds__(256) k_omega(const RhsDev<T> d, const StageParams p, const OmTile* __restrict__ tiles,
+__global__ void __launch_bounds__(256) k_omega(const RhsDev<T> d, const StageParams* __restrict__ pp, const OmTile* __restrict__ tiles,
                                                const typename cx<T>::t* __restrict__ G,
                                                const typename cx<T>::t* __restrict__ omA_in,
                                                const typename cx<T>::t* __restrict__ omB_in,
                                                typename cx<T>::t* __restrict__ omA_out,
                                                typename cx<T>::t* __restrict__ omB_out) {
+  const StageParams p = *pp;
   using C = typename cx<T>::t;
   const OmTile t = tiles[blockIdx.x];
   // K (the 2 n_c source terms) staged ZKO at a time, next stage prefetched into registers
@@ -530,7 +534,7 @@ __global__ void __launch_bounds__(256) k_omega(const RhsDev<T> d, const StagePar
 }
 
 template <typename T>
-int launch_omega(const RhsDev<T>& d, const StageParams& p, const OmTile* tiles, int ntiles, const typename cx<T>::t* G,
+int launch_omega(const RhsDev<T>& d, const StageParams* p, const OmTile* tiles, int ntiles, const typename cx<T>::t* G,
                  const typename cx<T>::t* omA_in, const typename cx<T>::t* omB_in, typename cx<T>::t* omA_out,
                  typename cx<T>::t* omB_out, cudaStream_t s) {
   if (ntiles == 0) return ZG_OK;
@@ -637,13 +641,13 @@ int launch_build_operands_mixed(int n, int np, const double2* H0, const float2* 
   template int launch_zgemm_batch<T>(GemmBatch<T>&, int64_t, cudaStream_t);                                         \
   template int launch_gathers<T>(const RhsDev<T>&, const cx<T>::t*, const cx<T>::t*, const cx<T>::t*, int64_t,      \
                                  cx<T>::t*, cx<T>::t*, cudaStream_t);                                                 \
-  template int launch_sigma_finalize<T>(const RhsDev<T>&, const StageParams&, const cx<T>::t*, int64_t,              \
+  template int launch_sigma_finalize<T>(const RhsDev<T>&, const StageParams*, const cx<T>::t*, int64_t,              \
                                         const cx<T>::t*, cx<T>::t*, cudaStream_t);                                    \
-  template int launch_currents<T>(const RhsDev<T>&, const StageParams&, const cx<T>::t*, double*, cudaStream_t);     \
-  template int launch_psi_finalize<T>(const RhsDev<T>&, const StageParams&, const cx<T>::t*, const cx<T>::t*,        \
+  template int launch_currents<T>(const RhsDev<T>&, const StageParams*, const cx<T>::t*, double*, cudaStream_t);     \
+  template int launch_psi_finalize<T>(const RhsDev<T>&, const StageParams*, const cx<T>::t*, const cx<T>::t*,        \
                                       int64_t, const cx<T>::t*, int64_t, const cx<T>::t*, const cx<T>::t*,           \
                                       const cx<T>::t*, cx<T>::t*, cudaStream_t);                                     \
-  template int launch_omega<T>(const RhsDev<T>&, const StageParams&, const OmTile*, int, const cx<T>::t*,            \
+  template int launch_omega<T>(const RhsDev<T>&, const StageParams*, const OmTile*, int, const cx<T>::t*,            \
                                const cx<T>::t*, const cx<T>::t*, cx<T>::t*, cx<T>::t*, cudaStream_t);
 ZG_INST(double)
 ZG_INST(float)

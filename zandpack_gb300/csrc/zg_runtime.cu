@@ -105,6 +105,25 @@ struct zg_traj {
   float2* ws32 = nullptr;
   int64_t ws64_cap = 0, ws32_cap = 0;
   TcGemm gT, gR1;
+  // stage parameters read by the RHS kernels, and the device-side controller
+  StageParams* d_params = nullptr;
+  DevCtl* ctl = nullptr;
+  DevCtl* ctl_host = nullptr;  // pinned mirror, written by the attempt graph
+  double* J_host = nullptr;    // pinned
+  int* tcerr_host = nullptr;   // pinned
+  zg_attempt_rec* d_recs = nullptr;     // ZG_GRAPH_MAX_BATCH records of the current batch
+  zg_attempt_rec* recs_host = nullptr;  // pinned
+  bool capturing = false;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  long long graph_kernels = 0;  // kernels of this library in one launch of the graph
+  bool g_prepared = false;      // bias and dH mode of the graph are set
+  zg_bias gbias;
+  int g_dH_mode = ZG_DH_NONE;
+  double g_U = 0.0;
+  // event pairs recorded inside the attempt graph (region, begin, end)
+  std::vector<int> gprof_r;
+  std::vector<cudaEvent_t> gprof_b, gprof_e;
   // profiling: CUDA event pairs on `stream` around each region, collected at host syncs
   struct Prof {
     bool on = false;
@@ -157,18 +176,74 @@ static void prof_collect(zg_traj* t) {
 static void prof_begin(zg_traj* t, int r) {
   auto& P = t->prof;
   if (!P.on) return;
+  if (t->capturing) {  // event record nodes inside the attempt graph
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    cudaEventRecordWithFlags(e, t->stream, cudaEventRecordExternal);
+    t->gprof_r.push_back(r);
+    t->gprof_b.push_back(e);
+    return;
+  }
   if (P.pending[r] == P.RING) prof_collect(t);
   cudaEventRecord(P.b[r][P.pending[r]], t->stream);
 }
 static void prof_end(zg_traj* t, int r) {
   auto& P = t->prof;
   if (!P.on) return;
+  if (t->capturing) {
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    cudaEventRecordWithFlags(e, t->stream, cudaEventRecordExternal);
+    // pair with the latest unmatched begin of this region
+    t->gprof_e.resize(t->gprof_b.size(), nullptr);
+    for (size_t i = t->gprof_b.size(); i-- > 0;)
+      if (t->gprof_r[i] == r && t->gprof_e[i] == nullptr) {
+        t->gprof_e[i] = e;
+        break;
+      }
+    return;
+  }
   cudaEventRecord(P.e[r][P.pending[r]], t->stream);
   P.pending[r] += 1;
+}
+// after a replay of the attempt graph: accumulate the regions it recorded
+static void graph_prof_collect(zg_traj* t) {
+  auto& P = t->prof;
+  if (!P.on) return;
+  for (size_t i = 0; i < t->gprof_b.size(); ++i) {
+    if (i >= t->gprof_e.size() || !t->gprof_e[i]) continue;
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, t->gprof_b[i], t->gprof_e[i]) == cudaSuccess) {
+      P.ms[t->gprof_r[i]] += ms;
+      P.cnt[t->gprof_r[i]] += 1;
+    }
+  }
+}
+
+static void drop_graph(zg_traj* t) {
+  if (t->gexec) cudaGraphExecDestroy(t->gexec);
+  if (t->graph) cudaGraphDestroy(t->graph);
+  t->gexec = nullptr;
+  t->graph = nullptr;
+  t->graph_kernels = 0;
+  for (auto e : t->gprof_b) cudaEventDestroy(e);
+  for (auto e : t->gprof_e)
+    if (e) cudaEventDestroy(e);
+  t->gprof_r.clear();
+  t->gprof_b.clear();
+  t->gprof_e.clear();
 }
 
 static void free_traj(zg_traj* t) {
   if (!t) return;
+  drop_graph(t);
+  if (t->recs_host) cudaFreeHost(t->recs_host);
+  if (t->d_recs) cudaFree(t->d_recs);
+  if (t->ctl_host) cudaFreeHost(t->ctl_host);
+  if (t->J_host) cudaFreeHost(t->J_host);
+  if (t->tcerr_host) cudaFreeHost(t->tcerr_host);
+  if (t->d_params) cudaFree(t->d_params);
+  if (t->ctl) cudaFree(t->ctl);
   if (t->prof.created)
     for (int r = 0; r < ZG_PROF_REGIONS; ++r)
       for (int i = 0; i < t->prof.RING; ++i) {
@@ -252,6 +327,9 @@ static void build_tiles(zg_traj* t, std::vector<OmTile>& out) {
           a, b, 1, 0, 1);
     }
 }
+
+// sizes the split-K workspaces from the fixed GEMM shapes of the trajectory
+static int presize_workspaces(zg_traj* t);
 
 static void to_f32(const double2* a, float2* b, size_t n) {
   for (size_t i = 0; i < n; ++i) b[i] = make_float2((float)a[i].x, (float)a[i].y);
@@ -399,6 +477,20 @@ int zg_traj_create(int device, const zg_layout* Lo, int precision, zg_traj** out
   ZG_STEP(dalloc(&t->dH, n * n));
   ZG_STEP(dalloc(&t->J, L));
   ZG_STEP(dalloc(&t->Jpart, L * 64));
+  ZG_STEP(dalloc(&t->d_params, 1));
+  ZG_STEP(dalloc(&t->ctl, 1));
+  ZG_STEP(dalloc(&t->d_recs, ZG_GRAPH_MAX_BATCH));
+  if (cudaMallocHost((void**)&t->ctl_host, sizeof(DevCtl)) != cudaSuccess ||
+      cudaMallocHost((void**)&t->J_host, ZG_MAX_LEADS * sizeof(double)) != cudaSuccess ||
+      cudaMallocHost((void**)&t->tcerr_host, sizeof(int)) != cudaSuccess ||
+      cudaMallocHost((void**)&t->recs_host, ZG_GRAPH_MAX_BATCH * sizeof(zg_attempt_rec)) != cudaSuccess) {
+    free_traj(t);
+    set_error("pinned host allocation failed");
+    return ZG_ENOMEM;
+  }
+  memset(t->ctl_host, 0, sizeof(DevCtl));
+  *t->tcerr_host = 0;
+  ZG_CHECK_CUDA(cudaMemsetAsync(t->ctl, 0, sizeof(DevCtl), t->stream));
   t->nblk_err = terr2_nblocks(t->S);
   ZG_STEP(dalloc(&t->partial, 3 * (size_t)t->nblk_err));
   ZG_STEP(dalloc(&t->err, 3));
@@ -419,6 +511,7 @@ int zg_traj_create(int device, const zg_layout* Lo, int precision, zg_traj** out
     CH[7] = 1.0;
     ZG_STEP(set_tableau_impl(t, 7, kDopA, B, CT, CH));
   }
+  ZG_STEP(presize_workspaces(t));
   t->cur_in = y64(t);
   if (precision == ZG_PREC_MIXED) ZG_STEP(launch_f64_to_f32(t->Y, t->y32, t->S, t->stream));
   // host vectors above must outlive their asynchronous copies
@@ -446,6 +539,8 @@ int zg_traj_info(const zg_traj* t, int64_t* out) {
 int zg_set_tableau(zg_traj* t, int stages, const double* A, const double* B, const double* CT, const double* CH) {
   ZG_REQUIRE(t && A && B && CT && CH, "null argument");
   ZG_CHECK_CUDA(cudaSetDevice(t->dev));
+  ZG_CHECK_CUDA(cudaStreamSynchronize(t->stream));
+  drop_graph(t);  // the captured attempt holds the old coefficients and slots
   ZG_TRY(set_tableau_impl(t, stages, A, B, CT, CH));
   t->cur_in = y64(t);
   ZG_CHECK_CUDA(cudaStreamSynchronize(t->stream));
@@ -574,11 +669,12 @@ static void gemm_prob_f32(std::vector<GemmProb<float>>& v, const float2* A, cons
 
 }  // extern "C"
 
-// split-K workspace of one precision, grown on first use (the first right-hand
-// side of a trajectory sizes it; later calls never allocate)
+// split-K workspace of one precision, sized when the trajectory is created
+// (plan_only pass); a later call that needs more (never, for fixed shapes)
+// grows it outside of graph capture
 template <typename R>
 static int run_batches(zg_traj* t, std::vector<GemmProb<R>>& all, typename cx<R>::t** ws, int64_t* cap,
-                       cudaStream_t s) {
+                       cudaStream_t s, bool plan_only) {
   // problems at most 32 wide (the n_c-wide products) run with 128x32 tiles
   std::vector<GemmProb<R>> probs;
   for (int pass = 0; pass < 2; ++pass)
@@ -594,6 +690,7 @@ static int run_batches(zg_traj* t, std::vector<GemmProb<R>>& all, typename cx<R>
     b0 += batch.nprob;
     const int64_t need = plan_zgemm_batch<R>(batch);
     if (need > *cap) {
+      ZG_REQUIRE(!t->capturing, "split-K workspace must be sized before graph capture");
       ZG_CHECK_CUDA(cudaStreamSynchronize(s));
       if (*ws) cudaFree(*ws);
       *ws = nullptr;
@@ -602,25 +699,30 @@ static int run_batches(zg_traj* t, std::vector<GemmProb<R>>& all, typename cx<R>
       *cap = need;
     }
     batch.ws = *ws;
-    ZG_TRY(launch_zgemm_batch<R>(batch, *cap, s));
+    if (!plan_only) ZG_TRY(launch_zgemm_batch<R>(batch, *cap, s));
   }
   return ZG_OK;
 }
 
 extern "C" {
 
-static int rhs_f64(zg_traj* t, int stage, const StageParams& p, int dH_mode, double hubbard_U, bool want_J) {
+// p: device pointer to the stage parameters.  plan_only: build the GEMM
+// problem list and size the split-K workspace, launch nothing.
+static int rhs_f64(zg_traj* t, int stage, const StageParams* p, int dH_mode, double hubbard_U, bool want_J,
+                   bool plan_only = false) {
   const RhsDev<double> d = t->dev_view<double>();
-  const double2* in = t->cur_in;
+  const double2* in = plan_only ? t->slot(t->stages) : t->cur_in;
   const double2* sig = in;
   const double2* psi = in + t->off_psi;
   double2* out = t->slot(stage);
   cudaStream_t s = t->stream;
   const int64_t n = t->n, N = t->N, Ns = t->Ns, Nf = t->Nf, L = t->L, nc = t->nc;
-  prof_begin(t, ZG_PROF_PREP);
-  ZG_TRY(launch_build_ht((int)n, t->H0, sig, t->dH, dH_mode, hubbard_U, t->Ht, s));
-  ZG_TRY(launch_gathers<double>(d, sig, psi, nullptr, n, t->sigC, t->G, s));
-  prof_end(t, ZG_PROF_PREP);
+  if (!plan_only) {
+    prof_begin(t, ZG_PROF_PREP);
+    ZG_TRY(launch_build_ht((int)n, t->H0, sig, t->dH, dH_mode, hubbard_U, t->Ht, s));
+    ZG_TRY(launch_gathers<double>(d, sig, psi, nullptr, n, t->sigC, t->G, s));
+    prof_end(t, ZG_PROF_PREP);
+  }
   std::vector<GemmProb<double>> probs;
   // T = H(t) sigma ; R1 = psi H(t)^T into k_psi
   gemm_prob_f64(probs, t->Ht, n, 0, sig, n, 0, t->T, n, (int)n, (int)n, (int)n);
@@ -646,8 +748,9 @@ static int rhs_f64(zg_traj* t, int stage, const StageParams& p, int dH_mode, dou
       gemm_prob_f64(probs, in + t->off_omB + (r0 - Ns), Nf, 0, t->XIS + r0 * nc, nc, 0, t->ZB + a * Ns * nc, nc,
                     (int)Ns, (int)nc, (int)(r1 - r0));
   }
+  if (plan_only) return run_batches<double>(t, probs, &t->ws64, &t->ws64_cap, s, true);
   prof_begin(t, ZG_PROF_GEMM);
-  ZG_TRY(run_batches<double>(t, probs, &t->ws64, &t->ws64_cap, s));
+  ZG_TRY(run_batches<double>(t, probs, &t->ws64, &t->ws64_cap, s, false));
   prof_end(t, ZG_PROF_GEMM);
   prof_begin(t, ZG_PROF_FINAL);
   ZG_TRY(launch_sigma_finalize<double>(d, p, t->T, n, t->Pc, out, s));
@@ -662,7 +765,8 @@ static int rhs_f64(zg_traj* t, int stage, const StageParams& p, int dH_mode, dou
   return ZG_OK;
 }
 
-static int rhs_mixed(zg_traj* t, int stage, const StageParams& p, int dH_mode, double hubbard_U, bool want_J) {
+static int rhs_mixed(zg_traj* t, int stage, const StageParams* p, int dH_mode, double hubbard_U, bool want_J,
+                     bool plan_only = false) {
   const RhsDev<float> d = t->dev_view<float>();
   const MixedLayout& ml = t->ml;
   const float2* sig = t->stage32;
@@ -673,18 +777,20 @@ static int rhs_mixed(zg_traj* t, int stage, const StageParams& p, int dH_mode, d
   float2* out = t->kslot(stage);
   cudaStream_t s = t->stream;
   const int64_t n = t->n, N = t->N, Ns = t->Ns, Nf = t->Nf, L = t->L, nc = t->nc, np = t->np;
-  prof_begin(t, ZG_PROF_PREP);
-  ZG_TRY(launch_build_operands_mixed((int)n, (int)np, t->H0, sig, t->dH, dH_mode, hubbard_U, t->Hth, t->Htl, t->BHh,
-                                     t->BHl, t->BSh, t->BSl, s));
-  ZG_TRY(launch_gathers<float>(d, sig, psih, psil, np, t->sigC32, t->G32, s));
-  prof_end(t, ZG_PROF_PREP);
-  // tensor cores: R1 = psi H(t)^T and T = H(t) sigma
-  prof_begin(t, ZG_PROF_GEMM);
-  ZG_TRY(tc_gemm_launch(t->gR1, s));
-  prof_end(t, ZG_PROF_GEMM);
-  prof_begin(t, ZG_PROF_GEMM2);
-  ZG_TRY(tc_gemm_launch(t->gT, s));
-  prof_end(t, ZG_PROF_GEMM2);
+  if (!plan_only) {
+    prof_begin(t, ZG_PROF_PREP);
+    ZG_TRY(launch_build_operands_mixed((int)n, (int)np, t->H0, sig, t->dH, dH_mode, hubbard_U, t->Hth, t->Htl,
+                                       t->BHh, t->BHl, t->BSh, t->BSl, s));
+    ZG_TRY(launch_gathers<float>(d, sig, psih, psil, np, t->sigC32, t->G32, s));
+    prof_end(t, ZG_PROF_PREP);
+    // tensor cores: R1 = psi H(t)^T and T = H(t) sigma
+    prof_begin(t, ZG_PROF_GEMM);
+    ZG_TRY(tc_gemm_launch(t->gR1, s));
+    prof_end(t, ZG_PROF_GEMM);
+    prof_begin(t, ZG_PROF_GEMM2);
+    ZG_TRY(tc_gemm_launch(t->gT, s));
+    prof_end(t, ZG_PROF_GEMM2);
+  }
   // SIMT FP32: PI partials, xi sigma^T rows, Omega xi
   std::vector<GemmProb<float>> probs;
   for (int a = 0; a < L; ++a) {
@@ -705,8 +811,9 @@ static int rhs_mixed(zg_traj* t, int stage, const StageParams& p, int dH_mode, d
       gemm_prob_f32(probs, omB + (r0 - Ns), nullptr, Nf, 0, t->XIS32 + r0 * nc, nc, 0, t->ZB32 + a * Ns * nc, nc,
                     (int)Ns, (int)nc, (int)(r1 - r0));
   }
+  if (plan_only) return run_batches<float>(t, probs, &t->ws32, &t->ws32_cap, s, true);
   prof_begin(t, ZG_PROF_SMALL);
-  ZG_TRY(run_batches<float>(t, probs, &t->ws32, &t->ws32_cap, s));
+  ZG_TRY(run_batches<float>(t, probs, &t->ws32, &t->ws32_cap, s, false));
   prof_end(t, ZG_PROF_SMALL);
   prof_begin(t, ZG_PROF_FINAL);
   ZG_TRY(launch_sigma_finalize<float>(d, p, t->T32, np, t->Pc32, out, s));
@@ -742,10 +849,11 @@ int zg_rhs(zg_traj* t, int stage, double ts, double h, const double* delta, int 
   p.h = h; p.ts = ts; p.hbar = t->hbar;
   for (int a = 0; a < ZG_MAX_LEADS; ++a) p.delta[a] = a < t->L ? delta[a] : 0.0;
   prof_begin(t, ZG_PROF_RHS);
+  ZG_TRY(launch_set_params(p, t->d_params, t->stream));
   if (t->precision == ZG_PREC_F64)
-    ZG_TRY(rhs_f64(t, stage, p, dH_mode, hubbard_U, currents != nullptr));
+    ZG_TRY(rhs_f64(t, stage, t->d_params, dH_mode, hubbard_U, currents != nullptr));
   else
-    ZG_TRY(rhs_mixed(t, stage, p, dH_mode, hubbard_U, currents != nullptr));
+    ZG_TRY(rhs_mixed(t, stage, t->d_params, dH_mode, hubbard_U, currents != nullptr));
   prof_end(t, ZG_PROF_RHS);
   if (currents) {
     ZG_CHECK_CUDA(cudaMemcpyAsync(currents, t->J, t->L * sizeof(double), cudaMemcpyDeviceToHost, t->stream));
@@ -754,9 +862,8 @@ int zg_rhs(zg_traj* t, int stage, double ts, double h, const double* delta, int 
   return ZG_OK;
 }
 
-int zg_error_norm2(zg_traj* t, double* err2) {
-  ZG_REQUIRE(t && err2, "null argument");
-  ZG_CHECK_CUDA(cudaSetDevice(t->dev));
+// t->err[0..2] = squared error norms of sigma, psi, Omega (no host sync)
+static int enqueue_error(zg_traj* t) {
   CombineCoefs cf;
   cf.n = 0;
   for (int j = 0; j < t->stages; ++j)
@@ -772,6 +879,31 @@ int zg_error_norm2(zg_traj* t, double* err2) {
   }
   ZG_TRY(launch_reduce_partials(t->partial, t->nblk_err, 3, t->err, t->stream));
   prof_end(t, ZG_PROF_ERROR);
+  return ZG_OK;
+}
+
+// y <- sum_j CH_j Y_j, skipped on the device when gate != null and *gate == 0
+static int enqueue_update(zg_traj* t, const int* gate) {
+  CombineCoefs cf;
+  cf.n = 0;
+  prof_begin(t, ZG_PROF_UPDATE);
+  if (t->precision == ZG_PREC_F64) {
+    for (int j = 0; j <= t->stages; ++j)
+      if (t->CH[j] != 0.0) { cf.idx[cf.n] = j; cf.c[cf.n] = t->CH[j]; ++cf.n; }
+    ZG_TRY(launch_step_fourth_c128(t->Y, t->S, t->stages, cf, t->S, t->stream, gate));
+  } else {
+    for (int j = 0; j < t->stages; ++j)
+      if (t->CH[j] != 0.0) { cf.idx[cf.n] = j; cf.c[cf.n] = t->CH[j]; ++cf.n; }
+    ZG_TRY(launch_update_mixed(t->Y, t->y32, t->K32, t->S, cf, t->S, t->stream, gate));
+  }
+  prof_end(t, ZG_PROF_UPDATE);
+  return ZG_OK;
+}
+
+int zg_error_norm2(zg_traj* t, double* err2) {
+  ZG_REQUIRE(t && err2, "null argument");
+  ZG_CHECK_CUDA(cudaSetDevice(t->dev));
+  ZG_TRY(enqueue_error(t));
   ZG_CHECK_CUDA(cudaMemcpyAsync(err2, t->err, 3 * sizeof(double), cudaMemcpyDeviceToHost, t->stream));
   int herr = 0;
   if (t->tc_err) ZG_CHECK_CUDA(cudaMemcpyAsync(&herr, t->tc_err, sizeof(int), cudaMemcpyDeviceToHost, t->stream));
@@ -787,24 +919,75 @@ int zg_error_norm2(zg_traj* t, double* err2) {
 int zg_step_fourth(zg_traj* t) {
   ZG_REQUIRE(t, "null argument");
   ZG_CHECK_CUDA(cudaSetDevice(t->dev));
-  CombineCoefs cf;
-  cf.n = 0;
-  prof_begin(t, ZG_PROF_UPDATE);
-  if (t->precision == ZG_PREC_F64) {
-    for (int j = 0; j <= t->stages; ++j)
-      if (t->CH[j] != 0.0) { cf.idx[cf.n] = j; cf.c[cf.n] = t->CH[j]; ++cf.n; }
-    ZG_TRY(launch_step_fourth_c128(t->Y, t->S, t->stages, cf, t->S, t->stream));
-  } else {
-    for (int j = 0; j < t->stages; ++j)
-      if (t->CH[j] != 0.0) { cf.idx[cf.n] = j; cf.c[cf.n] = t->CH[j]; ++cf.n; }
-    ZG_TRY(launch_update_mixed(t->Y, t->y32, t->K32, t->S, cf, t->S, t->stream));
-  }
-  prof_end(t, ZG_PROF_UPDATE);
+  ZG_TRY(enqueue_update(t, nullptr));
   ZG_CHECK_CUDA(cudaStreamSynchronize(t->stream));
   return ZG_OK;
 }
 
 }  // extern "C"
+
+static int presize_workspaces(zg_traj* t) {
+  if (t->precision == ZG_PREC_F64) return rhs_f64(t, 0, t->d_params, ZG_DH_NONE, 0.0, false, true);
+  return rhs_mixed(t, 0, t->d_params, ZG_DH_NONE, 0.0, false, true);
+}
+
+// One attempt with the controller on the device, enqueued without host syncs
+// (the body of the attempt graph): stages, error norm, control, gated update,
+// advance, then the controller and the tensor-core error flag to pinned memory.
+static int enqueue_attempt_device(zg_traj* t) {
+  cudaStream_t s = t->stream;
+  for (int i = 0; i < t->stages; ++i) {
+    ZG_TRY(zg_stage_input(t, i));
+    prof_begin(t, ZG_PROF_RHS);
+    ZG_TRY(launch_stage_prologue(t->ctl, t->gbias, t->A[i], t->hbar, t->d_params, s));
+    if (t->precision == ZG_PREC_F64)
+      ZG_TRY(rhs_f64(t, i, t->d_params, t->g_dH_mode, t->g_U, i == 0));
+    else
+      ZG_TRY(rhs_mixed(t, i, t->d_params, t->g_dH_mode, t->g_U, i == 0));
+    prof_end(t, ZG_PROF_RHS);
+  }
+  ZG_TRY(enqueue_error(t));
+  ZG_TRY(launch_control(t->err, t->ctl, s));
+  ZG_TRY(enqueue_update(t, &t->ctl->accepted));
+  ZG_TRY(launch_advance(t->ctl, t->J, t->L, t->d_recs, ZG_GRAPH_MAX_BATCH, s));
+  return ZG_OK;
+}
+
+static int capture_attempt_graph(zg_traj* t) {
+  drop_graph(t);
+  ZG_CHECK_CUDA(cudaStreamSynchronize(t->stream));
+  const long long k0 = t_launches;
+  ZG_CHECK_CUDA(cudaStreamBeginCapture(t->stream, cudaStreamCaptureModeThreadLocal));
+  t->capturing = true;
+  const int st = enqueue_attempt_device(t);
+  t->capturing = false;
+  cudaGraph_t g = nullptr;
+  const cudaError_t ce = cudaStreamEndCapture(t->stream, &g);
+  // nothing ran during capture: take the captured kernels off the launch count
+  t->graph_kernels = t_launches - k0;
+  g_launches.fetch_sub(t->graph_kernels);
+  t_launches = k0;
+  if (st != ZG_OK) {
+    if (g) cudaGraphDestroy(g);
+    t->graph_kernels = 0;
+    return st;
+  }
+  if (ce != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    t->graph_kernels = 0;
+    set_error("attempt graph capture failed: %s", cudaGetErrorString(ce));
+    return ZG_ECUDA;
+  }
+  t->graph = g;
+  const cudaError_t ie = cudaGraphInstantiate(&t->gexec, g, 0);
+  if (ie != cudaSuccess) {
+    t->gexec = nullptr;
+    drop_graph(t);
+    set_error("attempt graph instantiation failed: %s", cudaGetErrorString(ie));
+    return ZG_ECUDA;
+  }
+  return ZG_OK;
+}
 
 static double bias_value(const zg_bias& b, double t, int a) {
   double V = 0.0;
@@ -874,6 +1057,72 @@ int zg_get_sigma(zg_traj* t, int slot, double* host) {
   return ZG_OK;
 }
 
+int zg_graph_prepare(zg_traj* t, const zg_bias* bias, int dH_mode, double hubbard_U) {
+  ZG_REQUIRE(t && bias, "null argument");
+  ZG_REQUIRE(dH_mode == ZG_DH_NONE || dH_mode == ZG_DH_HUBBARD, "the attempt graph needs dH_mode NONE or HUBBARD");
+  ZG_REQUIRE(bias->kind >= ZG_BIAS_ZERO && bias->kind <= ZG_BIAS_BOX, "unknown bias kind %d", bias->kind);
+  ZG_CHECK_CUDA(cudaSetDevice(t->dev));
+  t->gbias = *bias;
+  for (int a = t->L; a < ZG_MAX_LEADS; ++a) t->gbias.w[a] = 0.0;
+  t->g_dH_mode = dH_mode;
+  t->g_U = hubbard_U;
+  t->g_prepared = false;
+  ZG_TRY(capture_attempt_graph(t));
+  t->g_prepared = true;
+  return ZG_OK;
+}
+
+int zg_graph_set(zg_traj* t, double time, double h, double eps, double t1) {
+  ZG_REQUIRE(t, "null argument");
+  ZG_REQUIRE(h > 0.0 && eps > 0.0 && std::isfinite(time) && std::isfinite(h), "bad controller values");
+  ZG_CHECK_CUDA(cudaSetDevice(t->dev));
+  ZG_CHECK_CUDA(cudaStreamSynchronize(t->stream));
+  DevCtl c;
+  memset(&c, 0, sizeof(c));
+  c.t = time; c.h = h; c.eps = eps; c.t1 = t1;
+  c.done = time >= t1 ? 1 : 0;
+  *t->ctl_host = c;
+  ZG_CHECK_CUDA(cudaMemcpyAsync(t->ctl, t->ctl_host, sizeof(DevCtl), cudaMemcpyHostToDevice, t->stream));
+  ZG_CHECK_CUDA(cudaStreamSynchronize(t->stream));
+  return ZG_OK;
+}
+
+int zg_graph_run(zg_traj* t, int count, zg_attempt_rec* recs, int* nrec, double* time, double* h, int* done) {
+  ZG_REQUIRE(t, "null argument");
+  ZG_REQUIRE(count >= 0 && count <= ZG_GRAPH_MAX_BATCH, "count %d out of range", count);
+  ZG_REQUIRE(t->g_prepared, "zg_graph_prepare must precede zg_graph_run");
+  ZG_CHECK_CUDA(cudaSetDevice(t->dev));
+  if (!t->gexec) ZG_TRY(capture_attempt_graph(t));  // dropped by zg_set_tableau or zg_profile
+  cudaStream_t s = t->stream;
+  ZG_CHECK_CUDA(cudaMemsetAsync(&t->ctl->rec_n, 0, sizeof(int), s));
+  for (int i = 0; i < count; ++i) {
+    ZG_CHECK_CUDA(cudaGraphLaunch(t->gexec, s));
+    g_launches.fetch_add(t->graph_kernels, std::memory_order_relaxed);
+  }
+  ZG_CHECK_CUDA(cudaMemcpyAsync(t->ctl_host, t->ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost, s));
+  ZG_CHECK_CUDA(cudaMemcpyAsync(t->recs_host, t->d_recs, (size_t)count * sizeof(zg_attempt_rec),
+                                cudaMemcpyDeviceToHost, s));
+  if (t->tc_err) ZG_CHECK_CUDA(cudaMemcpyAsync(t->tcerr_host, t->tc_err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  ZG_CHECK_CUDA(cudaStreamSynchronize(s));
+  if (count > 0) graph_prof_collect(t);  // regions of the last attempt of the batch
+  const DevCtl& c = *t->ctl_host;
+  const int n = std::min(c.rec_n, count);
+  if (recs && n > 0) memcpy(recs, t->recs_host, (size_t)n * sizeof(zg_attempt_rec));
+  if (nrec) *nrec = n;
+  if (time) *time = c.t;
+  if (h) *h = c.h;
+  if (done) *done = c.done;
+  if (t->tc_err && *t->tcerr_host != 0) {
+    set_error("a bounded wait in the tensor-core GEMM gave up (code %d)", *t->tcerr_host);
+    return ZG_ETIMEOUT;
+  }
+  if (c.status != ZG_OK) {
+    set_error("error norm is not finite (%g)", c.TE);
+    return c.status;
+  }
+  return ZG_OK;
+}
+
 int zg_profile(zg_traj* t, int enable) {
   ZG_REQUIRE(t, "null argument");
   ZG_CHECK_CUDA(cudaSetDevice(t->dev));
@@ -888,6 +1137,7 @@ int zg_profile(zg_traj* t, int enable) {
   }
   ZG_CHECK_CUDA(cudaStreamSynchronize(t->stream));
   prof_collect(t);
+  if (P.on != (enable != 0)) drop_graph(t);  // recaptured with or without event nodes
   P.on = enable != 0;
   for (int r = 0; r < ZG_PROF_REGIONS; ++r) { P.ms[r] = 0; P.cnt[r] = 0; }
   return ZG_OK;

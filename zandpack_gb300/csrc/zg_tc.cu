@@ -333,7 +333,7 @@ static int launch_tc(const TcGemm& g, cudaStream_t s) {
   dim3 grid((g.N + BN - 1) / BN, (g.M + TC_BM - 1) / TC_BM);
   k_gemm_tf32x3<BN, STAGES><<<grid, 192, C::SMEM, s>>>(g.Ah, g.Al, g.Bh, g.Bl, g.D, g.M, g.N, g.K, g.ldd, g.err);
   ZG_CHECK_LAUNCH();
-  g_launches.fetch_add(1, std::memory_order_relaxed);
+  count_launch();
   return ZG_OK;
 }
 
@@ -369,7 +369,7 @@ int launch_split_tf32(const float* x, float* hi, float* lo, int64_t n, cudaStrea
   if (n <= 0) return ZG_OK;
   k_split_tf32<<<grid_for(n, 256, 152 * 8), 256, 0, s>>>(x, hi, lo, n);
   ZG_CHECK_LAUNCH();
-  g_launches.fetch_add(1, std::memory_order_relaxed);
+  count_launch();
   return ZG_OK;
 }
 

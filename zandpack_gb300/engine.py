@@ -156,6 +156,28 @@ class Trajectory:
     def step_fourth(self):
         check(lib().zg_step_fourth(self._h))
 
+    # -- graph-launched attempts (controller on the device)
+    def graph_prepare(self, bias, hubbard_U=None):
+        """Capture one controller attempt as a CUDA graph (``zg_graph_prepare``)."""
+        mode = _lib.ZG_DH_HUBBARD if hubbard_U is not None else _lib.ZG_DH_NONE
+        check(lib().zg_graph_prepare(self._h, C.byref(bias), mode, float(hubbard_U or 0.0)))
+        if not hasattr(self, "_recs"):
+            self._recs = (_lib.zg_attempt_rec * _lib.ZG_GRAPH_MAX_BATCH)()
+
+    def graph_set(self, t, h, eps, t1):
+        check(lib().zg_graph_set(self._h, float(t), float(h), float(eps), float(t1)))
+
+    def graph_run(self, count):
+        """Launch ``count`` attempts, one host sync.  Returns (records, t, h,
+        done); each record is (t, h, TE, h_next, accepted, status, J[:L])."""
+        n, tt, hh, done = C.c_int(), C.c_double(), C.c_double(), C.c_int()
+        check(lib().zg_graph_run(self._h, int(count), C.cast(self._recs, C.c_void_p), C.byref(n), C.byref(tt),
+                                 C.byref(hh), C.byref(done)))
+        L = self.layout.NL
+        recs = [(r.t, r.h, r.TE, r.h_next, bool(r.accepted), r.status, np.array(r.J[:L]))
+                for r in self._recs[:n.value]]
+        return recs, tt.value, hh.value, bool(done.value)
+
 
 def native_bias(spec, n_leads):
     """``zg_bias`` for the analytic bias specifications of ``workloads``

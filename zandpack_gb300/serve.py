@@ -4,9 +4,12 @@ Requests arrive as a stream (their ``arrival`` times, seconds).  The server
 admits a request as soon as a slot is free and its estimated device footprint
 fits the HBM budget; an admitted request is built (host input preparation),
 given its own trajectory on the device -- its own CUDA stream, state and step
-size -- and propagated by a worker thread that calls one ``zg_attempt`` per
-Dormand-Prince attempt (the library releases the Python GIL during each
-call).  Trajectories therefore overlap on the GPU while requests that arrive
+size -- and propagated by a worker thread.  In the default ``graph`` mode the
+worker captures one Dormand-Prince attempt as a CUDA graph with the step-size
+controller on the device and launches batches of attempts with one host
+synchronisation each (``zg_graph_run``); ``host`` mode calls one
+``zg_attempt`` per attempt.  ctypes releases the Python GIL during each
+call.  Trajectories therefore overlap on the GPU while requests that arrive
 later wait for memory or a slot.  Each result is the final sigma, the last
 lead currents, the number of attempts and the latency (completion minus
 arrival).
@@ -18,6 +21,7 @@ identical to the same trajectory computed alone.
 from __future__ import annotations
 
 import dataclasses
+import math
 import queue
 import threading
 import time
@@ -68,11 +72,15 @@ class Result:
 
 class Server:
     def __init__(self, build: Callable, estimate: Callable, device=0, max_slots=16, hbm_budget=None,
-                 precision="mixed", keep_sigma=True):
+                 precision="mixed", keep_sigma=True, attempt_mode="graph", max_batch=32):
         self.build, self.estimate = build, estimate
         self.device, self.max_slots = device, max_slots
         self.precision = precision
         self.keep_sigma = keep_sigma
+        if attempt_mode not in ("graph", "host"):
+            raise ValueError("attempt_mode must be 'graph' or 'host'")
+        self.attempt_mode = attempt_mode
+        self.max_batch = max_batch
         if hbm_budget is None:
             import torch
             free, _ = torch.cuda.mem_get_info(device)
@@ -96,12 +104,26 @@ class Server:
             b = native_bias(w.bias, L.NL)
             t, h = w.t0, w.stepsize
             J = None
-            while t < w.t1:
-                TE, acc, t, h, J0 = tr.attempt_native(t, h, w.eps, b, w.hubbard_U)
-                res.attempts += 1
-                if acc:
-                    res.accepted += 1
-                    J = J0
+            if self.attempt_mode == "graph":
+                tr.graph_prepare(b, w.hubbard_U)
+                tr.graph_set(t, h, w.eps, w.t1)
+                finished = t >= w.t1
+                while not finished:
+                    # about as many attempts as the remaining span needs at the current step size
+                    batch = int(min(self.max_batch, max(1, math.ceil((w.t1 - t) / h) + 1)))
+                    recs, t, h, finished = tr.graph_run(batch)
+                    for r in recs:
+                        res.attempts += 1
+                        if r[4]:
+                            res.accepted += 1
+                            J = r[6]
+            else:
+                while t < w.t1:
+                    TE, acc, t, h, J0 = tr.attempt_native(t, h, w.eps, b, w.hubbard_U)
+                    res.attempts += 1
+                    if acc:
+                        res.accepted += 1
+                        J = J0
             res.t_end = t
             res.currents = J
             if self.keep_sigma:
