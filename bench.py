@@ -413,7 +413,8 @@ def run_ensemble(args):
     from zandpack_gb300.serve import Server, c4_estimate
     from zandpack_gb300.workloads import c4_requests, c4_workload
     reqs = c4_requests(args.ensemble, rate=50.0, seed=1004, t_span=args.ensemble_fs)
-    srv = Server(c4_workload, c4_estimate, max_slots=args.slots, precision=args.precision, keep_sigma=False)
+    srv = Server(c4_workload, c4_estimate, max_slots=args.slots, precision=args.precision, keep_sigma=False,
+                 prep_workers=args.prep_workers)
     res, stats = srv.run(reqs)
     stats["t_span_fs"] = args.ensemble_fs
     stats["rate_per_s"] = 50.0
@@ -453,6 +454,8 @@ def main():
     ap.add_argument("--ensemble", type=int, default=512, help="requests of the serving ensemble (0: skip)")
     ap.add_argument("--ensemble-fs", type=float, default=1.0, help="simulated fs per ensemble trajectory")
     ap.add_argument("--slots", type=int, default=32, help="concurrent trajectories of the ensemble")
+    ap.add_argument("--prep-workers", type=int, default=max(1, min(12, (os.cpu_count() or 4) - 4)),
+                    help="worker processes preparing ensemble requests on the host")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -93,6 +93,9 @@ int zg_set_tableau(zg_traj* t, int stages, const double* A, const double* B,
  * `stages` = y (SIGS[-1] etc.).  Flat compact vector of `state size` complex. */
 int zg_set_state(zg_traj* t, int slot, const double* host);
 int zg_get_state(zg_traj* t, int slot, double* host);
+/* y = (sigma, psi = 0, Omega = 0): the reference's initial state
+ * (Zandpack/mpi/zand:536-538) from the n*n sigma alone. */
+int zg_set_sigma(zg_traj* t, const double* sigma);
 
 /* Stage input Y_i = sum_{j in idxholder[i]} B[i,j] Y_j (Y_stages = y); for
  * i = 0 the input is y itself.  Replaces the MM / step_*_forward_nb stage

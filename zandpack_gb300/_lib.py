@@ -76,6 +76,7 @@ _SIGS = {
     "zg_set_tableau": ([_P, C.c_int, _P, _P, _P, _P], C.c_int),
     "zg_set_state": ([_P, C.c_int, _P], C.c_int),
     "zg_get_state": ([_P, C.c_int, _P], C.c_int),
+    "zg_set_sigma": ([_P, _P], C.c_int),
     "zg_stage_input": ([_P, C.c_int], C.c_int),
     "zg_get_stage_sigma": ([_P, _P], C.c_int),
     "zg_set_dH": ([_P, _P], C.c_int),

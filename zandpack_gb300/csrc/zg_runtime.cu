@@ -9,6 +9,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <vector>
 
 #include "zg_kernels.cuh"
@@ -24,13 +25,75 @@ void set_error(const char* fmt, ...) {
   va_end(ap);
 }
 
+// Device memory of trajectories comes from one stream-ordered pool per device
+// that keeps freed memory for the next trajectory: creating and destroying
+// trajectories (the serving loop) then neither maps memory nor synchronises
+// the device, as cudaMalloc/cudaFree would.  The pool is trimmed when the
+// device's last trajectory is destroyed.
+#define ZG_MAX_DEVICES 64
+static std::mutex g_pool_mu;
+static cudaMemPool_t g_pool[ZG_MAX_DEVICES] = {};
+static int g_live[ZG_MAX_DEVICES] = {};
+
+static int pool_for(int dev, cudaMemPool_t* out) {
+  ZG_REQUIRE(dev >= 0 && dev < ZG_MAX_DEVICES, "device %d out of range", dev);
+  std::lock_guard<std::mutex> lk(g_pool_mu);
+  if (!g_pool[dev]) {
+    cudaMemPoolProps props;
+    memset(&props, 0, sizeof(props));
+    props.allocType = cudaMemAllocationTypePinned;
+    props.handleTypes = cudaMemHandleTypeNone;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    ZG_CHECK_CUDA(cudaMemPoolCreate(&g_pool[dev], &props));
+    uint64_t keep = UINT64_MAX;
+    ZG_CHECK_CUDA(cudaMemPoolSetAttribute(g_pool[dev], cudaMemPoolAttrReleaseThreshold, &keep));
+  }
+  *out = g_pool[dev];
+  return ZG_OK;
+}
+
+// Pinned host blocks of the controller mirrors, recycled through a free list
+// (cudaMallocHost/cudaFreeHost are slow and serialise concurrent threads).
+static std::mutex g_pinned_mu;
+static std::vector<void*> g_pinned_free;
+static int pinned_get(size_t bytes, void** out) {
+  {
+    std::lock_guard<std::mutex> lk(g_pinned_mu);
+    if (!g_pinned_free.empty()) {
+      *out = g_pinned_free.back();
+      g_pinned_free.pop_back();
+      return ZG_OK;
+    }
+  }
+  if (cudaMallocHost(out, bytes) != cudaSuccess) {
+    set_error("pinned host allocation of %zu bytes failed", bytes);
+    return ZG_ENOMEM;
+  }
+  return ZG_OK;
+}
+static void pinned_put(void* p) {
+  if (!p) return;
+  std::lock_guard<std::mutex> lk(g_pinned_mu);
+  g_pinned_free.push_back(p);
+}
+
+}  // namespace zg
+struct zg_traj;
+namespace zg {
+static cudaStream_t traj_stream(const zg_traj* t);
+static int traj_device(const zg_traj* t);
+
 template <class T>
-static int dalloc(T** p, size_t count) {
+static int dalloc(const zg_traj* t, T** p, size_t count) {
   *p = nullptr;
   if (count == 0) count = 1;
-  cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+  cudaMemPool_t pool;
+  ZG_TRY(pool_for(traj_device(t), &pool));
+  cudaError_t e = cudaMallocFromPoolAsync((void**)p, count * sizeof(T), pool, traj_stream(t));
   if (e != cudaSuccess) {
-    set_error("cudaMalloc of %zu bytes failed: %s", count * sizeof(T), cudaGetErrorString(e));
+    *p = nullptr;
+    set_error("device allocation of %zu bytes failed: %s", count * sizeof(T), cudaGetErrorString(e));
     return e == cudaErrorMemoryAllocation ? ZG_ENOMEM : ZG_ECUDA;
   }
   return ZG_OK;
@@ -59,6 +122,12 @@ static const double kDopB[7][8] = {
     {35. / 384, 0, 500. / 1113, 125. / 192, -2187. / 6784, 11. / 84, 0, 1}};
 static const double kB5[7] = {35. / 384, 0, 500. / 1113, 125. / 192, -2187. / 6784, 11. / 84, 0};
 static const double kB4[7] = {5179. / 57600, 0, 7571. / 16695, 393. / 640, -92097. / 339200, 187. / 2100, 1. / 40};
+
+// one pinned host block per trajectory: controller mirror, currents, error flag, attempt records
+static const size_t kPinJ = (sizeof(DevCtl) + 63) / 64 * 64;
+static const size_t kPinErr = kPinJ + (ZG_MAX_LEADS * sizeof(double) + 63) / 64 * 64;
+static const size_t kPinRecs = kPinErr + 64;
+static const size_t kPinnedBytes = kPinRecs + ZG_GRAPH_MAX_BATCH * sizeof(zg_attempt_rec);
 
 struct zg_traj {
   int dev = 0;
@@ -114,6 +183,7 @@ struct zg_traj {
   zg_attempt_rec* d_recs = nullptr;     // ZG_GRAPH_MAX_BATCH records of the current batch
   zg_attempt_rec* recs_host = nullptr;  // pinned
   bool capturing = false;
+  bool counted = false;  // included in the live trajectories of its device
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
   long long graph_kernels = 0;  // kernels of this library in one launch of the graph
@@ -157,6 +227,11 @@ RhsDev<float> zg_traj::dev_view<float>() const {
   d.Xp = Xp32; d.Xm = Xm32; d.GLP = GLP32; d.dGP = dGP32; d.XI = XI32; d.U = U32; d.V = V32;
   return d;
 }
+
+namespace zg {
+static cudaStream_t traj_stream(const zg_traj* t) { return t->stream; }
+static int traj_device(const zg_traj* t) { return t->dev; }
+}  // namespace zg
 
 // ---------------------------------------------------------------- profiling
 static void prof_collect(zg_traj* t) {
@@ -234,16 +309,18 @@ static void drop_graph(zg_traj* t) {
   t->gprof_e.clear();
 }
 
+// stream-ordered release of a trajectory buffer back to the pool
+static void dfree(zg_traj* t, void* p) {
+  if (p) cudaFreeAsync(p, t->stream);
+}
+
 static void free_traj(zg_traj* t) {
   if (!t) return;
   drop_graph(t);
-  if (t->recs_host) cudaFreeHost(t->recs_host);
-  if (t->d_recs) cudaFree(t->d_recs);
-  if (t->ctl_host) cudaFreeHost(t->ctl_host);
-  if (t->J_host) cudaFreeHost(t->J_host);
-  if (t->tcerr_host) cudaFreeHost(t->tcerr_host);
-  if (t->d_params) cudaFree(t->d_params);
-  if (t->ctl) cudaFree(t->ctl);
+  pinned_put(t->ctl_host);  // one block: ctl_host, J_host, tcerr_host, recs_host
+  dfree(t, t->d_recs);
+  dfree(t, t->d_params);
+  dfree(t, t->ctl);
   if (t->prof.created)
     for (int r = 0; r < ZG_PROF_REGIONS; ++r)
       for (int i = 0; i < t->prof.RING; ++i) {
@@ -257,9 +334,18 @@ static void free_traj(zg_traj* t) {
                   t->XI32, t->XIS32, t->IXI32, t->U32, t->V32, t->y32, t->K32, t->stage32, t->Hth, t->Htl, t->BHh,
                   t->BHl, t->BSh, t->BSl, t->T32, t->R1p, t->Pc32, t->sigC32, t->G32, t->R2_32, t->ZA32, t->ZB32,
                   t->conv64, t->sig64, t->tc_err, t->ws64, t->ws32};
-  for (void* p : ptrs)
-    if (p) cudaFree(p);
-  if (t->stream) cudaStreamDestroy(t->stream);
+  for (void* p : ptrs) dfree(t, p);
+  if (t->stream) {
+    cudaStreamSynchronize(t->stream);
+    cudaStreamDestroy(t->stream);
+    bool trim = false;
+    {
+      std::lock_guard<std::mutex> lk(g_pool_mu);
+      if (t->counted && --g_live[t->dev] == 0) trim = true;
+    }
+    cudaMemPool_t pool;
+    if (trim && pool_for(t->dev, &pool) == ZG_OK) cudaMemPoolTrimTo(pool, 0);
+  }
   delete t;
 }
 
@@ -267,16 +353,16 @@ static int alloc_state(zg_traj* t, int stages) {
   const bool mixed = t->precision == ZG_PREC_MIXED;
   const int yslots = mixed ? 1 : stages + 1;
   if (!t->Y || t->y_slots != yslots) {
-    if (t->Y) cudaFree(t->Y);
+    dfree(t, t->Y);
     t->Y = nullptr;
-    ZG_TRY(dalloc(&t->Y, (size_t)yslots * t->S));
+    ZG_TRY(dalloc(t, &t->Y, (size_t)yslots * t->S));
     t->y_slots = yslots;
     ZG_CHECK_CUDA(cudaMemsetAsync(t->Y, 0, (size_t)yslots * t->S * sizeof(double2), t->stream));
   }
   if (mixed && (!t->K32 || t->k_slots != stages)) {
-    if (t->K32) cudaFree(t->K32);
+    dfree(t, t->K32);
     t->K32 = nullptr;
-    ZG_TRY(dalloc(&t->K32, (size_t)stages * t->S));
+    ZG_TRY(dalloc(t, &t->K32, (size_t)stages * t->S));
     t->k_slots = stages;
     ZG_CHECK_CUDA(cudaMemsetAsync(t->K32, 0, (size_t)stages * t->S * sizeof(float2), t->stream));
   }
@@ -347,12 +433,13 @@ static int create_mixed(zg_traj* t, const zg_layout* Lo, const std::vector<doubl
   ml.st_om = ml.st_psil + N * np;
   ml.st_S = ml.st_om + N * Ns + Ns * Nf;
   cudaStream_t s = t->stream;
-  std::vector<float2> tmp;
+  // host copies stay alive until the stream synchronisation at the end
+  std::vector<std::vector<float2>> keep;
   auto up32 = [&](float2** dst, const double* src, size_t cnt) -> int {
-    tmp.resize(cnt);
-    to_f32((const double2*)src, tmp.data(), cnt);
-    ZG_TRY(dalloc(dst, cnt));
-    ZG_CHECK_CUDA(cudaMemcpy(*dst, tmp.data(), cnt * sizeof(float2), cudaMemcpyHostToDevice));
+    keep.emplace_back(cnt);
+    to_f32((const double2*)src, keep.back().data(), cnt);
+    ZG_TRY(dalloc(t, dst, cnt));
+    ZG_CHECK_CUDA(cudaMemcpyAsync(*dst, keep.back().data(), cnt * sizeof(float2), cudaMemcpyHostToDevice, s));
     return ZG_OK;
   };
   ZG_TRY(up32(&t->Xp32, Lo->Xp, N));
@@ -364,18 +451,18 @@ static int create_mixed(zg_traj* t, const zg_layout* Lo, const std::vector<doubl
   ZG_TRY(up32(&t->IXI32, Lo->IXI, N * nc));
   ZG_TRY(up32(&t->U32, (const double*)U.data(), N * nc));
   ZG_TRY(up32(&t->V32, (const double*)V.data(), N * nc));
-  ZG_TRY(dalloc(&t->y32, t->S));
-  ZG_TRY(dalloc(&t->stage32, ml.st_S));
+  ZG_TRY(dalloc(t, &t->y32, t->S));
+  ZG_TRY(dalloc(t, &t->stage32, ml.st_S));
   ZG_CHECK_CUDA(cudaMemsetAsync(t->stage32, 0, ml.st_S * sizeof(float2), s));  // psi padding columns stay zero
-  ZG_TRY(dalloc(&t->Hth, n * 2 * np)); ZG_TRY(dalloc(&t->Htl, n * 2 * np));
-  ZG_TRY(dalloc(&t->BHh, 4 * np * np)); ZG_TRY(dalloc(&t->BHl, 4 * np * np));
-  ZG_TRY(dalloc(&t->BSh, 4 * np * np)); ZG_TRY(dalloc(&t->BSl, 4 * np * np));
-  ZG_TRY(dalloc(&t->T32, n * np)); ZG_TRY(dalloc(&t->R1p, N * np));
-  ZG_TRY(dalloc(&t->Pc32, 2 * L * n * nc)); ZG_TRY(dalloc(&t->sigC32, L * n * nc)); ZG_TRY(dalloc(&t->G32, N * L * nc));
-  ZG_TRY(dalloc(&t->R2_32, std::max<int64_t>(Ns, 1) * n));
-  ZG_TRY(dalloc(&t->ZA32, L * N * nc)); ZG_TRY(dalloc(&t->ZB32, L * std::max<int64_t>(Ns, 1) * nc));
-  ZG_TRY(dalloc(&t->sig64, n * n));
-  ZG_TRY(dalloc(&t->tc_err, 1));
+  ZG_TRY(dalloc(t, &t->Hth, n * 2 * np)); ZG_TRY(dalloc(t, &t->Htl, n * 2 * np));
+  ZG_TRY(dalloc(t, &t->BHh, 4 * np * np)); ZG_TRY(dalloc(t, &t->BHl, 4 * np * np));
+  ZG_TRY(dalloc(t, &t->BSh, 4 * np * np)); ZG_TRY(dalloc(t, &t->BSl, 4 * np * np));
+  ZG_TRY(dalloc(t, &t->T32, n * np)); ZG_TRY(dalloc(t, &t->R1p, N * np));
+  ZG_TRY(dalloc(t, &t->Pc32, 2 * L * n * nc)); ZG_TRY(dalloc(t, &t->sigC32, L * n * nc)); ZG_TRY(dalloc(t, &t->G32, N * L * nc));
+  ZG_TRY(dalloc(t, &t->R2_32, std::max<int64_t>(Ns, 1) * n));
+  ZG_TRY(dalloc(t, &t->ZA32, L * N * nc)); ZG_TRY(dalloc(t, &t->ZB32, L * std::max<int64_t>(Ns, 1) * nc));
+  ZG_TRY(dalloc(t, &t->sig64, n * n));
+  ZG_TRY(dalloc(t, &t->tc_err, 1));
   ZG_CHECK_CUDA(cudaMemsetAsync(t->tc_err, 0, sizeof(int), s));
   // tensor maps of the two tensor-core GEMMs (fixed buffers)
   const float* psih = (const float*)(t->stage32 + ml.st_psih);
@@ -384,6 +471,7 @@ static int create_mixed(zg_traj* t, const zg_layout* Lo, const std::vector<doubl
                          (int)(2 * np), (int)(2 * np), t->tc_err));
   ZG_TRY(tc_gemm_prepare(t->gR1, psih, psil, t->BHh, t->BHl, 2 * np, 2 * np, (float*)t->R1p, 2 * np, (int)N,
                          (int)(2 * np), (int)(2 * np), t->tc_err));
+  ZG_CHECK_CUDA(cudaStreamSynchronize(s));
   return ZG_OK;
 }
 
@@ -402,6 +490,7 @@ int zg_traj_create(int device, const zg_layout* Lo, int precision, zg_traj** out
                  Lo->n_sourced >= 0 && Lo->n_sourced <= Lo->n_modes && Lo->nc > 0,
              "bad layout sizes");
   ZG_REQUIRE(Lo->hbar > 0, "hbar must be positive");
+  ZG_REQUIRE(device >= 0 && device < ZG_MAX_DEVICES, "device %d out of range", device);
   ZG_CHECK_CUDA(cudaSetDevice(device));
   zg_traj* t = new zg_traj();
   t->dev = device;
@@ -438,11 +527,16 @@ int zg_traj_create(int device, const zg_layout* Lo, int precision, zg_traj** out
   if (cudaStreamCreateWithFlags(&t->stream, cudaStreamNonBlocking) != cudaSuccess) {
     free_traj(t); set_error("cudaStreamCreate failed"); return ZG_ECUDA;
   }
-  ZG_STEP(dalloc(&t->H0, n * n));
-  ZG_STEP(dalloc(&t->Xp, N)); ZG_STEP(dalloc(&t->Xm, N)); ZG_STEP(dalloc(&t->GLP, N)); ZG_STEP(dalloc(&t->dGP, N));
-  ZG_STEP(dalloc(&t->XI, N * nc)); ZG_STEP(dalloc(&t->IXI, N * nc)); ZG_STEP(dalloc(&t->XIS, N * nc));
-  ZG_STEP(dalloc(&t->U, N * nc)); ZG_STEP(dalloc(&t->V, N * nc));
-  ZG_STEP(dalloc(&t->mode_lead, N)); ZG_STEP(dalloc(&t->lead_cols, L * nc)); ZG_STEP(dalloc(&t->colmap, L * n));
+  {
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    ++g_live[t->dev];
+    t->counted = true;
+  }
+  ZG_STEP(dalloc(t, &t->H0, n * n));
+  ZG_STEP(dalloc(t, &t->Xp, N)); ZG_STEP(dalloc(t, &t->Xm, N)); ZG_STEP(dalloc(t, &t->GLP, N)); ZG_STEP(dalloc(t, &t->dGP, N));
+  ZG_STEP(dalloc(t, &t->XI, N * nc)); ZG_STEP(dalloc(t, &t->IXI, N * nc)); ZG_STEP(dalloc(t, &t->XIS, N * nc));
+  ZG_STEP(dalloc(t, &t->U, N * nc)); ZG_STEP(dalloc(t, &t->V, N * nc));
+  ZG_STEP(dalloc(t, &t->mode_lead, N)); ZG_STEP(dalloc(t, &t->lead_cols, L * nc)); ZG_STEP(dalloc(t, &t->colmap, L * n));
   ZG_STEP(upload<double2>(t->H0, Lo->H0, n * n, t->stream));
   ZG_STEP(upload<double2>(t->Xp, Lo->Xp, N, t->stream));
   ZG_STEP(upload<double2>(t->Xm, Lo->Xm, N, t->stream));
@@ -472,34 +566,35 @@ int zg_traj_create(int device, const zg_layout* Lo, int precision, zg_traj** out
   std::vector<OmTile> tiles;
   build_tiles(t, tiles);
   t->ntiles = (int)tiles.size();
-  ZG_STEP(dalloc(&t->tiles, tiles.size()));
+  ZG_STEP(dalloc(t, &t->tiles, tiles.size()));
   ZG_STEP(upload<OmTile>(t->tiles, tiles.data(), tiles.size(), t->stream));
-  ZG_STEP(dalloc(&t->dH, n * n));
-  ZG_STEP(dalloc(&t->J, L));
-  ZG_STEP(dalloc(&t->Jpart, L * 64));
-  ZG_STEP(dalloc(&t->d_params, 1));
-  ZG_STEP(dalloc(&t->ctl, 1));
-  ZG_STEP(dalloc(&t->d_recs, ZG_GRAPH_MAX_BATCH));
-  if (cudaMallocHost((void**)&t->ctl_host, sizeof(DevCtl)) != cudaSuccess ||
-      cudaMallocHost((void**)&t->J_host, ZG_MAX_LEADS * sizeof(double)) != cudaSuccess ||
-      cudaMallocHost((void**)&t->tcerr_host, sizeof(int)) != cudaSuccess ||
-      cudaMallocHost((void**)&t->recs_host, ZG_GRAPH_MAX_BATCH * sizeof(zg_attempt_rec)) != cudaSuccess) {
-    free_traj(t);
-    set_error("pinned host allocation failed");
-    return ZG_ENOMEM;
+  ZG_STEP(dalloc(t, &t->dH, n * n));
+  ZG_STEP(dalloc(t, &t->J, L));
+  ZG_STEP(dalloc(t, &t->Jpart, L * 64));
+  ZG_STEP(dalloc(t, &t->d_params, 1));
+  ZG_STEP(dalloc(t, &t->ctl, 1));
+  ZG_STEP(dalloc(t, &t->d_recs, ZG_GRAPH_MAX_BATCH));
+  {
+    void* blk = nullptr;
+    ZG_STEP(pinned_get(kPinnedBytes, &blk));
+    char* b = (char*)blk;
+    t->ctl_host = (DevCtl*)b;
+    t->J_host = (double*)(b + kPinJ);
+    t->tcerr_host = (int*)(b + kPinErr);
+    t->recs_host = (zg_attempt_rec*)(b + kPinRecs);
   }
   memset(t->ctl_host, 0, sizeof(DevCtl));
   *t->tcerr_host = 0;
   ZG_CHECK_CUDA(cudaMemsetAsync(t->ctl, 0, sizeof(DevCtl), t->stream));
   t->nblk_err = terr2_nblocks(t->S);
-  ZG_STEP(dalloc(&t->partial, 3 * (size_t)t->nblk_err));
-  ZG_STEP(dalloc(&t->err, 3));
+  ZG_STEP(dalloc(t, &t->partial, 3 * (size_t)t->nblk_err));
+  ZG_STEP(dalloc(t, &t->err, 3));
   if (precision == ZG_PREC_F64) {
-    ZG_STEP(dalloc(&t->Ystage, t->S));
-    ZG_STEP(dalloc(&t->Ht, n * n)); ZG_STEP(dalloc(&t->T, n * n));
-    ZG_STEP(dalloc(&t->Pc, 2 * L * n * nc)); ZG_STEP(dalloc(&t->sigC, L * n * nc)); ZG_STEP(dalloc(&t->G, N * L * nc));
-    ZG_STEP(dalloc(&t->R2, std::max<int64_t>(Ns, 1) * n));
-    ZG_STEP(dalloc(&t->ZA, L * N * nc)); ZG_STEP(dalloc(&t->ZB, L * std::max<int64_t>(Ns, 1) * nc));
+    ZG_STEP(dalloc(t, &t->Ystage, t->S));
+    ZG_STEP(dalloc(t, &t->Ht, n * n)); ZG_STEP(dalloc(t, &t->T, n * n));
+    ZG_STEP(dalloc(t, &t->Pc, 2 * L * n * nc)); ZG_STEP(dalloc(t, &t->sigC, L * n * nc)); ZG_STEP(dalloc(t, &t->G, N * L * nc));
+    ZG_STEP(dalloc(t, &t->R2, std::max<int64_t>(Ns, 1) * n));
+    ZG_STEP(dalloc(t, &t->ZA, L * N * nc)); ZG_STEP(dalloc(t, &t->ZB, L * std::max<int64_t>(Ns, 1) * nc));
   } else {
     ZG_STEP(create_mixed(t, Lo, U, V));
   }
@@ -548,7 +643,7 @@ int zg_set_tableau(zg_traj* t, int stages, const double* A, const double* B, con
 }
 
 static int ensure_conv64(zg_traj* t) {
-  if (!t->conv64) ZG_TRY(dalloc(&t->conv64, t->S));
+  if (!t->conv64) ZG_TRY(dalloc(t, &t->conv64, t->S));
   return ZG_OK;
 }
 
@@ -567,6 +662,17 @@ int zg_set_state(zg_traj* t, int slot, const double* host) {
     ZG_CHECK_CUDA(cudaMemcpyAsync(t->conv64, host, bytes, cudaMemcpyHostToDevice, t->stream));
     ZG_TRY(launch_f64_to_f32(t->conv64, t->kslot(slot), t->S, t->stream));
   }
+  ZG_CHECK_CUDA(cudaStreamSynchronize(t->stream));
+  return ZG_OK;
+}
+
+int zg_set_sigma(zg_traj* t, const double* sigma) {
+  ZG_REQUIRE(t && sigma, "null argument");
+  ZG_CHECK_CUDA(cudaSetDevice(t->dev));
+  double2* y = y64(t);
+  ZG_CHECK_CUDA(cudaMemsetAsync(y, 0, t->S * sizeof(double2), t->stream));
+  ZG_CHECK_CUDA(cudaMemcpyAsync(y, sigma, (size_t)t->n * t->n * sizeof(double2), cudaMemcpyHostToDevice, t->stream));
+  if (t->precision == ZG_PREC_MIXED) ZG_TRY(launch_f64_to_f32(t->Y, t->y32, t->S, t->stream));
   ZG_CHECK_CUDA(cudaStreamSynchronize(t->stream));
   return ZG_OK;
 }
@@ -692,10 +798,10 @@ static int run_batches(zg_traj* t, std::vector<GemmProb<R>>& all, typename cx<R>
     if (need > *cap) {
       ZG_REQUIRE(!t->capturing, "split-K workspace must be sized before graph capture");
       ZG_CHECK_CUDA(cudaStreamSynchronize(s));
-      if (*ws) cudaFree(*ws);
+      dfree(t, *ws);
       *ws = nullptr;
       *cap = 0;
-      ZG_TRY(dalloc(ws, need));
+      ZG_TRY(dalloc(t, ws, need));
       *cap = need;
     }
     batch.ws = *ws;

@@ -101,6 +101,10 @@ class Trajectory:
 
     def set_y(self, sig, psi=None, omg=None):
         L = self.layout
+        if psi is None and omg is None:  # psi = Omega = 0: only sigma crosses to the device
+            s = np.ascontiguousarray(np.asarray(sig, np.complex128).reshape(L.n, L.n))
+            check(lib().zg_set_sigma(self._h, _ptr(s)))
+            return
         if psi is None or omg is None:
             z = L.unpack(np.zeros(L.size, complex))
             psi = z[1] if psi is None else psi

@@ -1,9 +1,11 @@
 """Serving many independent propagations on one GPU (continuous batching).
 
-Requests arrive as a stream (their ``arrival`` times, seconds).  The server
-admits a request as soon as a slot is free and its estimated device footprint
-fits the HBM budget; an admitted request is built (host input preparation),
-given its own trajectory on the device -- its own CUDA stream, state and step
+Requests arrive as a stream (their ``arrival`` times, seconds).  A request's
+host input preparation (its Arrays and compact layout) starts when it arrives,
+in a pool of worker processes when ``prep_workers`` > 0 (numpy work holds the
+GIL, so threads alone serialise it).  The server admits a request as soon as a
+slot is free and its estimated device footprint fits the HBM budget; an
+admitted request is given its own trajectory on the device -- its own CUDA stream, state and step
 size -- and propagated by a worker thread.  In the default ``graph`` mode the
 worker captures one Dormand-Prince attempt as a CUDA graph with the step-size
 controller on the device and launches batches of attempts with one host
@@ -20,9 +22,11 @@ identical to the same trajectory computed alone.
 """
 from __future__ import annotations
 
+import concurrent.futures as cf
 import dataclasses
 import math
-import queue
+import multiprocessing as mp
+import os
 import threading
 import time
 from typing import Callable, List, Optional
@@ -72,7 +76,7 @@ class Result:
 
 class Server:
     def __init__(self, build: Callable, estimate: Callable, device=0, max_slots=16, hbm_budget=None,
-                 precision="mixed", keep_sigma=True, attempt_mode="graph", max_batch=32):
+                 precision="mixed", keep_sigma=True, attempt_mode="graph", max_batch=32, prep_workers=0):
         self.build, self.estimate = build, estimate
         self.device, self.max_slots = device, max_slots
         self.precision = precision
@@ -81,6 +85,7 @@ class Server:
             raise ValueError("attempt_mode must be 'graph' or 'host'")
         self.attempt_mode = attempt_mode
         self.max_batch = max_batch
+        self.prep_workers = int(prep_workers)
         if hbm_budget is None:
             import torch
             free, _ = torch.cuda.mem_get_info(device)
@@ -91,15 +96,14 @@ class Server:
         self.peak_in_use = 0
         self.peak_slots = 0
 
-    def _run_one(self, req, t_admit, fp, out: List[Result], done: threading.Semaphore):
+    def _run_one(self, req, t_admit, fp, out: List[Result], done: threading.Semaphore, prepared=None):
         res = Result(id=req["id"], arrival=req["arrival"], admitted=t_admit, finished=0.0, attempts=0, accepted=0,
                      t_end=0.0, sigma=None, currents=None, n=req.get("n", 0), modes=0)
         tr = None
         try:
-            w = self.build(req)
-            L = CompactLayout(w.arrays, w.hbar)
+            w, L = prepared.result() if prepared is not None else prepare(self.build, req)
             res.modes = L.N
-            tr = Trajectory(w.arrays, w.hbar, precision=self.precision, device=self.device, layout=L)
+            tr = Trajectory(None, w.hbar, precision=self.precision, device=self.device, layout=L)
             tr.set_y(w.arrays["DM_Ortho"])
             b = native_bias(w.bias, L.NL)
             t, h = w.t0, w.stepsize
@@ -139,16 +143,53 @@ class Server:
                 out.append(res)
             done.release()
 
+    def _start_pool(self):
+        """Worker processes for host preparation, started (spawn: the parent
+        already holds a CUDA context) and warmed before the request stream
+        begins, each with single-threaded BLAS."""
+        if self.prep_workers <= 0:
+            return None
+        keys = ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")
+        saved = {k: os.environ.get(k) for k in keys}
+        for k in keys:
+            os.environ[k] = "1"
+        try:
+            pool = cf.ProcessPoolExecutor(self.prep_workers, mp_context=mp.get_context("spawn"))
+            for f in [pool.submit(_warm) for _ in range(self.prep_workers)]:
+                f.result()
+        finally:
+            for k, v in saved.items():
+                if v is None:
+                    os.environ.pop(k, None)
+                else:
+                    os.environ[k] = v
+        return pool
+
     def run(self, requests, time_scale=1.0):
         """Serve ``requests`` (dicts with ``id``, ``arrival``); arrivals are
         replayed in wall time scaled by ``time_scale``.  Returns the results
         in completion order and summary statistics."""
         reqs = sorted(requests, key=lambda r: r["arrival"])
+        pool = self._start_pool()
         self.t_start = time.perf_counter()
         out: List[Result] = []
         slots = threading.Semaphore(self.max_slots)
         threads = []
         pending = list(reqs)
+        prepared = {}
+        if pool is not None:
+            # each request's host preparation starts when it arrives, while it may still wait for admission
+            prepared = {r["id"]: cf.Future() for r in reqs}
+
+            def feed():
+                for r in reqs:
+                    wait = r["arrival"] * time_scale - (time.perf_counter() - self.t_start)
+                    if wait > 0:
+                        time.sleep(wait)
+                    f = pool.submit(prepare, self.build, r)
+                    f.add_done_callback(lambda f, dst=prepared[r["id"]]: _forward(f, dst))
+
+            threading.Thread(target=feed, daemon=True).start()
         while pending:
             req = pending[0]
             due = req["arrival"] * time_scale
@@ -175,13 +216,16 @@ class Server:
             r = dict(req)
             r["arrival"] = due
             th = threading.Thread(target=self._run_one,
-                                  args=(r, time.perf_counter() - self.t_start, fp, out, slots), daemon=True)
+                                  args=(r, time.perf_counter() - self.t_start, fp, out, slots,
+                                        prepared.get(r["id"])), daemon=True)
             th.start()
             threads.append(th)
             self.peak_slots = max(self.peak_slots, sum(t.is_alive() for t in threads))
         for th in threads:
             th.join()
         wall = time.perf_counter() - self.t_start
+        if pool is not None:
+            pool.shutdown(wait=True, cancel_futures=True)
         ok = [r for r in out if r.error is None]
         lat = np.array([r.latency for r in ok]) if ok else np.zeros(1)
         stats = dict(requests=len(reqs), completed=len(ok), failed=len(out) - len(ok), wall_s=wall,
@@ -189,9 +233,30 @@ class Server:
                      p50_latency_s=float(np.percentile(lat, 50)), p99_latency_s=float(np.percentile(lat, 99)),
                      mean_latency_s=float(lat.mean()), attempts=int(sum(r.attempts for r in ok)),
                      peak_hbm_reserved=int(self.peak_in_use), hbm_budget=int(self.hbm_budget),
-                     max_slots=self.max_slots)
+                     max_slots=self.max_slots, prep_workers=self.prep_workers, attempt_mode=self.attempt_mode)
         stats["simulated_fs_per_s"] = stats["simulated_fs"] / wall
         return out, stats
+
+
+def prepare(build, req):
+    """Host input preparation of one request: its workload and compact layout.
+    Only what the device run needs travels back (sigma_0 of the arrays)."""
+    w = build(req)
+    L = CompactLayout(w.arrays, w.hbar)
+    slim = dataclasses.replace(w, arrays={"DM_Ortho": np.asarray(w.arrays["DM_Ortho"])})
+    return slim, L
+
+
+def _warm():
+    time.sleep(0.2)  # keeps this worker busy so that every worker gets started
+    return os.getpid()
+
+
+def _forward(src, dst):
+    if src.exception() is not None:
+        dst.set_exception(src.exception())
+    else:
+        dst.set_result(src.result())
 
 
 def c4_estimate(req, precision):
