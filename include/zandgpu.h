@@ -105,6 +105,11 @@ int zg_stage_input(zg_traj* t, int stage);
 int zg_get_stage_sigma(zg_traj* t, double* host);
 /* Upload the dH(t, sigma) matrix (n*n complex) that ZG_DH_MATRIX adds to H0. */
 int zg_set_dH(zg_traj* t, const double* host);
+/* dissipator(ts, sigma) of the coming zg_rhs calls (n*n complex), entering k_sigma
+ * as - hbar * dissipator (Zandpack/mpi/zand:343); NULL switches it off.  The
+ * reference evaluates it at every stage: set it before each zg_rhs.  zg_attempt
+ * and the graph path refuse to run while one is set. */
+int zg_set_dissipator(zg_traj* t, const double* host);
 
 /* k_stage = h f(ts, Y_stage): the stage body of zand (Zandpack/mpi/zand:318-387
  * master, :713-809 worker).  delta[NL] = bias(ts, a); dH_mode selects

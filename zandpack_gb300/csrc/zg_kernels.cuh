@@ -172,8 +172,9 @@ int launch_gathers(const RhsDev<T>& d, const typename cx<T>::t* sig, const typen
                    const typename cx<T>::t* psi_lo, int64_t ldpsi, typename cx<T>::t* sigC, typename cx<T>::t* G,
                    cudaStream_t s);
 template <typename T>
+// dis (may be null): the n x n FP64 dissipator of this stage, entering as - hbar * dis
 int launch_sigma_finalize(const RhsDev<T>& d, const StageParams* p, const typename cx<T>::t* Tm, int64_t ldT,
-                          const typename cx<T>::t* Pc, typename cx<T>::t* ksig, cudaStream_t s);
+                          const typename cx<T>::t* Pc, const double2* dis, typename cx<T>::t* ksig, cudaStream_t s);
 template <typename T>
 int launch_currents(const RhsDev<T>& d, const StageParams* p, const typename cx<T>::t* Pc, double* J, cudaStream_t s);
 template <typename T>

@@ -264,7 +264,7 @@ __device__ __forceinline__ typename cx<T>::t p_full(const RhsDev<T>& d, const ty
 // k_sig = (h/hbar) (-i (T - T^H) + (P + P^H)/hbar), T = H(t) sigma  (Zandpack/mpi/zand:340-387)
 template <typename T>
 __global__ void k_sigma_finalize(const RhsDev<T> d, const StageParams* __restrict__ pp, const typename cx<T>::t* __restrict__ Tm,
-                                 int64_t ldT, const typename cx<T>::t* __restrict__ Pc,
+                                 int64_t ldT, const typename cx<T>::t* __restrict__ Pc, const double2* __restrict__ dis,
                                  typename cx<T>::t* __restrict__ ksig) {
   const StageParams p = *pp;
   const int64_t nn = (int64_t)d.n * d.n;
@@ -276,6 +276,11 @@ __global__ void k_sigma_finalize(const RhsDev<T> d, const StageParams* __restric
     const typename cx<T>::t pij = p_full(d, Pc, i, j), pji = p_full(d, Pc, j, i);
     // -i (tij - conj(tji)) = (tij.y + tji.y, -(tij.x - tji.x))
     typename cx<T>::t v = cx<T>::make(tij.y + tji.y, -(tij.x - tji.x));
+    if (dis) {  // - hbar * dissipator(ts, sigma)  (Zandpack/mpi/zand:343)
+      const double2 q = dis[e];
+      v.x -= (T)(p.hbar * q.x);
+      v.y -= (T)(p.hbar * q.y);
+    }
     v.x += (pij.x + pji.x) * ih;
     v.y += (pij.y - pji.y) * ih;
     ksig[e] = cscale(v, sc);
@@ -284,9 +289,9 @@ __global__ void k_sigma_finalize(const RhsDev<T> d, const StageParams* __restric
 
 template <typename T>
 int launch_sigma_finalize(const RhsDev<T>& d, const StageParams* p, const typename cx<T>::t* Tm, int64_t ldT,
-                          const typename cx<T>::t* Pc, typename cx<T>::t* ksig, cudaStream_t s) {
+                          const typename cx<T>::t* Pc, const double2* dis, typename cx<T>::t* ksig, cudaStream_t s) {
   int64_t nn = (int64_t)d.n * d.n;
-  k_sigma_finalize<T><<<grid_for(nn, 256, 152 * 8), 256, 0, s>>>(d, p, Tm, ldT, Pc, ksig);
+  k_sigma_finalize<T><<<grid_for(nn, 256, 152 * 8), 256, 0, s>>>(d, p, Tm, ldT, Pc, dis, ksig);
   ZG_CHECK_LAUNCH();
   count_launch();
   return ZG_OK;
@@ -642,7 +647,7 @@ int launch_build_operands_mixed(int n, int np, const double2* H0, const float2* 
   template int launch_gathers<T>(const RhsDev<T>&, const cx<T>::t*, const cx<T>::t*, const cx<T>::t*, int64_t,      \
                                  cx<T>::t*, cx<T>::t*, cudaStream_t);                                                 \
   template int launch_sigma_finalize<T>(const RhsDev<T>&, const StageParams*, const cx<T>::t*, int64_t,              \
-                                        const cx<T>::t*, cx<T>::t*, cudaStream_t);                                    \
+                                        const cx<T>::t*, const double2*, cx<T>::t*, cudaStream_t);                    \
   template int launch_currents<T>(const RhsDev<T>&, const StageParams*, const cx<T>::t*, double*, cudaStream_t);     \
   template int launch_psi_finalize<T>(const RhsDev<T>&, const StageParams*, const cx<T>::t*, const cx<T>::t*,        \
                                       int64_t, const cx<T>::t*, int64_t, const cx<T>::t*, const cx<T>::t*,           \

@@ -158,6 +158,8 @@ struct zg_traj {
   double *J = nullptr, *Jpart = nullptr, *partial = nullptr, *err = nullptr;
   int nblk_err = 0;
   bool dH_set = false;
+  double2* dis = nullptr;  // dissipator of the coming stages (zg_set_dissipator)
+  bool dis_on = false;
   // ---- mixed path
   int np = 0;  // n padded to a multiple of 16
   MixedLayout ml;
@@ -333,7 +335,7 @@ static void free_traj(zg_traj* t) {
                   t->dGP32,
                   t->XI32, t->XIS32, t->IXI32, t->U32, t->V32, t->y32, t->K32, t->stage32, t->Hth, t->Htl, t->BHh,
                   t->BHl, t->BSh, t->BSl, t->T32, t->R1p, t->Pc32, t->sigC32, t->G32, t->R2_32, t->ZA32, t->ZB32,
-                  t->conv64, t->sig64, t->tc_err, t->ws64, t->ws32};
+                  t->conv64, t->sig64, t->tc_err, t->ws64, t->ws32, t->dis};
   for (void* p : ptrs) dfree(t, p);
   if (t->stream) {
     cudaStreamSynchronize(t->stream);
@@ -754,6 +756,21 @@ int zg_set_dH(zg_traj* t, const double* host) {
   return ZG_OK;
 }
 
+int zg_set_dissipator(zg_traj* t, const double* host) {
+  ZG_REQUIRE(t, "null argument");
+  ZG_CHECK_CUDA(cudaSetDevice(t->dev));
+  if (!host) {
+    t->dis_on = false;
+    return ZG_OK;
+  }
+  if (!t->dis) ZG_TRY(dalloc(t, &t->dis, (size_t)t->n * t->n));
+  ZG_CHECK_CUDA(cudaMemcpyAsync(t->dis, host, (size_t)t->n * t->n * sizeof(double2), cudaMemcpyHostToDevice,
+                                t->stream));
+  ZG_CHECK_CUDA(cudaStreamSynchronize(t->stream));
+  t->dis_on = true;
+  return ZG_OK;
+}
+
 static void gemm_prob_f64(std::vector<GemmProb<double>>& v, const double2* A, int64_t lda, int opA, const double2* B,
                           int64_t ldb, int opB, double2* C, int64_t ldc, int M, int N, int K) {
   GemmProb<double> P;
@@ -859,7 +876,7 @@ static int rhs_f64(zg_traj* t, int stage, const StageParams* p, int dH_mode, dou
   ZG_TRY(run_batches<double>(t, probs, &t->ws64, &t->ws64_cap, s, false));
   prof_end(t, ZG_PROF_GEMM);
   prof_begin(t, ZG_PROF_FINAL);
-  ZG_TRY(launch_sigma_finalize<double>(d, p, t->T, n, t->Pc, out, s));
+  ZG_TRY(launch_sigma_finalize<double>(d, p, t->T, n, t->Pc, t->dis_on ? t->dis : nullptr, out, s));
   if (want_J) ZG_TRY(launch_currents<double>(d, p, t->Pc, t->J, s));
   ZG_TRY(launch_psi_finalize<double>(d, p, psi, nullptr, n, out + t->off_psi, n, t->R2, t->ZA, t->ZB,
                                      out + t->off_psi, s));
@@ -922,7 +939,7 @@ static int rhs_mixed(zg_traj* t, int stage, const StageParams* p, int dH_mode, d
   ZG_TRY(run_batches<float>(t, probs, &t->ws32, &t->ws32_cap, s, false));
   prof_end(t, ZG_PROF_SMALL);
   prof_begin(t, ZG_PROF_FINAL);
-  ZG_TRY(launch_sigma_finalize<float>(d, p, t->T32, np, t->Pc32, out, s));
+  ZG_TRY(launch_sigma_finalize<float>(d, p, t->T32, np, t->Pc32, t->dis_on ? t->dis : nullptr, out, s));
   if (want_J) {
     if (stage == 0)  // the stage-0 input is y itself: currents from the FP64 state
     {
@@ -1115,6 +1132,7 @@ int zg_attempt(zg_traj* t, double* time, double* h, double eps, const zg_bias* b
                double* TE, int* accepted, double* currents) {
   ZG_REQUIRE(t && time && h && bias && TE && accepted, "null argument");
   ZG_REQUIRE(dH_mode == ZG_DH_NONE || dH_mode == ZG_DH_HUBBARD, "zg_attempt needs dH_mode NONE or HUBBARD");
+  ZG_REQUIRE(!t->dis_on, "a dissipator is applied through zg_rhs only: call zg_set_dissipator(t, NULL) first");
   ZG_REQUIRE(bias->kind >= ZG_BIAS_ZERO && bias->kind <= ZG_BIAS_BOX, "unknown bias kind %d", bias->kind);
   const double t0 = *time, h0 = *h;
   double delta[ZG_MAX_LEADS];
@@ -1166,6 +1184,7 @@ int zg_get_sigma(zg_traj* t, int slot, double* host) {
 int zg_graph_prepare(zg_traj* t, const zg_bias* bias, int dH_mode, double hubbard_U) {
   ZG_REQUIRE(t && bias, "null argument");
   ZG_REQUIRE(dH_mode == ZG_DH_NONE || dH_mode == ZG_DH_HUBBARD, "the attempt graph needs dH_mode NONE or HUBBARD");
+  ZG_REQUIRE(!t->dis_on, "a dissipator is applied through zg_rhs only: call zg_set_dissipator(t, NULL) first");
   ZG_REQUIRE(bias->kind >= ZG_BIAS_ZERO && bias->kind <= ZG_BIAS_BOX, "unknown bias kind %d", bias->kind);
   ZG_CHECK_CUDA(cudaSetDevice(t->dev));
   t->gbias = *bias;
@@ -1197,6 +1216,7 @@ int zg_graph_run(zg_traj* t, int count, zg_attempt_rec* recs, int* nrec, double*
   ZG_REQUIRE(t, "null argument");
   ZG_REQUIRE(count >= 0 && count <= ZG_GRAPH_MAX_BATCH, "count %d out of range", count);
   ZG_REQUIRE(t->g_prepared, "zg_graph_prepare must precede zg_graph_run");
+  ZG_REQUIRE(!t->dis_on, "a dissipator is applied through zg_rhs only: call zg_set_dissipator(t, NULL) first");
   ZG_CHECK_CUDA(cudaSetDevice(t->dev));
   if (!t->gexec) ZG_TRY(capture_attempt_graph(t));  // dropped by zg_set_tableau or zg_profile
   cudaStream_t s = t->stream;

@@ -126,6 +126,14 @@ class Trajectory:
         dH = np.ascontiguousarray(np.asarray(dH, np.complex128).reshape(self.layout.n, self.layout.n))
         check(lib().zg_set_dH(self._h, _ptr(dH)))
 
+    def set_dissipator(self, D):
+        """dissipator(ts, sigma) for the coming ``rhs`` calls ((1,n,n) or (n,n)); None: off."""
+        if D is None:
+            check(lib().zg_set_dissipator(self._h, None))
+            return
+        D = np.ascontiguousarray(np.asarray(D, np.complex128).reshape(self.layout.n, self.layout.n))
+        check(lib().zg_set_dissipator(self._h, _ptr(D)))
+
     def rhs(self, stage, ts, h, delta, dH_mode=_lib.ZG_DH_NONE, hubbard_U=0.0, currents=False):
         d = self._delta
         d[:] = 0.0
@@ -249,8 +257,7 @@ class Propagator:
                 mode = _lib.ZG_DH_MATRIX
         if self.dissipator is not None:
             dz = self.dissipator(ts, tr.stage_sigma()[None])
-            if not (np.isscalar(dz) and dz == 0):
-                raise NotImplementedError("a nonzero dissipator is not supported on the device path")
+            tr.set_dissipator(None if (np.isscalar(dz) and dz == 0) else dz)
         delta = [self.bias(ts, a) for a in range(self.NL)]
         self.n_rhs += 1
         return tr.rhs(i, ts, h, delta, mode, U, currents=want_J)
