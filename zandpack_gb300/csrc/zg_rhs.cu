@@ -9,6 +9,22 @@ namespace zg {
 #define GRID_STRIDE(e, count) \
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < (count); e += (int64_t)gridDim.x * blockDim.x)
 
+// Stage parameters as the kernels read them: the scalars in registers, the
+// per-lead biases through a pointer (a dynamically indexed copy of the whole
+// struct would live in local memory).
+struct StageScalars {
+  double h, ts, hbar;
+  const double* delta;
+};
+__device__ __forceinline__ StageScalars load_params(const StageParams* __restrict__ pp) {
+  StageScalars s;
+  s.h = pp->h;
+  s.ts = pp->ts;
+  s.hbar = pp->hbar;
+  s.delta = pp->delta;
+  return s;
+}
+
 template <typename T>
 __device__ __forceinline__ typename cx<T>::t czero() {
   return cx<T>::make((T)0, (T)0);
@@ -22,21 +38,23 @@ __device__ __forceinline__ typename cx<T>::t czero() {
 // coupling width (n_c <= 32), which would leave half of a 64-wide tile idle.
 #define ZK 8
 
+// Raw operand loads: nothing consumes the loaded values until they are stored
+// to shared memory a K stage later (the hi + lo sum and the conjugation of
+// opB = 2 happen there), so the loads stay in flight behind the compute.
 template <typename T>
-__device__ __forceinline__ typename cx<T>::t load_opA(const GemmProb<T>& P, int m, int k) {
-  using C = typename cx<T>::t;
-  if (m >= P.M || k >= P.K) return czero<T>();
+__device__ __forceinline__ void load_opA(const GemmProb<T>& P, int m, int k, typename cx<T>::t& v,
+                                         typename cx<T>::t& v2) {
+  v = czero<T>();
+  v2 = czero<T>();
+  if (m >= P.M || k >= P.K) return;
   const int64_t o = P.opA == 0 ? (int64_t)m * P.lda + k : (int64_t)k * P.lda + m;
-  C v = P.A[o];
-  if (P.A2) v = cadd(v, P.A2[o]);
-  return v;
+  v = P.A[o];
+  if (P.A2) v2 = P.A2[o];
 }
 template <typename T>
 __device__ __forceinline__ typename cx<T>::t load_opB(const GemmProb<T>& P, int k, int n) {
   if (n >= P.N || k >= P.K) return czero<T>();
-  if (P.opB == 0) return P.B[(int64_t)k * P.ldb + n];
-  const typename cx<T>::t v = P.B[(int64_t)n * P.ldb + k];
-  return P.opB == 2 ? cconj(v) : v;
+  return P.opB == 0 ? P.B[(int64_t)k * P.ldb + n] : P.B[(int64_t)n * P.ldb + k];
 }
 
 template <typename T, int BN>
@@ -66,34 +84,43 @@ __global__ void __launch_bounds__(256) k_zgemm(const __grid_constant__ GemmBatch
   for (int i = 0; i < 4; ++i)
 #pragma unroll
     for (int j = 0; j < 4; ++j) acc[i][j] = czero<T>();
-  int am[RA], ak[RA], bn_[RB], bk[RB];
+  // element r of this thread's share of a K stage (recomputed, not kept in registers)
+#define ZG_AM(r) (P.opA == 0 ? ((tid + 256 * (r)) >> 4) : ((tid + 256 * (r)) % BM))
+#define ZG_AK(r) (P.opA == 0 ? ((tid + 256 * (r)) & 15) : ((tid + 256 * (r)) / BM))
+#define ZG_BN(r) (P.opB == 0 ? ((tid + 256 * (r)) % BN) : ((tid + 256 * (r)) >> 4))
+#define ZG_BK(r) (P.opB == 0 ? ((tid + 256 * (r)) / BN) : ((tid + 256 * (r)) & 15))
+  C ra[RA], ra2[RA], rb[RB];
+  const bool conjB = P.opB == 2;
 #pragma unroll
   for (int r = 0; r < RA; ++r) {
-    const int idx = tid + 256 * r;
-    if (P.opA == 0) { am[r] = idx >> 4; ak[r] = idx & 15; } else { am[r] = idx % BM; ak[r] = idx / BM; }
+    if (kb0 + ZG_AK(r) < kb1) {
+      load_opA(P, m0 + ZG_AM(r), kb0 + ZG_AK(r), ra[r], ra2[r]);
+    } else {
+      ra[r] = czero<T>();
+      ra2[r] = czero<T>();
+    }
   }
 #pragma unroll
-  for (int r = 0; r < RB; ++r) {
-    const int idx = tid + 256 * r;
-    if (P.opB == 0) { bn_[r] = idx % BN; bk[r] = idx / BN; } else { bn_[r] = idx >> 4; bk[r] = idx & 15; }
-  }
-  C ra[RA], rb[RB];
-#pragma unroll
-  for (int r = 0; r < RA; ++r) ra[r] = kb0 + ak[r] < kb1 ? load_opA(P, m0 + am[r], kb0 + ak[r]) : czero<T>();
-#pragma unroll
-  for (int r = 0; r < RB; ++r) rb[r] = kb0 + bk[r] < kb1 ? load_opB(P, kb0 + bk[r], n0 + bn_[r]) : czero<T>();
+  for (int r = 0; r < RB; ++r) rb[r] = kb0 + ZG_BK(r) < kb1 ? load_opB(P, kb0 + ZG_BK(r), n0 + ZG_BN(r)) : czero<T>();
   for (int k0 = kb0; k0 < kb1; k0 += ZKG) {
 #pragma unroll
-    for (int r = 0; r < RA; ++r) As[ak[r]][am[r]] = ra[r];
+    for (int r = 0; r < RA; ++r) As[ZG_AK(r)][ZG_AM(r)] = cadd(ra[r], ra2[r]);
 #pragma unroll
-    for (int r = 0; r < RB; ++r) Bs[bk[r]][bn_[r]] = rb[r];
+    for (int r = 0; r < RB; ++r) Bs[ZG_BK(r)][ZG_BN(r)] = conjB ? cconj(rb[r]) : rb[r];
     __syncthreads();
     const int k1 = k0 + ZKG;
     if (k1 < kb1) {
 #pragma unroll
-      for (int r = 0; r < RA; ++r) ra[r] = k1 + ak[r] < kb1 ? load_opA(P, m0 + am[r], k1 + ak[r]) : czero<T>();
+      for (int r = 0; r < RA; ++r) {
+        if (k1 + ZG_AK(r) < kb1) {
+          load_opA(P, m0 + ZG_AM(r), k1 + ZG_AK(r), ra[r], ra2[r]);
+        } else {
+          ra[r] = czero<T>();
+          ra2[r] = czero<T>();
+        }
+      }
 #pragma unroll
-      for (int r = 0; r < RB; ++r) rb[r] = k1 + bk[r] < kb1 ? load_opB(P, k1 + bk[r], n0 + bn_[r]) : czero<T>();
+      for (int r = 0; r < RB; ++r) rb[r] = k1 + ZG_BK(r) < kb1 ? load_opB(P, k1 + ZG_BK(r), n0 + ZG_BN(r)) : czero<T>();
     }
 #pragma unroll
     for (int kk = 0; kk < ZKG; ++kk) {
@@ -128,6 +155,10 @@ __global__ void __launch_bounds__(256) k_zgemm(const __grid_constant__ GemmBatch
       *c = v;
     }
   }
+#undef ZG_AM
+#undef ZG_AK
+#undef ZG_BN
+#undef ZG_BK
 }
 
 // C = alpha * sum over splits of the partials, splits added in order
@@ -154,8 +185,11 @@ int64_t plan_zgemm_batch(GemmBatch<T>& b) {
   b.bn = maxN <= 32 ? 32 : 64;
   const int BN = b.bn, BM = 4 * (256 / (BN / 4));
   // A problem with few output tiles and a long K would serialise on a handful
-  // of CTAs: split its K into chunks of >= 256 until it has ~2 CTAs per SM.
-  const int64_t target = 2 * 152;
+  // of CTAs (the batch is then less than one wave, and its longest tile sets
+  // the time): split its K into chunks of >= KMIN until it has ~TARGET CTAs.
+  // FP32 tiles are cheap per K, so their chunks are shorter than FP64's.
+  const int64_t target = sizeof(T) == 4 ? 4 * 152 : 2 * 152;
+  const int KMIN = sizeof(T) == 4 ? 128 : 256;
   int tiles = 0;
   int64_t ws = 0;
   for (int i = 0; i < b.nprob; ++i) {
@@ -167,9 +201,9 @@ int64_t plan_zgemm_batch(GemmBatch<T>& b) {
     P.kchunk = P.K > 0 ? P.K : 1;
     P.ws_off = 0;
     const bool plain_beta = P.beta.x == (T)0 && P.beta.y == (T)0;
-    if (plain_beta && P.K >= 512 && tm * tn > 0 && tm * tn < 152) {
+    if (plain_beta && P.K >= 2 * KMIN && tm * tn > 0 && tm * tn < target) {
       int want = (int)((target + tm * tn - 1) / (tm * tn));
-      int maxs = P.K / 256;  // at least 256 of K per split
+      int maxs = P.K / KMIN;  // at least KMIN of K per split
       int ks = want < maxs ? want : maxs;
       if (ks > 1) {
         int chunk = (P.K + ks - 1) / ks;
@@ -266,7 +300,7 @@ template <typename T>
 __global__ void k_sigma_finalize(const RhsDev<T> d, const StageParams* __restrict__ pp, const typename cx<T>::t* __restrict__ Tm,
                                  int64_t ldT, const typename cx<T>::t* __restrict__ Pc, const double2* __restrict__ dis,
                                  typename cx<T>::t* __restrict__ ksig) {
-  const StageParams p = *pp;
+  const StageScalars p = load_params(pp);
   const int64_t nn = (int64_t)d.n * d.n;
   const T ih = (T)(1.0 / p.hbar);
   const T sc = (T)(p.h / p.hbar);
@@ -320,7 +354,7 @@ __device__ __forceinline__ double block_sum256_d(double v) {
 template <typename T>
 __global__ void k_currents(const RhsDev<T> d, const StageParams* __restrict__ pp, const typename cx<T>::t* __restrict__ Pc,
                            double* __restrict__ J) {
-  const StageParams p = *pp;
+  const StageScalars p = load_params(pp);
   const int a = blockIdx.x;
   double s = 0.0;
   for (int k = threadIdx.x; k < d.nc; k += blockDim.x) {
@@ -392,7 +426,7 @@ __global__ void k_psi_finalize(const RhsDev<T> d, const StageParams* __restrict_
                                const typename cx<T>::t* R1, int64_t ldR1, const typename cx<T>::t* __restrict__ R2,
                                const typename cx<T>::t* __restrict__ ZA, const typename cx<T>::t* __restrict__ ZB,
                                typename cx<T>::t* kpsi) {
-  const StageParams p = *pp;
+  const StageScalars p = load_params(pp);
   using C = typename cx<T>::t;
   const int64_t tot = (int64_t)d.N * d.n;
   const T ih = (T)(1.0 / p.hbar);
@@ -439,17 +473,17 @@ int launch_psi_finalize(const RhsDev<T>& d, const StageParams* p, const typename
 //          + h sum_k V[m][k] conj(G[l][a][k])        (term2, V = dGP * XIT2)
 //          + (i h/hbar)(X+_m + D_a - X-_l - D_b) Omega[m,l]
 template <typename T>
-__global__ void __launch_bounds__(256) k_omega(const RhsDev<T> d, const StageParams* __restrict__ pp, const OmTile* __restrict__ tiles,
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) k_omega(const RhsDev<T> d, const StageParams* __restrict__ pp, const OmTile* __restrict__ tiles,
                                                const typename cx<T>::t* __restrict__ G,
                                                const typename cx<T>::t* __restrict__ omA_in,
                                                const typename cx<T>::t* __restrict__ omB_in,
                                                typename cx<T>::t* __restrict__ omA_out,
                                                typename cx<T>::t* __restrict__ omB_out) {
-  const StageParams p = *pp;
+  const StageScalars p = load_params(pp);
   using C = typename cx<T>::t;
   const OmTile t = tiles[blockIdx.x];
   // K (the 2 n_c source terms) staged ZKO at a time, next stage prefetched into registers
-  constexpr int ZKO = sizeof(T) == 4 ? 32 : 16, RO = 64 * ZKO / 256;
+  constexpr int ZKO = 16, RO = 64 * ZKO / 256;
   // padded rows: stores run along k (column-wise), which would otherwise hit one bank
   __shared__ C As[ZKO][64 + 1];
   __shared__ C Bs[ZKO][64 + 1];
@@ -463,36 +497,39 @@ __global__ void __launch_bounds__(256) k_omega(const RhsDev<T> d, const StagePar
     for (int j = 0; j < 4; ++j) acc[i][j] = czero<T>();
   const int kbeg = t.term1 ? 0 : nc, kend = t.term2 ? 2 * nc : nc;
   C ra[RO], rb[RO];
-  auto fetch = [&](int k0) {
-#pragma unroll
-    for (int r = 0; r < RO; ++r) {
-      const int idx = tid + 256 * r;
-      const int rr = idx / ZKO, k = k0 + idx % ZKO;
-      C av = czero<T>(), bv = czero<T>();
-      if (k < kend) {
-        if (rr < t.nrows) {
-          const int64_t m = t.row0 + rr;
-          av = k < nc ? G[(m * d.L + t.b) * nc + k] : d.V[m * nc + (k - nc)];
-        }
-        if (rr < t.ncols) {
-          const int64_t l = colmode0 + rr;
-          bv = k < nc ? d.U[l * nc + k] : cconj(G[(l * d.L + t.a) * nc + (k - nc)]);
-        }
-      }
-      ra[r] = av;
-      rb[r] = bv;
-    }
-  };
-  fetch(kbeg);
+  // operands of K index k for local row/column rr (zero outside the tile and K range)
+#define ZG_OMEGA_FETCH(k0)                                                                  \
+  _Pragma("unroll") for (int r = 0; r < RO; ++r) {                                          \
+    const int idx = tid + 256 * r;                                                          \
+    const int rr = idx / ZKO, k = (k0) + idx % ZKO;                                         \
+    C av = czero<T>(), bv = czero<T>();                                                     \
+    if (k < kend) {                                                                         \
+      if (rr < t.nrows) {                                                                   \
+        const int64_t m = t.row0 + rr;                                                      \
+        av = k < nc ? G[(m * d.L + t.b) * nc + k] : d.V[m * nc + (k - nc)];                 \
+      }                                                                                     \
+      if (rr < t.ncols) {                                                                   \
+        const int64_t l = colmode0 + rr;                                                    \
+        bv = k < nc ? d.U[l * nc + k] : G[(l * d.L + t.a) * nc + (k - nc)];                 \
+      }                                                                                     \
+    }                                                                                       \
+    ra[r] = av;                                                                             \
+    rb[r] = bv;                                                                             \
+  }
+  ZG_OMEGA_FETCH(kbeg)
   for (int k0 = kbeg; k0 < kend; k0 += ZKO) {
 #pragma unroll
     for (int r = 0; r < RO; ++r) {
       const int idx = tid + 256 * r;
       As[idx % ZKO][idx / ZKO] = ra[r];
-      Bs[idx % ZKO][idx / ZKO] = rb[r];
+      // K indices >= n_c take conj(G) (the second source term), conjugated here
+      // rather than at the load so that the load is not waited for
+      Bs[idx % ZKO][idx / ZKO] = k0 + idx % ZKO >= nc ? cconj(rb[r]) : rb[r];
     }
     __syncthreads();
-    if (k0 + ZKO < kend) fetch(k0 + ZKO);
+    if (k0 + ZKO < kend) {
+      ZG_OMEGA_FETCH(k0 + ZKO)
+    }
 #pragma unroll
     for (int kk = 0; kk < ZKO; ++kk) {
       C a[4], b[4];
@@ -536,6 +573,7 @@ __global__ void __launch_bounds__(256) k_omega(const RhsDev<T> d, const StagePar
       out[e] = v;
     }
   }
+#undef ZG_OMEGA_FETCH
 }
 
 template <typename T>

@@ -17,7 +17,13 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["f64", "mixed"])
     ap.add_argument("--attempts", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=1)
+    ap.add_argument("--regions", action="store_true", help="print CUDA-event times per region of the timed attempts")
     args = ap.parse_args()
+    import ctypes as C
+
+    import numpy as np
+
+    from ._lib import PROF_REGIONS, check, lib
     from .engine import Propagator
     from .workloads import make_workload
     w = make_workload(args.config)
@@ -25,6 +31,8 @@ def main():
     pr.set_state(w.arrays["DM_Ortho"])
     t, h = w.t0, w.stepsize
     for i in range(args.warmup + args.attempts):
+        if args.regions and i == args.warmup:
+            check(lib().zg_profile(pr.traj._h, 1))
         t0 = time.perf_counter()
         TE, _, _ = pr.attempt(t, h)
         hn = pr.tab.hnew(h, TE, w.eps)
@@ -33,6 +41,12 @@ def main():
             t += hn
         h = hn
         print("attempt %d: TE=%.3e h=%.4g t=%.4g (%.2f ms host wall)" % (i, TE, h, t, (time.perf_counter() - t0) * 1e3))
+    if args.regions:
+        ms = np.zeros(len(PROF_REGIONS))
+        cnt = np.zeros(len(PROF_REGIONS), np.int64)
+        check(lib().zg_profile_read(pr.traj._h, ms.ctypes.data_as(C.c_void_p), cnt.ctypes.data_as(C.c_void_p)))
+        for name, m, c in zip(PROF_REGIONS, ms, cnt):
+            print("region %-8s %4d calls %9.4f ms/call %9.4f ms/attempt" % (name, c, m / max(c, 1), m / args.attempts))
     pr.traj.close()
 
 
