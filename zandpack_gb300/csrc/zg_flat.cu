@@ -139,27 +139,82 @@ __device__ __forceinline__ void split_tf32(float v, float& hi, float& lo) {
   lo = __uint_as_float(l);
 }
 
+// The slot count NS of a combination is a template parameter: the FP32
+// coefficients (converted from the FP64 tableau once per thread) and the slot
+// pointers sit in registers and the NS loads of an element are all issued
+// before their sum, instead of one double-to-float conversion and one
+// dependent load per slot and element.  NS < 0: runtime count (long tableaux).
+#define ZG_MAX_UNROLLED_SLOTS 8
+
+template <int NS>
+struct SlotSet {
+  float c[NS > 0 ? NS : 1];
+  const float2* p[NS > 0 ? NS : 1];
+  __device__ __forceinline__ SlotSet(const float2* K, int64_t stride, const CombineCoefs& cf) {
+#pragma unroll
+    for (int t = 0; t < (NS > 0 ? NS : 0); ++t) {
+      c[t] = (float)cf.c[t];
+      p[t] = K + cf.idx[t] * stride;
+    }
+  }
+  // acc + sum_t c[t] K_t[e]
+  __device__ __forceinline__ float2 sum(float2 acc, int64_t e, const float2* K, int64_t stride,
+                                        const CombineCoefs& cf) const {
+    if (NS >= 0) {
+      float2 v[NS > 0 ? NS : 1];
+#pragma unroll
+      for (int t = 0; t < NS; ++t) v[t] = p[t][e];
+#pragma unroll
+      for (int t = 0; t < NS; ++t) {
+        acc.x = fmaf(c[t], v[t].x, acc.x);
+        acc.y = fmaf(c[t], v[t].y, acc.y);
+      }
+    } else {
+      for (int t = 0; t < cf.n; ++t) {
+        const float ct = (float)cf.c[t];
+        const float2 k = K[cf.idx[t] * stride + e];
+        acc.x = fmaf(ct, k.x, acc.x);
+        acc.y = fmaf(ct, k.y, acc.y);
+      }
+    }
+    return acc;
+  }
+};
+
+// dispatch a kernel template on the slot count of cf
+#define ZG_SLOT_DISPATCH(cf, KERNEL, GRID, ...)                        \
+  switch ((cf).n) {                                                   \
+    case 0: KERNEL<0><<<GRID, 256, 0, s>>>(__VA_ARGS__); break;        \
+    case 1: KERNEL<1><<<GRID, 256, 0, s>>>(__VA_ARGS__); break;        \
+    case 2: KERNEL<2><<<GRID, 256, 0, s>>>(__VA_ARGS__); break;        \
+    case 3: KERNEL<3><<<GRID, 256, 0, s>>>(__VA_ARGS__); break;        \
+    case 4: KERNEL<4><<<GRID, 256, 0, s>>>(__VA_ARGS__); break;        \
+    case 5: KERNEL<5><<<GRID, 256, 0, s>>>(__VA_ARGS__); break;        \
+    case 6: KERNEL<6><<<GRID, 256, 0, s>>>(__VA_ARGS__); break;        \
+    case 7: KERNEL<7><<<GRID, 256, 0, s>>>(__VA_ARGS__); break;        \
+    case 8: KERNEL<8><<<GRID, 256, 0, s>>>(__VA_ARGS__); break;        \
+    default: KERNEL<-1><<<GRID, 256, 0, s>>>(__VA_ARGS__); break;     \
+  }
+
+template <int NS>
 __global__ void __launch_bounds__(256) k_stage_input_mixed(const float2* __restrict__ y32, const float2* __restrict__ K,
                                                            int64_t stride, CombineCoefs cf, MixedLayout ml,
                                                            float2* __restrict__ stage) {
+  const SlotSet<NS> ss(K, stride, cf);
+  const uint32_t n = (uint32_t)ml.n;
   GRID_STRIDE(e, ml.S) {
-    float2 v = y32[e];
-    for (int t = 0; t < cf.n; ++t) {
-      const float c = (float)cf.c[t];
-      const float2 k = K[cf.idx[t] * stride + e];
-      v.x = fmaf(c, k.x, v.x);
-      v.y = fmaf(c, k.y, v.y);
-    }
+    const float2 v = ss.sum(y32[e], e, K, stride, cf);
     if (e < ml.off_psi) {
       stage[e] = v;
     } else if (e < ml.off_omA) {
-      const int64_t r = e - ml.off_psi;
-      const int64_t m = r / ml.n, i = r % ml.n;
+      // psi row m, column i (the psi block is below 2^32 elements, checked at launch)
+      const uint32_t r = (uint32_t)(e - ml.off_psi);
+      const uint32_t m = r / n, i = r - m * n;
       float2 hi, lo;
       split_tf32(v.x, hi.x, lo.x);
       split_tf32(v.y, hi.y, lo.y);
-      stage[ml.st_psih + m * ml.np + i] = hi;
-      stage[ml.st_psil + m * ml.np + i] = lo;
+      stage[ml.st_psih + (int64_t)m * ml.np + i] = hi;
+      stage[ml.st_psil + (int64_t)m * ml.np + i] = lo;
     } else {
       stage[ml.st_om + (e - ml.off_omA)] = v;
     }
@@ -168,51 +223,57 @@ __global__ void __launch_bounds__(256) k_stage_input_mixed(const float2* __restr
 
 int launch_stage_input_mixed(const float2* y32, const float2* K, int64_t stride, const CombineCoefs& cf,
                              const MixedLayout& ml, float2* stage, cudaStream_t s) {
-  k_stage_input_mixed<<<grid_for(ml.S, 256, 152 * 16), 256, 0, s>>>(y32, K, stride, cf, ml, stage);
+  ZG_REQUIRE(ml.off_omA - ml.off_psi < (int64_t(1) << 32), "psi block too large (%lld elements)",
+             (long long)(ml.off_omA - ml.off_psi));
+  const int grid = grid_for(ml.S, 256, 152 * 16);
+  ZG_SLOT_DISPATCH(cf, k_stage_input_mixed, grid, y32, K, stride, cf, ml, stage)
   ZG_CHECK_LAUNCH();
   count_launch();
   return ZG_OK;
 }
 
+// Block sums of |sum_t c[t] K_t[e]|^2: squares summed in FP32 over groups of
+// four elements of a thread, the groups in FP64 (one FP64 add per four
+// elements instead of one per element; the FP64 pipe is 1/64 of FP32).
+template <int NS>
 __global__ void __launch_bounds__(256) k_terr2_mixed(const float2* __restrict__ K, int64_t stride, CombineCoefs cf,
                                                      int64_t begin, int64_t end, double* __restrict__ partial) {
+  const SlotSet<NS> ss(K, stride, cf);
   double s = 0.0;
+  float g = 0.f;
+  int cnt = 0;
   for (int64_t e = begin + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < end;
        e += (int64_t)gridDim.x * blockDim.x) {
-    float2 acc = make_float2(0.f, 0.f);
-    for (int t = 0; t < cf.n; ++t) {
-      const float c = (float)cf.c[t];
-      const float2 v = K[cf.idx[t] * stride + e];
-      acc.x = fmaf(c, v.x, acc.x);
-      acc.y = fmaf(c, v.y, acc.y);
+    const float2 acc = ss.sum(make_float2(0.f, 0.f), e, K, stride, cf);
+    g = fmaf(acc.x, acc.x, fmaf(acc.y, acc.y, g));
+    if (++cnt == 4) {
+      s += (double)g;
+      g = 0.f;
+      cnt = 0;
     }
-    s += (double)fmaf(acc.x, acc.x, acc.y * acc.y);
   }
+  s += (double)g;
   s = block_sum256(s);
   if (threadIdx.x == 0) partial[blockIdx.x] = s;
 }
 
 int launch_terr2_partials_mixed(const float2* K, int64_t stride, const CombineCoefs& cf, int64_t begin, int64_t end,
                                 double* partial, int nblocks, cudaStream_t s) {
-  k_terr2_mixed<<<nblocks, 256, 0, s>>>(K, stride, cf, begin, end, partial);
+  ZG_SLOT_DISPATCH(cf, k_terr2_mixed, nblocks, K, stride, cf, begin, end, partial)
   ZG_CHECK_LAUNCH();
   count_launch();
   return ZG_OK;
 }
 
+template <int NS>
 __global__ void __launch_bounds__(256) k_update_mixed(double2* __restrict__ y64, float2* __restrict__ y32,
                                                       const float2* __restrict__ K, int64_t stride, CombineCoefs cf,
                                                       int64_t count, const int* gate) {
   if (gate && *gate == 0) return;
+  const SlotSet<NS> ss(K, stride, cf);
   GRID_STRIDE(e, count) {
-    float2 d = make_float2(0.f, 0.f);
-    for (int t = 0; t < cf.n; ++t) {
-      const float c = (float)cf.c[t];
-      const float2 v = K[cf.idx[t] * stride + e];
-      d.x = fmaf(c, v.x, d.x);
-      d.y = fmaf(c, v.y, d.y);
-    }
     double2 y = y64[e];
+    const float2 d = ss.sum(make_float2(0.f, 0.f), e, K, stride, cf);
     y.x += (double)d.x;
     y.y += (double)d.y;
     y64[e] = y;
@@ -223,7 +284,8 @@ __global__ void __launch_bounds__(256) k_update_mixed(double2* __restrict__ y64,
 int launch_update_mixed(double2* y64, float2* y32, const float2* K, int64_t stride, const CombineCoefs& cf,
                         int64_t count, cudaStream_t s, const int* gate) {
   if (count <= 0) return ZG_OK;
-  k_update_mixed<<<grid_for(count, 256, 152 * 16), 256, 0, s>>>(y64, y32, K, stride, cf, count, gate);
+  const int grid = grid_for(count, 256, 152 * 16);
+  ZG_SLOT_DISPATCH(cf, k_update_mixed, grid, y64, y32, K, stride, cf, count, gate)
   ZG_CHECK_LAUNCH();
   count_launch();
   return ZG_OK;

@@ -419,39 +419,60 @@ int launch_currents64(int n, int L, int nc, const CurRows& rows, const int* lead
 }
 
 // k_psi = -i h [ R1/hbar - (X+ + Delta)/hbar psi + dGP R2 + Z(Omega xi) + GL_P xi ]
-// with R1 = psi H^T  (Zandpack/mpi/zand:745-778)
+// with R1 = psi H^T  (Zandpack/mpi/zand:745-778).
+// One block per mode row at a time: the row's constants are uniform, and its
+// coupling-column terms (ZA, ZB rows of every lead, XI row) are staged in
+// shared memory, so the per-element work is four streaming loads plus the
+// column map.  R1 may alias kpsi (the FP64 path finalises in place).
 template <typename T>
-__global__ void k_psi_finalize(const RhsDev<T> d, const StageParams* __restrict__ pp, const typename cx<T>::t* __restrict__ psi,
+__global__ void __launch_bounds__(256) k_psi_finalize(const RhsDev<T> d, const StageParams* __restrict__ pp, const typename cx<T>::t* __restrict__ psi,
                                const typename cx<T>::t* __restrict__ psi_lo, int64_t ldpsi,
                                const typename cx<T>::t* R1, int64_t ldR1, const typename cx<T>::t* __restrict__ R2,
                                const typename cx<T>::t* __restrict__ ZA, const typename cx<T>::t* __restrict__ ZB,
                                typename cx<T>::t* kpsi) {
-  const StageScalars p = load_params(pp);
   using C = typename cx<T>::t;
-  const int64_t tot = (int64_t)d.N * d.n;
+  extern __shared__ __align__(16) unsigned char psi_smem[];
+  C* sZ = reinterpret_cast<C*>(psi_smem);  // [L][nc]: ZA + ZB of this row
+  C* sX = sZ + d.L * d.nc;                 // [nc]: GL_P xi of this row on its lead's columns
+  const StageScalars p = load_params(pp);
   const T ih = (T)(1.0 / p.hbar);
   const T h = (T)p.h;
-  GRID_STRIDE(e, tot) {
-    const int64_t m = e / d.n;
-    const int i = (int)(e % d.n);
+  const int n = d.n, nc = d.nc, L = d.L;
+  for (int m = blockIdx.x; m < d.N; m += gridDim.x) {
+    const bool src = m < d.Ns;
     const int a = d.mode_lead[m];
+    const C glp = d.GLP[m];
+    for (int q = threadIdx.x; q < L * nc; q += blockDim.x) {
+      const int b = q / nc, k = q - b * nc;
+      C z = ZA[((int64_t)b * d.N + m) * nc + k];
+      if (src) z = cadd(z, ZB[((int64_t)b * d.Ns + m) * nc + k]);
+      sZ[q] = z;
+    }
+    for (int q = threadIdx.x; q < nc; q += blockDim.x) sX[q] = cmul(glp, d.XI[(int64_t)m * nc + q]);
     C xp = d.Xp[m];
     xp.x += (T)p.delta[a];
-    C ps = psi[m * ldpsi + i];
-    if (psi_lo) ps = cadd(ps, psi_lo[m * ldpsi + i]);
-    C v = cscale(R1[m * ldR1 + i], ih);
-    v = csub(v, cscale(cmul(xp, ps), ih));
-    if (m < d.Ns) v = cadd(v, cmul(d.dGP[m], R2[m * d.n + i]));
-    for (int b = 0; b < d.L; ++b) {
-      const int k = d.colmap[b * d.n + i];
-      if (k < 0) continue;
-      v = cadd(v, ZA[((int64_t)b * d.N + m) * d.nc + k]);
-      if (m < d.Ns) v = cadd(v, ZB[((int64_t)b * d.Ns + m) * d.nc + k]);
+    const C dgp = src ? d.dGP[m] : czero<T>();
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      C ps = psi[(int64_t)m * ldpsi + i];
+      const C pl = psi_lo ? psi_lo[(int64_t)m * ldpsi + i] : czero<T>();
+      const C r1 = R1[(int64_t)m * ldR1 + i];
+      const C r2 = src ? R2[(int64_t)m * n + i] : czero<T>();
+      ps = cadd(ps, pl);
+      C v = cscale(r1, ih);
+      v = csub(v, cscale(cmul(xp, ps), ih));
+      v = cadd(v, cmul(dgp, r2));
+      for (int b = 0; b < L; ++b) {
+        const int k = d.colmap[b * n + i];
+        if (k >= 0) {
+          v = cadd(v, sZ[b * nc + k]);
+          if (b == a) v = cadd(v, sX[k]);
+        }
+      }
+      // (-i h) v = (h v.y, -h v.x)
+      kpsi[(int64_t)m * n + i] = cx<T>::make(h * v.y, -h * v.x);
     }
-    const int ka = d.colmap[a * d.n + i];
-    if (ka >= 0) v = cadd(v, cmul(d.GLP[m], d.XI[m * d.nc + ka]));
-    // (-i h) v = (h v.y, -h v.x)
-    kpsi[e] = cx<T>::make(h * v.y, -h * v.x);
+    __syncthreads();
   }
 }
 
@@ -460,8 +481,11 @@ int launch_psi_finalize(const RhsDev<T>& d, const StageParams* p, const typename
                         const typename cx<T>::t* psi_lo, int64_t ldpsi, const typename cx<T>::t* R1, int64_t ldR1,
                         const typename cx<T>::t* R2, const typename cx<T>::t* ZA, const typename cx<T>::t* ZB,
                         typename cx<T>::t* kpsi, cudaStream_t s) {
-  int64_t tot = (int64_t)d.N * d.n;
-  k_psi_finalize<T><<<grid_for(tot, 256, 152 * 16), 256, 0, s>>>(d, p, psi, psi_lo, ldpsi, R1, ldR1, R2, ZA, ZB, kpsi);
+  if (d.N == 0) return ZG_OK;
+  const size_t smem = (size_t)(d.L + 1) * d.nc * sizeof(typename cx<T>::t);
+  ZG_REQUIRE(smem <= 48 * 1024, "coupling width too large for the psi finalisation (%zu B)", smem);
+  const int grid = d.N < 152 * 8 ? d.N : 152 * 8;
+  k_psi_finalize<T><<<grid, 256, smem, s>>>(d, p, psi, psi_lo, ldpsi, R1, ldR1, R2, ZA, ZB, kpsi);
   ZG_CHECK_LAUNCH();
   count_launch();
   return ZG_OK;
