@@ -10,11 +10,13 @@ Fermi density matrix with psi = Omega = 0.
 
 A step is one Dormand-Prince 5(4) attempt of the reference controller (seven
 right-hand sides, the embedded error norm, the accept test and, on
-acceptance, the update).  ``value`` = simulated fs advanced over the K timed
-steps / their wall time measured with CUDA events on the trajectory's stream.
-``e2e`` repeats it through the public API with the initial state uploaded from
-pinned host memory and sigma plus the lead currents read back after every
-accepted step, as ``zand`` records them.
+acceptance, the update), launched as the captured attempt graph with the
+controller on the device (``zg_graph_run``, one launch and one host
+synchronisation per attempt).  ``value`` = simulated fs advanced over the K
+timed steps / their wall time measured with CUDA events on the trajectory's
+stream.  ``e2e`` repeats it through the public C ABI with the initial state
+uploaded from pinned host memory and every attempt's record plus sigma after
+every accepted step read back, as ``zand`` records them.
 
 ``--impl reference`` times the CPU restatement of the reference (the oracle,
 NumPy/BLAS on all host cores) on the same workload; its step is one stage of
@@ -112,9 +114,11 @@ def rhs_flops(L):
 
 
 def run_ours(args):
+    import ctypes
+
     import torch
     from zandpack_gb300 import _lib
-    from zandpack_gb300.engine import Propagator
+    from zandpack_gb300.engine import Trajectory, native_bias
     from zandpack_gb300.workloads import make_workload
     ws, rank = _dist()
     dev = int(os.environ.get("LOCAL_RANK", "0"))
@@ -123,37 +127,35 @@ def run_ours(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     w = make_workload(args.config)
-    pr = Propagator(w.arrays, w.hbar, w.bias_fn(), hubbard_U=w.hubbard_U, precision=args.precision, device=dev)
-    tr = pr.traj
+    tr = Trajectory(w.arrays, w.hbar, precision=args.precision, device=dev)
     L = tr.layout
     stream = torch.cuda.ExternalStream(_lib.lib().zg_traj_stream(tr._h), device=dev)
-    eps = w.eps
+    bias = native_bias(w.bias, L.NL)
+    # one attempt = one launch of the captured attempt graph (controller on the device)
+    tr.graph_prepare(bias, w.hubbard_U)
+    tr.set_y(w.arrays["DM_Ortho"])
+    tr.graph_set(w.t0, w.stepsize, w.eps, 1e30)
 
-    def attempts(state, k):
-        t, h = state
-        adv = 0.0
+    def attempts(k):
+        adv, n_acc = 0.0, 0
         for _ in range(k):
-            TE, J0, _ = pr.attempt(t, h)
-            hn = pr.tab.hnew(h, TE, eps)
-            if TE < eps:
-                tr.step_fourth()
-                t += hn
-                adv += hn
-            h = hn
-        return (t, h), adv
+            recs, _, _, _ = tr.graph_run(1)
+            for r in recs:
+                if r[4]:
+                    adv += r[3]
+                    n_acc += 1
+        return adv, n_acc
 
-    pr.set_state(w.arrays["DM_Ortho"])
-    state = (w.t0, w.stepsize)
-    state, _ = attempts(state, args.warmup)
+    attempts(args.warmup)
     # the e2e leg replays the timed attempts from this state, uploaded from pinned memory
     snap = torch.empty(2 * L.size, dtype=torch.float64).pin_memory()
-    import ctypes
     _lib.check(_lib.lib().zg_get_state(tr._h, tr.stages, ctypes.c_void_p(snap.data_ptr())))
-    state0 = state
+    recs0, t0_, h0_, _ = tr.graph_run(0)
+    state0 = (t0_, h0_)
     peaks = np.zeros(2)
-    _lib.check(_lib.lib().zg_measure_peaks(dev, peaks.ctypes.data_as(__import__("ctypes").c_void_p)))
-    import ctypes
+    _lib.check(_lib.lib().zg_measure_peaks(dev, peaks.ctypes.data_as(ctypes.c_void_p)))
     _lib.check(_lib.lib().zg_profile(tr._h, 1))
+    tr.graph_run(0)  # recapture with the profiling event nodes before the timed region
     n0 = _lib.lib().zg_launch_count()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -162,15 +164,18 @@ def run_ours(args):
     torch.cuda.synchronize()
     with ClockSampler(dev) as clk:
         e0.record(stream)
-        state, adv = attempts(state, args.steps)
+        adv, n_acc = attempts(args.steps)
         e1.record(stream)
         torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     launches = _lib.lib().zg_launch_count() - n0
+    _, t_end, h_end, _ = tr.graph_run(0)
+    state = (t_end, h_end)
     pms = np.zeros(len(_lib.PROF_REGIONS))
     pcnt = np.zeros(len(_lib.PROF_REGIONS), np.int64)
     _lib.check(_lib.lib().zg_profile_read(tr._h, pms.ctypes.data_as(ctypes.c_void_p), pcnt.ctypes.data_as(ctypes.c_void_p)))
     _lib.check(_lib.lib().zg_profile(tr._h, 0))
+    tr.graph_run(0)  # recapture without event nodes, outside the e2e timed region
     if ws > 1:
         t = torch.tensor([ms, adv], device="cuda", dtype=torch.float64)
         tmax = t.clone()
@@ -182,7 +187,7 @@ def run_ours(args):
         adv_total = adv
     value = adv_total / (ms / 1e3)
     # ---- e2e through the public API: pinned upload + per-step sigma/current readback
-    e2e = run_e2e(pr, w, args, state0, snap, stream)
+    e2e = run_e2e(tr, w, args, state0, snap, stream)
     reg = dict(zip(_lib.PROF_REGIONS, zip(pms.tolist(), pcnt.tolist())))
     gemm_f, omega_f = rhs_flops(L)
     g_ms, g_n = reg["gemm"]
@@ -298,44 +303,44 @@ def f64_reference_timing(w, dev, state, mixed_value, mixed_ms):
             "note": "FP64 attempt time at the mixed run's step size; value_same_h = mixed value x time ratio"}
 
 
-def run_e2e(pr, w, args, state0, pinned, stream):
-    """The timed attempts again through the public API: the state they start
-    from is uploaded from pinned host memory inside the timed region, and sigma
-    (plus the lead currents of every attempt) comes back to the host after
-    every accepted step."""
+def run_e2e(tr, w, args, state0, pinned, stream):
+    """The timed attempts again through the public C ABI: the state they start
+    from is uploaded from pinned host memory and the controller set inside the
+    timed region, each attempt's record (error norm, step sizes, stage-0
+    currents) comes back to the host, and sigma after every accepted step, as
+    zand records them."""
+    import ctypes
+
     import torch
-    tr = pr.traj
+    from zandpack_gb300._lib import check, lib
     L = tr.layout
     sig_host = torch.empty((L.n, L.n * 2), dtype=torch.float64).pin_memory()
-    import ctypes
-    from zandpack_gb300._lib import check, lib
-    eps = w.eps
-    t, h = state0
+    rec_bytes = ctypes.sizeof(__import__("zandpack_gb300._lib", fromlist=["zg_attempt_rec"]).zg_attempt_rec)
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     check(lib().zg_set_state(tr._h, tr.stages, ctypes.c_void_p(pinned.data_ptr())))
+    tr.graph_set(state0[0], state0[1], w.eps, 1e30)
     adv = 0.0
     d2h = 0
     for _ in range(args.steps):
-        TE, J0, _ = pr.attempt(t, h)
-        hn = pr.tab.hnew(h, TE, eps)
-        d2h += 3 * 8 + L.NL * 8
-        if TE < eps:
-            tr.step_fourth()
-            check(lib().zg_get_sigma(tr._h, tr.stages, ctypes.c_void_p(sig_host.data_ptr())))
-            d2h += L.n * L.n * 16
-            t += hn
-            adv += hn
-        h = hn
+        recs, _, _, _ = tr.graph_run(1)
+        d2h += rec_bytes
+        for r in recs:
+            if r[4]:
+                check(lib().zg_get_sigma(tr._h, tr.stages, ctypes.c_void_p(sig_host.data_ptr())))
+                d2h += L.n * L.n * 16
+                adv += r[3]
     e1.record(stream)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     return {"value": adv / (ms / 1e3), "unit": "fs/s", "h2d_bytes_per_step": int(L.size * 16 / args.steps),
             "d2h_bytes_per_step": int(d2h / args.steps),
+            "api": "zg_set_state (pinned host) + zg_graph_set + zg_graph_run per attempt + zg_get_sigma per "
+                   "accepted step",
             "note": "the timed attempts repeated from their starting state, uploaded once from pinned memory "
-                    "(bytes amortised over the steps); sigma and currents read back after every accepted step"}
+                    "(bytes amortised over the steps); attempt records and sigma read back as zand records them"}
 
 
 def _oracle_stages(w, nstages, warm_stages=0):

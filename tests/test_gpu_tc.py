@@ -33,8 +33,10 @@ def test_split_tf32():
     assert err.max() < 2.0 ** -21
 
 
+# the last two shapes take the 256-wide tiles (enough tiles to fill the GPU), the
+# very last with partial tiles in M, N and K
 @pytest.mark.parametrize("M,N,K", [(128, 256, 32), (128, 128, 64), (200, 96, 100), (1024, 2048, 2048),
-                                   (4480, 2048, 2048)])
+                                   (4480, 2048, 2048), (4500, 2016, 1000)])
 def test_gemm_tf32x3(M, N, K):
     import torch
     from zandpack_gb300._lib import check, lib

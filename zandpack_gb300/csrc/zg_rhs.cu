@@ -161,19 +161,27 @@ __global__ void __launch_bounds__(256) k_zgemm(const __grid_constant__ GemmBatch
 #undef ZG_BK
 }
 
-// C = alpha * sum over splits of the partials, splits added in order
+// C = alpha * sum over splits of the partials, splits added in order.  The
+// output elements of all split problems form one index space (problem after
+// problem), so every problem is reduced by the whole grid at once.
 template <typename T>
-__global__ void k_zgemm_reduce(const __grid_constant__ GemmBatch<T> batch) {
+__global__ void k_zgemm_reduce(const __grid_constant__ GemmBatch<T> batch, int64_t total) {
   using C = typename cx<T>::t;
-  for (int pi = 0; pi < batch.nprob; ++pi) {
-    const GemmProb<T>& P = batch.p[pi];
-    if (P.ksplit <= 1) continue;
-    const int64_t mn = (int64_t)P.M * P.N;
-    GRID_STRIDE(e, mn) {
-      C v = czero<T>();
-      for (int sp = 0; sp < P.ksplit; ++sp) v = cadd(v, batch.ws[P.ws_off + sp * mn + e]);
-      P.Cm[(e / P.N) * P.ldc + (e % P.N)] = cmul(P.alpha, v);
+  GRID_STRIDE(g, total) {
+    int64_t e = g;
+    int pi = 0;
+    for (; pi < batch.nprob; ++pi) {
+      const GemmProb<T>& P = batch.p[pi];
+      if (P.ksplit <= 1) continue;
+      const int64_t mn = (int64_t)P.M * P.N;
+      if (e < mn) break;
+      e -= mn;
     }
+    const GemmProb<T>& P = batch.p[pi];
+    const int64_t mn = (int64_t)P.M * P.N;
+    C v = czero<T>();
+    for (int sp = 0; sp < P.ksplit; ++sp) v = cadd(v, batch.ws[P.ws_off + sp * mn + e]);
+    P.Cm[(e / P.N) * P.ldc + (e % P.N)] = cmul(P.alpha, v);
   }
 }
 
@@ -237,7 +245,10 @@ int launch_zgemm_batch(GemmBatch<T>& b, int64_t ws_capacity, cudaStream_t s) {
   ZG_CHECK_LAUNCH();
   count_launch();
   if (need > 0) {
-    k_zgemm_reduce<T><<<152 * 4, 256, 0, s>>>(b);
+    int64_t total = 0;
+    for (int i = 0; i < b.nprob; ++i)
+      if (b.p[i].ksplit > 1) total += (int64_t)b.p[i].M * b.p[i].N;
+    k_zgemm_reduce<T><<<grid_for(total, 256, 152 * 8), 256, 0, s>>>(b, total);
     ZG_CHECK_LAUNCH();
     count_launch();
   }
@@ -296,20 +307,36 @@ __device__ __forceinline__ typename cx<T>::t p_full(const RhsDev<T>& d, const ty
 }
 
 // k_sig = (h/hbar) (-i (T - T^H) + (P + P^H)/hbar), T = H(t) sigma  (Zandpack/mpi/zand:340-387)
+// One 32 x 32 block of k_sig per CTA; the transposed block of T it needs is
+// staged through shared memory so that both reads of T are row-contiguous.
 template <typename T>
-__global__ void k_sigma_finalize(const RhsDev<T> d, const StageParams* __restrict__ pp, const typename cx<T>::t* __restrict__ Tm,
-                                 int64_t ldT, const typename cx<T>::t* __restrict__ Pc, const double2* __restrict__ dis,
-                                 typename cx<T>::t* __restrict__ ksig) {
+__global__ void __launch_bounds__(256) k_sigma_finalize(const RhsDev<T> d, const StageParams* __restrict__ pp,
+                                                        const typename cx<T>::t* __restrict__ Tm, int64_t ldT,
+                                                        const typename cx<T>::t* __restrict__ Pc,
+                                                        const double2* __restrict__ dis,
+                                                        typename cx<T>::t* __restrict__ ksig) {
+  using C = typename cx<T>::t;
+  __shared__ C tile[32][33];  // tile[r][c] = T[j0 + r][i0 + c]
   const StageScalars p = load_params(pp);
-  const int64_t nn = (int64_t)d.n * d.n;
   const T ih = (T)(1.0 / p.hbar);
   const T sc = (T)(p.h / p.hbar);
-  GRID_STRIDE(e, nn) {
-    const int i = (int)(e / d.n), j = (int)(e % d.n);
-    const typename cx<T>::t tij = Tm[(int64_t)i * ldT + j], tji = Tm[(int64_t)j * ldT + i];
-    const typename cx<T>::t pij = p_full(d, Pc, i, j), pji = p_full(d, Pc, j, i);
+  const int n = d.n;
+  const int i0 = blockIdx.y * 32, j0 = blockIdx.x * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  for (int r = ty; r < 32; r += 8) {
+    const int j = j0 + r, i = i0 + tx;
+    tile[r][tx] = (j < n && i < n) ? Tm[(int64_t)j * ldT + i] : czero<T>();
+  }
+  __syncthreads();
+  for (int r = ty; r < 32; r += 8) {
+    const int i = i0 + r, j = j0 + tx;
+    if (i >= n || j >= n) continue;
+    const C tij = Tm[(int64_t)i * ldT + j];
+    const C tji = tile[tx][r];
+    const C pij = p_full(d, Pc, i, j), pji = p_full(d, Pc, j, i);
     // -i (tij - conj(tji)) = (tij.y + tji.y, -(tij.x - tji.x))
-    typename cx<T>::t v = cx<T>::make(tij.y + tji.y, -(tij.x - tji.x));
+    C v = cx<T>::make(tij.y + tji.y, -(tij.x - tji.x));
+    const int64_t e = (int64_t)i * n + j;
     if (dis) {  // - hbar * dissipator(ts, sigma)  (Zandpack/mpi/zand:343)
       const double2 q = dis[e];
       v.x -= (T)(p.hbar * q.x);
@@ -324,8 +351,8 @@ __global__ void k_sigma_finalize(const RhsDev<T> d, const StageParams* __restric
 template <typename T>
 int launch_sigma_finalize(const RhsDev<T>& d, const StageParams* p, const typename cx<T>::t* Tm, int64_t ldT,
                           const typename cx<T>::t* Pc, const double2* dis, typename cx<T>::t* ksig, cudaStream_t s) {
-  int64_t nn = (int64_t)d.n * d.n;
-  k_sigma_finalize<T><<<grid_for(nn, 256, 152 * 8), 256, 0, s>>>(d, p, Tm, ldT, Pc, dis, ksig);
+  const int nb = (d.n + 31) / 32;
+  k_sigma_finalize<T><<<dim3(nb, nb), dim3(32, 8), 0, s>>>(d, p, Tm, ldT, Pc, dis, ksig);
   ZG_CHECK_LAUNCH();
   count_launch();
   return ZG_OK;

@@ -6,22 +6,24 @@
 //
 // A is M x K and B is N x K, both row-major with K contiguous (K-major), FP32
 // arrays whose values are exact TF32 numbers (zg_split_tf32 produces them).
-// Complex products use the real embedding of the complex operand (see
-// zg_mixed.cu), so this kernel only sees real matrices.
+// Complex products use the real embedding of the complex operand (built by
+// k_build_operands_mixed in zg_rhs.cu), so this kernel only sees real matrices.
 //
 // One CTA computes a BM x BN tile (BM = 128 lanes of TMEM, BN fp32 columns):
-//   * one elected thread of warp 4 streams K-blocks of 32 elements (one
+//   * one elected thread of warp 8 streams K-blocks of 32 elements (one
 //     128-byte swizzle row) of Ahi, Alo, Bhi, Blo into a STAGES-deep ring of
 //     shared-memory buffers with TMA (cp.async.bulk.tensor, SWIZZLE_128B);
-//   * one elected thread of warp 5 issues tcgen05.mma (kind::tf32, M=128,
-//     N=BN, K=8) for the three products of a K-block into one of two TMEM
+//   * one elected thread of warp 9 issues tcgen05.mma (kind::tf32, M=128,
+//     N=BN, K=8) for the three products of a K-block into one of NACC TMEM
 //     accumulator buffers and commits to the smem buffer's "empty" barrier
 //     and to the TMEM buffer's "full" barrier;
-//   * warps 0-3 read each K-block's partial sum from TMEM (tcgen05.ld
-//     32x32b), add it into FP32 registers and release the TMEM buffer.
+//   * warps 0-7 read each K-block's partial sum from TMEM (tcgen05.ld
+//     32x32b; warps w and w+4 share TMEM lane quarter w and take one half of
+//     the columns each), add it into FP32 registers and release the buffer.
 // The tensor core truncates inside its accumulation, so a single accumulator
 // over K = 2048 drifts by ~1e-5 relative; per-K-block partials summed with
-// round-to-nearest keep the product at ~1e-7.
+// round-to-nearest keep the product at ~1e-7.  Eight drain warps and four
+// accumulator buffers keep the drain off the MMA issue path.
 // Every wait on an mbarrier is bounded by a clock64 budget; on timeout the
 // thread records an error code in *err and stops issuing, the MMA thread
 // waits for its own MMAs, the producer for its copies in flight, and TMEM is
@@ -114,7 +116,14 @@ struct TcCfg {
   static constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
   static constexpr int BAR_OFF = STAGES * STAGE_BYTES;
   static constexpr int SMEM = BAR_OFF + 256 + 1024;  // barriers, TMEM slot, alignment slack
-  static constexpr uint32_t TMEM_COLS = 2 * BN;      // two accumulator buffers
+  static constexpr int NACC = 512 / BN;               // accumulator buffers: all 512 TMEM columns
+  static constexpr uint32_t TMEM_COLS = NACC * BN;
+  static constexpr int DCOLS = 64;                    // columns of one drain warp
+  static constexpr int NDW = 4 * BN / DCOLS;          // drain warps (four TMEM lane quarters)
+  static constexpr int THREADS = 32 * (NDW + 2);      // + TMA warp + MMA warp
+  // SMEM > 114 KB keeps one CTA per SM, so the 512-column allocation never waits
+  static_assert(SMEM > 116 * 1024, "one CTA per SM is required by the full TMEM allocation");
+  static_assert(NACC >= 2 && (NACC & (NACC - 1)) == 0, "accumulator buffer count");
 };
 
 __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
@@ -131,18 +140,26 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
         "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])                  \
       : "r"(taddr))
 
-// Warp roles (192 threads): warps 0-3 drain the accumulator (TMEM lane
-// quarter = warp), warp 4 lane 0 loads with TMA, warp 5 lane 0 issues MMAs
-// and owns the TMEM allocation.  Each K-block of 32 is accumulated alone in
-// one of two TMEM buffers and added into FP32 registers (round to nearest),
-// so the tensor core's truncating accumulation never spans more than 12
-// instructions.
+#define TC_LD16(r, taddr)                                                                                        \
+  asm volatile(                                                                                                  \
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"      \
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), \
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])                  \
+      : "r"(taddr))
+
+// Warp roles (32 * (NDW + 2) threads): warps 0..NDW-1 drain the accumulators
+// (TMEM lane quarter = warp % 4, 64-column part = warp / 4), warp NDW lane 0
+// loads with TMA, warp NDW+1 lane 0 issues MMAs and that warp owns the TMEM
+// allocation.  Each K-block of 32 is accumulated alone in one of NACC TMEM
+// buffers and added into FP32 registers (round to nearest), so the tensor
+// core's truncating accumulation never spans more than 12 instructions.
 template <int BN, int STAGES>
-__global__ void __launch_bounds__(192, 1)
+__global__ void __launch_bounds__(TcCfg<BN, STAGES>::THREADS, 1)
     k_gemm_tf32x3(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtensorMap mAl,
                   const __grid_constant__ CUtensorMap mBh, const __grid_constant__ CUtensorMap mBl, float* __restrict__ D,
                   int M, int N, int K, long long ldd, int* err) {
   using C = TcCfg<BN, STAGES>;
+  constexpr int NACC = C::NACC, NDW = C::NDW;
   extern __shared__ uint8_t smem_raw[];
   const uint32_t raw = smem_u32(smem_raw);
   const uint32_t pad = (1024u - (raw & 1023u)) & 1023u;
@@ -150,10 +167,10 @@ __global__ void __launch_bounds__(192, 1)
   const uint32_t sbase = raw + pad;
   const uint32_t bar_full = sbase + C::BAR_OFF;        // STAGES x 8 B
   const uint32_t bar_empty = bar_full + 8 * STAGES;    // STAGES x 8 B
-  const uint32_t bar_tfull = bar_empty + 8 * STAGES;   // 2 x 8 B
-  const uint32_t bar_tempty = bar_tfull + 16;          // 2 x 8 B
-  const uint32_t bar_done = bar_tempty + 16;           // 8 B
-  uint32_t* tmem_slot = (uint32_t*)(smem + C::BAR_OFF + 16 * STAGES + 40);
+  const uint32_t bar_tfull = bar_empty + 8 * STAGES;   // NACC x 8 B
+  const uint32_t bar_tempty = bar_tfull + 8 * NACC;    // NACC x 8 B
+  const uint32_t bar_done = bar_tempty + 8 * NACC;     // 8 B
+  uint32_t* tmem_slot = (uint32_t*)(smem + C::BAR_OFF + 16 * STAGES + 16 * NACC + 8);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * BN;
   const int nk = (K + TC_BK - 1) / TC_BK;
@@ -163,14 +180,14 @@ __global__ void __launch_bounds__(192, 1)
       mbar_init(bar_full + 8 * s, 1);
       mbar_init(bar_empty + 8 * s, 1);
     }
-    for (int b = 0; b < 2; ++b) {
+    for (int b = 0; b < NACC; ++b) {
       mbar_init(bar_tfull + 8 * b, 1);
-      mbar_init(bar_tempty + 8 * b, 128);
+      mbar_init(bar_tempty + 8 * b, 32 * NDW);  // every thread of the drain warps
     }
     mbar_init(bar_done, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 5) {
+  if (warp == NDW + 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
                  "r"(C::TMEM_COLS)
                  : "memory");
@@ -181,7 +198,7 @@ __global__ void __launch_bounds__(192, 1)
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
 
-  if (warp == 4) {
+  if (warp == NDW) {
     if (lane == 0) {
       // ---------------- TMA producer
       int issued[STAGES];
@@ -207,16 +224,16 @@ __global__ void __launch_bounds__(192, 1)
           if (issued[s] > 0) mbar_wait(bar_full + 8 * s, (uint32_t)(issued[s] - 1) & 1u, err, 4);
       }
     }
-  } else if (warp == 5) {
+  } else if (warp == NDW + 1) {
     if (lane == 0) {
       // ---------------- MMA issuer
       constexpr uint32_t idesc = idesc_tf32(TC_BM, BN);
       for (int kb = 0; kb < nk; ++kb) {
         const int s = kb % STAGES;
         const uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
-        const int b = kb & 1;
+        const int b = kb % NACC;
         if (!mbar_wait(bar_full + 8 * s, ph, err, 2)) break;
-        if (!mbar_wait(bar_tempty + 8 * b, ((uint32_t)(kb >> 1) & 1u) ^ 1u, err, 5)) break;
+        if (!mbar_wait(bar_tempty + 8 * b, ((uint32_t)(kb / NACC) & 1u) ^ 1u, err, 5)) break;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t st = sbase + s * C::STAGE_BYTES;
         const uint32_t aH = st, aL = st + C::A_BYTES, bH = st + 2 * C::A_BYTES, bL = bH + C::B_BYTES;
@@ -235,49 +252,54 @@ __global__ void __launch_bounds__(192, 1)
       mbar_wait(bar_done, 0, err, 6);  // every MMA issued above has completed
     }
   } else {
-    // ---------------- drain warps 0-3: row m0 + 32*warp + lane
-    float acc[BN];
+    // ---------------- drain warps: row m0 + 32*(warp%4) + lane, columns part*DCOLS ...
+    const int quarter = warp & 3, part = warp >> 2;
+    float acc[C::DCOLS];
 #pragma unroll
-    for (int i = 0; i < BN; ++i) acc[i] = 0.f;
-    const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+    for (int i = 0; i < C::DCOLS; ++i) acc[i] = 0.f;
+    const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
     bool ok = true;
     for (int kb = 0; kb < nk; ++kb) {
-      const int b = kb & 1;
-      ok = __all_sync(0xffffffffu, mbar_wait(bar_tfull + 8 * b, (uint32_t)(kb >> 1) & 1u, err, 3));
+      const int b = kb % NACC;
+      ok = __all_sync(0xffffffffu, mbar_wait(bar_tfull + 8 * b, (uint32_t)(kb / NACC) & 1u, err, 3));
       if (!ok) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t t0 = tmem + lane_base + (uint32_t)(b * BN);
+      const uint32_t t0 = tmem + lane_base + (uint32_t)(b * BN + part * C::DCOLS);
+      // 32-column loads where registers allow (BN = 128: 320 threads), else 16
+      constexpr int LDW = C::THREADS <= 320 ? 32 : 16;
 #pragma unroll
-      for (int c = 0; c < BN; c += 64) {
-        uint32_t r0[32], r1[32];
-        TC_LD32(r0, t0 + c);
-        TC_LD32(r1, t0 + c + 32);
+      for (int c = 0; c < C::DCOLS; c += LDW) {
+        uint32_t r0[LDW];
+        if constexpr (LDW == 32) {
+          TC_LD32(r0, t0 + c);
+        } else {
+          TC_LD16(r0, t0 + c);
+        }
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-        for (int i = 0; i < 32; ++i) {
-          acc[c + i] += __uint_as_float(r0[i]);
-          acc[c + 32 + i] += __uint_as_float(r1[i]);
-        }
+        for (int i = 0; i < LDW; ++i) acc[c + i] += __uint_as_float(r0[i]);
       }
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       mbar_arrive(bar_tempty + 8 * b);
     }
-    const int row = m0 + warp * 32 + lane;
+    const int row = m0 + quarter * 32 + lane;
+    const int c0 = n0 + part * C::DCOLS;
     if (ok && row < M) {
-      float* dst = D + (long long)row * ldd + n0;
-      if (n0 + BN <= N && (((uintptr_t)dst) & 15) == 0) {
+      float* dst = D + (long long)row * ldd + c0;
+      if (c0 + C::DCOLS <= N && (((uintptr_t)dst) & 15) == 0) {
 #pragma unroll
-        for (int i = 0; i < BN; i += 4) *(float4*)(dst + i) = make_float4(acc[i], acc[i + 1], acc[i + 2], acc[i + 3]);
+        for (int i = 0; i < C::DCOLS; i += 4)
+          *(float4*)(dst + i) = make_float4(acc[i], acc[i + 1], acc[i + 2], acc[i + 3]);
       } else {
 #pragma unroll
-        for (int i = 0; i < BN; ++i)
-          if (n0 + i < N) dst[i] = acc[i];
+        for (int i = 0; i < C::DCOLS; ++i)
+          if (c0 + i < N) dst[i] = acc[i];
       }
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  if (warp == 5) {
+  if (warp == NDW + 1) {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(C::TMEM_COLS) : "memory");
   }
@@ -323,15 +345,16 @@ int make_tmap_f32(CUtensorMap* map, const float* base, int64_t rows, int64_t col
 template <int BN, int STAGES>
 static int launch_tc(const TcGemm& g, cudaStream_t s) {
   using C = TcCfg<BN, STAGES>;
-  static bool configured[64] = {};
+  static std::atomic<bool> configured[64];
   int dev = 0;
   ZG_CHECK_CUDA(cudaGetDevice(&dev));
-  if (dev < 64 && !configured[dev]) {
+  if (dev < 64 && !configured[dev].load()) {
     ZG_CHECK_CUDA(cudaFuncSetAttribute(k_gemm_tf32x3<BN, STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
     configured[dev] = true;
   }
   dim3 grid((g.N + BN - 1) / BN, (g.M + TC_BM - 1) / TC_BM);
-  k_gemm_tf32x3<BN, STAGES><<<grid, 192, C::SMEM, s>>>(g.Ah, g.Al, g.Bh, g.Bl, g.D, g.M, g.N, g.K, g.ldd, g.err);
+  k_gemm_tf32x3<BN, STAGES><<<grid, C::THREADS, C::SMEM, s>>>(g.Ah, g.Al, g.Bh, g.Bl, g.D, g.M, g.N, g.K, g.ldd,
+                                                              g.err);
   ZG_CHECK_LAUNCH();
   count_launch();
   return ZG_OK;
@@ -341,7 +364,11 @@ int tc_gemm_prepare(TcGemm& g, const float* Ah, const float* Al, const float* Bh
                     int64_t ldb, float* D, int64_t ldd, int M, int N, int K, int* err) {
   ZG_REQUIRE(M > 0 && N > 0 && K > 0, "empty tensor-core GEMM");
   ZG_REQUIRE(N % 32 == 0, "tensor-core GEMM needs N a multiple of 32 (got %d)", N);
-  g.BN = 128;
+  // 256-wide tiles halve the shared-memory operand traffic per MMA (the
+  // 128 x 128 x 8 MMA reads 8 KB of operands for 262 kflop) when there are
+  // enough of them to fill the GPU; otherwise 128-wide tiles
+  const int64_t tiles256 = (int64_t)((M + TC_BM - 1) / TC_BM) * ((N + 255) / 256);
+  g.BN = tiles256 >= 152 ? 256 : 128;
   ZG_TRY(make_tmap_f32(&g.Ah, Ah, M, K, lda, TC_BM));
   ZG_TRY(make_tmap_f32(&g.Al, Al, M, K, lda, TC_BM));
   ZG_TRY(make_tmap_f32(&g.Bh, Bh, N, K, ldb, g.BN));
@@ -350,7 +377,9 @@ int tc_gemm_prepare(TcGemm& g, const float* Ah, const float* Al, const float* Bh
   return ZG_OK;
 }
 
-int tc_gemm_launch(const TcGemm& g, cudaStream_t s) { return launch_tc<128, 3>(g, s); }
+int tc_gemm_launch(const TcGemm& g, cudaStream_t s) {
+  return g.BN == 256 ? launch_tc<256, 2>(g, s) : launch_tc<128, 3>(g, s);
+}
 
 // hi = rna_tf32(x), lo = rna_tf32(x - hi)
 __global__ void k_split_tf32(const float* __restrict__ x, float* __restrict__ hi, float* __restrict__ lo, int64_t n) {
