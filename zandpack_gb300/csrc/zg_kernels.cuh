@@ -25,10 +25,11 @@ struct TcGemm {
   CUtensorMap Ah, Al, Bh, Bl;
   float* D;
   long long ldd;
-  int M, N, K, BN;
+  int M, N, K, BN, BK;
   int* err;  // device int, nonzero after a timed-out wait
 };
-int make_tmap_f32(CUtensorMap* map, const float* base, int64_t rows, int64_t cols, int64_t ld, int box_rows);
+int make_tmap_f32(CUtensorMap* map, const float* base, int64_t rows, int64_t cols, int64_t ld, int box_rows,
+                  int box_k);
 int tc_gemm_prepare(TcGemm& g, const float* Ah, const float* Al, const float* Bh, const float* Bl, int64_t lda,
                     int64_t ldb, float* D, int64_t ldd, int M, int N, int K, int* err);
 int tc_gemm_launch(const TcGemm& g, cudaStream_t s);

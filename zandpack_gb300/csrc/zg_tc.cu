@@ -82,14 +82,18 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
       : "memory");
 }
 
-// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row core groups 1024 B apart
-__device__ __forceinline__ uint64_t umma_desc_sw128(uint32_t addr) {
+// shared-memory matrix descriptor, K-major with the swizzle of a BK-float row:
+// BK = 32 -> 128-byte rows, SWIZZLE_128B, 8-row core groups 1024 B apart;
+// BK = 16 ->  64-byte rows, SWIZZLE_64B,  8-row core groups  512 B apart
+template <int BK>
+__device__ __forceinline__ uint64_t umma_desc_k(uint32_t addr) {
+  static_assert(BK == 32 || BK == 16, "K block of 16 or 32 floats");
   uint64_t d = 0;
   d |= (uint64_t)((addr & 0x3FFFF) >> 4);        // start address
   d |= (uint64_t)(16 >> 4) << 16;                // leading byte offset (unused for swizzled K-major)
-  d |= (uint64_t)(1024 >> 4) << 32;              // stride byte offset
+  d |= (uint64_t)((8 * BK * 4) >> 4) << 32;      // stride byte offset: 8 rows
   d |= (uint64_t)1 << 46;                        // descriptor version (sm_100 family)
-  d |= (uint64_t)2 << 61;                        // SWIZZLE_128B
+  d |= (uint64_t)(BK == 32 ? 2 : 4) << 61;       // SWIZZLE_128B : SWIZZLE_64B
   return d;
 }
 
@@ -109,10 +113,14 @@ __device__ __forceinline__ void umma_commit(uint32_t bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
 
-template <int BN, int STAGES>
+// BK: K elements per shared-memory stage (32 or 16); a TMEM accumulation
+// group always spans K = 32 (KPG stages), so the drain granularity and hence
+// the accuracy do not depend on BK.
+template <int BN, int STAGES, int BK>
 struct TcCfg {
-  static constexpr int A_BYTES = TC_BM * TC_BK * 4;   // 16 KB
-  static constexpr int B_BYTES = BN * TC_BK * 4;      // 16 KB at BN = 128
+  static constexpr int A_BYTES = TC_BM * BK * 4;      // 16 KB at BK = 32
+  static constexpr int B_BYTES = BN * BK * 4;         // 32 KB at BN = 256, BK = 32
+  static constexpr int KPG = TC_BK / BK;              // stages per accumulation group
   static constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
   static constexpr int BAR_OFF = STAGES * STAGE_BYTES;
   static constexpr int SMEM = BAR_OFF + 256 + 1024;  // barriers, TMEM slot, alignment slack
@@ -153,13 +161,13 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
 // allocation.  Each K-block of 32 is accumulated alone in one of NACC TMEM
 // buffers and added into FP32 registers (round to nearest), so the tensor
 // core's truncating accumulation never spans more than 12 instructions.
-template <int BN, int STAGES>
-__global__ void __launch_bounds__(TcCfg<BN, STAGES>::THREADS, 1)
+template <int BN, int STAGES, int BK>
+__global__ void __launch_bounds__(TcCfg<BN, STAGES, BK>::THREADS, 1)
     k_gemm_tf32x3(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtensorMap mAl,
                   const __grid_constant__ CUtensorMap mBh, const __grid_constant__ CUtensorMap mBl, float* __restrict__ D,
                   int M, int N, int K, long long ldd, int* err) {
-  using C = TcCfg<BN, STAGES>;
-  constexpr int NACC = C::NACC, NDW = C::NDW;
+  using C = TcCfg<BN, STAGES, BK>;
+  constexpr int NACC = C::NACC, NDW = C::NDW, KPG = C::KPG;
   extern __shared__ uint8_t smem_raw[];
   const uint32_t raw = smem_u32(smem_raw);
   const uint32_t pad = (1024u - (raw & 1023u)) & 1023u;
@@ -173,7 +181,8 @@ __global__ void __launch_bounds__(TcCfg<BN, STAGES>::THREADS, 1)
   uint32_t* tmem_slot = (uint32_t*)(smem + C::BAR_OFF + 16 * STAGES + 16 * NACC + 8);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * BN;
-  const int nk = (K + TC_BK - 1) / TC_BK;
+  const int nk = (K + BK - 1) / BK;       // shared-memory stages of BK
+  const int ng = (nk + KPG - 1) / KPG;    // TMEM accumulation groups of K = 32
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -211,7 +220,7 @@ __global__ void __launch_bounds__(TcCfg<BN, STAGES>::THREADS, 1)
         if (!ok) break;
         const uint32_t st = sbase + s * C::STAGE_BYTES;
         mbar_expect_tx(bar_full + 8 * s, C::STAGE_BYTES);
-        const int kx = kb * TC_BK;
+        const int kx = kb * BK;
         tma_load_2d(st, &mAh, bar_full + 8 * s, kx, m0);
         tma_load_2d(st + C::A_BYTES, &mAl, bar_full + 8 * s, kx, m0);
         tma_load_2d(st + 2 * C::A_BYTES, &mBh, bar_full + 8 * s, kx, n0);
@@ -228,25 +237,35 @@ __global__ void __launch_bounds__(TcCfg<BN, STAGES>::THREADS, 1)
     if (lane == 0) {
       // ---------------- MMA issuer
       constexpr uint32_t idesc = idesc_tf32(TC_BM, BN);
-      for (int kb = 0; kb < nk; ++kb) {
-        const int s = kb % STAGES;
-        const uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
-        const int b = kb % NACC;
-        if (!mbar_wait(bar_full + 8 * s, ph, err, 2)) break;
-        if (!mbar_wait(bar_tempty + 8 * b, ((uint32_t)(kb / NACC) & 1u) ^ 1u, err, 5)) break;
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t st = sbase + s * C::STAGE_BYTES;
-        const uint32_t aH = st, aL = st + C::A_BYTES, bH = st + 2 * C::A_BYTES, bL = bH + C::B_BYTES;
+      bool ok = true;
+      for (int g = 0; g < ng && ok; ++g) {
+        const int b = g % NACC;
+        if (!mbar_wait(bar_tempty + 8 * b, ((uint32_t)(g / NACC) & 1u) ^ 1u, err, 5)) break;
         const uint32_t d = tmem + (uint32_t)(b * BN);
+        for (int q = 0; q < KPG; ++q) {
+          const int kb = g * KPG + q;
+          if (kb >= nk) break;
+          const int s = kb % STAGES;
+          const uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
+          if (!mbar_wait(bar_full + 8 * s, ph, err, 2)) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t st = sbase + s * C::STAGE_BYTES;
+          const uint32_t aH = st, aL = st + C::A_BYTES, bH = st + 2 * C::A_BYTES, bL = bH + C::B_BYTES;
 #pragma unroll
-        for (int j = 0; j < TC_BK / 8; ++j) {
-          const uint32_t off = j * 32;  // 8 tf32 = 32 bytes along K inside the swizzle row
-          umma_tf32(d, umma_desc_sw128(aH + off), umma_desc_sw128(bH + off), idesc, j > 0 ? 1u : 0u);
-          umma_tf32(d, umma_desc_sw128(aH + off), umma_desc_sw128(bL + off), idesc, 1u);
-          umma_tf32(d, umma_desc_sw128(aL + off), umma_desc_sw128(bH + off), idesc, 1u);
+          for (int j = 0; j < BK / 8; ++j) {
+            const uint32_t off = j * 32;  // 8 tf32 = 32 bytes along K inside the swizzle row
+            const uint32_t first = (q == 0 && j == 0) ? 0u : 1u;
+            umma_tf32(d, umma_desc_k<BK>(aH + off), umma_desc_k<BK>(bH + off), idesc, first);
+            umma_tf32(d, umma_desc_k<BK>(aH + off), umma_desc_k<BK>(bL + off), idesc, 1u);
+            umma_tf32(d, umma_desc_k<BK>(aL + off), umma_desc_k<BK>(bH + off), idesc, 1u);
+          }
+          umma_commit(bar_empty + 8 * s);  // frees the smem buffer once these MMAs have read it
         }
-        umma_commit(bar_empty + 8 * s);  // frees the smem buffer once these MMAs have read it
-        umma_commit(bar_tfull + 8 * b);  // hands the K-block sum to the drain warps
+        if (!ok) break;
+        umma_commit(bar_tfull + 8 * b);  // hands the group's K = 32 sum to the drain warps
       }
       umma_commit(bar_done);
       mbar_wait(bar_done, 0, err, 6);  // every MMA issued above has completed
@@ -259,9 +278,9 @@ __global__ void __launch_bounds__(TcCfg<BN, STAGES>::THREADS, 1)
     for (int i = 0; i < C::DCOLS; ++i) acc[i] = 0.f;
     const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
     bool ok = true;
-    for (int kb = 0; kb < nk; ++kb) {
-      const int b = kb % NACC;
-      ok = __all_sync(0xffffffffu, mbar_wait(bar_tfull + 8 * b, (uint32_t)(kb / NACC) & 1u, err, 3));
+    for (int g = 0; g < ng; ++g) {
+      const int b = g % NACC;
+      ok = __all_sync(0xffffffffu, mbar_wait(bar_tfull + 8 * b, (uint32_t)(g / NACC) & 1u, err, 3));
       if (!ok) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const uint32_t t0 = tmem + lane_base + (uint32_t)(b * BN + part * C::DCOLS);
@@ -321,19 +340,23 @@ static int tmap_encode_fn() {
   return ZG_OK;
 }
 
-// rows x cols fp32 row-major (cols contiguous, row stride ld elements), box = 32 x box_rows
-int make_tmap_f32(CUtensorMap* map, const float* base, int64_t rows, int64_t cols, int64_t ld, int box_rows) {
+// rows x cols fp32 row-major (cols contiguous, row stride ld elements), box = box_k x box_rows,
+// swizzled to match the tcgen05 descriptor of a box_k-float row (128 B or 64 B)
+int make_tmap_f32(CUtensorMap* map, const float* base, int64_t rows, int64_t cols, int64_t ld, int box_rows,
+                  int box_k) {
   ZG_TRY(tmap_encode_fn());
   ZG_REQUIRE(((uintptr_t)base & 15) == 0, "TMA base address must be 16-byte aligned");
   ZG_REQUIRE((ld * 4) % 16 == 0, "TMA row stride must be a multiple of 16 bytes");
   ZG_REQUIRE(rows > 0 && cols > 0, "empty TMA tensor");
   cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
   cuuint64_t strides[1] = {(cuuint64_t)(ld * 4)};
-  cuuint32_t box[2] = {TC_BK, (cuuint32_t)box_rows};
+  ZG_REQUIRE(box_k == 32 || box_k == 16, "TMA box of 16 or 32 floats along K");
+  cuuint32_t box[2] = {(cuuint32_t)box_k, (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1, 1};
   CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)base, dims, strides, box, estr,
-                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                        CU_TENSOR_MAP_INTERLEAVE_NONE,
+                        box_k == 32 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) {
     set_error("cuTensorMapEncodeTiled failed (%d) for %lld x %lld, ld %lld", (int)r, (long long)rows,
               (long long)cols, (long long)ld);
@@ -342,19 +365,20 @@ int make_tmap_f32(CUtensorMap* map, const float* base, int64_t rows, int64_t col
   return ZG_OK;
 }
 
-template <int BN, int STAGES>
+template <int BN, int STAGES, int BK>
 static int launch_tc(const TcGemm& g, cudaStream_t s) {
-  using C = TcCfg<BN, STAGES>;
+  using C = TcCfg<BN, STAGES, BK>;
   static std::atomic<bool> configured[64];
   int dev = 0;
   ZG_CHECK_CUDA(cudaGetDevice(&dev));
   if (dev < 64 && !configured[dev].load()) {
-    ZG_CHECK_CUDA(cudaFuncSetAttribute(k_gemm_tf32x3<BN, STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
+    ZG_CHECK_CUDA(
+        cudaFuncSetAttribute(k_gemm_tf32x3<BN, STAGES, BK>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
     configured[dev] = true;
   }
   dim3 grid((g.N + BN - 1) / BN, (g.M + TC_BM - 1) / TC_BM);
-  k_gemm_tf32x3<BN, STAGES><<<grid, C::THREADS, C::SMEM, s>>>(g.Ah, g.Al, g.Bh, g.Bl, g.D, g.M, g.N, g.K, g.ldd,
-                                                              g.err);
+  k_gemm_tf32x3<BN, STAGES, BK><<<grid, C::THREADS, C::SMEM, s>>>(g.Ah, g.Al, g.Bh, g.Bl, g.D, g.M, g.N, g.K,
+                                                                  g.ldd, g.err);
   ZG_CHECK_LAUNCH();
   count_launch();
   return ZG_OK;
@@ -369,16 +393,20 @@ int tc_gemm_prepare(TcGemm& g, const float* Ah, const float* Al, const float* Bh
   // enough of them to fill the GPU; otherwise 128-wide tiles
   const int64_t tiles256 = (int64_t)((M + TC_BM - 1) / TC_BM) * ((N + 255) / 256);
   g.BN = tiles256 >= 152 ? 256 : 128;
-  ZG_TRY(make_tmap_f32(&g.Ah, Ah, M, K, lda, TC_BM));
-  ZG_TRY(make_tmap_f32(&g.Al, Al, M, K, lda, TC_BM));
-  ZG_TRY(make_tmap_f32(&g.Bh, Bh, N, K, ldb, g.BN));
-  ZG_TRY(make_tmap_f32(&g.Bl, Bl, N, K, ldb, g.BN));
+  // 256-wide tiles take 16-float K stages: four 48 KB ring stages instead of
+  // two 96 KB ones (measured 15 % faster at 4480 x 2048 x 2048); 128-wide
+  // tiles keep three 64 KB stages of 32 floats (six 32 KB stages were slower)
+  g.BK = g.BN == 256 ? 16 : 32;
+  ZG_TRY(make_tmap_f32(&g.Ah, Ah, M, K, lda, TC_BM, g.BK));
+  ZG_TRY(make_tmap_f32(&g.Al, Al, M, K, lda, TC_BM, g.BK));
+  ZG_TRY(make_tmap_f32(&g.Bh, Bh, N, K, ldb, g.BN, g.BK));
+  ZG_TRY(make_tmap_f32(&g.Bl, Bl, N, K, ldb, g.BN, g.BK));
   g.D = D; g.ldd = ldd; g.M = M; g.N = N; g.K = K; g.err = err;
   return ZG_OK;
 }
 
 int tc_gemm_launch(const TcGemm& g, cudaStream_t s) {
-  return g.BN == 256 ? launch_tc<256, 2>(g, s) : launch_tc<128, 3>(g, s);
+  return g.BN == 256 ? launch_tc<256, 4, 16>(g, s) : launch_tc<128, 3, 32>(g, s);
 }
 
 // hi = rna_tf32(x), lo = rna_tf32(x - hi)
