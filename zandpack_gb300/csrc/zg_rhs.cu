@@ -547,6 +547,24 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) k_omega(const Rhs
 #pragma unroll
     for (int j = 0; j < 4; ++j) acc[i][j] = czero<T>();
   const int kbeg = t.term1 ? 0 : nc, kend = t.term2 ? 2 * nc : nc;
+  const int64_t ld = t.blk == 0 ? d.Ns : d.Nf;
+  const C* in = t.blk == 0 ? omA_in : omB_in;
+  // FP32: the Omega tile of the diagonal term is copied to shared memory
+  // (cp.async) while the source products run, instead of being waited for in
+  // the epilogue
+  extern __shared__ __align__(16) unsigned char om_smem[];
+  C* Os = reinterpret_cast<C*>(om_smem);  // [64][64], FP32 only
+  if constexpr (sizeof(T) == 4) {
+    for (int q = tid; q < 64 * 64; q += 256) {
+      const int r = q >> 6, c = q & 63;
+      if (r < t.nrows && c < t.ncols) {
+        const C* src = in + (int64_t)(t.row0 + r) * ld + t.col0 + c;
+        const uint32_t dst = (uint32_t)__cvta_generic_to_shared(Os + q);
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(dst), "l"(src) : "memory");
+      }
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  }
   C ra[RO], rb[RO];
   // operands of K index k for local row/column rr (zero outside the tile and K range)
 #define ZG_OMEGA_FETCH(k0)                                                                  \
@@ -595,10 +613,12 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) k_omega(const Rhs
     }
     __syncthreads();
   }
+  if constexpr (sizeof(T) == 4) {
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    __syncthreads();
+  }
   const T sc = (T)(p.h / p.hbar);
   const T h = (T)p.h;
-  const int64_t ld = t.blk == 0 ? d.Ns : d.Nf;
-  const C* in = t.blk == 0 ? omA_in : omB_in;
   C* out = t.blk == 0 ? omA_out : omB_out;
   const T da = (T)p.delta[t.a], db = (T)p.delta[t.b];
 #pragma unroll
@@ -616,7 +636,8 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) k_omega(const Rhs
       C xm = d.Xm[l];
       xm.x += db;
       const int64_t e = m * ld + (t.col0 + c);
-      const C dd = cmul(csub(xp, xm), in[e]);  // (X+ - X-) Omega
+      const C om = sizeof(T) == 4 ? Os[r * 64 + c] : in[e];
+      const C dd = cmul(csub(xp, xm), om);  // (X+ - X-) Omega
       // (i h/hbar) dd = sc * (-dd.y, dd.x)
       C v = cscale(acc[i][j], h);
       v.x -= sc * dd.y;
@@ -632,7 +653,17 @@ int launch_omega(const RhsDev<T>& d, const StageParams* p, const OmTile* tiles, 
                  const typename cx<T>::t* omA_in, const typename cx<T>::t* omB_in, typename cx<T>::t* omA_out,
                  typename cx<T>::t* omB_out, cudaStream_t s) {
   if (ntiles == 0) return ZG_OK;
-  k_omega<T><<<ntiles, 256, 0, s>>>(d, p, tiles, G, omA_in, omB_in, omA_out, omB_out);
+  const int smem = sizeof(T) == 4 ? 64 * 64 * (int)sizeof(typename cx<T>::t) : 0;
+  if (smem > 0) {
+    static std::atomic<bool> configured[64];
+    int dev = 0;
+    ZG_CHECK_CUDA(cudaGetDevice(&dev));
+    if (dev < 64 && !configured[dev].load()) {
+      ZG_CHECK_CUDA(cudaFuncSetAttribute(k_omega<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+      configured[dev] = true;
+    }
+  }
+  k_omega<T><<<ntiles, 256, smem, s>>>(d, p, tiles, G, omA_in, omB_in, omA_out, omB_out);
   ZG_CHECK_LAUNCH();
   count_launch();
   return ZG_OK;
