@@ -159,3 +159,42 @@ def test_mixed_trajectory_on_reference_grid(case):
     assert dsig <= ATOL_TRAJ
     assert dJ <= ATOL_TRAJ
     pr.traj.close()
+
+
+def test_h_operands_after_a_full_dH_matrix():
+    """The mixed path builds H0's tensor-core operands once and then rebuilds
+    only their diagonal (Hubbard term); a stage with a full dH matrix
+    overwrites them.  A Hubbard stage or a graph attempt that follows must
+    give exactly what a fresh trajectory gives."""
+    from zandpack_gb300 import _lib
+    from zandpack_gb300.engine import Trajectory, native_bias
+    from zandpack_gb300.workloads import make_workload
+    w = make_workload("mini2")
+    U = w.hubbard_U
+    trA = Trajectory(w.arrays, w.hbar, precision="mixed")
+    trB = Trajectory(w.arrays, w.hbar, precision="mixed")
+    n = trA.layout.n
+    rng = np.random.default_rng(3)
+    D = rng.standard_normal((n, n)) * 0.05
+    D = (D + D.T).astype(complex)
+    delta = [0.1, -0.1]
+    for tr in (trA, trB):
+        tr.set_y(w.arrays["DM_Ortho"])
+    trA.stage_input(0)
+    trA.set_dH(D)
+    trA.rhs(0, 0.0, 0.02, delta, _lib.ZG_DH_MATRIX)
+    for tr in (trA, trB):
+        tr.stage_input(0)
+        tr.rhs(0, 0.0, 0.02, delta, _lib.ZG_DH_HUBBARD, U)
+    assert np.array_equal(trA.get_slot(0), trB.get_slot(0))
+    trA.stage_input(0)
+    trA.rhs(0, 0.0, 0.02, delta, _lib.ZG_DH_MATRIX)  # operands hold dH again
+    b = native_bias(w.bias, trA.layout.NL)
+    out = []
+    for tr in (trA, trB):
+        tr.graph_prepare(b, U)
+        tr.graph_set(w.t0, w.stepsize, w.eps, w.t1)
+        recs, _, _, _ = tr.graph_run(2)
+        out.append([r[2] for r in recs])
+        tr.close()
+    assert out[0] == out[1] and len(out[0]) == 2

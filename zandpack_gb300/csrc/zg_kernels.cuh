@@ -195,9 +195,11 @@ int launch_build_ht(int n, const double2* H0, const double2* sig, const double2*
 //   Ht (n x np complex = n x 2np real)             A of  T = H(t) sigma
 //   BH (2np x 2np real embedding of H(t)^T form)    B of  R1 = psi H(t)^T
 //   BS (2np x 2np real embedding of sigma)          B of  T
+// h_part: 0 = all of the H(t) operands, 1 = their diagonal only (off-diagonal
+// entries already hold H0), 2 = leave them; BS is always rebuilt
 int launch_build_operands_mixed(int n, int np, const double2* H0, const float2* sig32, const double2* dH, int dH_mode,
-                                double U, float* Hth, float* Htl, float* BHh, float* BHl, float* BSh, float* BSl,
-                                cudaStream_t s);
+                                double U, int h_part, float* Hth, float* Htl, float* BHh, float* BHl, float* BSh,
+                                float* BSl, cudaStream_t s);
 // Lead currents in FP64 from the FP64 state: J_a = 2 Re sum_{m in a} sum_k psi[m][C_a[k]] IXI[m][k] / hbar^2
 // row ranges per lead: sourced rows [s[a], s[a+1]), free rows [f[a], f[a+1])
 struct CurRows {

@@ -707,54 +707,69 @@ __device__ __forceinline__ void split_tf32_r(float v, float& hi, float& lo) {
 //   BS rows 2r, 2r+1, cols 2c, 2c+1 = [[Sr, -Si], [Si, Sr]] of sigma[c][r]
 // Padding (r or c >= n) is written as zero.
 __global__ void k_build_operands_mixed(int n, int np, const double2* __restrict__ H0, const float2* __restrict__ sig32,
-                                       const double2* __restrict__ dH, int dH_mode, double U, float* __restrict__ Hth,
-                                       float* __restrict__ Htl, float* __restrict__ BHh, float* __restrict__ BHl,
-                                       float* __restrict__ BSh, float* __restrict__ BSl) {
-  const int64_t tot = (int64_t)np * np;
+                                       const double2* __restrict__ dH, int dH_mode, double U, int h_part,
+                                       float* __restrict__ Hth, float* __restrict__ Htl, float* __restrict__ BHh,
+                                       float* __restrict__ BHl, float* __restrict__ BSh, float* __restrict__ BSl) {
   const int64_t ld = 2 * (int64_t)np;
-  GRID_STRIDE(e, tot) {
+  // h_part: 0 = every entry of the H(t) operands, 1 = their diagonal only
+  // (the rest already holds H0's embedding), 2 = none; the sigma operand
+  // BS is always rebuilt.  Threads [0, np*np) cover BS (and H when h_part == 0),
+  // threads [np*np, np*np + np) the diagonal when h_part == 1.
+  const int64_t tot = (int64_t)np * np + (h_part == 1 ? np : 0);
+  GRID_STRIDE(q, tot) {
+    const bool diag_job = q >= (int64_t)np * np;
+    const int64_t e = diag_job ? (q - (int64_t)np * np) * (np + 1) : q;
     const int r = (int)(e / np), c = (int)(e % np);
-    float hr = 0.f, hi = 0.f, sr = 0.f, si = 0.f;
-    if (r < n && c < n) {
-      double2 v = H0[(int64_t)r * n + c];
-      if (dH_mode == ZG_DH_MATRIX) v = cadd(v, dH[(int64_t)r * n + c]);
-      if (dH_mode == ZG_DH_HUBBARD && r == c) v.x += U * ((double)sig32[(int64_t)r * n + r].x - 0.5);
-      hr = (float)v.x;
-      hi = (float)v.y;
-      const float2 sv = sig32[(int64_t)c * n + r];
-      sr = sv.x;
-      si = sv.y;
-    }
     float a, b;
-    if (r < n) {
-      split_tf32_r(hr, a, b);
-      Hth[(int64_t)r * ld + 2 * c] = a;
-      Htl[(int64_t)r * ld + 2 * c] = b;
-      split_tf32_r(hi, a, b);
-      Hth[(int64_t)r * ld + 2 * c + 1] = a;
-      Htl[(int64_t)r * ld + 2 * c + 1] = b;
-    }
     const int64_t o0 = (int64_t)(2 * r) * ld + 2 * c, o1 = o0 + ld;
-    float xr_h, xr_l, xi_h, xi_l, mi_h, mi_l;
-    split_tf32_r(hr, xr_h, xr_l);
-    split_tf32_r(hi, xi_h, xi_l);
-    split_tf32_r(-hi, mi_h, mi_l);
-    BHh[o0] = xr_h; BHl[o0] = xr_l; BHh[o0 + 1] = mi_h; BHl[o0 + 1] = mi_l;
-    BHh[o1] = xi_h; BHl[o1] = xi_l; BHh[o1 + 1] = xr_h; BHl[o1 + 1] = xr_l;
-    split_tf32_r(sr, xr_h, xr_l);
-    split_tf32_r(si, xi_h, xi_l);
-    split_tf32_r(-si, mi_h, mi_l);
-    BSh[o0] = xr_h; BSl[o0] = xr_l; BSh[o0 + 1] = mi_h; BSl[o0 + 1] = mi_l;
-    BSh[o1] = xi_h; BSl[o1] = xi_l; BSh[o1 + 1] = xr_h; BSl[o1 + 1] = xr_l;
+    if (h_part == 0 || diag_job) {
+      float hr = 0.f, hi = 0.f;
+      if (r < n && c < n) {
+        double2 v = H0[(int64_t)r * n + c];
+        if (dH_mode == ZG_DH_MATRIX) v = cadd(v, dH[(int64_t)r * n + c]);
+        if (dH_mode == ZG_DH_HUBBARD && r == c) v.x += U * ((double)sig32[(int64_t)r * n + r].x - 0.5);
+        hr = (float)v.x;
+        hi = (float)v.y;
+      }
+      if (r < n) {
+        split_tf32_r(hr, a, b);
+        Hth[(int64_t)r * ld + 2 * c] = a;
+        Htl[(int64_t)r * ld + 2 * c] = b;
+        split_tf32_r(hi, a, b);
+        Hth[(int64_t)r * ld + 2 * c + 1] = a;
+        Htl[(int64_t)r * ld + 2 * c + 1] = b;
+      }
+      float xr_h, xr_l, xi_h, xi_l, mi_h, mi_l;
+      split_tf32_r(hr, xr_h, xr_l);
+      split_tf32_r(hi, xi_h, xi_l);
+      split_tf32_r(-hi, mi_h, mi_l);
+      BHh[o0] = xr_h; BHl[o0] = xr_l; BHh[o0 + 1] = mi_h; BHl[o0 + 1] = mi_l;
+      BHh[o1] = xi_h; BHl[o1] = xi_l; BHh[o1 + 1] = xr_h; BHl[o1 + 1] = xr_l;
+    }
+    if (!diag_job) {
+      float sr = 0.f, si = 0.f;
+      if (r < n && c < n) {
+        const float2 sv = sig32[(int64_t)c * n + r];
+        sr = sv.x;
+        si = sv.y;
+      }
+      float xr_h, xr_l, xi_h, xi_l, mi_h, mi_l;
+      split_tf32_r(sr, xr_h, xr_l);
+      split_tf32_r(si, xi_h, xi_l);
+      split_tf32_r(-si, mi_h, mi_l);
+      BSh[o0] = xr_h; BSl[o0] = xr_l; BSh[o0 + 1] = mi_h; BSl[o0 + 1] = mi_l;
+      BSh[o1] = xi_h; BSl[o1] = xi_l; BSh[o1 + 1] = xr_h; BSl[o1 + 1] = xr_l;
+    }
   }
 }
 
 int launch_build_operands_mixed(int n, int np, const double2* H0, const float2* sig32, const double2* dH, int dH_mode,
-                                double U, float* Hth, float* Htl, float* BHh, float* BHl, float* BSh, float* BSl,
-                                cudaStream_t s) {
-  int64_t tot = (int64_t)np * np;
-  k_build_operands_mixed<<<grid_for(tot, 256, 152 * 16), 256, 0, s>>>(n, np, H0, sig32, dH, dH_mode, U, Hth, Htl, BHh,
-                                                                      BHl, BSh, BSl);
+                                double U, int h_part, float* Hth, float* Htl, float* BHh, float* BHl, float* BSh,
+                                float* BSl, cudaStream_t s) {
+  ZG_REQUIRE(h_part >= 0 && h_part <= 2, "bad operand part %d", h_part);
+  const int64_t tot = (int64_t)np * np + (h_part == 1 ? np : 0);
+  k_build_operands_mixed<<<grid_for(tot, 256, 152 * 16), 256, 0, s>>>(n, np, H0, sig32, dH, dH_mode, U, h_part, Hth,
+                                                                      Htl, BHh, BHl, BSh, BSl);
   ZG_CHECK_LAUNCH();
   count_launch();
   return ZG_OK;

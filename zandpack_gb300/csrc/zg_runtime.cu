@@ -158,6 +158,10 @@ struct zg_traj {
   double *J = nullptr, *Jpart = nullptr, *partial = nullptr, *err = nullptr;
   int nblk_err = 0;
   bool dH_set = false;
+  // mixed path: the H(t) tensor-core operands hold H0's off-diagonal entries
+  // (built once; only the diagonal then changes with the Hubbard term)
+  bool h_offdiag_ready = false;
+  int h_diag_mode = -1;  // dH mode of the diagonal currently in the operands
   double2* dis = nullptr;  // dissipator of the coming stages (zg_set_dissipator)
   bool dis_on = false;
   // ---- mixed path
@@ -902,8 +906,18 @@ static int rhs_mixed(zg_traj* t, int stage, const StageParams* p, int dH_mode, d
   const int64_t n = t->n, N = t->N, Ns = t->Ns, Nf = t->Nf, L = t->L, nc = t->nc, np = t->np;
   if (!plan_only) {
     prof_begin(t, ZG_PROF_PREP);
-    ZG_TRY(launch_build_operands_mixed((int)n, (int)np, t->H0, sig, t->dH, dH_mode, hubbard_U, t->Hth, t->Htl,
-                                       t->BHh, t->BHl, t->BSh, t->BSl, s));
+    // H(t) = H0 + dH changes only on the diagonal unless dH is a full matrix
+    int h_part = 0;
+    if (dH_mode == ZG_DH_MATRIX) {
+      t->h_offdiag_ready = false;
+    } else if (t->h_offdiag_ready) {
+      h_part = dH_mode == ZG_DH_HUBBARD || t->h_diag_mode != dH_mode ? 1 : 2;
+    } else {
+      t->h_offdiag_ready = true;
+    }
+    t->h_diag_mode = dH_mode;
+    ZG_TRY(launch_build_operands_mixed((int)n, (int)np, t->H0, sig, t->dH, dH_mode, hubbard_U, h_part, t->Hth,
+                                       t->Htl, t->BHh, t->BHl, t->BSh, t->BSl, s));
     ZG_TRY(launch_gathers<float>(d, sig, psih, psil, np, t->sigC32, t->G32, s));
     prof_end(t, ZG_PROF_PREP);
     // tensor cores: R1 = psi H(t)^T and T = H(t) sigma
@@ -1076,8 +1090,26 @@ static int enqueue_attempt_device(zg_traj* t) {
   return ZG_OK;
 }
 
+// The attempt graph rebuilds only the diagonal of the mixed path's H(t)
+// operands: make sure their off-diagonal part holds H0 before it runs (a
+// host-driven stage with a full dH matrix may have overwritten it).
+static int ensure_h_operands(zg_traj* t) {
+  if (t->precision != ZG_PREC_MIXED || t->h_offdiag_ready) return ZG_OK;
+  ZG_TRY(launch_build_operands_mixed(t->n, t->np, t->H0, t->stage32, t->dH, t->g_dH_mode, t->g_U, 0, t->Hth, t->Htl,
+                                     t->BHh, t->BHl, t->BSh, t->BSl, t->stream));
+  t->h_offdiag_ready = true;
+  t->h_diag_mode = t->g_dH_mode;
+  return ZG_OK;
+}
+
 static int capture_attempt_graph(zg_traj* t) {
   drop_graph(t);
+  ZG_TRY(ensure_h_operands(t));
+  if (t->precision == ZG_PREC_MIXED && t->h_diag_mode != t->g_dH_mode) {
+    // the captured stages then skip (NONE) or rebuild (HUBBARD) the diagonal
+    t->h_offdiag_ready = false;
+    ZG_TRY(ensure_h_operands(t));
+  }
   ZG_CHECK_CUDA(cudaStreamSynchronize(t->stream));
   const long long k0 = t_launches;
   ZG_CHECK_CUDA(cudaStreamBeginCapture(t->stream, cudaStreamCaptureModeThreadLocal));
@@ -1219,6 +1251,10 @@ int zg_graph_run(zg_traj* t, int count, zg_attempt_rec* recs, int* nrec, double*
   ZG_REQUIRE(!t->dis_on, "a dissipator is applied through zg_rhs only: call zg_set_dissipator(t, NULL) first");
   ZG_CHECK_CUDA(cudaSetDevice(t->dev));
   if (!t->gexec) ZG_TRY(capture_attempt_graph(t));  // dropped by zg_set_tableau or zg_profile
+  if (t->precision == ZG_PREC_MIXED && (!t->h_offdiag_ready || t->h_diag_mode != t->g_dH_mode)) {
+    t->h_offdiag_ready = false;
+    ZG_TRY(ensure_h_operands(t));
+  }
   cudaStream_t s = t->stream;
   ZG_CHECK_CUDA(cudaMemsetAsync(&t->ctl->rec_n, 0, sizeof(int), s));
   for (int i = 0; i < count; ++i) {
