@@ -266,7 +266,7 @@ int launch_terr2_partials_mixed(const float2* K, int64_t stride, const CombineCo
 }
 
 template <int NS>
-__global__ void __launch_bounds__(256) k_update_mixed(double2* __restrict__ y64, float2* __restrict__ y32,
+__global__ void __launch_bounds__(256, 4) k_update_mixed(double2* __restrict__ y64, float2* __restrict__ y32,
                                                       const float2* __restrict__ K, int64_t stride, CombineCoefs cf,
                                                       int64_t count, const int* gate) {
   if (gate && *gate == 0) return;

@@ -156,6 +156,9 @@ struct RhsDev {  // device pointers and sizes of one trajectory
   const int* mode_lead;
   const int* lead_cols;
   const int* colmap;
+  int nu;             // orbitals that are a coupling column of some lead
+  const int* ucols;   // [nu] those orbitals, ascending
+  const int* umap;    // [n] position in ucols, or -1
   const C *Xp, *Xm, *GLP, *dGP, *XI, *U, *V;
 };
 
@@ -172,8 +175,10 @@ template <typename T>
 int launch_gathers(const RhsDev<T>& d, const typename cx<T>::t* sig, const typename cx<T>::t* psi,
                    const typename cx<T>::t* psi_lo, int64_t ldpsi, typename cx<T>::t* sigC, typename cx<T>::t* G,
                    cudaStream_t s);
-template <typename T>
+// k_sig without the lead terms, then the lead terms (P + P^H)/hbar added to
+// the rows and columns of the coupling orbitals only (where P is nonzero).
 // dis (may be null): the n x n FP64 dissipator of this stage, entering as - hbar * dis
+template <typename T>
 int launch_sigma_finalize(const RhsDev<T>& d, const StageParams* p, const typename cx<T>::t* Tm, int64_t ldT,
                           const typename cx<T>::t* Pc, const double2* dis, typename cx<T>::t* ksig, cudaStream_t s);
 template <typename T>

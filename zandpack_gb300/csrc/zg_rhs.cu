@@ -179,8 +179,15 @@ __global__ void k_zgemm_reduce(const __grid_constant__ GemmBatch<T> batch, int64
     }
     const GemmProb<T>& P = batch.p[pi];
     const int64_t mn = (int64_t)P.M * P.N;
+    const C* src = batch.ws + P.ws_off + e;
     C v = czero<T>();
-    for (int sp = 0; sp < P.ksplit; ++sp) v = cadd(v, batch.ws[P.ws_off + sp * mn + e]);
+    // four partials loaded together, added in split order
+    int sp = 0;
+    for (; sp + 4 <= P.ksplit; sp += 4) {
+      const C v0 = src[sp * mn], v1 = src[(sp + 1) * mn], v2 = src[(sp + 2) * mn], v3 = src[(sp + 3) * mn];
+      v = cadd(cadd(cadd(cadd(v, v0), v1), v2), v3);
+    }
+    for (; sp < P.ksplit; ++sp) v = cadd(v, src[sp * mn]);
     P.Cm[(e / P.N) * P.ldc + (e % P.N)] = cmul(P.alpha, v);
   }
 }
@@ -307,18 +314,17 @@ __device__ __forceinline__ typename cx<T>::t p_full(const RhsDev<T>& d, const ty
 }
 
 // k_sig = (h/hbar) (-i (T - T^H) + (P + P^H)/hbar), T = H(t) sigma  (Zandpack/mpi/zand:340-387)
-// One 32 x 32 block of k_sig per CTA; the transposed block of T it needs is
-// staged through shared memory so that both reads of T are row-contiguous.
+// Pass 1: the commutator (and the dissipator) for every element, one 32 x 32
+// block per CTA with the transposed block of T staged through shared memory
+// so that both reads of T are row-contiguous.
 template <typename T>
 __global__ void __launch_bounds__(256) k_sigma_finalize(const RhsDev<T> d, const StageParams* __restrict__ pp,
                                                         const typename cx<T>::t* __restrict__ Tm, int64_t ldT,
-                                                        const typename cx<T>::t* __restrict__ Pc,
                                                         const double2* __restrict__ dis,
                                                         typename cx<T>::t* __restrict__ ksig) {
   using C = typename cx<T>::t;
   __shared__ C tile[32][33];  // tile[r][c] = T[j0 + r][i0 + c]
   const StageScalars p = load_params(pp);
-  const T ih = (T)(1.0 / p.hbar);
   const T sc = (T)(p.h / p.hbar);
   const int n = d.n;
   const int i0 = blockIdx.y * 32, j0 = blockIdx.x * 32;
@@ -333,7 +339,6 @@ __global__ void __launch_bounds__(256) k_sigma_finalize(const RhsDev<T> d, const
     if (i >= n || j >= n) continue;
     const C tij = Tm[(int64_t)i * ldT + j];
     const C tji = tile[tx][r];
-    const C pij = p_full(d, Pc, i, j), pji = p_full(d, Pc, j, i);
     // -i (tij - conj(tji)) = (tij.y + tji.y, -(tij.x - tji.x))
     C v = cx<T>::make(tij.y + tji.y, -(tij.x - tji.x));
     const int64_t e = (int64_t)i * n + j;
@@ -342,9 +347,40 @@ __global__ void __launch_bounds__(256) k_sigma_finalize(const RhsDev<T> d, const
       v.x -= (T)(p.hbar * q.x);
       v.y -= (T)(p.hbar * q.y);
     }
-    v.x += (pij.x + pji.x) * ih;
-    v.y += (pij.y - pji.y) * ih;
     ksig[e] = cscale(v, sc);
+  }
+}
+
+// Pass 2: + (h/hbar^2)(P + P^H) on the elements (i, j) with i or j a coupling
+// orbital, each element once: columns j in U for every row i, then rows i in U
+// for the columns j not in U.
+template <typename T>
+__global__ void __launch_bounds__(256) k_sigma_leads(const RhsDev<T> d, const StageParams* __restrict__ pp,
+                                                     const typename cx<T>::t* __restrict__ Pc,
+                                                     typename cx<T>::t* __restrict__ ksig) {
+  using C = typename cx<T>::t;
+  const StageScalars p = load_params(pp);
+  const T f = (T)(p.h / (p.hbar * p.hbar));
+  const int n = d.n, nu = d.nu;
+  const int64_t half = (int64_t)nu * n;
+  GRID_STRIDE(q, 2 * half) {
+    int i, j;
+    if (q < half) {
+      i = (int)(q / nu);
+      j = d.ucols[q - (int64_t)i * nu];
+    } else {
+      const int64_t q2 = q - half;
+      const int u = (int)(q2 / n);
+      j = (int)(q2 - (int64_t)u * n);
+      if (d.umap[j] >= 0) continue;  // done in the column pass
+      i = d.ucols[u];
+    }
+    const C pij = p_full(d, Pc, i, j), pji = p_full(d, Pc, j, i);
+    const int64_t e = (int64_t)i * n + j;
+    C v = ksig[e];
+    v.x += f * (pij.x + pji.x);
+    v.y += f * (pij.y - pji.y);
+    ksig[e] = v;
   }
 }
 
@@ -352,9 +388,15 @@ template <typename T>
 int launch_sigma_finalize(const RhsDev<T>& d, const StageParams* p, const typename cx<T>::t* Tm, int64_t ldT,
                           const typename cx<T>::t* Pc, const double2* dis, typename cx<T>::t* ksig, cudaStream_t s) {
   const int nb = (d.n + 31) / 32;
-  k_sigma_finalize<T><<<dim3(nb, nb), dim3(32, 8), 0, s>>>(d, p, Tm, ldT, Pc, dis, ksig);
+  k_sigma_finalize<T><<<dim3(nb, nb), dim3(32, 8), 0, s>>>(d, p, Tm, ldT, dis, ksig);
   ZG_CHECK_LAUNCH();
   count_launch();
+  if (d.nu > 0) {
+    const int64_t tot = 2 * (int64_t)d.nu * d.n;
+    k_sigma_leads<T><<<grid_for(tot, 256, 152 * 8), 256, 0, s>>>(d, p, Pc, ksig);
+    ZG_CHECK_LAUNCH();
+    count_launch();
+  }
   return ZG_OK;
 }
 

@@ -144,6 +144,8 @@ struct zg_traj {
   double2 *H0 = nullptr, *Xp = nullptr, *Xm = nullptr, *GLP = nullptr, *dGP = nullptr, *XI = nullptr,
           *IXI = nullptr, *XIS = nullptr, *U = nullptr, *V = nullptr;
   int *mode_lead = nullptr, *lead_cols = nullptr, *colmap = nullptr;
+  int *ucols = nullptr, *umap = nullptr;  // coupling orbitals of any lead
+  int nu = 0;
   OmTile* tiles = nullptr;
   int ntiles = 0;
   // FP64 path: (stages+1) slots of S complex128, slot `stages` is y.
@@ -222,6 +224,7 @@ RhsDev<double> zg_traj::dev_view<double>() const {
   RhsDev<double> d;
   d.n = n; d.L = L; d.N = N; d.Ns = Ns; d.Nf = Nf; d.nc = nc;
   d.mode_lead = mode_lead; d.lead_cols = lead_cols; d.colmap = colmap;
+  d.nu = nu; d.ucols = ucols; d.umap = umap;
   d.Xp = Xp; d.Xm = Xm; d.GLP = GLP; d.dGP = dGP; d.XI = XI; d.U = U; d.V = V;
   return d;
 }
@@ -230,6 +233,7 @@ RhsDev<float> zg_traj::dev_view<float>() const {
   RhsDev<float> d;
   d.n = n; d.L = L; d.N = N; d.Ns = Ns; d.Nf = Nf; d.nc = nc;
   d.mode_lead = mode_lead; d.lead_cols = lead_cols; d.colmap = colmap;
+  d.nu = nu; d.ucols = ucols; d.umap = umap;
   d.Xp = Xp32; d.Xm = Xm32; d.GLP = GLP32; d.dGP = dGP32; d.XI = XI32; d.U = U32; d.V = V32;
   return d;
 }
@@ -339,7 +343,7 @@ static void free_traj(zg_traj* t) {
                   t->dGP32,
                   t->XI32, t->XIS32, t->IXI32, t->U32, t->V32, t->y32, t->K32, t->stage32, t->Hth, t->Htl, t->BHh,
                   t->BHl, t->BSh, t->BSl, t->T32, t->R1p, t->Pc32, t->sigC32, t->G32, t->R2_32, t->ZA32, t->ZB32,
-                  t->conv64, t->sig64, t->tc_err, t->ws64, t->ws32, t->dis};
+                  t->conv64, t->sig64, t->tc_err, t->ws64, t->ws32, t->dis, t->ucols, t->umap};
   for (void* p : ptrs) dfree(t, p);
   if (t->stream) {
     cudaStreamSynchronize(t->stream);
@@ -554,6 +558,22 @@ int zg_traj_create(int device, const zg_layout* Lo, int precision, zg_traj** out
   ZG_STEP(upload<int>(t->mode_lead, Lo->mode_lead, N, t->stream));
   ZG_STEP(upload<int>(t->lead_cols, Lo->lead_cols, L * nc, t->stream));
   ZG_STEP(upload<int>(t->colmap, Lo->colmap, L * n, t->stream));
+  // orbitals that are a coupling column of some lead: the only rows and
+  // columns where the lead terms of the sigma equation are nonzero
+  std::vector<int> ucols_h, umap_h(n, -1);
+  for (int64_t j = 0; j < n; ++j) {
+    bool in = false;
+    for (int64_t a = 0; a < L; ++a) in = in || Lo->colmap[a * n + j] >= 0;
+    if (in) {
+      umap_h[j] = (int)ucols_h.size();
+      ucols_h.push_back((int)j);
+    }
+  }
+  t->nu = (int)ucols_h.size();
+  ZG_STEP(dalloc(t, &t->ucols, std::max<size_t>(ucols_h.size(), 1)));
+  ZG_STEP(dalloc(t, &t->umap, n));
+  if (t->nu > 0) ZG_STEP(upload<int>(t->ucols, ucols_h.data(), ucols_h.size(), t->stream));
+  ZG_STEP(upload<int>(t->umap, umap_h.data(), n, t->stream));
   // U = dGM * IXI (per column mode), V = dGP * XIT2 (per row mode)
   std::vector<double2> U(N * nc), V(N * nc);
   {
