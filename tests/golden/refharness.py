@@ -274,3 +274,41 @@ def worker_roles(nranks, arrays):
         info = sp.partition_scheme3(r, nranks, NK, NL, NX, noT_lead)
         roles[r] = (int(info[2][0]), np.asarray(info[3]), np.asarray(info[4]))
     return roles, noT_lead
+
+
+def run_psinought(workdir: str, file_dir: str, options=()):
+    """Execute the reference ``cmdtools/psinought`` (the steady-state solver)
+    in ``workdir`` (holding Initial.py/Bias.py) on ``file_dir/Arrays``; return
+    (PSI, OMG, stdout) as saved in ``file_dir + '_save'``.  Extra stubs for
+    modules the solver imports but that need absent packages:
+    ``Zandpack.TimedependentTransport`` (only ``Q_nb``, used by the derivative
+    printout, which these runs switch off), ``Zandpack.Louivillian`` (only with
+    ``L_info``) and ``Zandpack.docstrings`` (banner strings)."""
+    _install_stubs()
+    for name, attrs in (("Zandpack.TimedependentTransport", {"Q_nb": None}),
+                        ("Zandpack.Louivillian", {"Louivillian": None}),
+                        ("Zandpack.docstrings", {"psi0_docstring": "", "CoolLine": ""})):
+        if name not in sys.modules:
+            m = types.ModuleType(name)
+            for k, v in attrs.items():
+                setattr(m, k, v)
+            sys.modules[name] = m
+    path = os.path.join(ZDIR, "cmdtools", "psinought")
+    code = compile(open(path).read(), path, "exec")
+    old = os.getcwd()
+    saved_argv = sys.argv
+    sys.path.insert(0, workdir)
+    for m in ("Initial", "Bias"):
+        sys.modules.pop(m, None)
+    sys.argv = ["psinought", "Dir=" + workdir, "file=" + file_dir, "checkderivative=False",
+                "printfile=None"] + list(options)
+    out = io.StringIO()
+    try:
+        with contextlib.redirect_stdout(out):
+            exec(code, {"__name__": "__psinought__", "__file__": path})
+    finally:
+        os.chdir(old)
+        sys.path.remove(workdir)
+        sys.argv = saved_argv
+    save = os.path.join(workdir, file_dir + "_save")
+    return np.load(os.path.join(save, "last_psi.npy")), np.load(os.path.join(save, "last_omg.npy")), out.getvalue()
