@@ -152,6 +152,23 @@ int zg_attempt(zg_traj* t, double* time, double* h, double eps, const zg_bias* b
  * after every accepted step (Zandpack/mpi/zand:428-430). */
 int zg_get_sigma(zg_traj* t, int slot, double* host);
 
+/* Steady state (Zandpack/cmdtools/psinought:180-451), on an FP64 trajectory
+ * whose y holds the fixed density matrix (zg_set_sigma).  The stationary psi
+ * solves k_psi(sigma, psi, Omega(psi)) = 0 where Omega(psi) solves
+ * dOmega/dt = 0; a Krylov solver on the caller's side drives:
+ *   zg_stationary_setup: stage time, lead biases, dH mode, and the eigenpairs
+ *     (V: n*n complex, columns; lam: n) of H = H0 + dH used by the
+ *     preconditioner;
+ *   zg_stationary_apply: kpsi = k_psi(psi) with h = 1 (affine in psi); psi and
+ *     kpsi are N*n complex device arrays (compact layout); afterwards y holds
+ *     (sigma, psi, Omega(psi));
+ *   zg_stationary_precond: out = i hbar r_m (H^T - X+_m - Delta)^{-1} per mode
+ *     row m, the inverse of k_psi's dominant term. */
+int zg_stationary_setup(zg_traj* t, double ts, const double* delta, int dH_mode, double hubbard_U, const double* V,
+                        const double* lam);
+int zg_stationary_apply(zg_traj* t, const double* psi_dev, double* kpsi_dev);
+int zg_stationary_precond(zg_traj* t, const double* r_dev, double* out_dev);
+
 /* Graph-launched attempts.  The same attempt as zg_attempt, with the
  * controller (t, h, TE, accept, next step size) kept on the device and the
  * whole attempt captured once as a CUDA graph, so that a run of attempts needs

@@ -60,6 +60,9 @@ class zg_attempt_rec(C.Structure):
 
 _P = C.c_void_p
 _SIGS = {
+    "zg_stationary_setup": ([_P, C.c_double, _P, C.c_int, C.c_double, _P, _P], C.c_int),
+    "zg_stationary_apply": ([_P, _P, _P], C.c_int),
+    "zg_stationary_precond": ([_P, _P, _P], C.c_int),
     "zg_graph_prepare": ([_P, C.POINTER(zg_bias), C.c_int, C.c_double], C.c_int),
     "zg_graph_set": ([_P, C.c_double, C.c_double, C.c_double, C.c_double], C.c_int),
     "zg_graph_run": ([_P, C.c_int, _P, C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_double),

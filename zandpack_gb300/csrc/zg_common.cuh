@@ -44,6 +44,11 @@ __host__ __device__ __forceinline__ double2 cadd(double2 a, double2 b) { return 
 __host__ __device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
 __host__ __device__ __forceinline__ double2 cconj(double2 a) { return make_double2(a.x, -a.y); }
 __host__ __device__ __forceinline__ double2 cscale(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
+// a / b
+__host__ __device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
+  const double d = b.x * b.x + b.y * b.y;
+  return make_double2((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
+}
 // acc += a*b
 __host__ __device__ __forceinline__ void cfma(double2& acc, double2 a, double2 b) {
   acc.x = fma(a.x, b.x, acc.x);
@@ -58,6 +63,10 @@ __host__ __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return mak
 __host__ __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
 __host__ __device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
 __host__ __device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+__host__ __device__ __forceinline__ float2 cdiv(float2 a, float2 b) {
+  const float d = b.x * b.x + b.y * b.y;
+  return make_float2((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
+}
 __host__ __device__ __forceinline__ void cfma(float2& acc, float2 a, float2 b) {
   acc.x = fmaf(a.x, b.x, acc.x);
   acc.x = fmaf(-a.y, b.y, acc.x);

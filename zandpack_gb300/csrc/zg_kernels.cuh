@@ -188,10 +188,15 @@ int launch_psi_finalize(const RhsDev<T>& d, const StageParams* p, const typename
                         const typename cx<T>::t* psi_lo, int64_t ldpsi, const typename cx<T>::t* R1, int64_t ldR1,
                         const typename cx<T>::t* R2, const typename cx<T>::t* ZA, const typename cx<T>::t* ZB,
                         typename cx<T>::t* kpsi, cudaStream_t s);
+// stationary != 0: writes the Omega of dOmega/dt = 0, i hbar S / (X+ + D_a - X- - D_b),
+// instead of the stage derivative (the input Omega is not read)
 template <typename T>
 int launch_omega(const RhsDev<T>& d, const StageParams* p, const OmTile* tiles, int ntiles, const typename cx<T>::t* G,
                  const typename cx<T>::t* omA_in, const typename cx<T>::t* omB_in, typename cx<T>::t* omA_out,
-                 typename cx<T>::t* omB_out, cudaStream_t s);
+                 typename cx<T>::t* omB_out, cudaStream_t s, int stationary = 0);
+// steady-state preconditioner middle: W[m][k] *= i hbar / (lam_k - X+_m - Delta_lead(m))
+int launch_stationary_scale(int N, int n, const double2* Xp, const int* mode_lead, const double* delta,
+                            const double* lam, double hbar, double2* W, cudaStream_t s);
 
 // H(t) = H0 + dH (FP64 path)
 int launch_build_ht(int n, const double2* H0, const double2* sig, const double2* dH, int dH_mode, double U,

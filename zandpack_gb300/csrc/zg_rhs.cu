@@ -571,7 +571,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) k_omega(const Rhs
                                                const typename cx<T>::t* __restrict__ omA_in,
                                                const typename cx<T>::t* __restrict__ omB_in,
                                                typename cx<T>::t* __restrict__ omA_out,
-                                               typename cx<T>::t* __restrict__ omB_out) {
+                                               typename cx<T>::t* __restrict__ omB_out, int stationary) {
   const StageScalars p = load_params(pp);
   using C = typename cx<T>::t;
   const OmTile t = tiles[blockIdx.x];
@@ -596,7 +596,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) k_omega(const Rhs
   // the epilogue
   extern __shared__ __align__(16) unsigned char om_smem[];
   C* Os = reinterpret_cast<C*>(om_smem);  // [64][64], FP32 only
-  if constexpr (sizeof(T) == 4) {
+  if (sizeof(T) == 4 && !stationary) {
     for (int q = tid; q < 64 * 64; q += 256) {
       const int r = q >> 6, c = q & 63;
       if (r < t.nrows && c < t.ncols) {
@@ -655,7 +655,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) k_omega(const Rhs
     }
     __syncthreads();
   }
-  if constexpr (sizeof(T) == 4) {
+  if (sizeof(T) == 4 && !stationary) {
     asm volatile("cp.async.wait_group 0;" ::: "memory");
     __syncthreads();
   }
@@ -678,6 +678,12 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) k_omega(const Rhs
       C xm = d.Xm[l];
       xm.x += db;
       const int64_t e = m * ld + (t.col0 + c);
+      if (stationary) {
+        // dOmega/dt = 0: Omega = i hbar S / (X+ + D_a - X- - D_b)  (Zandpack/cmdtools/psinought:443-451)
+        const C q = cdiv(acc[i][j], csub(xp, xm));
+        out[e] = cx<T>::make((T)(-p.hbar) * q.y, (T)p.hbar * q.x);
+        continue;
+      }
       const C om = sizeof(T) == 4 ? Os[r * 64 + c] : in[e];
       const C dd = cmul(csub(xp, xm), om);  // (X+ - X-) Omega
       // (i h/hbar) dd = sc * (-dd.y, dd.x)
@@ -693,7 +699,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) k_omega(const Rhs
 template <typename T>
 int launch_omega(const RhsDev<T>& d, const StageParams* p, const OmTile* tiles, int ntiles, const typename cx<T>::t* G,
                  const typename cx<T>::t* omA_in, const typename cx<T>::t* omB_in, typename cx<T>::t* omA_out,
-                 typename cx<T>::t* omB_out, cudaStream_t s) {
+                 typename cx<T>::t* omB_out, cudaStream_t s, int stationary) {
   if (ntiles == 0) return ZG_OK;
   const int smem = sizeof(T) == 4 ? 64 * 64 * (int)sizeof(typename cx<T>::t) : 0;
   if (smem > 0) {
@@ -705,7 +711,7 @@ int launch_omega(const RhsDev<T>& d, const StageParams* p, const OmTile* tiles, 
       configured[dev] = true;
     }
   }
-  k_omega<T><<<ntiles, 256, smem, s>>>(d, p, tiles, G, omA_in, omB_in, omA_out, omB_out);
+  k_omega<T><<<ntiles, 256, smem, s>>>(d, p, tiles, G, omA_in, omB_in, omA_out, omB_out, stationary);
   ZG_CHECK_LAUNCH();
   count_launch();
   return ZG_OK;
@@ -817,6 +823,32 @@ int launch_build_operands_mixed(int n, int np, const double2* H0, const float2* 
   return ZG_OK;
 }
 
+// W[m][k] *= i hbar / (lam_k - x_m), x_m = X+_m + Delta_{lead(m)}: the middle of
+// the steady-state preconditioner  r -> i hbar r (H^T - x_m)^{-1}
+__global__ void k_stationary_scale(int N, int n, const double2* __restrict__ Xp, const int* __restrict__ mode_lead,
+                                   const double* __restrict__ delta, const double* __restrict__ lam, double hbar,
+                                   double2* __restrict__ W) {
+  const int64_t tot = (int64_t)N * n;
+  GRID_STRIDE(e, tot) {
+    const int m = (int)(e / n), k = (int)(e % n);
+    double2 x = Xp[m];
+    x.x += delta[mode_lead[m]];
+    const double2 den = make_double2(lam[k] - x.x, -x.y);
+    const double2 q = cdiv(W[e], den);
+    W[e] = make_double2(-hbar * q.y, hbar * q.x);
+  }
+}
+
+int launch_stationary_scale(int N, int n, const double2* Xp, const int* mode_lead, const double* delta,
+                            const double* lam, double hbar, double2* W, cudaStream_t s) {
+  const int64_t tot = (int64_t)N * n;
+  if (tot == 0) return ZG_OK;
+  k_stationary_scale<<<grid_for(tot, 256, 152 * 8), 256, 0, s>>>(N, n, Xp, mode_lead, delta, lam, hbar, W);
+  ZG_CHECK_LAUNCH();
+  count_launch();
+  return ZG_OK;
+}
+
 // ----------------------------------------------------------- instantiate
 #define ZG_INST(T)                                                                                                   \
   template int64_t plan_zgemm_batch<T>(GemmBatch<T>&);                                                               \
@@ -830,7 +862,7 @@ int launch_build_operands_mixed(int n, int np, const double2* H0, const float2* 
                                       int64_t, const cx<T>::t*, int64_t, const cx<T>::t*, const cx<T>::t*,           \
                                       const cx<T>::t*, cx<T>::t*, cudaStream_t);                                     \
   template int launch_omega<T>(const RhsDev<T>&, const StageParams*, const OmTile*, int, const cx<T>::t*,            \
-                               const cx<T>::t*, const cx<T>::t*, cx<T>::t*, cx<T>::t*, cudaStream_t);
+                               const cx<T>::t*, const cx<T>::t*, cx<T>::t*, cx<T>::t*, cudaStream_t, int);
 ZG_INST(double)
 ZG_INST(float)
 

@@ -166,6 +166,14 @@ struct zg_traj {
   int h_diag_mode = -1;  // dH mode of the diagonal currently in the operands
   double2* dis = nullptr;  // dissipator of the coming stages (zg_set_dissipator)
   bool dis_on = false;
+  // steady state (zg_stationary_*): eigenpairs of H, stage parameters, scratch
+  double2 *st_V = nullptr, *st_Vc = nullptr, *st_W = nullptr;
+  double* st_lam = nullptr;
+  double* st_delta = nullptr;  // device copy of the lead biases
+  StageParams st_p;
+  int st_mode = ZG_DH_NONE;
+  double st_U = 0.0;
+  bool st_ready = false;
   // ---- mixed path
   int np = 0;  // n padded to a multiple of 16
   MixedLayout ml;
@@ -343,7 +351,8 @@ static void free_traj(zg_traj* t) {
                   t->dGP32,
                   t->XI32, t->XIS32, t->IXI32, t->U32, t->V32, t->y32, t->K32, t->stage32, t->Hth, t->Htl, t->BHh,
                   t->BHl, t->BSh, t->BSl, t->T32, t->R1p, t->Pc32, t->sigC32, t->G32, t->R2_32, t->ZA32, t->ZB32,
-                  t->conv64, t->sig64, t->tc_err, t->ws64, t->ws32, t->dis, t->ucols, t->umap};
+                  t->conv64, t->sig64, t->tc_err, t->ws64, t->ws32, t->dis, t->ucols, t->umap,
+                  t->st_V, t->st_Vc, t->st_W, t->st_lam, t->st_delta};
   for (void* p : ptrs) dfree(t, p);
   if (t->stream) {
     cudaStreamSynchronize(t->stream);
@@ -1302,6 +1311,82 @@ int zg_graph_run(zg_traj* t, int count, zg_attempt_rec* recs, int* nrec, double*
     set_error("error norm is not finite (%g)", c.TE);
     return c.status;
   }
+  return ZG_OK;
+}
+
+// ------------------------------------------------------------ steady state
+int zg_stationary_setup(zg_traj* t, double ts, const double* delta, int dH_mode, double hubbard_U, const double* V,
+                        const double* lam) {
+  ZG_REQUIRE(t && delta && V && lam, "null argument");
+  ZG_REQUIRE(t->precision == ZG_PREC_F64, "the steady state is solved on an FP64 trajectory");
+  ZG_REQUIRE(dH_mode == ZG_DH_NONE || dH_mode == ZG_DH_HUBBARD || (dH_mode == ZG_DH_MATRIX && t->dH_set),
+             "bad dH mode %d (ZG_DH_MATRIX needs zg_set_dH first)", dH_mode);
+  ZG_CHECK_CUDA(cudaSetDevice(t->dev));
+  const size_t nn = (size_t)t->n * t->n;
+  if (!t->st_V) {
+    ZG_TRY(dalloc(t, &t->st_V, nn));
+    ZG_TRY(dalloc(t, &t->st_Vc, nn));
+    ZG_TRY(dalloc(t, &t->st_W, (size_t)t->N * t->n));
+    ZG_TRY(dalloc(t, &t->st_lam, (size_t)t->n));
+    ZG_TRY(dalloc(t, &t->st_delta, ZG_MAX_LEADS));
+  }
+  std::vector<double2> Vc(nn);
+  const double2* Vh = (const double2*)V;
+  for (size_t e = 0; e < nn; ++e) Vc[e] = cconj(Vh[e]);
+  t->st_p.h = 1.0;
+  t->st_p.ts = ts;
+  t->st_p.hbar = t->hbar;
+  for (int a = 0; a < ZG_MAX_LEADS; ++a) t->st_p.delta[a] = a < t->L ? delta[a] : 0.0;
+  ZG_CHECK_CUDA(cudaMemcpyAsync(t->st_V, V, nn * sizeof(double2), cudaMemcpyHostToDevice, t->stream));
+  ZG_CHECK_CUDA(cudaMemcpyAsync(t->st_Vc, Vc.data(), nn * sizeof(double2), cudaMemcpyHostToDevice, t->stream));
+  ZG_CHECK_CUDA(cudaMemcpyAsync(t->st_lam, lam, (size_t)t->n * sizeof(double), cudaMemcpyHostToDevice, t->stream));
+  ZG_CHECK_CUDA(cudaMemcpyAsync(t->st_delta, t->st_p.delta, ZG_MAX_LEADS * sizeof(double), cudaMemcpyHostToDevice,
+                                t->stream));
+  ZG_CHECK_CUDA(cudaStreamSynchronize(t->stream));
+  t->st_mode = dH_mode;
+  t->st_U = hubbard_U;
+  t->st_ready = true;
+  return ZG_OK;
+}
+
+int zg_stationary_apply(zg_traj* t, const double* psi_dev, double* kpsi_dev) {
+  ZG_REQUIRE(t && psi_dev && kpsi_dev, "null argument");
+  ZG_REQUIRE(t->st_ready, "zg_stationary_setup must precede zg_stationary_apply");
+  ZG_CHECK_CUDA(cudaSetDevice(t->dev));
+  cudaStream_t s = t->stream;
+  double2* y = t->slot(t->stages);
+  const int64_t n = t->n, N = t->N;
+  // y = (sigma, psi, Omega(psi)); Omega from dOmega/dt = 0 given psi
+  ZG_CHECK_CUDA(cudaMemcpyAsync(y + t->off_psi, psi_dev, (size_t)N * n * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+  ZG_TRY(launch_set_params(t->st_p, t->d_params, s));
+  const RhsDev<double> d = t->dev_view<double>();
+  ZG_TRY(launch_gathers<double>(d, y, y + t->off_psi, nullptr, n, t->sigC, t->G, s));
+  ZG_TRY(launch_omega<double>(d, t->d_params, t->tiles, t->ntiles, t->G, y + t->off_omA, y + t->off_omB,
+                              y + t->off_omA, y + t->off_omB, s, 1));
+  // k_psi of that state with h = 1: zero at the steady state
+  ZG_TRY(zg_stage_input(t, 0));
+  ZG_TRY(launch_set_params(t->st_p, t->d_params, s));
+  ZG_TRY(rhs_f64(t, 0, t->d_params, t->st_mode, t->st_U, false));
+  ZG_CHECK_CUDA(cudaMemcpyAsync(kpsi_dev, t->slot(0) + t->off_psi, (size_t)N * n * sizeof(double2),
+                                cudaMemcpyDeviceToDevice, s));
+  ZG_CHECK_CUDA(cudaStreamSynchronize(s));
+  return ZG_OK;
+}
+
+int zg_stationary_precond(zg_traj* t, const double* r_dev, double* out_dev) {
+  ZG_REQUIRE(t && r_dev && out_dev, "null argument");
+  ZG_REQUIRE(t->st_ready, "zg_stationary_setup must precede zg_stationary_precond");
+  ZG_CHECK_CUDA(cudaSetDevice(t->dev));
+  cudaStream_t s = t->stream;
+  const int64_t n = t->n, N = t->N;
+  // out_m = i hbar r_m (H^T - x_m)^{-1} = i hbar [(r_m conj V) / (lam - x_m)] V^T
+  std::vector<GemmProb<double>> p1, p2;
+  gemm_prob_f64(p1, (const double2*)r_dev, n, 0, t->st_Vc, n, 0, t->st_W, n, (int)N, (int)n, (int)n);
+  ZG_TRY(run_batches<double>(t, p1, &t->ws64, &t->ws64_cap, s, false));
+  ZG_TRY(launch_stationary_scale((int)N, (int)n, t->Xp, t->mode_lead, t->st_delta, t->st_lam, t->hbar, t->st_W, s));
+  gemm_prob_f64(p2, t->st_W, n, 0, t->st_V, n, 1, (double2*)out_dev, n, (int)N, (int)n, (int)n);
+  ZG_TRY(run_batches<double>(t, p2, &t->ws64, &t->ws64_cap, s, false));
+  ZG_CHECK_CUDA(cudaStreamSynchronize(s));
   return ZG_OK;
 }
 
