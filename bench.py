@@ -239,6 +239,8 @@ def run_ours(args):
     if rank == 0:
         if args.ensemble > 0:
             out["ensemble"] = run_ensemble(args)
+        if args.steady:
+            out["steady_state"] = run_steady(args)
         out["cpu_baseline"] = cpu_baseline(args, w, adv_total / (args.steps * ws))
         print(json.dumps(out))
     if ws > 1:
@@ -427,6 +429,22 @@ def run_ensemble(args):
     return stats
 
 
+def run_steady(args):
+    """The steady state (psinought) of a workload at its initial density matrix:
+    GMRES on the device to a relative residual of 1e-8, as the reference's
+    default steptol; wall time of the solve (operator and preconditioner in
+    libzandgpu, FP64)."""
+    from zandpack_gb300.layout import CompactLayout
+    from zandpack_gb300.psinought import steady_state
+    from zandpack_gb300.workloads import make_workload
+    w = make_workload(args.steady)
+    L = CompactLayout(w.arrays, w.hbar)
+    res = steady_state(w.arrays, w.hbar, w.bias_fn(), w.dH_fn(), t0=w.t0, tol=1e-8, layout=L)
+    return {"workload": args.steady, "n": L.n, "modes": L.N, "unknowns_complex": L.N * L.n,
+            "iterations": res.iterations, "relative_residual": res.residual, "converged": res.converged,
+            "seconds": res.seconds}
+
+
 def run_reference(args):
     ws, rank = _dist()
     if rank != 0:
@@ -461,6 +479,7 @@ def main():
     ap.add_argument("--slots", type=int, default=32, help="concurrent trajectories of the ensemble")
     ap.add_argument("--prep-workers", type=int, default=max(1, min(12, (os.cpu_count() or 4) - 4)),
                     help="worker processes preparing ensemble requests on the host")
+    ap.add_argument("--steady", default="c2", help="workload of the steady-state (psinought) timing ('' to skip)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
