@@ -50,3 +50,39 @@ def test_steady_state_matches_reference(case):
     scale = np.abs(kp0).max()
     assert np.abs(kp).max() <= 1e-9 * scale
     assert np.abs(ko).max() <= 1e-9 * scale
+
+
+def test_psinought_command_line(tmp_path):
+    """``python -m zandpack_gb300.psinought Dir=... file=...``: reads a run
+    directory like the reference and writes ``<file>_save/last_psi.npy``,
+    ``last_omg.npy`` (padded layout) and the MESSAGE files."""
+    import json
+    import sys
+    from zandpack_gb300 import psinought
+    from zandpack_gb300.arrays_io import write_arrays
+    from zandpack_gb300.workloads import make_workload
+    z = load_golden("mini2")
+    ref = np.load(os.path.join(os.path.dirname(__file__), "golden", "psi0_mini2.npz"))
+    p = z["params"]
+    keys = ("H_Ortho", "DM_Ortho", "psi_shape", "Xpp", "Xpm", "GG_P", "GL_P", "GG_M", "GL_M", "diff_GGP_GLP",
+            "diff_GGM_GLM", "xi", "Ixi", "zero_tol")
+    write_arrays(str(tmp_path / "SaveFile" / "Arrays"), {k: z[k] for k in keys})
+    (tmp_path / "Initial.py").write_text("hbar=%r\nt0=%r\n" % (p["hbar"], p["t0"]))
+    (tmp_path / "Bias.py").write_text(make_workload("mini2").bias_source())
+    cwd = os.getcwd()
+    try:
+        for m in ("Initial", "Bias"):
+            sys.modules.pop(m, None)
+        res = psinought.main(["Dir=" + str(tmp_path), "file=SaveFile", "steptol=1e-12"])
+    finally:
+        os.chdir(cwd)
+        sys.path[:] = [q for q in sys.path if os.path.realpath(q) != os.path.realpath(str(tmp_path))]
+        for m in ("Initial", "Bias"):
+            sys.modules.pop(m, None)
+    assert res.converged
+    P = np.load(tmp_path / "SaveFile_save" / "last_psi.npy")
+    O = np.load(tmp_path / "SaveFile_save" / "last_omg.npy")
+    nt = P.shape[3]
+    assert np.abs(P - ref["PSI"][..., :nt, :]).max() <= 1e-8 * np.abs(ref["PSI"]).max()
+    assert O.shape[3] == nt and np.abs(O).max() > 0
+    assert (tmp_path / "psinought_dpsi_MESSAGE.txt").read_text() == "Success"
