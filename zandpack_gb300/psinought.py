@@ -210,7 +210,7 @@ def main(argv=None):
     dh = Bias.dH(float(Initial.t0), np.asarray(A["DM_Ortho"]))
     h0 = np.asarray(A["H_Ortho"], np.complex128)[0] + (0 if np.isscalar(dh) else np.asarray(dh)[0])
     L = CompactLayout(A, hbar)
-    Ixi = np.asarray(A["Ixi"])[0][..., :L.NOT]
+    Ixi = np.asarray(A["Ixi"])[0][:, :, :L.NOT]
     P = res.psi[0]
     PI = sum((lambda pa, ia: (pa.reshape(-1, L.n).T @ ia.reshape(-1, L.n))
               + (pa.reshape(-1, L.n).T @ ia.reshape(-1, L.n)).conj().T)(P[a], Ixi[a]) for a in range(L.NL)) / hbar
