@@ -133,6 +133,11 @@ struct zg_traj {
   int dev = 0;
   int precision = ZG_PREC_F64;
   cudaStream_t stream = nullptr;
+  // mixed path: the H sigma tensor-core GEMM and the Omega derivative run on a
+  // second stream while the SIMT products run on the first (fork and join
+  // events; both are captured into the attempt graph as dependencies)
+  cudaStream_t stream2 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int n = 0, L = 0, N = 0, Ns = 0, Nf = 0, nc = 0;
   double hbar = 0;
   int64_t off_psi = 0, off_omA = 0, off_omB = 0, S = 0;
@@ -266,27 +271,30 @@ static void prof_collect(zg_traj* t) {
     P.pending[r] = 0;
   }
 }
-static void prof_begin(zg_traj* t, int r) {
+// region r begins / ends on stream st (default: the trajectory's stream)
+static void prof_begin(zg_traj* t, int r, cudaStream_t st = nullptr) {
   auto& P = t->prof;
   if (!P.on) return;
+  if (!st) st = t->stream;
   if (t->capturing) {  // event record nodes inside the attempt graph
     cudaEvent_t e;
     cudaEventCreate(&e);
-    cudaEventRecordWithFlags(e, t->stream, cudaEventRecordExternal);
+    cudaEventRecordWithFlags(e, st, cudaEventRecordExternal);
     t->gprof_r.push_back(r);
     t->gprof_b.push_back(e);
     return;
   }
   if (P.pending[r] == P.RING) prof_collect(t);
-  cudaEventRecord(P.b[r][P.pending[r]], t->stream);
+  cudaEventRecord(P.b[r][P.pending[r]], st);
 }
-static void prof_end(zg_traj* t, int r) {
+static void prof_end(zg_traj* t, int r, cudaStream_t st = nullptr) {
   auto& P = t->prof;
   if (!P.on) return;
+  if (!st) st = t->stream;
   if (t->capturing) {
     cudaEvent_t e;
     cudaEventCreate(&e);
-    cudaEventRecordWithFlags(e, t->stream, cudaEventRecordExternal);
+    cudaEventRecordWithFlags(e, st, cudaEventRecordExternal);
     // pair with the latest unmatched begin of this region
     t->gprof_e.resize(t->gprof_b.size(), nullptr);
     for (size_t i = t->gprof_b.size(); i-- > 0;)
@@ -296,7 +304,7 @@ static void prof_end(zg_traj* t, int r) {
       }
     return;
   }
-  cudaEventRecord(P.e[r][P.pending[r]], t->stream);
+  cudaEventRecord(P.e[r][P.pending[r]], st);
   P.pending[r] += 1;
 }
 // after a replay of the attempt graph: accumulate the regions it recorded
@@ -354,6 +362,12 @@ static void free_traj(zg_traj* t) {
                   t->conv64, t->sig64, t->tc_err, t->ws64, t->ws32, t->dis, t->ucols, t->umap,
                   t->st_V, t->st_Vc, t->st_W, t->st_lam, t->st_delta};
   for (void* p : ptrs) dfree(t, p);
+  if (t->stream2) {
+    cudaStreamSynchronize(t->stream2);
+    cudaStreamDestroy(t->stream2);
+  }
+  if (t->ev_fork) cudaEventDestroy(t->ev_fork);
+  if (t->ev_join) cudaEventDestroy(t->ev_join);
   if (t->stream) {
     cudaStreamSynchronize(t->stream);
     cudaStreamDestroy(t->stream);
@@ -545,6 +559,12 @@ int zg_traj_create(int device, const zg_layout* Lo, int precision, zg_traj** out
     if (Lo->colmap[i] < -1 || Lo->colmap[i] >= nc) { free_traj(t); set_error("colmap out of range"); return ZG_EINVAL; }
   if (cudaStreamCreateWithFlags(&t->stream, cudaStreamNonBlocking) != cudaSuccess) {
     free_traj(t); set_error("cudaStreamCreate failed"); return ZG_ECUDA;
+  }
+  if (precision == ZG_PREC_MIXED &&
+      (cudaStreamCreateWithFlags(&t->stream2, cudaStreamNonBlocking) != cudaSuccess ||
+       cudaEventCreateWithFlags(&t->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+       cudaEventCreateWithFlags(&t->ev_join, cudaEventDisableTiming) != cudaSuccess)) {
+    free_traj(t); set_error("second stream or events could not be created"); return ZG_ECUDA;
   }
   {
     std::lock_guard<std::mutex> lk(g_pool_mu);
@@ -949,13 +969,22 @@ static int rhs_mixed(zg_traj* t, int stage, const StageParams* p, int dH_mode, d
                                        t->Htl, t->BHh, t->BHl, t->BSh, t->BSl, s));
     ZG_TRY(launch_gathers<float>(d, sig, psih, psil, np, t->sigC32, t->G32, s));
     prof_end(t, ZG_PROF_PREP);
-    // tensor cores: R1 = psi H(t)^T and T = H(t) sigma
+    // tensor cores: R1 = psi H(t)^T
     prof_begin(t, ZG_PROF_GEMM);
     ZG_TRY(tc_gemm_launch(t->gR1, s));
     prof_end(t, ZG_PROF_GEMM);
-    prof_begin(t, ZG_PROF_GEMM2);
-    ZG_TRY(tc_gemm_launch(t->gT, s));
-    prof_end(t, ZG_PROF_GEMM2);
+    // fork: T = H(t) sigma (tensor cores) and then the Omega derivative run on
+    // the second stream, concurrently with the SIMT products below
+    cudaStream_t s2 = t->stream2;
+    ZG_CHECK_CUDA(cudaEventRecord(t->ev_fork, s));
+    ZG_CHECK_CUDA(cudaStreamWaitEvent(s2, t->ev_fork, 0));
+    prof_begin(t, ZG_PROF_GEMM2, s2);
+    ZG_TRY(tc_gemm_launch(t->gT, s2));
+    prof_end(t, ZG_PROF_GEMM2, s2);
+    prof_begin(t, ZG_PROF_OMEGA, s2);
+    ZG_TRY(launch_omega<float>(d, p, t->tiles, t->ntiles, t->G32, omA, omB, out + t->off_omA, out + t->off_omB, s2));
+    prof_end(t, ZG_PROF_OMEGA, s2);
+    ZG_CHECK_CUDA(cudaEventRecord(t->ev_join, s2));
   }
   // SIMT FP32: PI partials, xi sigma^T rows, Omega xi
   std::vector<GemmProb<float>> probs;
@@ -981,6 +1010,8 @@ static int rhs_mixed(zg_traj* t, int stage, const StageParams* p, int dH_mode, d
   prof_begin(t, ZG_PROF_SMALL);
   ZG_TRY(run_batches<float>(t, probs, &t->ws32, &t->ws32_cap, s, false));
   prof_end(t, ZG_PROF_SMALL);
+  // join: the finalisation needs T; the next stage overwrites what Omega reads
+  ZG_CHECK_CUDA(cudaStreamWaitEvent(s, t->ev_join, 0));
   prof_begin(t, ZG_PROF_FINAL);
   ZG_TRY(launch_sigma_finalize<float>(d, p, t->T32, np, t->Pc32, t->dis_on ? t->dis : nullptr, out, s));
   if (want_J) {
@@ -997,9 +1028,6 @@ static int rhs_mixed(zg_traj* t, int stage, const StageParams* p, int dH_mode, d
   ZG_TRY(launch_psi_finalize<float>(d, p, psih, psil, np, t->R1p, np, t->R2_32, t->ZA32, t->ZB32, out + t->off_psi,
                                     s));
   prof_end(t, ZG_PROF_FINAL);
-  prof_begin(t, ZG_PROF_OMEGA);
-  ZG_TRY(launch_omega<float>(d, p, t->tiles, t->ntiles, t->G32, omA, omB, out + t->off_omA, out + t->off_omB, s));
-  prof_end(t, ZG_PROF_OMEGA);
   return ZG_OK;
 }
 
