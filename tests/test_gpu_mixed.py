@@ -72,8 +72,11 @@ def test_mixed_rhs_against_oracle(case):
         tr.close()
 
 
-def test_mixed_rhs_random_dense_state():
-    """All live entries nonzero and a dense host dH: mixed k vs oracle."""
+@pytest.mark.parametrize("complex_dH", [False, True])
+def test_mixed_rhs_random_dense_state(complex_dH):
+    """All live entries nonzero and a dense host dH: mixed k vs oracle.  A
+    real dH keeps H(t) real (the tensor-core products then skip Im H); a
+    complex Hermitian dH takes the complex form of both products."""
     from oracle import zand_np as zo
     from zandpack_gb300 import _lib
     from zandpack_gb300.engine import Trajectory
@@ -91,7 +94,10 @@ def test_mixed_rhs_random_dense_state():
     tr = Trajectory(z, p["hbar"], precision="mixed", layout=L)
     tr.set_slot(tr.stages, y)
     dHm = rng.standard_normal((L.n, L.n)) * 0.05
-    dHm = (dHm + dHm.T).astype(complex)
+    if complex_dH:
+        dHm = dHm + 1j * rng.standard_normal((L.n, L.n)) * 0.05
+    dHm = ((dHm + dHm.conj().T) / 2).astype(complex)
+    assert complex_dH == bool(np.abs(dHm.imag).max() > 0)
     delta = rng.uniform(-0.3, 0.3, L.NL)
     tr.stage_input(0)
     tr.set_dH(dHm)

@@ -213,8 +213,14 @@ __global__ void __launch_bounds__(256) k_stage_input_mixed(const float2* __restr
       float2 hi, lo;
       split_tf32(v.x, hi.x, lo.x);
       split_tf32(v.y, hi.y, lo.y);
-      stage[ml.st_psih + (int64_t)m * ml.np + i] = hi;
-      stage[ml.st_psil + (int64_t)m * ml.np + i] = lo;
+      // planar: real parts, then the imaginary parts ml.plane floats further
+      float* ph = reinterpret_cast<float*>(stage + ml.st_psih);
+      float* pl = reinterpret_cast<float*>(stage + ml.st_psil);
+      const int64_t q = (int64_t)m * ml.np + i;
+      ph[q] = hi.x;
+      ph[ml.plane + q] = hi.y;
+      pl[q] = lo.x;
+      pl[ml.plane + q] = lo.y;
     } else {
       stage[ml.st_om + (e - ml.off_omA)] = v;
     }

@@ -58,6 +58,7 @@ struct MixedLayout {
   int64_t n, N, np;
   int64_t off_psi, off_omA, S;            // flat state offsets
   int64_t st_psih, st_psil, st_om, st_S;  // stage buffer offsets / size
+  int64_t plane;  // psi hi and lo are planar: N x np real parts, then N x np imaginary parts (floats)
 };
 // stage = y32 + sum_t c[t] K[idx[t]] in FP32, psi written as TF32 hi/lo parts
 int launch_stage_input_mixed(const float2* y32, const float2* K, int64_t stride, const CombineCoefs& cf,
@@ -85,6 +86,7 @@ struct GemmProb {
   int opA, opB;
   int tile_begin, tiles_n, tiles_mn;
   int ksplit, kchunk;  // split-K: ksplit partial products of kchunk, summed in a fixed order
+  int64_t planeA;      // 0: A interleaved complex; > 0: A planar, imaginary part planeA reals after the real
   int64_t ws_off;      // offset of this problem's partials in the workspace
   int64_t lda, ldb, ldc;
   C alpha, beta;
@@ -170,24 +172,33 @@ struct OmTile {
   int term1, term2;     // which source products apply
 };
 
-// sigC[a][i][k] = sig[i][C_a[k]], G[m][a][k] = (psi + psi_lo)[m][C_a[k]]
+// sigC[a][i][k] = sig[i][C_a[k]], G[m][a][k] = (psi + psi_lo)[m][C_a[k]];
+// plane > 0: psi (and psi_lo) planar, imaginary parts plane reals after the real parts
 template <typename T>
 int launch_gathers(const RhsDev<T>& d, const typename cx<T>::t* sig, const typename cx<T>::t* psi,
                    const typename cx<T>::t* psi_lo, int64_t ldpsi, typename cx<T>::t* sigC, typename cx<T>::t* G,
-                   cudaStream_t s);
+                   cudaStream_t s, int64_t plane = 0);
 // k_sig without the lead terms, then the lead terms (P + P^H)/hbar added to
 // the rows and columns of the coupling orbitals only (where P is nonzero).
 // dis (may be null): the n x n FP64 dissipator of this stage, entering as - hbar * dis
 template <typename T>
+// tmode 0: T interleaved complex (row stride ldT complex); planar (row stride
+// ldT reals, imaginary columns npl further): 1 = T = [Tr | Ti] (real H),
+// 2 = rows [Hr sigma_r | Hr sigma_i] then, npl rows further, [Hi sigma_r | Hi sigma_i]
 int launch_sigma_finalize(const RhsDev<T>& d, const StageParams* p, const typename cx<T>::t* Tm, int64_t ldT,
-                          const typename cx<T>::t* Pc, const double2* dis, typename cx<T>::t* ksig, cudaStream_t s);
+                          const typename cx<T>::t* Pc, const double2* dis, typename cx<T>::t* ksig, cudaStream_t s,
+                          int tmode = 0, int npl = 0);
 template <typename T>
 int launch_currents(const RhsDev<T>& d, const StageParams* p, const typename cx<T>::t* Pc, double* J, cudaStream_t s);
 template <typename T>
+// plane > 0: psi planar (see launch_gathers).  rmode 0: R1 interleaved complex
+// (row stride ldR1 complex); planar R1 (row stride ldR1 reals, rows of the
+// real parts of psi, then N rows of the imaginary parts): 1 = columns H_r
+// (real H), 2 = columns [H_r | H_i] with H_i npl columns further
 int launch_psi_finalize(const RhsDev<T>& d, const StageParams* p, const typename cx<T>::t* psi,
                         const typename cx<T>::t* psi_lo, int64_t ldpsi, const typename cx<T>::t* R1, int64_t ldR1,
                         const typename cx<T>::t* R2, const typename cx<T>::t* ZA, const typename cx<T>::t* ZB,
-                        typename cx<T>::t* kpsi, cudaStream_t s);
+                        typename cx<T>::t* kpsi, cudaStream_t s, int64_t plane = 0, int rmode = 0, int npl = 0);
 // stationary != 0: writes the Omega of dOmega/dt = 0, i hbar S / (X+ + D_a - X- - D_b),
 // instead of the stage derivative (the input Omega is not read)
 template <typename T>
@@ -205,11 +216,13 @@ int launch_build_ht(int n, const double2* H0, const double2* sig, const double2*
 //   Ht (n x np complex = n x 2np real)             A of  T = H(t) sigma
 //   BH (2np x 2np real embedding of H(t)^T form)    B of  R1 = psi H(t)^T
 //   BS (2np x 2np real embedding of sigma)          B of  T
-// h_part: 0 = all of the H(t) operands, 1 = their diagonal only (off-diagonal
-// entries already hold H0), 2 = leave them; BS is always rebuilt
+// Planar TF32 hi/lo operands of the two tensor-core GEMMs (np x np blocks):
+//   Ht rows [0, np): Re H(t), rows [np, 2 np): Im H(t)          (K = column)
+//   BS rows [0, np): Re sigma^T, rows [np, 2 np): Im sigma^T    (K = row of sigma)
+// h_part: 0 = all of Ht, 1 = its diagonal only (off-diagonal entries already
+// hold H0), 2 = leave it; BS is always rebuilt.  Padding is zero.
 int launch_build_operands_mixed(int n, int np, const double2* H0, const float2* sig32, const double2* dH, int dH_mode,
-                                double U, int h_part, float* Hth, float* Htl, float* BHh, float* BHl, float* BSh,
-                                float* BSl, cudaStream_t s);
+                                double U, int h_part, float* Hth, float* Htl, float* BSh, float* BSl, cudaStream_t s);
 // Lead currents in FP64 from the FP64 state: J_a = 2 Re sum_{m in a} sum_k psi[m][C_a[k]] IXI[m][k] / hbar^2
 // row ranges per lead: sourced rows [s[a], s[a+1]), free rows [f[a], f[a+1])
 struct CurRows {

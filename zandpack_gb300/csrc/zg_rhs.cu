@@ -48,6 +48,15 @@ __device__ __forceinline__ void load_opA(const GemmProb<T>& P, int m, int k, typ
   v2 = czero<T>();
   if (m >= P.M || k >= P.K) return;
   const int64_t o = P.opA == 0 ? (int64_t)m * P.lda + k : (int64_t)k * P.lda + m;
+  if (P.planeA) {  // planar A: real part at element index o, imaginary part planeA reals further
+    const T* a = reinterpret_cast<const T*>(P.A);
+    v = cx<T>::make(a[o], a[o + P.planeA]);
+    if (P.A2) {
+      const T* a2 = reinterpret_cast<const T*>(P.A2);
+      v2 = cx<T>::make(a2[o], a2[o + P.planeA]);
+    }
+    return;
+  }
   v = P.A[o];
   if (P.A2) v2 = P.A2[o];
 }
@@ -266,7 +275,8 @@ int launch_zgemm_batch(GemmBatch<T>& b, int64_t ws_capacity, cudaStream_t s) {
 template <typename T>
 __global__ void k_gathers(const RhsDev<T> d, const typename cx<T>::t* __restrict__ sig,
                           const typename cx<T>::t* __restrict__ psi, const typename cx<T>::t* __restrict__ psi_lo,
-                          int64_t ldpsi, typename cx<T>::t* __restrict__ sigC, typename cx<T>::t* __restrict__ G) {
+                          int64_t ldpsi, typename cx<T>::t* __restrict__ sigC, typename cx<T>::t* __restrict__ G,
+                          int64_t plane) {
   const int64_t ns = (int64_t)d.L * d.n * d.nc;
   const int64_t ng = (int64_t)d.N * d.L * d.nc;
   GRID_STRIDE(e, ns + ng) {
@@ -282,8 +292,18 @@ __global__ void k_gathers(const RhsDev<T> d, const typename cx<T>::t* __restrict
       const int a = (int)(r % d.L);
       const int64_t m = r / d.L;
       const int64_t o = m * ldpsi + d.lead_cols[a * d.nc + k];
-      typename cx<T>::t v = psi[o];
-      if (psi_lo) v = cadd(v, psi_lo[o]);
+      typename cx<T>::t v;
+      if (plane) {  // planar psi: real parts, imaginary parts plane reals further
+        const T* ph = reinterpret_cast<const T*>(psi);
+        v = cx<T>::make(ph[o], ph[o + plane]);
+        if (psi_lo) {
+          const T* pl = reinterpret_cast<const T*>(psi_lo);
+          v = cadd(v, cx<T>::make(pl[o], pl[o + plane]));
+        }
+      } else {
+        v = psi[o];
+        if (psi_lo) v = cadd(v, psi_lo[o]);
+      }
       G[g] = v;
     }
   }
@@ -292,9 +312,9 @@ __global__ void k_gathers(const RhsDev<T> d, const typename cx<T>::t* __restrict
 template <typename T>
 int launch_gathers(const RhsDev<T>& d, const typename cx<T>::t* sig, const typename cx<T>::t* psi,
                    const typename cx<T>::t* psi_lo, int64_t ldpsi, typename cx<T>::t* sigC, typename cx<T>::t* G,
-                   cudaStream_t s) {
+                   cudaStream_t s, int64_t plane) {
   int64_t tot = (int64_t)d.L * d.n * d.nc + (int64_t)d.N * d.L * d.nc;
-  k_gathers<T><<<grid_for(tot, 256, 152 * 8), 256, 0, s>>>(d, sig, psi, psi_lo, ldpsi, sigC, G);
+  k_gathers<T><<<grid_for(tot, 256, 152 * 8), 256, 0, s>>>(d, sig, psi, psi_lo, ldpsi, sigC, G, plane);
   ZG_CHECK_LAUNCH();
   count_launch();
   return ZG_OK;
@@ -317,11 +337,23 @@ __device__ __forceinline__ typename cx<T>::t p_full(const RhsDev<T>& d, const ty
 // Pass 1: the commutator (and the dissipator) for every element, one 32 x 32
 // block per CTA with the transposed block of T staged through shared memory
 // so that both reads of T are row-contiguous.
+// element (i, j) of T = H(t) sigma in the layouts of launch_sigma_finalize
+template <typename T>
+__device__ __forceinline__ typename cx<T>::t load_T(const typename cx<T>::t* Tm, int64_t ldT, int tmode, int npl, int i,
+                                                    int j) {
+  if (tmode == 0) return Tm[(int64_t)i * ldT + j];
+  const T* f = reinterpret_cast<const T*>(Tm);
+  const int64_t r = (int64_t)i * ldT;
+  if (tmode == 1) return cx<T>::make(f[r + j], f[r + npl + j]);
+  const int64_t r2 = (int64_t)(npl + i) * ldT;  // rows of Im H
+  return cx<T>::make(f[r + j] - f[r2 + npl + j], f[r + npl + j] + f[r2 + j]);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_sigma_finalize(const RhsDev<T> d, const StageParams* __restrict__ pp,
                                                         const typename cx<T>::t* __restrict__ Tm, int64_t ldT,
                                                         const double2* __restrict__ dis,
-                                                        typename cx<T>::t* __restrict__ ksig) {
+                                                        typename cx<T>::t* __restrict__ ksig, int tmode, int npl) {
   using C = typename cx<T>::t;
   __shared__ C tile[32][33];  // tile[r][c] = T[j0 + r][i0 + c]
   const StageScalars p = load_params(pp);
@@ -331,13 +363,13 @@ __global__ void __launch_bounds__(256) k_sigma_finalize(const RhsDev<T> d, const
   const int tx = threadIdx.x, ty = threadIdx.y;
   for (int r = ty; r < 32; r += 8) {
     const int j = j0 + r, i = i0 + tx;
-    tile[r][tx] = (j < n && i < n) ? Tm[(int64_t)j * ldT + i] : czero<T>();
+    tile[r][tx] = (j < n && i < n) ? load_T<T>(Tm, ldT, tmode, npl, j, i) : czero<T>();
   }
   __syncthreads();
   for (int r = ty; r < 32; r += 8) {
     const int i = i0 + r, j = j0 + tx;
     if (i >= n || j >= n) continue;
-    const C tij = Tm[(int64_t)i * ldT + j];
+    const C tij = load_T<T>(Tm, ldT, tmode, npl, i, j);
     const C tji = tile[tx][r];
     // -i (tij - conj(tji)) = (tij.y + tji.y, -(tij.x - tji.x))
     C v = cx<T>::make(tij.y + tji.y, -(tij.x - tji.x));
@@ -386,9 +418,11 @@ __global__ void __launch_bounds__(256) k_sigma_leads(const RhsDev<T> d, const St
 
 template <typename T>
 int launch_sigma_finalize(const RhsDev<T>& d, const StageParams* p, const typename cx<T>::t* Tm, int64_t ldT,
-                          const typename cx<T>::t* Pc, const double2* dis, typename cx<T>::t* ksig, cudaStream_t s) {
+                          const typename cx<T>::t* Pc, const double2* dis, typename cx<T>::t* ksig, cudaStream_t s,
+                          int tmode, int npl) {
+  ZG_REQUIRE(tmode >= 0 && tmode <= 2, "bad T layout %d", tmode);
   const int nb = (d.n + 31) / 32;
-  k_sigma_finalize<T><<<dim3(nb, nb), dim3(32, 8), 0, s>>>(d, p, Tm, ldT, dis, ksig);
+  k_sigma_finalize<T><<<dim3(nb, nb), dim3(32, 8), 0, s>>>(d, p, Tm, ldT, dis, ksig, tmode, npl);
   ZG_CHECK_LAUNCH();
   count_launch();
   if (d.nu > 0) {
@@ -498,7 +532,7 @@ __global__ void __launch_bounds__(256) k_psi_finalize(const RhsDev<T> d, const S
                                const typename cx<T>::t* __restrict__ psi_lo, int64_t ldpsi,
                                const typename cx<T>::t* R1, int64_t ldR1, const typename cx<T>::t* __restrict__ R2,
                                const typename cx<T>::t* __restrict__ ZA, const typename cx<T>::t* __restrict__ ZB,
-                               typename cx<T>::t* kpsi) {
+                               typename cx<T>::t* kpsi, int64_t plane, int rmode, int npl) {
   using C = typename cx<T>::t;
   extern __shared__ __align__(16) unsigned char psi_smem[];
   C* sZ = reinterpret_cast<C*>(psi_smem);  // [L][nc]: ZA + ZB of this row
@@ -523,9 +557,30 @@ __global__ void __launch_bounds__(256) k_psi_finalize(const RhsDev<T> d, const S
     const C dgp = src ? d.dGP[m] : czero<T>();
     __syncthreads();
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
-      C ps = psi[(int64_t)m * ldpsi + i];
-      const C pl = psi_lo ? psi_lo[(int64_t)m * ldpsi + i] : czero<T>();
-      const C r1 = R1[(int64_t)m * ldR1 + i];
+      C ps, pl, r1;
+      const int64_t o = (int64_t)m * ldpsi + i;
+      if (plane) {
+        const T* ph = reinterpret_cast<const T*>(psi);
+        ps = cx<T>::make(ph[o], ph[o + plane]);
+        if (psi_lo) {
+          const T* plo = reinterpret_cast<const T*>(psi_lo);
+          pl = cx<T>::make(plo[o], plo[o + plane]);
+        } else {
+          pl = czero<T>();
+        }
+      } else {
+        ps = psi[o];
+        pl = psi_lo ? psi_lo[o] : czero<T>();
+      }
+      if (rmode == 0) {
+        r1 = R1[(int64_t)m * ldR1 + i];
+      } else {
+        // planar R1: rows (Re psi) m and (Im psi) N + m; columns H_r, then H_i npl further
+        const T* f = reinterpret_cast<const T*>(R1);
+        const int64_t a0 = (int64_t)m * ldR1 + i, a1 = (int64_t)(d.N + m) * ldR1 + i;
+        r1 = rmode == 1 ? cx<T>::make(f[a0], f[a1])
+                        : cx<T>::make(f[a0] - f[a1 + npl], f[a0 + npl] + f[a1]);
+      }
       const C r2 = src ? R2[(int64_t)m * n + i] : czero<T>();
       ps = cadd(ps, pl);
       C v = cscale(r1, ih);
@@ -549,12 +604,13 @@ template <typename T>
 int launch_psi_finalize(const RhsDev<T>& d, const StageParams* p, const typename cx<T>::t* psi,
                         const typename cx<T>::t* psi_lo, int64_t ldpsi, const typename cx<T>::t* R1, int64_t ldR1,
                         const typename cx<T>::t* R2, const typename cx<T>::t* ZA, const typename cx<T>::t* ZB,
-                        typename cx<T>::t* kpsi, cudaStream_t s) {
+                        typename cx<T>::t* kpsi, cudaStream_t s, int64_t plane, int rmode, int npl) {
   if (d.N == 0) return ZG_OK;
+  ZG_REQUIRE(rmode >= 0 && rmode <= 2, "bad R1 layout %d", rmode);
   const size_t smem = (size_t)(d.L + 1) * d.nc * sizeof(typename cx<T>::t);
   ZG_REQUIRE(smem <= 48 * 1024, "coupling width too large for the psi finalisation (%zu B)", smem);
   const int grid = d.N < 152 * 8 ? d.N : 152 * 8;
-  k_psi_finalize<T><<<grid, 256, smem, s>>>(d, p, psi, psi_lo, ldpsi, R1, ldR1, R2, ZA, ZB, kpsi);
+  k_psi_finalize<T><<<grid, 256, smem, s>>>(d, p, psi, psi_lo, ldpsi, R1, ldR1, R2, ZA, ZB, kpsi, plane, rmode, npl);
   ZG_CHECK_LAUNCH();
   count_launch();
   return ZG_OK;
@@ -749,27 +805,24 @@ __device__ __forceinline__ void split_tf32_r(float v, float& hi, float& lo) {
   lo = __uint_as_float(l);
 }
 
-// One thread per complex element (r, c) of the np x np padded grid:
-//   Ht[r][c]                      -> Hth/Htl at row r, real columns 2c, 2c+1
-//   BH rows 2r, 2r+1, cols 2c, 2c+1 = [[Hr, -Hi], [Hi, Hr]] of H(t)[r][c]
-//   BS rows 2r, 2r+1, cols 2c, 2c+1 = [[Sr, -Si], [Si, Sr]] of sigma[c][r]
+// Planar TF32 hi/lo operands of the two tensor-core GEMMs (np x np blocks, K
+// along the row):  Ht rows [0, np) = Re H(t), rows [np, 2 np) = Im H(t);
+// BS rows [0, np) = Re sigma^T, rows [np, 2 np) = Im sigma^T.  Thread q < np*np
+// handles element (r, c) = (q / np, q % np) of BS and, when h_part == 0, of
+// Ht; threads np*np + r rebuild the diagonal (r, r) of Ht when h_part == 1.
 // Padding (r or c >= n) is written as zero.
 __global__ void k_build_operands_mixed(int n, int np, const double2* __restrict__ H0, const float2* __restrict__ sig32,
                                        const double2* __restrict__ dH, int dH_mode, double U, int h_part,
-                                       float* __restrict__ Hth, float* __restrict__ Htl, float* __restrict__ BHh,
-                                       float* __restrict__ BHl, float* __restrict__ BSh, float* __restrict__ BSl) {
-  const int64_t ld = 2 * (int64_t)np;
-  // h_part: 0 = every entry of the H(t) operands, 1 = their diagonal only
-  // (the rest already holds H0's embedding), 2 = none; the sigma operand
-  // BS is always rebuilt.  Threads [0, np*np) cover BS (and H when h_part == 0),
-  // threads [np*np, np*np + np) the diagonal when h_part == 1.
-  const int64_t tot = (int64_t)np * np + (h_part == 1 ? np : 0);
+                                       float* __restrict__ Hth, float* __restrict__ Htl, float* __restrict__ BSh,
+                                       float* __restrict__ BSl) {
+  const int64_t nn = (int64_t)np * np;
+  const int64_t tot = nn + (h_part == 1 ? np : 0);
   GRID_STRIDE(q, tot) {
-    const bool diag_job = q >= (int64_t)np * np;
-    const int64_t e = diag_job ? (q - (int64_t)np * np) * (np + 1) : q;
-    const int r = (int)(e / np), c = (int)(e % np);
+    const bool diag_job = q >= nn;
+    const int r = diag_job ? (int)(q - nn) : (int)(q / np);
+    const int c = diag_job ? r : (int)(q % np);
+    const int64_t o = (int64_t)r * np + c;
     float a, b;
-    const int64_t o0 = (int64_t)(2 * r) * ld + 2 * c, o1 = o0 + ld;
     if (h_part == 0 || diag_job) {
       float hr = 0.f, hi = 0.f;
       if (r < n && c < n) {
@@ -779,45 +832,36 @@ __global__ void k_build_operands_mixed(int n, int np, const double2* __restrict_
         hr = (float)v.x;
         hi = (float)v.y;
       }
-      if (r < n) {
-        split_tf32_r(hr, a, b);
-        Hth[(int64_t)r * ld + 2 * c] = a;
-        Htl[(int64_t)r * ld + 2 * c] = b;
-        split_tf32_r(hi, a, b);
-        Hth[(int64_t)r * ld + 2 * c + 1] = a;
-        Htl[(int64_t)r * ld + 2 * c + 1] = b;
-      }
-      float xr_h, xr_l, xi_h, xi_l, mi_h, mi_l;
-      split_tf32_r(hr, xr_h, xr_l);
-      split_tf32_r(hi, xi_h, xi_l);
-      split_tf32_r(-hi, mi_h, mi_l);
-      BHh[o0] = xr_h; BHl[o0] = xr_l; BHh[o0 + 1] = mi_h; BHl[o0 + 1] = mi_l;
-      BHh[o1] = xi_h; BHl[o1] = xi_l; BHh[o1 + 1] = xr_h; BHl[o1 + 1] = xr_l;
+      split_tf32_r(hr, a, b);
+      Hth[o] = a;
+      Htl[o] = b;
+      split_tf32_r(hi, a, b);
+      Hth[nn + o] = a;
+      Htl[nn + o] = b;
     }
     if (!diag_job) {
       float sr = 0.f, si = 0.f;
       if (r < n && c < n) {
-        const float2 sv = sig32[(int64_t)c * n + r];
+        const float2 sv = sig32[(int64_t)c * n + r];  // sigma[c][r]: row j = r, K index k = c
         sr = sv.x;
         si = sv.y;
       }
-      float xr_h, xr_l, xi_h, xi_l, mi_h, mi_l;
-      split_tf32_r(sr, xr_h, xr_l);
-      split_tf32_r(si, xi_h, xi_l);
-      split_tf32_r(-si, mi_h, mi_l);
-      BSh[o0] = xr_h; BSl[o0] = xr_l; BSh[o0 + 1] = mi_h; BSl[o0 + 1] = mi_l;
-      BSh[o1] = xi_h; BSl[o1] = xi_l; BSh[o1 + 1] = xr_h; BSl[o1 + 1] = xr_l;
+      split_tf32_r(sr, a, b);
+      BSh[o] = a;
+      BSl[o] = b;
+      split_tf32_r(si, a, b);
+      BSh[nn + o] = a;
+      BSl[nn + o] = b;
     }
   }
 }
 
 int launch_build_operands_mixed(int n, int np, const double2* H0, const float2* sig32, const double2* dH, int dH_mode,
-                                double U, int h_part, float* Hth, float* Htl, float* BHh, float* BHl, float* BSh,
-                                float* BSl, cudaStream_t s) {
+                                double U, int h_part, float* Hth, float* Htl, float* BSh, float* BSl, cudaStream_t s) {
   ZG_REQUIRE(h_part >= 0 && h_part <= 2, "bad operand part %d", h_part);
   const int64_t tot = (int64_t)np * np + (h_part == 1 ? np : 0);
   k_build_operands_mixed<<<grid_for(tot, 256, 152 * 16), 256, 0, s>>>(n, np, H0, sig32, dH, dH_mode, U, h_part, Hth,
-                                                                      Htl, BHh, BHl, BSh, BSl);
+                                                                      Htl, BSh, BSl);
   ZG_CHECK_LAUNCH();
   count_launch();
   return ZG_OK;
@@ -854,13 +898,13 @@ int launch_stationary_scale(int N, int n, const double2* Xp, const int* mode_lea
   template int64_t plan_zgemm_batch<T>(GemmBatch<T>&);                                                               \
   template int launch_zgemm_batch<T>(GemmBatch<T>&, int64_t, cudaStream_t);                                         \
   template int launch_gathers<T>(const RhsDev<T>&, const cx<T>::t*, const cx<T>::t*, const cx<T>::t*, int64_t,      \
-                                 cx<T>::t*, cx<T>::t*, cudaStream_t);                                                 \
+                                 cx<T>::t*, cx<T>::t*, cudaStream_t, int64_t);                                        \
   template int launch_sigma_finalize<T>(const RhsDev<T>&, const StageParams*, const cx<T>::t*, int64_t,              \
-                                        const cx<T>::t*, const double2*, cx<T>::t*, cudaStream_t);                    \
+                                        const cx<T>::t*, const double2*, cx<T>::t*, cudaStream_t, int, int);          \
   template int launch_currents<T>(const RhsDev<T>&, const StageParams*, const cx<T>::t*, double*, cudaStream_t);     \
   template int launch_psi_finalize<T>(const RhsDev<T>&, const StageParams*, const cx<T>::t*, const cx<T>::t*,        \
                                       int64_t, const cx<T>::t*, int64_t, const cx<T>::t*, const cx<T>::t*,           \
-                                      const cx<T>::t*, cx<T>::t*, cudaStream_t);                                     \
+                                      const cx<T>::t*, cx<T>::t*, cudaStream_t, int64_t, int, int);                  \
   template int launch_omega<T>(const RhsDev<T>&, const StageParams*, const OmTile*, int, const cx<T>::t*,            \
                                const cx<T>::t*, const cx<T>::t*, cx<T>::t*, cx<T>::t*, cudaStream_t, int);
 ZG_INST(double)

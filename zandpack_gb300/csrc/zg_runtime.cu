@@ -186,7 +186,13 @@ struct zg_traj {
          *IXI32 = nullptr, *U32 = nullptr, *V32 = nullptr;
   float2 *y32 = nullptr, *K32 = nullptr, *stage32 = nullptr;
   int k_slots = 0;
-  float *Hth = nullptr, *Htl = nullptr, *BHh = nullptr, *BHl = nullptr, *BSh = nullptr, *BSl = nullptr;
+  // mixed-path tensor-core operands, planar (real part rows, then imaginary
+  // part rows np further), TF32 hi/lo: H(t) (A of H sigma, B of psi H^T) and
+  // the transposed sigma (B of H sigma)
+  float *Hth = nullptr, *Htl = nullptr, *BSh = nullptr, *BSl = nullptr;
+  bool h0_real = false;   // H0 has no imaginary part
+  bool dH_real = false;   // the uploaded dH matrix has no imaginary part
+  TcGemm gTc, gR1c;       // complex H(t) forms of the two products (gT, gR1: real H(t))
   float2 *T32 = nullptr, *R1p = nullptr, *Pc32 = nullptr, *sigC32 = nullptr, *G32 = nullptr, *R2_32 = nullptr,
          *ZA32 = nullptr, *ZB32 = nullptr;
   double2 *conv64 = nullptr, *sig64 = nullptr;
@@ -357,8 +363,8 @@ static void free_traj(zg_traj* t) {
                   t->lead_cols, t->colmap, t->tiles, t->Y, t->Ystage, t->Ht, t->dH, t->T, t->Pc, t->sigC,
                   t->G, t->R2, t->ZA, t->ZB, t->J, t->Jpart, t->partial, t->err, t->Xp32, t->Xm32, t->GLP32,
                   t->dGP32,
-                  t->XI32, t->XIS32, t->IXI32, t->U32, t->V32, t->y32, t->K32, t->stage32, t->Hth, t->Htl, t->BHh,
-                  t->BHl, t->BSh, t->BSl, t->T32, t->R1p, t->Pc32, t->sigC32, t->G32, t->R2_32, t->ZA32, t->ZB32,
+                  t->XI32, t->XIS32, t->IXI32, t->U32, t->V32, t->y32, t->K32, t->stage32, t->Hth, t->Htl,
+                  t->BSh, t->BSl, t->T32, t->R1p, t->Pc32, t->sigC32, t->G32, t->R2_32, t->ZA32, t->ZB32,
                   t->conv64, t->sig64, t->tc_err, t->ws64, t->ws32, t->dis, t->ucols, t->umap,
                   t->st_V, t->st_Vc, t->st_W, t->st_lam, t->st_delta};
   for (void* p : ptrs) dfree(t, p);
@@ -465,6 +471,12 @@ static int create_mixed(zg_traj* t, const zg_layout* Lo, const std::vector<doubl
   ml.st_psil = ml.st_psih + N * np;
   ml.st_om = ml.st_psil + N * np;
   ml.st_S = ml.st_om + N * Ns + Ns * Nf;
+  ml.plane = N * np;  // psi hi and lo are stored planar: real rows, then imaginary rows
+  {
+    bool real = true;
+    for (int64_t e = 0; e < n * n && real; ++e) real = Lo->H0[2 * e + 1] == 0.0;
+    t->h0_real = real;
+  }
   cudaStream_t s = t->stream;
   // host copies stay alive until the stream synchronisation at the end
   std::vector<std::vector<float2>> keep;
@@ -487,23 +499,34 @@ static int create_mixed(zg_traj* t, const zg_layout* Lo, const std::vector<doubl
   ZG_TRY(dalloc(t, &t->y32, t->S));
   ZG_TRY(dalloc(t, &t->stage32, ml.st_S));
   ZG_CHECK_CUDA(cudaMemsetAsync(t->stage32, 0, ml.st_S * sizeof(float2), s));  // psi padding columns stay zero
-  ZG_TRY(dalloc(t, &t->Hth, n * 2 * np)); ZG_TRY(dalloc(t, &t->Htl, n * 2 * np));
-  ZG_TRY(dalloc(t, &t->BHh, 4 * np * np)); ZG_TRY(dalloc(t, &t->BHl, 4 * np * np));
-  ZG_TRY(dalloc(t, &t->BSh, 4 * np * np)); ZG_TRY(dalloc(t, &t->BSl, 4 * np * np));
-  ZG_TRY(dalloc(t, &t->T32, n * np)); ZG_TRY(dalloc(t, &t->R1p, N * np));
+  ZG_TRY(dalloc(t, &t->Hth, 2 * np * np)); ZG_TRY(dalloc(t, &t->Htl, 2 * np * np));
+  ZG_TRY(dalloc(t, &t->BSh, 2 * np * np)); ZG_TRY(dalloc(t, &t->BSl, 2 * np * np));
+  ZG_CHECK_CUDA(cudaMemsetAsync(t->Hth, 0, 2 * np * np * sizeof(float), s));
+  ZG_CHECK_CUDA(cudaMemsetAsync(t->Htl, 0, 2 * np * np * sizeof(float), s));
+  ZG_TRY(dalloc(t, &t->T32, 2 * np * np)); ZG_TRY(dalloc(t, &t->R1p, N * 2 * np));
   ZG_TRY(dalloc(t, &t->Pc32, 2 * L * n * nc)); ZG_TRY(dalloc(t, &t->sigC32, L * n * nc)); ZG_TRY(dalloc(t, &t->G32, N * L * nc));
   ZG_TRY(dalloc(t, &t->R2_32, std::max<int64_t>(Ns, 1) * n));
   ZG_TRY(dalloc(t, &t->ZA32, L * N * nc)); ZG_TRY(dalloc(t, &t->ZB32, L * std::max<int64_t>(Ns, 1) * nc));
   ZG_TRY(dalloc(t, &t->sig64, n * n));
   ZG_TRY(dalloc(t, &t->tc_err, 1));
   ZG_CHECK_CUDA(cudaMemsetAsync(t->tc_err, 0, sizeof(int), s));
-  // tensor maps of the two tensor-core GEMMs (fixed buffers)
+  // Tensor maps of the two tensor-core GEMMs (fixed buffers), planar operands
+  // with K = np, every output row 2 np floats wide:
+  //   psi H^T:  A = psi (2N rows: real, imaginary), B = H rows (real H: the
+  //             real part, nb32 rows; complex H: 2 np rows, real then imaginary)
+  //   H sigma:  A = H rows (real H: n rows; complex H: 2 np), B = sigma^T
+  //             (2 np rows: real part columns, imaginary part columns)
   const float* psih = (const float*)(t->stage32 + ml.st_psih);
   const float* psil = (const float*)(t->stage32 + ml.st_psil);
-  ZG_TRY(tc_gemm_prepare(t->gT, t->Hth, t->Htl, t->BSh, t->BSl, 2 * np, 2 * np, (float*)t->T32, 2 * np, (int)n,
-                         (int)(2 * np), (int)(2 * np), t->tc_err));
-  ZG_TRY(tc_gemm_prepare(t->gR1, psih, psil, t->BHh, t->BHl, 2 * np, 2 * np, (float*)t->R1p, 2 * np, (int)N,
-                         (int)(2 * np), (int)(2 * np), t->tc_err));
+  const int64_t nb32 = (n + 31) / 32 * 32;  // <= 2 np; rows n.. of H are zero
+  ZG_TRY(tc_gemm_prepare(t->gT, t->Hth, t->Htl, t->BSh, t->BSl, np, np, (float*)t->T32, 2 * np, (int)n,
+                         (int)(2 * np), (int)np, t->tc_err));
+  ZG_TRY(tc_gemm_prepare(t->gTc, t->Hth, t->Htl, t->BSh, t->BSl, np, np, (float*)t->T32, 2 * np, (int)(2 * np),
+                         (int)(2 * np), (int)np, t->tc_err));
+  ZG_TRY(tc_gemm_prepare(t->gR1, psih, psil, t->Hth, t->Htl, np, np, (float*)t->R1p, 2 * np, (int)(2 * N),
+                         (int)nb32, (int)np, t->tc_err));
+  ZG_TRY(tc_gemm_prepare(t->gR1c, psih, psil, t->Hth, t->Htl, np, np, (float*)t->R1p, 2 * np, (int)(2 * N),
+                         (int)(2 * np), (int)np, t->tc_err));
   ZG_CHECK_CUDA(cudaStreamSynchronize(s));
   return ZG_OK;
 }
@@ -802,6 +825,11 @@ int zg_get_stage_sigma(zg_traj* t, double* host) {
 int zg_set_dH(zg_traj* t, const double* host) {
   ZG_REQUIRE(t && host, "null argument");
   ZG_CHECK_CUDA(cudaSetDevice(t->dev));
+  {
+    bool real = true;
+    for (int64_t e = 0; e < (int64_t)t->n * t->n && real; ++e) real = host[2 * e + 1] == 0.0;
+    t->dH_real = real;
+  }
   ZG_CHECK_CUDA(cudaMemcpyAsync(t->dH, host, (size_t)t->n * t->n * sizeof(double2), cudaMemcpyHostToDevice,
                                 t->stream));
   ZG_CHECK_CUDA(cudaStreamSynchronize(t->stream));
@@ -828,15 +856,20 @@ static void gemm_prob_f64(std::vector<GemmProb<double>>& v, const double2* A, in
                           int64_t ldb, int opB, double2* C, int64_t ldc, int M, int N, int K) {
   GemmProb<double> P;
   P.A = A; P.A2 = nullptr; P.B = B; P.Cm = C; P.M = M; P.N = N; P.K = K; P.opA = opA; P.opB = opB;
+  P.planeA = 0;
   P.lda = lda; P.ldb = ldb; P.ldc = ldc;
   P.alpha = make_double2(1.0, 0.0); P.beta = make_double2(0.0, 0.0);
   P.tile_begin = 0; P.tiles_n = 1;
   v.push_back(P);
 }
+// planeA > 0: A (and A2) are planar, element (r, c) = (A_f[i], A_f[i + planeA]) with i
+// the element index, A_f the floats at A
 static void gemm_prob_f32(std::vector<GemmProb<float>>& v, const float2* A, const float2* A2, int64_t lda, int opA,
-                          const float2* B, int64_t ldb, int opB, float2* C, int64_t ldc, int M, int N, int K) {
+                          const float2* B, int64_t ldb, int opB, float2* C, int64_t ldc, int M, int N, int K,
+                          int64_t planeA = 0) {
   GemmProb<float> P;
   P.A = A; P.A2 = A2; P.B = B; P.Cm = C; P.M = M; P.N = N; P.K = K; P.opA = opA; P.opB = opB;
+  P.planeA = planeA;
   P.lda = lda; P.ldb = ldb; P.ldc = ldc;
   P.alpha = make_float2(1.f, 0.f); P.beta = make_float2(0.f, 0.f);
   P.tile_begin = 0; P.tiles_n = 1;
@@ -946,8 +979,12 @@ static int rhs_mixed(zg_traj* t, int stage, const StageParams* p, int dH_mode, d
   const RhsDev<float> d = t->dev_view<float>();
   const MixedLayout& ml = t->ml;
   const float2* sig = t->stage32;
-  const float2* psih = t->stage32 + ml.st_psih;
-  const float2* psil = t->stage32 + ml.st_psil;
+  // psi hi and lo, planar: real parts (N x np floats), then imaginary parts
+  const float* psih_f = (const float*)(t->stage32 + ml.st_psih);
+  const float* psil_f = (const float*)(t->stage32 + ml.st_psil);
+  const bool hreal = t->h0_real && (dH_mode != ZG_DH_MATRIX || t->dH_real);
+  const TcGemm& gR1 = hreal ? t->gR1 : t->gR1c;
+  const TcGemm& gT = hreal ? t->gT : t->gTc;
   const float2* omA = t->stage32 + ml.st_om;
   const float2* omB = omA + (int64_t)t->N * t->Ns;
   float2* out = t->kslot(stage);
@@ -966,12 +1003,13 @@ static int rhs_mixed(zg_traj* t, int stage, const StageParams* p, int dH_mode, d
     }
     t->h_diag_mode = dH_mode;
     ZG_TRY(launch_build_operands_mixed((int)n, (int)np, t->H0, sig, t->dH, dH_mode, hubbard_U, h_part, t->Hth,
-                                       t->Htl, t->BHh, t->BHl, t->BSh, t->BSl, s));
-    ZG_TRY(launch_gathers<float>(d, sig, psih, psil, np, t->sigC32, t->G32, s));
+                                       t->Htl, t->BSh, t->BSl, s));
+    ZG_TRY(launch_gathers<float>(d, sig, (const float2*)psih_f, (const float2*)psil_f, np, t->sigC32, t->G32, s,
+                                 ml.plane));
     prof_end(t, ZG_PROF_PREP);
     // tensor cores: R1 = psi H(t)^T
     prof_begin(t, ZG_PROF_GEMM);
-    ZG_TRY(tc_gemm_launch(t->gR1, s));
+    ZG_TRY(tc_gemm_launch(gR1, s));
     prof_end(t, ZG_PROF_GEMM);
     // fork: T = H(t) sigma (tensor cores) and then the Omega derivative run on
     // the second stream, concurrently with the SIMT products below
@@ -979,7 +1017,7 @@ static int rhs_mixed(zg_traj* t, int stage, const StageParams* p, int dH_mode, d
     ZG_CHECK_CUDA(cudaEventRecord(t->ev_fork, s));
     ZG_CHECK_CUDA(cudaStreamWaitEvent(s2, t->ev_fork, 0));
     prof_begin(t, ZG_PROF_GEMM2, s2);
-    ZG_TRY(tc_gemm_launch(t->gT, s2));
+    ZG_TRY(tc_gemm_launch(gT, s2));
     prof_end(t, ZG_PROF_GEMM2, s2);
     prof_begin(t, ZG_PROF_OMEGA, s2);
     ZG_TRY(launch_omega<float>(d, p, t->tiles, t->ntiles, t->G32, omA, omB, out + t->off_omA, out + t->off_omB, s2));
@@ -990,11 +1028,13 @@ static int rhs_mixed(zg_traj* t, int stage, const StageParams* p, int dH_mode, d
   std::vector<GemmProb<float>> probs;
   for (int a = 0; a < L; ++a) {
     int64_t r0 = t->s_start[a], r1 = t->s_start[a + 1];
-    gemm_prob_f32(probs, psih + r0 * np, psil + r0 * np, np, 1, t->IXI32 + r0 * nc, nc, 0,
-                  t->Pc32 + ((0 * L + a) * n) * nc, nc, (int)n, (int)nc, (int)(r1 - r0));
+    gemm_prob_f32(probs, (const float2*)(psih_f + r0 * np), (const float2*)(psil_f + r0 * np), np, 1,
+                  t->IXI32 + r0 * nc, nc, 0, t->Pc32 + ((0 * L + a) * n) * nc, nc, (int)n, (int)nc, (int)(r1 - r0),
+                  ml.plane);
     r0 = t->f_start[a]; r1 = t->f_start[a + 1];
-    gemm_prob_f32(probs, psih + r0 * np, psil + r0 * np, np, 1, t->IXI32 + r0 * nc, nc, 0,
-                  t->Pc32 + ((1 * L + a) * n) * nc, nc, (int)n, (int)nc, (int)(r1 - r0));
+    gemm_prob_f32(probs, (const float2*)(psih_f + r0 * np), (const float2*)(psil_f + r0 * np), np, 1,
+                  t->IXI32 + r0 * nc, nc, 0, t->Pc32 + ((1 * L + a) * n) * nc, nc, (int)n, (int)nc, (int)(r1 - r0),
+                  ml.plane);
     r0 = t->s_start[a]; r1 = t->s_start[a + 1];
     if (r1 > r0)
       gemm_prob_f32(probs, t->XI32 + r0 * nc, nullptr, nc, 0, t->sigC32 + a * n * nc, nc, 1, t->R2_32 + r0 * n, n,
@@ -1013,7 +1053,8 @@ static int rhs_mixed(zg_traj* t, int stage, const StageParams* p, int dH_mode, d
   // join: the finalisation needs T; the next stage overwrites what Omega reads
   ZG_CHECK_CUDA(cudaStreamWaitEvent(s, t->ev_join, 0));
   prof_begin(t, ZG_PROF_FINAL);
-  ZG_TRY(launch_sigma_finalize<float>(d, p, t->T32, np, t->Pc32, t->dis_on ? t->dis : nullptr, out, s));
+  ZG_TRY(launch_sigma_finalize<float>(d, p, t->T32, 2 * np, t->Pc32, t->dis_on ? t->dis : nullptr, out, s,
+                                      hreal ? 1 : 2, (int)np));
   if (want_J) {
     if (stage == 0)  // the stage-0 input is y itself: currents from the FP64 state
     {
@@ -1025,8 +1066,9 @@ static int rhs_mixed(zg_traj* t, int stage, const StageParams* p, int dH_mode, d
     else
       ZG_TRY(launch_currents<float>(d, p, t->Pc32, t->J, s));
   }
-  ZG_TRY(launch_psi_finalize<float>(d, p, psih, psil, np, t->R1p, np, t->R2_32, t->ZA32, t->ZB32, out + t->off_psi,
-                                    s));
+  ZG_TRY(launch_psi_finalize<float>(d, p, (const float2*)psih_f, (const float2*)psil_f, np, t->R1p, 2 * np,
+                                    t->R2_32, t->ZA32, t->ZB32, out + t->off_psi, s, ml.plane, hreal ? 1 : 2,
+                                    (int)np));
   prof_end(t, ZG_PROF_FINAL);
   return ZG_OK;
 }
@@ -1153,7 +1195,7 @@ static int enqueue_attempt_device(zg_traj* t) {
 static int ensure_h_operands(zg_traj* t) {
   if (t->precision != ZG_PREC_MIXED || t->h_offdiag_ready) return ZG_OK;
   ZG_TRY(launch_build_operands_mixed(t->n, t->np, t->H0, t->stage32, t->dH, t->g_dH_mode, t->g_U, 0, t->Hth, t->Htl,
-                                     t->BHh, t->BHl, t->BSh, t->BSl, t->stream));
+                                     t->BSh, t->BSl, t->stream));
   t->h_offdiag_ready = true;
   t->h_diag_mode = t->g_dH_mode;
   return ZG_OK;
