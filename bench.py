@@ -200,14 +200,19 @@ def run_ours(args):
                 "peak_source": "live DFMA probe zg_measure_peaks (FP64 is not in MEASURED_PEAKS.json)",
                 "algorithmic_flops_per_launch": gemm_f}
     else:
-        # psi H(t)^T on tcgen05: real-embedded complex GEMM M x 2np x 2np, three TF32 products
+        # psi H(t)^T on tcgen05, planar operands, three TF32 products: A = (Re psi; Im psi)
+        # (2N x np), B = the rows of Re H (real H(t): nb32 of them) or of (Re H; Im H) (2 np)
         np_ = (L.n + 15) // 16 * 16
-        tc_flops = 3 * 2 * L.N * (2 * np_) * (2 * np_)
-        alg_flops = 8 * L.N * L.n * L.n
+        nb32 = (L.n + 31) // 32 * 32
+        h_real = not np.any(np.asarray(w.arrays["H_Ortho"]).imag)  # the Hubbard term is real
+        tc_flops = 3 * 2 * (2 * L.N) * (nb32 if h_real else 2 * np_) * np_
+        alg_flops = 8 * L.N * L.n * L.n if not h_real else 4 * L.N * L.n * L.n
         t_launch = g_ms / g_n / 1e3 if g_n else None
         tf32 = measure_tf32_peak()
         achieved = tc_flops / t_launch / 1e12 if t_launch else None
-        roof = {"bound": "tensor", "kernel": "k_gemm_tf32x3<128,3> (psi H(t)^T, tcgen05 kind::tf32, 3xTF32)",
+        roof = {"bound": "tensor",
+                "kernel": "k_gemm_tf32x3<256,4,16> (psi H(t)^T, tcgen05 kind::tf32, 3xTF32, %s H(t))"
+                          % ("real" if h_real else "complex"),
                 "achieved": achieved, "peak": tf32, "unit": "TFLOP/s",
                 "frac": (achieved / tf32) if achieved and tf32 else None, "traffic": None,
                 "peak_source": "live cuBLAS TF32 GEMM 8192^3 (torch.matmul, allow_tf32); TF32 is not in "
