@@ -431,6 +431,13 @@ def run_ensemble(args):
     stats["t_span_fs"] = args.ensemble_fs
     stats["rate_per_s"] = 50.0
     stats["errors"] = sorted({r.error for r in res if r.error})[:3]
+    # capacity: the same requests all present at t = 0 (the Poisson stream above
+    # arrives slower than the server completes, so its throughput is the rate)
+    srv2 = Server(c4_workload, c4_estimate, max_slots=args.slots, precision=args.precision, keep_sigma=False,
+                  prep_workers=args.prep_workers)
+    _, burst = srv2.run(reqs, time_scale=0.0)
+    stats["capacity"] = {k: burst[k] for k in ("wall_s", "throughput_traj_per_s", "simulated_fs_per_s",
+                                               "p50_latency_s", "p99_latency_s", "completed")}
     return stats
 
 
