@@ -105,6 +105,19 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
+def aggregate_ranks(ms, adv, device):
+    """Replicas: the job's time is the slowest rank's, its simulated time the
+    sum over ranks (each rank propagates its own trajectory)."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms, adv], device=device, dtype=torch.float64)
+    tmax = t.clone()
+    dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+    tsum = t.clone()
+    dist.all_reduce(tsum)
+    return float(tmax[0]), float(tsum[1])
+
+
 def rhs_flops(L):
     """Algorithmic real flops of one right-hand side (structurally nonzero work)."""
     n, N, Ns, Nf, nc = L.n, L.N, L.Ns, L.Nf, L.nc
@@ -177,12 +190,7 @@ def run_ours(args):
     _lib.check(_lib.lib().zg_profile(tr._h, 0))
     tr.graph_run(0)  # recapture without event nodes, outside the e2e timed region
     if ws > 1:
-        t = torch.tensor([ms, adv], device="cuda", dtype=torch.float64)
-        tmax = t.clone()
-        torch.distributed.all_reduce(tmax, op=torch.distributed.ReduceOp.MAX)
-        tsum = t.clone()
-        torch.distributed.all_reduce(tsum)
-        ms, adv_total = float(tmax[0]), float(tsum[1])
+        ms, adv_total = aggregate_ranks(ms, adv, "cuda")
     else:
         adv_total = adv
     value = adv_total / (ms / 1e3)
