@@ -44,3 +44,12 @@ def golden(request):
     if not os.path.exists(path):
         pytest.skip("fixture %s missing" % request.param)
     return request.param, load_golden(request.param)
+
+
+@pytest.fixture(params=["nz_mini2", "nz_mini3"])
+def golden_nz(request):
+    """Fixtures of the reference ``nozand`` (non-orthogonal basis)."""
+    path = os.path.join(GOLDEN, request.param + ".npz")
+    if not os.path.exists(path):
+        pytest.skip("fixture %s missing" % request.param)
+    return request.param, load_golden(request.param)

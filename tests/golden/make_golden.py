@@ -1,8 +1,10 @@
-"""Generate golden fixtures by running the UNMODIFIED reference ``zand``.
+"""Generate golden fixtures by running the UNMODIFIED reference ``zand`` (and,
+for the ``nz_*`` cases, ``nozand`` on the same cases posed in a
+non-orthogonal basis, ``make_nonorth_workload``).
 
 Usage (in a container that has the reference checkout; see ``refharness``):
 
-    python tests/golden/make_golden.py [c1 mini2 mini3]
+    python tests/golden/make_golden.py [c1 mini2 mini3 nz_mini2 nz_mini3]
 
 For each case this writes ``tests/golden/<case>.npz`` holding
 
@@ -34,7 +36,7 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, HERE)
 
 import refharness  # noqa: E402
-from zandpack_gb300.workloads import make_workload  # noqa: E402
+from zandpack_gb300.workloads import make_workload, make_nonorth_workload  # noqa: E402
 from zandpack_gb300.arrays_io import write_arrays  # noqa: E402
 
 CASES = {
@@ -43,6 +45,9 @@ CASES = {
     "c1": (1.0, 0.01, (0, 7), 4),
     "mini2": (2.0, 0.3, (0, 1, 12), 1),
     "mini3": (1.0, 0.3, (0, 1, 9), 1),
+    # the same cases posed in a non-orthogonal basis, run through ``nozand``
+    "nz_mini2": (1.0, 0.3, (0, 1, 9), 1),
+    "nz_mini3": (1.0, 0.3, (0, 1, 9), 1),
 }
 
 
@@ -62,7 +67,8 @@ def initial_py(w, t1, stepsize, saveevery=1):
 
 def make_case(name):
     t1, stepsize, keep, keep_every = CASES[name]
-    w = make_workload(name)
+    nonorth = name.startswith("nz_")
+    w = make_nonorth_workload(name[3:]) if nonorth else make_workload(name)
     A = w.arrays
     L = int(A["psi_shape"][1])
     nranks = L + 1
@@ -72,7 +78,7 @@ def make_case(name):
             f.write(initial_py(w, t1, stepsize))
         with open(os.path.join(d, "Bias.py"), "w") as f:
             f.write(w.bias_source())
-        rec = refharness.run_zand(d, nranks, keep_attempts=keep)
+        rec = refharness.run_zand(d, nranks, keep_attempts=keep, script="nozand" if nonorth else "zand")
     roles, noT_lead = refharness.worker_roles(nranks, A)
     RK_N = 7
     NK = 1

@@ -1,4 +1,5 @@
-"""Run the UNMODIFIED reference ``zand`` in-process to make golden fixtures.
+"""Run the UNMODIFIED reference ``zand`` (or ``nozand``) in-process to make
+golden fixtures.
 
 Fixture generation only: needs the reference checkout (``ZANDPACK_REF``,
 default ``/root/reference``) and is never imported by the GPU tests, ``smoke()``
@@ -95,6 +96,34 @@ class _Comm:
         raise SystemExit(0)
 
 
+class _Win:
+    """``MPI.Win`` shared-memory window: every rank sees rank 0's buffer
+    (what ``nozand`` uses for the global psi and the H/sigma broadcast)."""
+
+    def __init__(self, buf, itemsize):
+        self.buf, self.itemsize = buf, itemsize
+
+    @staticmethod
+    def Allocate_shared(nbytes, itemsize, comm=None):
+        if _tl.rank == 0:
+            _W.slot = bytearray(max(int(nbytes), 16))
+        _W.bar.wait(timeout=600)
+        buf = _W.slot
+        _W.bar.wait(timeout=600)
+        return _Win(buf, itemsize)
+
+    def Shared_query(self, rank):
+        return memoryview(self.buf), self.itemsize
+
+
+class _Dtype:
+    def __init__(self, size):
+        self.size = size
+
+    def Get_size(self):
+        return self.size
+
+
 def _install_stubs():
     if getattr(_install_stubs, "done", False):
         return
@@ -120,6 +149,8 @@ def _install_stubs():
     m = types.ModuleType("mpi4py")
     mpi = types.ModuleType("mpi4py.MPI")
     mpi.COMM_WORLD = _Comm()
+    mpi.Win = _Win
+    mpi.DOUBLE_COMPLEX = _Dtype(16)
     mpi.Finalize = lambda: None
     m.MPI = mpi
     sys.modules["mpi4py"] = m
@@ -162,21 +193,24 @@ class Recorder:
         return a
 
 
-def run_zand(workdir: str, nranks: int, keep_attempts=(0,), keep_states=True):
-    """Execute the reference ``zand`` in ``workdir`` (holding Initial.py/Bias.py)
-    with ``nranks`` thread-ranks; return the Recorder."""
+def run_zand(workdir: str, nranks: int, keep_attempts=(0,), keep_states=True, script="zand"):
+    """Execute the reference ``zand`` (or ``nozand``, ``script="nozand"``) in
+    ``workdir`` (holding Initial.py/Bias.py) with ``nranks`` thread-ranks;
+    return the Recorder."""
     global _W
     os.environ.setdefault("OMP_NUM_THREADS", "1")  # start_print reads it
     mods = reference_modules()
     mf = sys.modules["Zandpack.mpi_funcs"]
+    fsf = sys.modules["Zandpack.func_step_forward"]
     rk = sys.modules["Zandpack.mpi_RK4pars_dev"]
     rec = Recorder(keep_attempts)
     orig = {k: getattr(mf, k) for k in ("TERR2_sig", "TERR2_psi", "TERR2_omg",
                                         "step_fourth_sig", "step_fourth_psi", "step_fourth_omg")}
+    orig_nb = {k: getattr(fsf, "TERR2_%s_nb" % k) for k in ("sig", "psi", "omg")}
     orig_hnew = rk.hnew_func
 
-    def wrap_terr(kind):
-        f = orig["TERR2_" + kind]
+    def wrap_terr(kind, nb=False):
+        f = orig_nb[kind] if nb else orig["TERR2_" + kind]
 
         def w(Y, CT):
             a = rec.next_attempt(kind)
@@ -214,11 +248,12 @@ def run_zand(workdir: str, nranks: int, keep_attempts=(0,), keep_states=True):
 
     for kind in ("sig", "psi", "omg"):
         setattr(mf, "TERR2_" + kind, wrap_terr(kind))
+        setattr(fsf, "TERR2_%s_nb" % kind, wrap_terr(kind, nb=True))
         setattr(mf, "step_fourth_" + kind, wrap_sf(kind))
     rk.hnew_func = hnew
     np.save = save
-    src = open(os.path.join(ZDIR, "mpi", "zand")).read()
-    code = compile(src, os.path.join(ZDIR, "mpi", "zand"), "exec")
+    spath = os.path.join(ZDIR, "mpi", script)
+    code = compile(open(spath).read(), spath, "exec")
     _W = _World(nranks)
     errs = {}
     old = os.getcwd()
@@ -232,7 +267,7 @@ def run_zand(workdir: str, nranks: int, keep_attempts=(0,), keep_states=True):
     def run(r):
         _tl.rank = r
         try:
-            exec(code, {"__name__": "__zand__", "__file__": os.path.join(ZDIR, "mpi", "zand")})
+            exec(code, {"__name__": "__zand__", "__file__": spath})
         except SystemExit:
             pass
         except Exception as e:  # workers end on bcast(None) unpacking
@@ -253,6 +288,8 @@ def run_zand(workdir: str, nranks: int, keep_attempts=(0,), keep_states=True):
         np.save = np_save
         for k, f in orig.items():
             setattr(mf, k, f)
+        for k, f in orig_nb.items():
+            setattr(fsf, "TERR2_%s_nb" % k, f)
         rk.hnew_func = orig_hnew
     rec.stdout = out.getvalue()
     rec.errors = errs

@@ -35,7 +35,7 @@ import numpy as np
 from .constants import HBAR
 from .pade import psd_poles, fermi_expanded
 
-__all__ = ["Workload", "make_workload", "CONFIGS", "bias_value"]
+__all__ = ["Workload", "make_workload", "make_nonorth_workload", "CONFIGS", "bias_value"]
 
 
 # ---------------------------------------------------------------- lattices
@@ -450,3 +450,34 @@ def make_workload(name: str) -> Workload:
     A, coupling, p = fn(rng)
     return Workload(name=name, arrays=A, t0=p["t0"], t1=p["t1"], eps=p["eps"], stepsize=p["stepsize"],
                     hbar=HBAR, bias=p["bias"], hubbard_U=p["hubbard_U"], kT=0.025, coupling=coupling)
+
+
+# ------------------------------------------------- non-orthogonal basis
+def make_nonorth_workload(name: str, s: float = 0.08) -> Workload:
+    """A workload of ``name`` posed in a non-orthogonal basis, for the
+    ``nozand`` path (Zandpack/mpi/nozand:259-320).
+
+    The named workload's H, xi, Ixi are taken as the NON-orthogonal quantities
+    H', xi', Ixi' (H' banded, xi' on the coupling orbitals), with the overlap
+    S = 1 + s * (the bond pattern of H'), real symmetric positive definite.
+    The ``Arrays`` hold them in the Loewdin-orthogonal basis as the reference
+    stores them (``S^(-0.5)`` is the Loewdin factor, Zandpack/Writer.py:83,229):
+    ``H_Ortho = S^-1/2 H' S^-1/2``, ``xi`` rows ``S^-1/2 xi'``, ``Ixi`` rows
+    ``Ixi' S^-1/2``; ``nozand`` maps them back (``S^1/2`` on both sides,
+    ``transform_vec_Tv/vT``).  ``DM_Ortho`` is kept: ``nozand`` starts from
+    ``S^-1/2 DM_Ortho S^-1/2``."""
+    w = make_workload(name)
+    A = dict(w.arrays)
+    Hp = np.asarray(A["H_Ortho"])[0]
+    bonds = (np.abs(Hp) > 0) & ~np.eye(Hp.shape[0], dtype=bool)
+    S = np.eye(Hp.shape[0]) + s * bonds.astype(np.float64)
+    e, V = np.linalg.eigh(S)
+    if e.min() <= 0.1:
+        raise ValueError("overlap not safely positive definite (min eigenvalue %.3g)" % e.min())
+    Sm05 = (V * e ** -0.5) @ V.T
+    Sm05 = (Sm05 + Sm05.T) / 2
+    A["H_Ortho"] = (Sm05 @ Hp @ Sm05)[None].astype(np.complex128)
+    A["xi"] = np.asarray(A["xi"]) @ Sm05.T
+    A["Ixi"] = np.asarray(A["Ixi"]) @ Sm05
+    A["S^(-0.5)"] = Sm05[None].astype(np.complex128)
+    return dataclasses.replace(w, name=w.name + "-nonorth", arrays=A)
