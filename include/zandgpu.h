@@ -111,6 +111,21 @@ int zg_set_dH(zg_traj* t, const double* host);
  * and the graph path refuse to run while one is set. */
 int zg_set_dissipator(zg_traj* t, const double* host);
 
+/* Non-orthogonal basis: the equations of the reference's nozand
+ * (Zandpack/mpi/nozand:259-320, :456-500, :1003-1290) for sigma' =
+ * S^-1/2 sigma S^-1/2 and psi' (rows S^-1/2 psi).  The trajectory's layout
+ * must already hold the nozand constants: H0 = H0' (S^1/2 H_Ortho S^1/2), XI
+ * and IXI from xi' (rows S^1/2 xi) and Ixi' (rows Ixi S^1/2).  Sm1 = S^-1
+ * (n*n complex), C0 = the constant term S^-1 (GL_P xi') of every compact mode
+ * row (N*n complex, computed from the full xi').  Then every stage uses
+ * S^-1 H(t) in place of H(t) (the Hubbard term enters as S^-1 diag(u), an
+ * uploaded dH matrix is multiplied by S^-1 on the device), the lead terms of
+ * sigma become (P S^-1 + h.c.)/hbar, and psi gains S^-1 (Omega xi'/hbar^2)
+ * and C0 in place of the coupling-column terms.  Sm1 = NULL returns to the
+ * orthogonal equations.  The steady-state entry points refuse a trajectory
+ * in this mode. */
+int zg_set_overlap(zg_traj* t, const double* Sm1, const double* C0);
+
 /* k_stage = h f(ts, Y_stage): the stage body of zand (Zandpack/mpi/zand:318-387
  * master, :713-809 worker).  delta[NL] = bias(ts, a); dH_mode selects
  * H(t) = H0 (+ uploaded dH | + hubbard_U*diag(Re sigma_ii - 0.5)).  If

@@ -185,9 +185,11 @@ template <typename T>
 // tmode 0: T interleaved complex (row stride ldT complex); planar (row stride
 // ldT reals, imaginary columns npl further): 1 = T = [Tr | Ti] (real H),
 // 2 = rows [Hr sigma_r | Hr sigma_i] then, npl rows further, [Hi sigma_r | Hi sigma_i]
+// W (may be null; non-orthogonal basis): the n x n product P S^-1, whose
+// (h/hbar^2)(W + W^H) replaces the lead terms (Pc is then not read)
 int launch_sigma_finalize(const RhsDev<T>& d, const StageParams* p, const typename cx<T>::t* Tm, int64_t ldT,
                           const typename cx<T>::t* Pc, const double2* dis, typename cx<T>::t* ksig, cudaStream_t s,
-                          int tmode = 0, int npl = 0);
+                          int tmode = 0, int npl = 0, const typename cx<T>::t* W = nullptr);
 template <typename T>
 int launch_currents(const RhsDev<T>& d, const StageParams* p, const typename cx<T>::t* Pc, double* J, cudaStream_t s);
 template <typename T>
@@ -198,7 +200,18 @@ template <typename T>
 int launch_psi_finalize(const RhsDev<T>& d, const StageParams* p, const typename cx<T>::t* psi,
                         const typename cx<T>::t* psi_lo, int64_t ldpsi, const typename cx<T>::t* R1, int64_t ldR1,
                         const typename cx<T>::t* R2, const typename cx<T>::t* ZA, const typename cx<T>::t* ZB,
-                        typename cx<T>::t* kpsi, cudaStream_t s, int64_t plane = 0, int rmode = 0, int npl = 0);
+                        typename cx<T>::t* kpsi, cudaStream_t s, int64_t plane = 0, int rmode = 0, int npl = 0,
+                        const typename cx<T>::t* R3 = nullptr, const typename cx<T>::t* C0 = nullptr);
+// R3 and C0 (non-orthogonal basis, both N x n): the Omega xi term already
+// multiplied by S^-1 and the constant S^-1 (GL_P xi'), added in place of the
+// coupling-column terms (ZA, ZB and GL_P XI are then not read).
+// Non-orthogonal basis: Qcat (n x L nc) = the two row classes of Pc summed per
+// lead; Zcat (N x L nc) = ZA + ZB per lead; K operands of W = Qcat SmR and
+// R3 = Zcat SmT
+template <typename T>
+int launch_nonorth_gather(const RhsDev<T>& d, const typename cx<T>::t* Pc, const typename cx<T>::t* ZA,
+                          const typename cx<T>::t* ZB, typename cx<T>::t* Qcat, typename cx<T>::t* Zcat,
+                          cudaStream_t s);
 // stationary != 0: writes the Omega of dOmega/dt = 0, i hbar S / (X+ + D_a - X- - D_b),
 // instead of the stage derivative (the input Omega is not read)
 template <typename T>
@@ -209,9 +222,11 @@ int launch_omega(const RhsDev<T>& d, const StageParams* p, const OmTile* tiles, 
 int launch_stationary_scale(int N, int n, const double2* Xp, const int* mode_lead, const double* delta,
                             const double* lam, double hbar, double2* W, cudaStream_t s);
 
-// H(t) = H0 + dH (FP64 path)
+// H(t) = H0 + dH (FP64 path).  Sm1 (may be null; non-orthogonal basis): H0
+// and dH already carry the factor S^-1 and the Hubbard term enters as
+// S^-1 diag(U (sigma_jj - 0.5)), i.e. column j of S^-1 scaled
 int launch_build_ht(int n, const double2* H0, const double2* sig, const double2* dH, int dH_mode, double U,
-                    double2* Ht, cudaStream_t s);
+                    double2* Ht, cudaStream_t s, const double2* Sm1 = nullptr);
 // Mixed path operands of the two tensor-core GEMMs, TF32 hi/lo parts:
 //   Ht (n x np complex = n x 2np real)             A of  T = H(t) sigma
 //   BH (2np x 2np real embedding of H(t)^T form)    B of  R1 = psi H(t)^T
@@ -221,8 +236,10 @@ int launch_build_ht(int n, const double2* H0, const double2* sig, const double2*
 //   BS rows [0, np): Re sigma^T, rows [np, 2 np): Im sigma^T    (K = row of sigma)
 // h_part: 0 = all of Ht, 1 = its diagonal only (off-diagonal entries already
 // hold H0), 2 = leave it; BS is always rebuilt.  Padding is zero.
+// Sm1: as for launch_build_ht (needs h_part 0 with the Hubbard term)
 int launch_build_operands_mixed(int n, int np, const double2* H0, const float2* sig32, const double2* dH, int dH_mode,
-                                double U, int h_part, float* Hth, float* Htl, float* BSh, float* BSl, cudaStream_t s);
+                                double U, int h_part, float* Hth, float* Htl, float* BSh, float* BSl, cudaStream_t s,
+                                const double2* Sm1 = nullptr);
 // Lead currents in FP64 from the FP64 state: J_a = 2 Re sum_{m in a} sum_k psi[m][C_a[k]] IXI[m][k] / hbar^2
 // row ranges per lead: sourced rows [s[a], s[a+1]), free rows [f[a], f[a+1])
 struct CurRows {

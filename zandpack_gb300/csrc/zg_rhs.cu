@@ -353,17 +353,22 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_sigma_finalize(const RhsDev<T> d, const StageParams* __restrict__ pp,
                                                         const typename cx<T>::t* __restrict__ Tm, int64_t ldT,
                                                         const double2* __restrict__ dis,
-                                                        typename cx<T>::t* __restrict__ ksig, int tmode, int npl) {
+                                                        typename cx<T>::t* __restrict__ ksig, int tmode, int npl,
+                                                        const typename cx<T>::t* __restrict__ W) {
   using C = typename cx<T>::t;
-  __shared__ C tile[32][33];  // tile[r][c] = T[j0 + r][i0 + c]
+  __shared__ C tile[32][33];   // tile[r][c] = T[j0 + r][i0 + c]
+  __shared__ C wtile[32][33];  // the same of W (non-orthogonal basis)
   const StageScalars p = load_params(pp);
   const T sc = (T)(p.h / p.hbar);
+  const T fw = (T)(p.h / (p.hbar * p.hbar));
   const int n = d.n;
   const int i0 = blockIdx.y * 32, j0 = blockIdx.x * 32;
   const int tx = threadIdx.x, ty = threadIdx.y;
   for (int r = ty; r < 32; r += 8) {
     const int j = j0 + r, i = i0 + tx;
-    tile[r][tx] = (j < n && i < n) ? load_T<T>(Tm, ldT, tmode, npl, j, i) : czero<T>();
+    const bool in = j < n && i < n;
+    tile[r][tx] = in ? load_T<T>(Tm, ldT, tmode, npl, j, i) : czero<T>();
+    if (W) wtile[r][tx] = in ? W[(int64_t)j * n + i] : czero<T>();
   }
   __syncthreads();
   for (int r = ty; r < 32; r += 8) {
@@ -379,7 +384,13 @@ __global__ void __launch_bounds__(256) k_sigma_finalize(const RhsDev<T> d, const
       v.x -= (T)(p.hbar * q.x);
       v.y -= (T)(p.hbar * q.y);
     }
-    ksig[e] = cscale(v, sc);
+    v = cscale(v, sc);
+    if (W) {  // (h/hbar^2)(P S^-1 + (P S^-1)^H)  (Zandpack/mpi/nozand:489-499)
+      const C wij = W[e], wji = wtile[tx][r];
+      v.x += fw * (wij.x + wji.x);
+      v.y += fw * (wij.y - wji.y);
+    }
+    ksig[e] = v;
   }
 }
 
@@ -419,13 +430,13 @@ __global__ void __launch_bounds__(256) k_sigma_leads(const RhsDev<T> d, const St
 template <typename T>
 int launch_sigma_finalize(const RhsDev<T>& d, const StageParams* p, const typename cx<T>::t* Tm, int64_t ldT,
                           const typename cx<T>::t* Pc, const double2* dis, typename cx<T>::t* ksig, cudaStream_t s,
-                          int tmode, int npl) {
+                          int tmode, int npl, const typename cx<T>::t* W) {
   ZG_REQUIRE(tmode >= 0 && tmode <= 2, "bad T layout %d", tmode);
   const int nb = (d.n + 31) / 32;
-  k_sigma_finalize<T><<<dim3(nb, nb), dim3(32, 8), 0, s>>>(d, p, Tm, ldT, dis, ksig, tmode, npl);
+  k_sigma_finalize<T><<<dim3(nb, nb), dim3(32, 8), 0, s>>>(d, p, Tm, ldT, dis, ksig, tmode, npl, W);
   ZG_CHECK_LAUNCH();
   count_launch();
-  if (d.nu > 0) {
+  if (d.nu > 0 && !W) {
     const int64_t tot = 2 * (int64_t)d.nu * d.n;
     k_sigma_leads<T><<<grid_for(tot, 256, 152 * 8), 256, 0, s>>>(d, p, Pc, ksig);
     ZG_CHECK_LAUNCH();
@@ -532,7 +543,8 @@ __global__ void __launch_bounds__(256) k_psi_finalize(const RhsDev<T> d, const S
                                const typename cx<T>::t* __restrict__ psi_lo, int64_t ldpsi,
                                const typename cx<T>::t* R1, int64_t ldR1, const typename cx<T>::t* __restrict__ R2,
                                const typename cx<T>::t* __restrict__ ZA, const typename cx<T>::t* __restrict__ ZB,
-                               typename cx<T>::t* kpsi, int64_t plane, int rmode, int npl) {
+                               typename cx<T>::t* kpsi, int64_t plane, int rmode, int npl,
+                               const typename cx<T>::t* __restrict__ R3, const typename cx<T>::t* __restrict__ C0) {
   using C = typename cx<T>::t;
   extern __shared__ __align__(16) unsigned char psi_smem[];
   C* sZ = reinterpret_cast<C*>(psi_smem);  // [L][nc]: ZA + ZB of this row
@@ -545,13 +557,15 @@ __global__ void __launch_bounds__(256) k_psi_finalize(const RhsDev<T> d, const S
     const bool src = m < d.Ns;
     const int a = d.mode_lead[m];
     const C glp = d.GLP[m];
-    for (int q = threadIdx.x; q < L * nc; q += blockDim.x) {
-      const int b = q / nc, k = q - b * nc;
-      C z = ZA[((int64_t)b * d.N + m) * nc + k];
-      if (src) z = cadd(z, ZB[((int64_t)b * d.Ns + m) * nc + k]);
-      sZ[q] = z;
+    if (!R3) {
+      for (int q = threadIdx.x; q < L * nc; q += blockDim.x) {
+        const int b = q / nc, k = q - b * nc;
+        C z = ZA[((int64_t)b * d.N + m) * nc + k];
+        if (src) z = cadd(z, ZB[((int64_t)b * d.Ns + m) * nc + k]);
+        sZ[q] = z;
+      }
+      for (int q = threadIdx.x; q < nc; q += blockDim.x) sX[q] = cmul(glp, d.XI[(int64_t)m * nc + q]);
     }
-    for (int q = threadIdx.x; q < nc; q += blockDim.x) sX[q] = cmul(glp, d.XI[(int64_t)m * nc + q]);
     C xp = d.Xp[m];
     xp.x += (T)p.delta[a];
     const C dgp = src ? d.dGP[m] : czero<T>();
@@ -586,11 +600,16 @@ __global__ void __launch_bounds__(256) k_psi_finalize(const RhsDev<T> d, const S
       C v = cscale(r1, ih);
       v = csub(v, cscale(cmul(xp, ps), ih));
       v = cadd(v, cmul(dgp, r2));
-      for (int b = 0; b < L; ++b) {
-        const int k = d.colmap[b * n + i];
-        if (k >= 0) {
-          v = cadd(v, sZ[b * nc + k]);
-          if (b == a) v = cadd(v, sX[k]);
+      if (R3) {  // S^-1 (Omega xi'/hbar^2) + S^-1 (GL_P xi')  (Zandpack/mpi/nozand:1003,1208-1210)
+        const int64_t e = (int64_t)m * n + i;
+        v = cadd(v, cadd(R3[e], C0[e]));
+      } else {
+        for (int b = 0; b < L; ++b) {
+          const int k = d.colmap[b * n + i];
+          if (k >= 0) {
+            v = cadd(v, sZ[b * nc + k]);
+            if (b == a) v = cadd(v, sX[k]);
+          }
         }
       }
       // (-i h) v = (h v.y, -h v.x)
@@ -604,13 +623,55 @@ template <typename T>
 int launch_psi_finalize(const RhsDev<T>& d, const StageParams* p, const typename cx<T>::t* psi,
                         const typename cx<T>::t* psi_lo, int64_t ldpsi, const typename cx<T>::t* R1, int64_t ldR1,
                         const typename cx<T>::t* R2, const typename cx<T>::t* ZA, const typename cx<T>::t* ZB,
-                        typename cx<T>::t* kpsi, cudaStream_t s, int64_t plane, int rmode, int npl) {
+                        typename cx<T>::t* kpsi, cudaStream_t s, int64_t plane, int rmode, int npl,
+                        const typename cx<T>::t* R3, const typename cx<T>::t* C0) {
   if (d.N == 0) return ZG_OK;
   ZG_REQUIRE(rmode >= 0 && rmode <= 2, "bad R1 layout %d", rmode);
-  const size_t smem = (size_t)(d.L + 1) * d.nc * sizeof(typename cx<T>::t);
+  ZG_REQUIRE((R3 == nullptr) == (C0 == nullptr), "R3 and C0 come together");
+  const size_t smem = R3 ? 0 : (size_t)(d.L + 1) * d.nc * sizeof(typename cx<T>::t);
   ZG_REQUIRE(smem <= 48 * 1024, "coupling width too large for the psi finalisation (%zu B)", smem);
   const int grid = d.N < 152 * 8 ? d.N : 152 * 8;
-  k_psi_finalize<T><<<grid, 256, smem, s>>>(d, p, psi, psi_lo, ldpsi, R1, ldR1, R2, ZA, ZB, kpsi, plane, rmode, npl);
+  k_psi_finalize<T><<<grid, 256, smem, s>>>(d, p, psi, psi_lo, ldpsi, R1, ldR1, R2, ZA, ZB, kpsi, plane, rmode, npl,
+                                            R3, C0);
+  ZG_CHECK_LAUNCH();
+  count_launch();
+  return ZG_OK;
+}
+
+// Non-orthogonal basis: K-concatenated operands of the two S^-1 products,
+//   Qcat[i][a nc + k] = Pc[sourced rows of a][i][k] + Pc[free rows of a][i][k]   (n x L nc)
+//   Zcat[m][b nc + k] = ZA[b][m][k] + (m sourced ? ZB[b][m][k] : 0)              (N x L nc)
+template <typename T>
+__global__ void k_nonorth_gather(const RhsDev<T> d, const typename cx<T>::t* __restrict__ Pc,
+                                 const typename cx<T>::t* __restrict__ ZA, const typename cx<T>::t* __restrict__ ZB,
+                                 typename cx<T>::t* __restrict__ Qcat, typename cx<T>::t* __restrict__ Zcat) {
+  using C = typename cx<T>::t;
+  const int64_t W = (int64_t)d.L * d.nc;
+  const int64_t nq = (int64_t)d.n * W, tot = nq + (int64_t)d.N * W;
+  GRID_STRIDE(q, tot) {
+    if (q < nq) {
+      const int64_t i = q / W, r = q - i * W;
+      const int64_t a = r / d.nc, k = r - a * d.nc;
+      const C p0 = Pc[((0 * d.L + a) * d.n + i) * d.nc + k];
+      const C p1 = Pc[((1 * d.L + a) * d.n + i) * d.nc + k];
+      Qcat[q] = cadd(p0, p1);
+    } else {
+      const int64_t q2 = q - nq;
+      const int64_t m = q2 / W, r = q2 - m * W;
+      const int64_t b = r / d.nc, k = r - b * d.nc;
+      C z = ZA[(b * d.N + m) * d.nc + k];
+      if (m < d.Ns) z = cadd(z, ZB[(b * d.Ns + m) * d.nc + k]);
+      Zcat[q2] = z;
+    }
+  }
+}
+
+template <typename T>
+int launch_nonorth_gather(const RhsDev<T>& d, const typename cx<T>::t* Pc, const typename cx<T>::t* ZA,
+                          const typename cx<T>::t* ZB, typename cx<T>::t* Qcat, typename cx<T>::t* Zcat,
+                          cudaStream_t s) {
+  const int64_t tot = ((int64_t)d.n + d.N) * d.L * d.nc;
+  k_nonorth_gather<T><<<grid_for(tot, 256, 152 * 8), 256, 0, s>>>(d, Pc, ZA, ZB, Qcat, Zcat);
   ZG_CHECK_LAUNCH();
   count_launch();
   return ZG_OK;
@@ -776,21 +837,30 @@ int launch_omega(const RhsDev<T>& d, const StageParams* p, const OmTile* tiles, 
 // ========================================================= H(t), operands
 // Ht = H0 + dH, dH = uploaded matrix or U*diag(Re sigma_ii - 0.5)
 __global__ void k_build_ht(int n, const double2* __restrict__ H0, const double2* __restrict__ sig,
-                           const double2* __restrict__ dH, int dH_mode, double U, double2* __restrict__ Ht) {
+                           const double2* __restrict__ dH, int dH_mode, double U, double2* __restrict__ Ht,
+                           const double2* __restrict__ Sm1) {
   const int64_t nn = (int64_t)n * n;
   GRID_STRIDE(e, nn) {
     double2 v = H0[e];
     if (dH_mode == ZG_DH_MATRIX) v = cadd(v, dH[e]);
     const int i = (int)(e / n), j = (int)(e % n);
-    if (dH_mode == ZG_DH_HUBBARD && i == j) v.x += U * (sig[e].x - 0.5);
+    if (dH_mode == ZG_DH_HUBBARD) {
+      if (Sm1) {  // S^-1 diag(u): column j of S^-1 times u_j (Zandpack/mpi/nozand:1075-1083)
+        const double u = U * (sig[(int64_t)j * n + j].x - 0.5);
+        v.x += Sm1[e].x * u;
+        v.y += Sm1[e].y * u;
+      } else if (i == j) {
+        v.x += U * (sig[e].x - 0.5);
+      }
+    }
     Ht[e] = v;
   }
 }
 
 int launch_build_ht(int n, const double2* H0, const double2* sig, const double2* dH, int dH_mode, double U,
-                    double2* Ht, cudaStream_t s) {
+                    double2* Ht, cudaStream_t s, const double2* Sm1) {
   int64_t nn = (int64_t)n * n;
-  k_build_ht<<<grid_for(nn, 256, 152 * 8), 256, 0, s>>>(n, H0, sig, dH, dH_mode, U, Ht);
+  k_build_ht<<<grid_for(nn, 256, 152 * 8), 256, 0, s>>>(n, H0, sig, dH, dH_mode, U, Ht, Sm1);
   ZG_CHECK_LAUNCH();
   count_launch();
   return ZG_OK;
@@ -814,7 +884,7 @@ __device__ __forceinline__ void split_tf32_r(float v, float& hi, float& lo) {
 __global__ void k_build_operands_mixed(int n, int np, const double2* __restrict__ H0, const float2* __restrict__ sig32,
                                        const double2* __restrict__ dH, int dH_mode, double U, int h_part,
                                        float* __restrict__ Hth, float* __restrict__ Htl, float* __restrict__ BSh,
-                                       float* __restrict__ BSl) {
+                                       float* __restrict__ BSl, const double2* __restrict__ Sm1) {
   const int64_t nn = (int64_t)np * np;
   const int64_t tot = nn + (h_part == 1 ? np : 0);
   GRID_STRIDE(q, tot) {
@@ -828,7 +898,16 @@ __global__ void k_build_operands_mixed(int n, int np, const double2* __restrict_
       if (r < n && c < n) {
         double2 v = H0[(int64_t)r * n + c];
         if (dH_mode == ZG_DH_MATRIX) v = cadd(v, dH[(int64_t)r * n + c]);
-        if (dH_mode == ZG_DH_HUBBARD && r == c) v.x += U * ((double)sig32[(int64_t)r * n + r].x - 0.5);
+        if (dH_mode == ZG_DH_HUBBARD) {
+          if (Sm1) {  // column c of S^-1 scaled by the Hubbard term of orbital c
+            const double u = U * ((double)sig32[(int64_t)c * n + c].x - 0.5);
+            const double2 sv = Sm1[(int64_t)r * n + c];
+            v.x += sv.x * u;
+            v.y += sv.y * u;
+          } else if (r == c) {
+            v.x += U * ((double)sig32[(int64_t)r * n + r].x - 0.5);
+          }
+        }
         hr = (float)v.x;
         hi = (float)v.y;
       }
@@ -857,11 +936,13 @@ __global__ void k_build_operands_mixed(int n, int np, const double2* __restrict_
 }
 
 int launch_build_operands_mixed(int n, int np, const double2* H0, const float2* sig32, const double2* dH, int dH_mode,
-                                double U, int h_part, float* Hth, float* Htl, float* BSh, float* BSl, cudaStream_t s) {
+                                double U, int h_part, float* Hth, float* Htl, float* BSh, float* BSl, cudaStream_t s,
+                                const double2* Sm1) {
   ZG_REQUIRE(h_part >= 0 && h_part <= 2, "bad operand part %d", h_part);
+  ZG_REQUIRE(!(Sm1 && dH_mode == ZG_DH_HUBBARD && h_part == 1), "the overlap's Hubbard term changes every entry");
   const int64_t tot = (int64_t)np * np + (h_part == 1 ? np : 0);
   k_build_operands_mixed<<<grid_for(tot, 256, 152 * 16), 256, 0, s>>>(n, np, H0, sig32, dH, dH_mode, U, h_part, Hth,
-                                                                      Htl, BSh, BSl);
+                                                                      Htl, BSh, BSl, Sm1);
   ZG_CHECK_LAUNCH();
   count_launch();
   return ZG_OK;
@@ -900,11 +981,15 @@ int launch_stationary_scale(int N, int n, const double2* Xp, const int* mode_lea
   template int launch_gathers<T>(const RhsDev<T>&, const cx<T>::t*, const cx<T>::t*, const cx<T>::t*, int64_t,      \
                                  cx<T>::t*, cx<T>::t*, cudaStream_t, int64_t);                                        \
   template int launch_sigma_finalize<T>(const RhsDev<T>&, const StageParams*, const cx<T>::t*, int64_t,              \
-                                        const cx<T>::t*, const double2*, cx<T>::t*, cudaStream_t, int, int);          \
+                                        const cx<T>::t*, const double2*, cx<T>::t*, cudaStream_t, int, int,           \
+                                        const cx<T>::t*);                                                            \
   template int launch_currents<T>(const RhsDev<T>&, const StageParams*, const cx<T>::t*, double*, cudaStream_t);     \
   template int launch_psi_finalize<T>(const RhsDev<T>&, const StageParams*, const cx<T>::t*, const cx<T>::t*,        \
                                       int64_t, const cx<T>::t*, int64_t, const cx<T>::t*, const cx<T>::t*,           \
-                                      const cx<T>::t*, cx<T>::t*, cudaStream_t, int64_t, int, int);                  \
+                                      const cx<T>::t*, cx<T>::t*, cudaStream_t, int64_t, int, int, const cx<T>::t*,  \
+                                      const cx<T>::t*);                                                              \
+  template int launch_nonorth_gather<T>(const RhsDev<T>&, const cx<T>::t*, const cx<T>::t*, const cx<T>::t*,         \
+                                        cx<T>::t*, cx<T>::t*, cudaStream_t);                                         \
   template int launch_omega<T>(const RhsDev<T>&, const StageParams*, const OmTile*, int, const cx<T>::t*,            \
                                const cx<T>::t*, const cx<T>::t*, cx<T>::t*, cx<T>::t*, cudaStream_t, int);
 ZG_INST(double)

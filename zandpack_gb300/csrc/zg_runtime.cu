@@ -179,6 +179,18 @@ struct zg_traj {
   int st_mode = ZG_DH_NONE;
   double st_U = 0.0;
   bool st_ready = false;
+  // non-orthogonal basis (zg_set_overlap): S^-1, S^-1 H0, S^-1 dH, the
+  // S^-1 rows/columns at the coupling orbitals (K operands of the two S^-1
+  // products), the constant psi term, and the products' scratch
+  bool nonorth = false;
+  bool h0_real_orth = false;  // H0 itself is real (h0_real then also covers S^-1)
+  bool sm1_real = false;
+  bool dH_raw_real = false;
+  std::vector<int> lead_cols_h, colmap_h;
+  double2 *Sm1 = nullptr, *Hn0 = nullptr, *dHn = nullptr, *SmR = nullptr, *SmT = nullptr, *C0 = nullptr;
+  double2 *Qcat = nullptr, *Wn = nullptr, *Zcat = nullptr, *R3 = nullptr;
+  float2 *SmR32 = nullptr, *SmT32 = nullptr, *C0_32 = nullptr, *Qcat32 = nullptr, *Wn32 = nullptr,
+         *Zcat32 = nullptr, *R3_32 = nullptr;
   // ---- mixed path
   int np = 0;  // n padded to a multiple of 16
   MixedLayout ml;
@@ -366,7 +378,9 @@ static void free_traj(zg_traj* t) {
                   t->XI32, t->XIS32, t->IXI32, t->U32, t->V32, t->y32, t->K32, t->stage32, t->Hth, t->Htl,
                   t->BSh, t->BSl, t->T32, t->R1p, t->Pc32, t->sigC32, t->G32, t->R2_32, t->ZA32, t->ZB32,
                   t->conv64, t->sig64, t->tc_err, t->ws64, t->ws32, t->dis, t->ucols, t->umap,
-                  t->st_V, t->st_Vc, t->st_W, t->st_lam, t->st_delta};
+                  t->st_V, t->st_Vc, t->st_W, t->st_lam, t->st_delta,
+                  t->Sm1, t->Hn0, t->dHn, t->SmR, t->SmT, t->C0, t->Qcat, t->Wn, t->Zcat, t->R3,
+                  t->SmR32, t->SmT32, t->C0_32, t->Qcat32, t->Wn32, t->Zcat32, t->R3_32};
   for (void* p : ptrs) dfree(t, p);
   if (t->stream2) {
     cudaStreamSynchronize(t->stream2);
@@ -476,6 +490,7 @@ static int create_mixed(zg_traj* t, const zg_layout* Lo, const std::vector<doubl
     bool real = true;
     for (int64_t e = 0; e < n * n && real; ++e) real = Lo->H0[2 * e + 1] == 0.0;
     t->h0_real = real;
+    t->h0_real_orth = real;
   }
   cudaStream_t s = t->stream;
   // host copies stay alive until the stream synchronisation at the end
@@ -610,6 +625,8 @@ int zg_traj_create(int device, const zg_layout* Lo, int precision, zg_traj** out
   ZG_STEP(upload<int>(t->mode_lead, Lo->mode_lead, N, t->stream));
   ZG_STEP(upload<int>(t->lead_cols, Lo->lead_cols, L * nc, t->stream));
   ZG_STEP(upload<int>(t->colmap, Lo->colmap, L * n, t->stream));
+  t->lead_cols_h.assign(Lo->lead_cols, Lo->lead_cols + L * nc);
+  t->colmap_h.assign(Lo->colmap, Lo->colmap + L * n);
   // orbitals that are a coupling column of some lead: the only rows and
   // columns where the lead terms of the sigma equation are nonzero
   std::vector<int> ucols_h, umap_h(n, -1);
@@ -822,16 +839,20 @@ int zg_get_stage_sigma(zg_traj* t, double* host) {
   return ZG_OK;
 }
 
+static int sm1_times(zg_traj* t, const double2* X, double2* out);
+
 int zg_set_dH(zg_traj* t, const double* host) {
   ZG_REQUIRE(t && host, "null argument");
   ZG_CHECK_CUDA(cudaSetDevice(t->dev));
   {
     bool real = true;
     for (int64_t e = 0; e < (int64_t)t->n * t->n && real; ++e) real = host[2 * e + 1] == 0.0;
-    t->dH_real = real;
+    t->dH_raw_real = real;
+    t->dH_real = real && (!t->nonorth || t->sm1_real);
   }
   ZG_CHECK_CUDA(cudaMemcpyAsync(t->dH, host, (size_t)t->n * t->n * sizeof(double2), cudaMemcpyHostToDevice,
                                 t->stream));
+  if (t->nonorth) ZG_TRY(sm1_times(t, t->dH, t->dHn));  // the stages add S^-1 dH
   ZG_CHECK_CUDA(cudaStreamSynchronize(t->stream));
   t->dH_set = true;
   return ZG_OK;
@@ -928,7 +949,10 @@ static int rhs_f64(zg_traj* t, int stage, const StageParams* p, int dH_mode, dou
   const int64_t n = t->n, N = t->N, Ns = t->Ns, Nf = t->Nf, L = t->L, nc = t->nc;
   if (!plan_only) {
     prof_begin(t, ZG_PROF_PREP);
-    ZG_TRY(launch_build_ht((int)n, t->H0, sig, t->dH, dH_mode, hubbard_U, t->Ht, s));
+    if (t->nonorth)  // S^-1 H(t) (Zandpack/mpi/nozand:1075-1085)
+      ZG_TRY(launch_build_ht((int)n, t->Hn0, sig, t->dHn, dH_mode, hubbard_U, t->Ht, s, t->Sm1));
+    else
+      ZG_TRY(launch_build_ht((int)n, t->H0, sig, t->dH, dH_mode, hubbard_U, t->Ht, s));
     ZG_TRY(launch_gathers<double>(d, sig, psi, nullptr, n, t->sigC, t->G, s));
     prof_end(t, ZG_PROF_PREP);
   }
@@ -957,15 +981,31 @@ static int rhs_f64(zg_traj* t, int stage, const StageParams* p, int dH_mode, dou
       gemm_prob_f64(probs, in + t->off_omB + (r0 - Ns), Nf, 0, t->XIS + r0 * nc, nc, 0, t->ZB + a * Ns * nc, nc,
                     (int)Ns, (int)nc, (int)(r1 - r0));
   }
-  if (plan_only) return run_batches<double>(t, probs, &t->ws64, &t->ws64_cap, s, true);
+  // non-orthogonal basis: W = P S^-1 and R3 = S^-1 (Omega xi'/hbar^2), K = L nc
+  std::vector<GemmProb<double>> probs2;
+  if (t->nonorth) {
+    const int64_t K = L * nc;
+    gemm_prob_f64(probs2, t->Qcat, K, 0, t->SmR, n, 0, t->Wn, n, (int)n, (int)n, (int)K);
+    gemm_prob_f64(probs2, t->Zcat, K, 0, t->SmT, n, 0, t->R3, n, (int)N, (int)n, (int)K);
+  }
+  if (plan_only) {
+    ZG_TRY(run_batches<double>(t, probs, &t->ws64, &t->ws64_cap, s, true));
+    return run_batches<double>(t, probs2, &t->ws64, &t->ws64_cap, s, true);
+  }
   prof_begin(t, ZG_PROF_GEMM);
   ZG_TRY(run_batches<double>(t, probs, &t->ws64, &t->ws64_cap, s, false));
+  if (t->nonorth) {
+    ZG_TRY(launch_nonorth_gather<double>(d, t->Pc, t->ZA, t->ZB, t->Qcat, t->Zcat, s));
+    ZG_TRY(run_batches<double>(t, probs2, &t->ws64, &t->ws64_cap, s, false));
+  }
   prof_end(t, ZG_PROF_GEMM);
   prof_begin(t, ZG_PROF_FINAL);
-  ZG_TRY(launch_sigma_finalize<double>(d, p, t->T, n, t->Pc, t->dis_on ? t->dis : nullptr, out, s));
+  ZG_TRY(launch_sigma_finalize<double>(d, p, t->T, n, t->Pc, t->dis_on ? t->dis : nullptr, out, s, 0, 0,
+                                       t->nonorth ? t->Wn : nullptr));
   if (want_J) ZG_TRY(launch_currents<double>(d, p, t->Pc, t->J, s));
   ZG_TRY(launch_psi_finalize<double>(d, p, psi, nullptr, n, out + t->off_psi, n, t->R2, t->ZA, t->ZB,
-                                     out + t->off_psi, s));
+                                     out + t->off_psi, s, 0, 0, 0, t->nonorth ? t->R3 : nullptr,
+                                     t->nonorth ? t->C0 : nullptr));
   prof_end(t, ZG_PROF_FINAL);
   prof_begin(t, ZG_PROF_OMEGA);
   ZG_TRY(launch_omega<double>(d, p, t->tiles, t->ntiles, t->G, in + t->off_omA, in + t->off_omB, out + t->off_omA,
@@ -994,7 +1034,8 @@ static int rhs_mixed(zg_traj* t, int stage, const StageParams* p, int dH_mode, d
     prof_begin(t, ZG_PROF_PREP);
     // H(t) = H0 + dH changes only on the diagonal unless dH is a full matrix
     int h_part = 0;
-    if (dH_mode == ZG_DH_MATRIX) {
+    if (dH_mode == ZG_DH_MATRIX || (t->nonorth && dH_mode == ZG_DH_HUBBARD)) {
+      // a full matrix, or S^-1 diag(u): every entry changes
       t->h_offdiag_ready = false;
     } else if (t->h_offdiag_ready) {
       h_part = dH_mode == ZG_DH_HUBBARD || t->h_diag_mode != dH_mode ? 1 : 2;
@@ -1002,8 +1043,9 @@ static int rhs_mixed(zg_traj* t, int stage, const StageParams* p, int dH_mode, d
       t->h_offdiag_ready = true;
     }
     t->h_diag_mode = dH_mode;
-    ZG_TRY(launch_build_operands_mixed((int)n, (int)np, t->H0, sig, t->dH, dH_mode, hubbard_U, h_part, t->Hth,
-                                       t->Htl, t->BSh, t->BSl, s));
+    ZG_TRY(launch_build_operands_mixed((int)n, (int)np, t->nonorth ? t->Hn0 : t->H0, sig, t->nonorth ? t->dHn : t->dH,
+                                       dH_mode, hubbard_U, h_part, t->Hth, t->Htl, t->BSh, t->BSl, s,
+                                       t->nonorth ? t->Sm1 : nullptr));
     ZG_TRY(launch_gathers<float>(d, sig, (const float2*)psih_f, (const float2*)psil_f, np, t->sigC32, t->G32, s,
                                  ml.plane));
     prof_end(t, ZG_PROF_PREP);
@@ -1046,15 +1088,28 @@ static int rhs_mixed(zg_traj* t, int stage, const StageParams* p, int dH_mode, d
       gemm_prob_f32(probs, omB + (r0 - Ns), nullptr, Nf, 0, t->XIS32 + r0 * nc, nc, 0, t->ZB32 + a * Ns * nc, nc,
                     (int)Ns, (int)nc, (int)(r1 - r0));
   }
-  if (plan_only) return run_batches<float>(t, probs, &t->ws32, &t->ws32_cap, s, true);
+  std::vector<GemmProb<float>> probs2;
+  if (t->nonorth) {
+    const int64_t K = L * nc;
+    gemm_prob_f32(probs2, t->Qcat32, nullptr, K, 0, t->SmR32, n, 0, t->Wn32, n, (int)n, (int)n, (int)K);
+    gemm_prob_f32(probs2, t->Zcat32, nullptr, K, 0, t->SmT32, n, 0, t->R3_32, n, (int)N, (int)n, (int)K);
+  }
+  if (plan_only) {
+    ZG_TRY(run_batches<float>(t, probs, &t->ws32, &t->ws32_cap, s, true));
+    return run_batches<float>(t, probs2, &t->ws32, &t->ws32_cap, s, true);
+  }
   prof_begin(t, ZG_PROF_SMALL);
   ZG_TRY(run_batches<float>(t, probs, &t->ws32, &t->ws32_cap, s, false));
+  if (t->nonorth) {
+    ZG_TRY(launch_nonorth_gather<float>(d, t->Pc32, t->ZA32, t->ZB32, t->Qcat32, t->Zcat32, s));
+    ZG_TRY(run_batches<float>(t, probs2, &t->ws32, &t->ws32_cap, s, false));
+  }
   prof_end(t, ZG_PROF_SMALL);
   // join: the finalisation needs T; the next stage overwrites what Omega reads
   ZG_CHECK_CUDA(cudaStreamWaitEvent(s, t->ev_join, 0));
   prof_begin(t, ZG_PROF_FINAL);
   ZG_TRY(launch_sigma_finalize<float>(d, p, t->T32, 2 * np, t->Pc32, t->dis_on ? t->dis : nullptr, out, s,
-                                      hreal ? 1 : 2, (int)np));
+                                      hreal ? 1 : 2, (int)np, t->nonorth ? t->Wn32 : nullptr));
   if (want_J) {
     if (stage == 0)  // the stage-0 input is y itself: currents from the FP64 state
     {
@@ -1068,7 +1123,7 @@ static int rhs_mixed(zg_traj* t, int stage, const StageParams* p, int dH_mode, d
   }
   ZG_TRY(launch_psi_finalize<float>(d, p, (const float2*)psih_f, (const float2*)psil_f, np, t->R1p, 2 * np,
                                     t->R2_32, t->ZA32, t->ZB32, out + t->off_psi, s, ml.plane, hreal ? 1 : 2,
-                                    (int)np));
+                                    (int)np, t->nonorth ? t->R3_32 : nullptr, t->nonorth ? t->C0_32 : nullptr));
   prof_end(t, ZG_PROF_FINAL);
   return ZG_OK;
 }
@@ -1167,6 +1222,85 @@ static int presize_workspaces(zg_traj* t) {
   return rhs_mixed(t, 0, t->d_params, ZG_DH_NONE, 0.0, false, true);
 }
 
+// out = S^-1 X (n x n, FP64, on the trajectory's stream)
+static int sm1_times(zg_traj* t, const double2* X, double2* out) {
+  std::vector<GemmProb<double>> pr;
+  const int n = t->n;
+  gemm_prob_f64(pr, t->Sm1, n, 0, X, n, 0, out, n, n, n, n);
+  return run_batches<double>(t, pr, &t->ws64, &t->ws64_cap, t->stream, false);
+}
+
+extern "C" int zg_set_overlap(zg_traj* t, const double* Sm1, const double* C0) {
+  ZG_REQUIRE(t, "null argument");
+  ZG_REQUIRE(!Sm1 || C0, "the constant term C0 comes with S^-1");
+  ZG_CHECK_CUDA(cudaSetDevice(t->dev));
+  ZG_CHECK_CUDA(cudaStreamSynchronize(t->stream));
+  drop_graph(t);  // captured stages hold the old operands
+  t->h_offdiag_ready = false;
+  if (!Sm1) {
+    t->nonorth = false;
+    t->h0_real = t->h0_real_orth;
+    t->dH_real = t->dH_raw_real;
+    return ZG_OK;
+  }
+  const int64_t n = t->n, N = t->N, L = t->L, nc = t->nc, K = L * nc;
+  const double2* S = (const double2*)Sm1;
+  bool real = true;
+  for (int64_t e = 0; e < n * n && real; ++e) real = S[e].y == 0.0;
+  t->sm1_real = real;
+  // S^-1 rows (SmR) and columns (SmT) at the coupling orbitals; padding rows zero
+  std::vector<double2> R((size_t)(K * n), make_double2(0, 0)), Tt((size_t)(K * n), make_double2(0, 0));
+  for (int64_t a = 0; a < L; ++a)
+    for (int64_t k = 0; k < nc; ++k) {
+      const int c = t->lead_cols_h[a * nc + k];
+      if (t->colmap_h[a * n + c] != k) continue;
+      for (int64_t j = 0; j < n; ++j) {
+        R[(a * nc + k) * n + j] = S[c * n + j];
+        Tt[(a * nc + k) * n + j] = S[j * n + c];
+      }
+    }
+  if (!t->Sm1) {
+    ZG_TRY(dalloc(t, &t->Sm1, n * n));
+    ZG_TRY(dalloc(t, &t->Hn0, n * n));
+    ZG_TRY(dalloc(t, &t->dHn, n * n));
+    ZG_TRY(dalloc(t, &t->C0, N * n));
+    if (t->precision == ZG_PREC_F64) {
+      ZG_TRY(dalloc(t, &t->SmR, K * n)); ZG_TRY(dalloc(t, &t->SmT, K * n));
+      ZG_TRY(dalloc(t, &t->Qcat, n * K)); ZG_TRY(dalloc(t, &t->Wn, n * n));
+      ZG_TRY(dalloc(t, &t->Zcat, N * K)); ZG_TRY(dalloc(t, &t->R3, N * n));
+    } else {
+      ZG_TRY(dalloc(t, &t->SmR32, K * n)); ZG_TRY(dalloc(t, &t->SmT32, K * n)); ZG_TRY(dalloc(t, &t->C0_32, N * n));
+      ZG_TRY(dalloc(t, &t->Qcat32, n * K)); ZG_TRY(dalloc(t, &t->Wn32, n * n));
+      ZG_TRY(dalloc(t, &t->Zcat32, N * K)); ZG_TRY(dalloc(t, &t->R3_32, N * n));
+    }
+  }
+  cudaStream_t s = t->stream;
+  ZG_TRY(upload<double2>(t->Sm1, Sm1, n * n, s));
+  ZG_TRY(upload<double2>(t->C0, C0, N * n, s));
+  std::vector<float2> R32, T32, C32;
+  if (t->precision == ZG_PREC_F64) {
+    ZG_TRY(upload<double2>(t->SmR, R.data(), K * n, s));
+    ZG_TRY(upload<double2>(t->SmT, Tt.data(), K * n, s));
+  } else {
+    R32.resize(K * n); T32.resize(K * n); C32.resize(N * n);
+    to_f32(R.data(), R32.data(), K * n);
+    to_f32(Tt.data(), T32.data(), K * n);
+    to_f32((const double2*)C0, C32.data(), N * n);
+    ZG_TRY(upload<float2>(t->SmR32, R32.data(), K * n, s));
+    ZG_TRY(upload<float2>(t->SmT32, T32.data(), K * n, s));
+    ZG_TRY(upload<float2>(t->C0_32, C32.data(), N * n, s));
+  }
+  ZG_TRY(sm1_times(t, t->H0, t->Hn0));
+  if (t->dH_set) ZG_TRY(sm1_times(t, t->dH, t->dHn));
+  t->nonorth = true;
+  t->h0_real = t->h0_real_orth && t->sm1_real;
+  t->dH_real = t->dH_raw_real && t->sm1_real;
+  ZG_TRY(presize_workspaces(t));
+  // the host vectors above must outlive their asynchronous copies
+  ZG_CHECK_CUDA(cudaStreamSynchronize(s));
+  return ZG_OK;
+}
+
 // One attempt with the controller on the device, enqueued without host syncs
 // (the body of the attempt graph): stages, error norm, control, gated update,
 // advance, then the controller and the tensor-core error flag to pinned memory.
@@ -1194,8 +1328,9 @@ static int enqueue_attempt_device(zg_traj* t) {
 // host-driven stage with a full dH matrix may have overwritten it).
 static int ensure_h_operands(zg_traj* t) {
   if (t->precision != ZG_PREC_MIXED || t->h_offdiag_ready) return ZG_OK;
-  ZG_TRY(launch_build_operands_mixed(t->n, t->np, t->H0, t->stage32, t->dH, t->g_dH_mode, t->g_U, 0, t->Hth, t->Htl,
-                                     t->BSh, t->BSl, t->stream));
+  ZG_TRY(launch_build_operands_mixed(t->n, t->np, t->nonorth ? t->Hn0 : t->H0, t->stage32,
+                                     t->nonorth ? t->dHn : t->dH, t->g_dH_mode, t->g_U, 0, t->Hth, t->Htl, t->BSh,
+                                     t->BSl, t->stream, t->nonorth ? t->Sm1 : nullptr));
   t->h_offdiag_ready = true;
   t->h_diag_mode = t->g_dH_mode;
   return ZG_OK;
@@ -1389,6 +1524,7 @@ int zg_stationary_setup(zg_traj* t, double ts, const double* delta, int dH_mode,
                         const double* lam) {
   ZG_REQUIRE(t && delta && V && lam, "null argument");
   ZG_REQUIRE(t->precision == ZG_PREC_F64, "the steady state is solved on an FP64 trajectory");
+  ZG_REQUIRE(!t->nonorth, "the steady state is solved in the orthogonal basis (no overlap set)");
   ZG_REQUIRE(dH_mode == ZG_DH_NONE || dH_mode == ZG_DH_HUBBARD || (dH_mode == ZG_DH_MATRIX && t->dH_set),
              "bad dH mode %d (ZG_DH_MATRIX needs zg_set_dH first)", dH_mode);
   ZG_CHECK_CUDA(cudaSetDevice(t->dev));

@@ -34,7 +34,15 @@ class Trajectory:
     """One AME propagation resident on the GPU."""
 
     def __init__(self, arrays, hbar, precision="f64", device=0, psi0=None, omg0=None,
-                 dot_prod_zero_tol=1e-10, layout: Optional[CompactLayout] = None):
+                 dot_prod_zero_tol=1e-10, layout: Optional[CompactLayout] = None, nonorth: bool = False):
+        """``nonorth``: propagate in the non-orthogonal basis of ``arrays['S^(-0.5)']``
+        as the reference's ``nozand`` does; states (``set_y``, ``get_y``) are then
+        sigma' and psi' (``NonorthBasis.sigma``/``psi`` map orthogonal ones)."""
+        self.basis = None
+        if nonorth:
+            from .nonorth import NonorthBasis
+            self.basis = NonorthBasis(arrays, dot_prod_zero_tol)
+            arrays = self.basis.arrays
         L = layout if layout is not None else CompactLayout(arrays, hbar, dot_prod_zero_tol, psi0=psi0, omg0=omg0)
         self.layout = L
         self.precision = precision
@@ -65,6 +73,10 @@ class Trajectory:
         self._sig = np.empty((L.n, L.n), np.complex128)
         self._delta = np.zeros(_lib.ZG_MAX_LEADS, np.float64)
         self._J = np.zeros(L.NL, np.float64)
+        if self.basis is not None:
+            Sm1 = np.ascontiguousarray(self.basis.Sm1[0])
+            C0 = self.basis.constant_term(L)
+            check(lib().zg_set_overlap(self._h, _ptr(Sm1), _ptr(C0)))
 
     def close(self):
         if getattr(self, "_h", None):
@@ -220,14 +232,17 @@ class Propagator:
     receives sigma with the k axis, shape (1, n, n), and may return 0.0.
     ``hubbard_U`` selects the built-in density-dependent term
     U * diag(Re sigma_ii - 0.5) evaluated on the device instead of ``dH``.
+    ``nonorth=True`` runs the reference's ``nozand`` instead (non-orthogonal
+    basis of ``arrays['S^(-0.5)']``): the state, the callbacks' sigma and the
+    returned sigma are then sigma' (start from ``traj.basis.sigma(DM_Ortho)``).
     """
 
     def __init__(self, arrays, hbar, bias: Callable, dH: Optional[Callable] = None,
                  dissipator: Optional[Callable] = None, hubbard_U: Optional[float] = None,
                  precision="f64", device=0, tableau: Tableau = DOP54, psi0=None, omg0=None,
-                 dot_prod_zero_tol=1e-10, dH_depends_on_sigma=True):
+                 dot_prod_zero_tol=1e-10, dH_depends_on_sigma=True, nonorth: bool = False):
         self.traj = Trajectory(arrays, hbar, precision, device, psi0=psi0, omg0=omg0,
-                               dot_prod_zero_tol=dot_prod_zero_tol)
+                               dot_prod_zero_tol=dot_prod_zero_tol, nonorth=nonorth)
         if tableau is not DOP54:
             self.traj.set_tableau(tableau)
         self.tab = tableau
