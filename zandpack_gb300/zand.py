@@ -33,6 +33,17 @@ The controller is the reference's: seven DOP54 stages per attempt, accept
 iff TE < eps, h <- 0.9 h (eps/TE)^(1/5) after every attempt, time advanced by
 the step size proposed for the next step, currents from stage 0 of each
 accepted attempt.
+
+``ZandRun(nonorth=True)`` (``python -m zandpack_gb300.nozand Dir=...``) is the
+reference's ``nozand`` (Zandpack/mpi/nozand): the same run directory plus
+``Arrays/S^(-0.5)``; it propagates sigma' = S^-1/2 sigma S^-1/2, starts from
+S^-1/2 DM_Ortho S^-1/2 (:306), saves sigma' (``DM*``, ``last_sig``) and
+``PIa`` without the conjugate term (:120-140), and honours nozand's
+``Initial.py`` flags (:84-95, :547-577): ``compress_mat`` (``.npz`` archives for
+``DM``/``PIa``), ``dm_triu_only`` (strict lower triangle zeroed, with
+``compress_mat``) and ``dm_occ_only`` (entries where |S| <= 1e-6 zeroed).
+``last_psi`` is loaded (``LoadFromFull``) and written in the orthogonal basis,
+as ``psinought`` writes it: rows S^-1/2 psi on load (:722), S^1/2 psi' on save.
 """
 from __future__ import annotations
 
@@ -104,8 +115,9 @@ def parse_dir(args):
 class ZandRun:
     """One propagation as ``zand`` runs it, driven through the GPU engine."""
 
-    def __init__(self, run_dir=None, precision=None, device=0, log=print):
+    def __init__(self, run_dir=None, precision=None, device=0, log=print, nonorth=False):
         _install_standins()
+        self.nonorth = bool(nonorth)
         if run_dir is not None:
             os.chdir(run_dir)
         cwd = os.getcwd()
@@ -134,8 +146,12 @@ class ZandRun:
         self.checkpoints = cps[cps < self.t1]
         self.checkpoint_done = np.zeros(len(self.checkpoints), dtype=int)
         self.save_checkpoints = bool(getattr(I, "save_checkpoints", False))
-        from .arrays_io import read_arrays
-        self.arrays = read_arrays(I.Arrs)
+        from .arrays_io import REQUIRED_KEYS, read_arrays
+        self.arrays = read_arrays(I.Arrs, REQUIRED_KEYS + (("S^(-0.5)",) if self.nonorth else ()))
+        # output flags that only nozand reads (Zandpack/mpi/nozand:84-95)
+        self.compress_mat = bool(getattr(I, "compress_mat", False)) and self.nonorth
+        self.dm_triu_only = bool(getattr(I, "dm_triu_only", False)) and self.nonorth
+        self.dm_occ_only = bool(getattr(I, "dm_occ_only", False)) and self.nonorth
 
     # ---------------------------------------------------------------- run
     def run(self):
@@ -148,7 +164,10 @@ class ZandRun:
             if f[0:2] == "DM":
                 os.remove(save + f)
         t0, h = self.t0, self.stepsize
+        Sm05 = np.asarray(self.arrays["S^(-0.5)"], np.complex128) if self.nonorth else None
         sig0 = self.arrays["DM_Ortho"]
+        if self.nonorth:
+            sig0 = Sm05 @ np.asarray(sig0, np.complex128) @ Sm05  # Zandpack/mpi/nozand:306
         psi0 = omg0 = None
         if self.usesave:
             try:
@@ -163,19 +182,25 @@ class ZandRun:
             if self.LoadFromFull:
                 psi0 = np.load(save + "last_psi.npy")
                 omg0 = np.load(save + "last_omg.npy")
+                if self.nonorth:  # rows S^-1/2 psi (Zandpack/mpi/nozand:722)
+                    psi0 = np.asarray(psi0, np.complex128) @ Sm05[0].T
         dh_dev = getattr(B, "dH_device", None)
         hub = float(dh_dev["U"]) if isinstance(dh_dev, dict) and dh_dev.get("kind") == "hubbard" else None
         diss = getattr(B, "dissipator", None)
         pr = Propagator(self.arrays, self.hbar, B.bias, dH=None if hub is not None else B.dH,
                         dissipator=diss, hubbard_U=hub, precision=self.precision, device=self.device,
-                        tableau=selected(), psi0=psi0, omg0=omg0)
+                        tableau=selected(), psi0=psi0, omg0=omg0, nonorth=self.nonorth)
         self.prop = pr
         tr = pr.traj
         L = tr.layout
         z = L.unpack(np.zeros(L.size, complex))
         pr.set_state(sig0, z[1] if psi0 is None else psi0, z[2] if omg0 is None else omg0)
-        self.log("zandpack_gb300 zand: %s, precision %s, n=%d, %d live modes of %d padded, eps=%g" % (
-            self.name, self.precision, L.n, L.N, L.padded_modes, self.eps))
+        self.log("zandpack_gb300 %s: %s, precision %s, n=%d, %d live modes of %d padded, eps=%g" % (
+            "nozand" if self.nonorth else "zand", self.name, self.precision, L.n, L.N, L.padded_modes, self.eps))
+        occ_mask = None
+        if self.dm_occ_only:
+            S05 = tr.basis.S05
+            occ_mask = np.abs(S05 @ S05) > 1e-6                    # Zandpack/mpi/nozand:261-262
         self.log("Timedependent Bias:\n" + _source(B.bias))
         NL = L.NL
         currents = [[] for _ in range(NL)]
@@ -204,6 +229,8 @@ class ZandRun:
                 np.save(save + "last_sig", sig)
                 np.save(save + "last_time", t)
                 np.save(save + "last_stepsize", old_h)
+                if self.nonorth:  # back to the orthogonal basis: rows S^1/2 psi'
+                    psi = psi @ tr.basis.S05[0].T
                 np.save(save + "last_psi", psi)
                 np.save(save + "last_omg", omg)
                 self.checkpoint_done[np.where(passed)[0][0]] = 1
@@ -213,12 +240,23 @@ class ZandRun:
             times.append(t + 0.0)
             step_count += 1
             if np.mod(step_count, self.saveevery) == 0 and step_count >= self.saveevery:
-                np.save(save + "DM" + str(step_count), np.array(DM[::self.n_dm_compress]).astype(np.complex64))
+                dm_arr = np.array(DM[::self.n_dm_compress]).astype(np.complex64)
+                if occ_mask is not None:
+                    dm_arr = dm_arr * occ_mask
+                if self.compress_mat:
+                    if self.dm_triu_only:
+                        dm_arr = np.triu(dm_arr)
+                    np.savez_compressed(save + "DM" + str(step_count), dm_arr)
+                else:
+                    np.save(save + "DM" + str(step_count), dm_arr)
                 dm_times = np.array(times[-len(DM):])
                 np.save(save + "DMt" + str(step_count), dm_times[::self.n_dm_compress])
                 if self.save_PI:
-                    np.save(save + "PIa" + str(step_count),
-                            np.array(PI_holder[::self.n_dm_compress]).astype(np.complex64))
+                    pi_arr = np.array(PI_holder[::self.n_dm_compress]).astype(np.complex64)
+                    if self.compress_mat:
+                        np.savez_compressed(save + "PIa" + str(step_count), pi_arr)
+                    else:
+                        np.save(save + "PIa" + str(step_count), pi_arr)
                 np.save(save + "times" + str(step_count), times[-len(DM):])
                 for k, c in enumerate(currents):
                     np.save(save + "current_" + str(k) + "_" + str(step_count), c[-len(DM):])
@@ -241,7 +279,8 @@ class ZandRun:
         return buf[None]
 
     def _pi_from_state(self, L, tr):
-        """PI_a = (P_a + P_a^H)/hbar of the stage-0 state (Zandpack/mpi/zand:91-110,363-366)."""
+        """PI_a = (P_a + P_a^H)/hbar of the stage-0 state (Zandpack/mpi/zand:91-110,363-366);
+        nozand keeps P_a/hbar (Zandpack/mpi/nozand:120-140)."""
         sig, psi, _ = tr.get_y()
         n = L.n
         PI = np.zeros((1, L.NL, n, n), complex)
@@ -252,7 +291,7 @@ class ZandRun:
             P = np.zeros((n, n), complex)
             k = L.lead_ncols[a]
             P[:, L.lead_cols[a, :k]] = pa.T @ L.IXI[rows][:, :k]
-            PI[0, a] = (P + P.conj().T) / L.hbar
+            PI[0, a] = (P if self.nonorth else P + P.conj().T) / L.hbar
         return PI
 
 
