@@ -18,6 +18,8 @@ def main():
     ap.add_argument("--attempts", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=1)
     ap.add_argument("--regions", action="store_true", help="print CUDA-event times per region of the timed attempts")
+    ap.add_argument("--nonorth", action="store_true",
+                    help="the workload posed in a non-orthogonal basis, propagated as nozand does")
     args = ap.parse_args()
     import ctypes as C
 
@@ -25,10 +27,12 @@ def main():
 
     from ._lib import PROF_REGIONS, check, lib
     from .engine import Propagator
-    from .workloads import make_workload
-    w = make_workload(args.config)
-    pr = Propagator(w.arrays, w.hbar, w.bias_fn(), hubbard_U=w.hubbard_U, precision=args.precision)
-    pr.set_state(w.arrays["DM_Ortho"])
+    from .workloads import make_nonorth_workload, make_workload
+    w = make_nonorth_workload(args.config) if args.nonorth else make_workload(args.config)
+    pr = Propagator(w.arrays, w.hbar, w.bias_fn(), hubbard_U=w.hubbard_U, precision=args.precision,
+                    nonorth=args.nonorth)
+    sig0 = w.arrays["DM_Ortho"]
+    pr.set_state(pr.traj.basis.sigma(sig0) if args.nonorth else sig0)
     t, h = w.t0, w.stepsize
     for i in range(args.warmup + args.attempts):
         if args.regions and i == args.warmup:
