@@ -120,6 +120,14 @@ def test_driver_matches_reference_run(tmp_path, device_dH):
     # DM files hold every accepted sigma (complex64)
     assert np.abs(dm[z["sig_traj_idx"] + 1] - z["sig_traj"]).max() < 1e-6
     assert os.path.exists(tmp_path / "run_save" / "last_psi.npy")
+    # the reference's readers (mpi_tools names) read the same run back
+    from zandpack_gb300.mpi_tools import combine_currents, combine_dm
+    T, C = combine_currents([str(tmp_path / "run_save")])
+    np.testing.assert_allclose(T, z["times"][:-1], rtol=0, atol=1e-10)
+    assert np.abs(np.hstack([c[:, 0][:, None] for c in C]).T - z["currents"]).max() < 1e-10
+    Td, DMr = combine_dm([str(tmp_path / "run_save")])
+    np.testing.assert_allclose(Td, z["times"], rtol=0, atol=1e-10)
+    np.testing.assert_array_equal(DMr, dm)
 
 
 def test_driver_restart_from_checkpoint(tmp_path):
