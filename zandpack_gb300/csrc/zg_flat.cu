@@ -336,11 +336,23 @@ __global__ void k_stage_prologue(const DevCtl* __restrict__ ctl, zg_bias b, doub
   const double t = ctl->t, h = ctl->h;
   const double ts = t + A_i * h;
   const int a = threadIdx.x;
-  if (a < ZG_MAX_LEADS) out->delta[a] = zg_bias_value(b, ts, a);
+  if (a < ZG_MAX_LEADS) {
+    const double v = zg_bias_value(b, ts, a);
+    out->delta[a] = v;
+    out->fdelta[a] = (float)v;
+  }
   if (a == 0) {
     out->h = h;
     out->ts = ts;
     out->hbar = hbar;
+    out->h_hb = h / hbar;
+    out->inv_hb = 1.0 / hbar;
+    out->h_hb2 = h / (hbar * hbar);
+    out->fh = (float)h;
+    out->fhbar = (float)hbar;
+    out->fh_hb = (float)out->h_hb;
+    out->finv_hb = (float)out->inv_hb;
+    out->fh_hb2 = (float)out->h_hb2;
   }
 }
 

@@ -113,7 +113,23 @@ int launch_zgemm_batch(GemmBatch<T>& b, int64_t ws_capacity, cudaStream_t s);
 struct StageParams {
   double h, ts, hbar;
   double delta[ZG_MAX_LEADS];
+  // derived once per stage by whoever writes the above (derive_params), so
+  // that no kernel thread divides in FP64 (a slow pipe on this GPU)
+  double h_hb, inv_hb, h_hb2;  // h/hbar, 1/hbar, h/hbar^2
+  float fh, fhbar, fh_hb, finv_hb, fh_hb2;
+  float fdelta[ZG_MAX_LEADS];
 };
+__host__ __device__ inline void derive_params(StageParams& p) {
+  p.h_hb = p.h / p.hbar;
+  p.inv_hb = 1.0 / p.hbar;
+  p.h_hb2 = p.h / (p.hbar * p.hbar);
+  p.fh = (float)p.h;
+  p.fhbar = (float)p.hbar;
+  p.fh_hb = (float)p.h_hb;
+  p.finv_hb = (float)p.inv_hb;
+  p.fh_hb2 = (float)p.h_hb2;
+  for (int a = 0; a < ZG_MAX_LEADS; ++a) p.fdelta[a] = (float)p.delta[a];
+}
 
 // ------------------------------------------------ device-side controller
 // State of the zand controller kept on the device, so that one attempt runs

@@ -13,17 +13,35 @@ namespace zg {
 // per-lead biases through a pointer (a dynamically indexed copy of the whole
 // struct would live in local memory).
 struct StageScalars {
-  double h, ts, hbar;
+  double h, ts, hbar, h_hb, inv_hb, h_hb2;
+  float fh, fhbar, fh_hb, finv_hb, fh_hb2;
   const double* delta;
+  const float* fdelta;
 };
 __device__ __forceinline__ StageScalars load_params(const StageParams* __restrict__ pp) {
   StageScalars s;
   s.h = pp->h;
   s.ts = pp->ts;
   s.hbar = pp->hbar;
+  s.h_hb = pp->h_hb;
+  s.inv_hb = pp->inv_hb;
+  s.h_hb2 = pp->h_hb2;
+  s.fh = pp->fh;
+  s.fhbar = pp->fhbar;
+  s.fh_hb = pp->fh_hb;
+  s.finv_hb = pp->finv_hb;
+  s.fh_hb2 = pp->fh_hb2;
   s.delta = pp->delta;
+  s.fdelta = pp->fdelta;
   return s;
 }
+// the stage scalar of the kernel's real type: the FP64 value or its FP32 copy
+template <typename T>
+__device__ __forceinline__ T pv(double d, float f);
+template <>
+__device__ __forceinline__ double pv<double>(double d, float) { return d; }
+template <>
+__device__ __forceinline__ float pv<float>(double, float f) { return f; }
 
 template <typename T>
 __device__ __forceinline__ typename cx<T>::t czero() {
@@ -349,7 +367,9 @@ __device__ __forceinline__ typename cx<T>::t load_T(const typename cx<T>::t* Tm,
   return cx<T>::make(f[r + j] - f[r2 + npl + j], f[r + npl + j] + f[r2 + j]);
 }
 
-template <typename T>
+// DIS: a dissipator is set (a template parameter: a runtime branch would be
+// if-converted into predicated FP64 multiplies issued for every element)
+template <typename T, bool DIS>
 __global__ void __launch_bounds__(256) k_sigma_finalize(const RhsDev<T> d, const StageParams* __restrict__ pp,
                                                         const typename cx<T>::t* __restrict__ Tm, int64_t ldT,
                                                         const double2* __restrict__ dis,
@@ -359,8 +379,8 @@ __global__ void __launch_bounds__(256) k_sigma_finalize(const RhsDev<T> d, const
   __shared__ C tile[32][33];   // tile[r][c] = T[j0 + r][i0 + c]
   __shared__ C wtile[32][33];  // the same of W (non-orthogonal basis)
   const StageScalars p = load_params(pp);
-  const T sc = (T)(p.h / p.hbar);
-  const T fw = (T)(p.h / (p.hbar * p.hbar));
+  const T sc = pv<T>(p.h_hb, p.fh_hb);
+  const T fw = pv<T>(p.h_hb2, p.fh_hb2);
   const int n = d.n;
   const int i0 = blockIdx.y * 32, j0 = blockIdx.x * 32;
   const int tx = threadIdx.x, ty = threadIdx.y;
@@ -379,7 +399,7 @@ __global__ void __launch_bounds__(256) k_sigma_finalize(const RhsDev<T> d, const
     // -i (tij - conj(tji)) = (tij.y + tji.y, -(tij.x - tji.x))
     C v = cx<T>::make(tij.y + tji.y, -(tij.x - tji.x));
     const int64_t e = (int64_t)i * n + j;
-    if (dis) {  // - hbar * dissipator(ts, sigma)  (Zandpack/mpi/zand:343)
+    if (DIS) {  // - hbar * dissipator(ts, sigma)  (Zandpack/mpi/zand:343)
       const double2 q = dis[e];
       v.x -= (T)(p.hbar * q.x);
       v.y -= (T)(p.hbar * q.y);
@@ -403,7 +423,7 @@ __global__ void __launch_bounds__(256) k_sigma_leads(const RhsDev<T> d, const St
                                                      typename cx<T>::t* __restrict__ ksig) {
   using C = typename cx<T>::t;
   const StageScalars p = load_params(pp);
-  const T f = (T)(p.h / (p.hbar * p.hbar));
+  const T f = pv<T>(p.h_hb2, p.fh_hb2);
   const int n = d.n, nu = d.nu;
   const int64_t half = (int64_t)nu * n;
   GRID_STRIDE(q, 2 * half) {
@@ -433,7 +453,10 @@ int launch_sigma_finalize(const RhsDev<T>& d, const StageParams* p, const typena
                           int tmode, int npl, const typename cx<T>::t* W) {
   ZG_REQUIRE(tmode >= 0 && tmode <= 2, "bad T layout %d", tmode);
   const int nb = (d.n + 31) / 32;
-  k_sigma_finalize<T><<<dim3(nb, nb), dim3(32, 8), 0, s>>>(d, p, Tm, ldT, dis, ksig, tmode, npl, W);
+  if (dis)
+    k_sigma_finalize<T, true><<<dim3(nb, nb), dim3(32, 8), 0, s>>>(d, p, Tm, ldT, dis, ksig, tmode, npl, W);
+  else
+    k_sigma_finalize<T, false><<<dim3(nb, nb), dim3(32, 8), 0, s>>>(d, p, Tm, ldT, dis, ksig, tmode, npl, W);
   ZG_CHECK_LAUNCH();
   count_launch();
   if (d.nu > 0 && !W) {
@@ -550,8 +573,8 @@ __global__ void __launch_bounds__(256) k_psi_finalize(const RhsDev<T> d, const S
   C* sZ = reinterpret_cast<C*>(psi_smem);  // [L][nc]: ZA + ZB of this row
   C* sX = sZ + d.L * d.nc;                 // [nc]: GL_P xi of this row on its lead's columns
   const StageScalars p = load_params(pp);
-  const T ih = (T)(1.0 / p.hbar);
-  const T h = (T)p.h;
+  const T ih = pv<T>(p.inv_hb, p.finv_hb);
+  const T h = pv<T>(p.h, p.fh);
   const int n = d.n, nc = d.nc, L = d.L;
   for (int m = blockIdx.x; m < d.N; m += gridDim.x) {
     const bool src = m < d.Ns;
@@ -567,7 +590,7 @@ __global__ void __launch_bounds__(256) k_psi_finalize(const RhsDev<T> d, const S
       for (int q = threadIdx.x; q < nc; q += blockDim.x) sX[q] = cmul(glp, d.XI[(int64_t)m * nc + q]);
     }
     C xp = d.Xp[m];
-    xp.x += (T)p.delta[a];
+    xp.x += pv<T>(p.delta[a], p.fdelta[a]);
     const C dgp = src ? d.dGP[m] : czero<T>();
     __syncthreads();
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
@@ -619,6 +642,106 @@ __global__ void __launch_bounds__(256) k_psi_finalize(const RhsDev<T> d, const S
   }
 }
 
+// Mixed path, planar psi hi/lo and planar R1, n a multiple of V: one thread
+// per (row, V consecutive columns), no shared memory and no block barriers,
+// 8-byte (V = 2) loads of the planar operands.  The terms are added in the
+// order of k_psi_finalize, so both give the same bits.
+template <int V>
+struct fvec {
+  float v[V];
+};
+template <int V>
+__device__ __forceinline__ fvec<V> ldv(const float* p) {
+  fvec<V> r;
+  if constexpr (V == 2) {
+    const float2 t = __ldg(reinterpret_cast<const float2*>(p));
+    r.v[0] = t.x;
+    r.v[1] = t.y;
+  } else {
+    const float4 t = __ldg(reinterpret_cast<const float4*>(p));
+    r.v[0] = t.x;
+    r.v[1] = t.y;
+    r.v[2] = t.z;
+    r.v[3] = t.w;
+  }
+  return r;
+}
+
+template <int RMODE, int V>
+__global__ void __launch_bounds__(256) k_psi_finalize_v4(const RhsDev<float> d, const StageParams* __restrict__ pp,
+                                                         const float* __restrict__ ph, const float* __restrict__ pl,
+                                                         int64_t ldpsi, int64_t plane, const float* __restrict__ R1,
+                                                         int64_t ldR1, int npl, const float2* __restrict__ R2,
+                                                         const float2* __restrict__ ZA, const float2* __restrict__ ZB,
+                                                         float2* __restrict__ kpsi, const float2* __restrict__ R3,
+                                                         const float2* __restrict__ C0) {
+  const StageScalars p = load_params(pp);
+  const float ih = p.finv_hb;
+  const float h = p.fh;
+  const int n = d.n, nq = n / V, nc = d.nc, L = d.L;
+  const int64_t total = (int64_t)d.N * nq;
+  GRID_STRIDE(q, total) {
+    const int m = (int)(q / nq);
+    const int i0 = (int)(q - (int64_t)m * nq) * V;
+    const bool src = m < d.Ns;
+    const int a = d.mode_lead[m];
+    float2 xp = d.Xp[m];
+    xp.x += p.fdelta[a];
+    const float2 dgp = src ? d.dGP[m] : czero<float>();
+    const int64_t o = (int64_t)m * ldpsi + i0;
+    const fvec<V> pr = ldv<V>(ph + o), pim = ldv<V>(ph + o + plane);
+    const fvec<V> lr = ldv<V>(pl + o), lim = ldv<V>(pl + o + plane);
+    const int64_t a0 = (int64_t)m * ldR1 + i0, a1 = (int64_t)(d.N + m) * ldR1 + i0;
+    fvec<V> r1r = ldv<V>(R1 + a0), r1i, r1x, r1y;
+    if (RMODE == 1) {
+      r1i = ldv<V>(R1 + a1);
+    } else {  // columns [H_r | H_i]: (f[a0] - f[a1 + npl], f[a0 + npl] + f[a1])
+      r1x = ldv<V>(R1 + a1 + npl);
+      r1i = ldv<V>(R1 + a0 + npl);
+      r1y = ldv<V>(R1 + a1);
+    }
+    const int64_t e0 = (int64_t)m * n + i0;
+#pragma unroll
+    for (int j = 0; j < V; ++j) {
+      const float2 r2 = src ? R2[e0 + j] : czero<float>();
+      float2 ps = make_float2(pr.v[j], pim.v[j]);
+      const float2 pz = make_float2(lr.v[j], lim.v[j]);
+      const float2 r1 = RMODE == 1 ? make_float2(r1r.v[j], r1i.v[j])
+                                   : make_float2(r1r.v[j] - r1x.v[j], r1i.v[j] + r1y.v[j]);
+      ps = cadd(ps, pz);
+      float2 v = cscale(r1, ih);
+      v = csub(v, cscale(cmul(xp, ps), ih));
+      v = cadd(v, cmul(dgp, r2));
+      const int i = i0 + j;
+      if (R3) {
+        v = cadd(v, cadd(R3[e0 + j], C0[e0 + j]));
+      } else if (d.umap[i] >= 0) {  // a coupling orbital of some lead
+        for (int b = 0; b < L; ++b) {
+          const int k = d.colmap[b * n + i];
+          if (k >= 0) {
+            float2 z = ZA[((int64_t)b * d.N + m) * nc + k];
+            if (src) z = cadd(z, ZB[((int64_t)b * d.Ns + m) * nc + k]);
+            v = cadd(v, z);
+            if (b == a) v = cadd(v, cmul(d.GLP[m], d.XI[(int64_t)m * nc + k]));
+          }
+        }
+      }
+      kpsi[e0 + j] = make_float2(h * v.y, -h * v.x);
+    }
+  }
+}
+
+constexpr int kPsiV = 2;  // columns per thread of k_psi_finalize_v4
+
+template <typename T>
+static bool psi_v4_ok(const RhsDev<T>& d, const void* psi, const void* psi_lo, int64_t ldpsi, const void* R1,
+                      int64_t ldR1, int64_t plane, int rmode, int npl) {
+  if (sizeof(T) != 4 || !plane || !psi_lo || (rmode != 1 && rmode != 2)) return false;
+  if (d.n % kPsiV || ldpsi % kPsiV || plane % kPsiV || ldR1 % kPsiV || npl % kPsiV) return false;
+  auto al = [](const void* q) { return ((uintptr_t)q & (4 * kPsiV - 1)) == 0; };
+  return al(psi) && al(psi_lo) && al(R1);
+}
+
 template <typename T>
 int launch_psi_finalize(const RhsDev<T>& d, const StageParams* p, const typename cx<T>::t* psi,
                         const typename cx<T>::t* psi_lo, int64_t ldpsi, const typename cx<T>::t* R1, int64_t ldR1,
@@ -628,6 +751,24 @@ int launch_psi_finalize(const RhsDev<T>& d, const StageParams* p, const typename
   if (d.N == 0) return ZG_OK;
   ZG_REQUIRE(rmode >= 0 && rmode <= 2, "bad R1 layout %d", rmode);
   ZG_REQUIRE((R3 == nullptr) == (C0 == nullptr), "R3 and C0 come together");
+  if constexpr (sizeof(T) == 4) {
+    if (psi_v4_ok(d, psi, psi_lo, ldpsi, R1, ldR1, plane, rmode, npl)) {
+      const int64_t total = (int64_t)d.N * (d.n / kPsiV);
+      const int grid = grid_for(total, 256, 152 * 16);
+      const float* ph = reinterpret_cast<const float*>(psi);
+      const float* plo = reinterpret_cast<const float*>(psi_lo);
+      const float* r1 = reinterpret_cast<const float*>(R1);
+      if (rmode == 1)
+        k_psi_finalize_v4<1, kPsiV><<<grid, 256, 0, s>>>(d, p, ph, plo, ldpsi, plane, r1, ldR1, npl, R2, ZA, ZB, kpsi,
+                                                         R3, C0);
+      else
+        k_psi_finalize_v4<2, kPsiV><<<grid, 256, 0, s>>>(d, p, ph, plo, ldpsi, plane, r1, ldR1, npl, R2, ZA, ZB, kpsi,
+                                                         R3, C0);
+      ZG_CHECK_LAUNCH();
+      count_launch();
+      return ZG_OK;
+    }
+  }
   const size_t smem = R3 ? 0 : (size_t)(d.L + 1) * d.nc * sizeof(typename cx<T>::t);
   ZG_REQUIRE(smem <= 48 * 1024, "coupling width too large for the psi finalisation (%zu B)", smem);
   const int grid = d.N < 152 * 8 ? d.N : 152 * 8;
@@ -776,10 +917,10 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) k_omega(const Rhs
     asm volatile("cp.async.wait_group 0;" ::: "memory");
     __syncthreads();
   }
-  const T sc = (T)(p.h / p.hbar);
-  const T h = (T)p.h;
+  const T sc = pv<T>(p.h_hb, p.fh_hb);
+  const T h = pv<T>(p.h, p.fh);
   C* out = t.blk == 0 ? omA_out : omB_out;
-  const T da = (T)p.delta[t.a], db = (T)p.delta[t.b];
+  const T da = pv<T>(p.delta[t.a], p.fdelta[t.a]), db = pv<T>(p.delta[t.b], p.fdelta[t.b]);
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
     const int r = ty + 16 * i;
@@ -798,7 +939,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) k_omega(const Rhs
       if (stationary) {
         // dOmega/dt = 0: Omega = i hbar S / (X+ + D_a - X- - D_b)  (Zandpack/cmdtools/psinought:443-451)
         const C q = cdiv(acc[i][j], csub(xp, xm));
-        out[e] = cx<T>::make((T)(-p.hbar) * q.y, (T)p.hbar * q.x);
+        out[e] = cx<T>::make(-pv<T>(p.hbar, p.fhbar) * q.y, pv<T>(p.hbar, p.fhbar) * q.x);
         continue;
       }
       const C om = sizeof(T) == 4 ? Os[r * 64 + c] : in[e];

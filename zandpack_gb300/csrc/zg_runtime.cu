@@ -1139,6 +1139,7 @@ int zg_rhs(zg_traj* t, int stage, double ts, double h, const double* delta, int 
   StageParams p;
   p.h = h; p.ts = ts; p.hbar = t->hbar;
   for (int a = 0; a < ZG_MAX_LEADS; ++a) p.delta[a] = a < t->L ? delta[a] : 0.0;
+  derive_params(p);
   prof_begin(t, ZG_PROF_RHS);
   ZG_TRY(launch_set_params(p, t->d_params, t->stream));
   if (t->precision == ZG_PREC_F64)
@@ -1543,6 +1544,7 @@ int zg_stationary_setup(zg_traj* t, double ts, const double* delta, int dH_mode,
   t->st_p.ts = ts;
   t->st_p.hbar = t->hbar;
   for (int a = 0; a < ZG_MAX_LEADS; ++a) t->st_p.delta[a] = a < t->L ? delta[a] : 0.0;
+  derive_params(t->st_p);
   ZG_CHECK_CUDA(cudaMemcpyAsync(t->st_V, V, nn * sizeof(double2), cudaMemcpyHostToDevice, t->stream));
   ZG_CHECK_CUDA(cudaMemcpyAsync(t->st_Vc, Vc.data(), nn * sizeof(double2), cudaMemcpyHostToDevice, t->stream));
   ZG_CHECK_CUDA(cudaMemcpyAsync(t->st_lam, lam, (size_t)t->n * sizeof(double), cudaMemcpyHostToDevice, t->stream));
