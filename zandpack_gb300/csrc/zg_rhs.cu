@@ -1016,62 +1016,72 @@ __device__ __forceinline__ void split_tf32_r(float v, float& hi, float& lo) {
   lo = __uint_as_float(l);
 }
 
-// Planar TF32 hi/lo operands of the two tensor-core GEMMs (np x np blocks, K
-// along the row):  Ht rows [0, np) = Re H(t), rows [np, 2 np) = Im H(t);
-// BS rows [0, np) = Re sigma^T, rows [np, 2 np) = Im sigma^T.  Thread q < np*np
-// handles element (r, c) = (q / np, q % np) of BS and, when h_part == 0, of
-// Ht; threads np*np + r rebuild the diagonal (r, r) of Ht when h_part == 1.
-// Padding (r or c >= n) is written as zero.
-__global__ void k_build_operands_mixed(int n, int np, const double2* __restrict__ H0, const float2* __restrict__ sig32,
-                                       const double2* __restrict__ dH, int dH_mode, double U, int h_part,
-                                       float* __restrict__ Hth, float* __restrict__ Htl, float* __restrict__ BSh,
-                                       float* __restrict__ BSl, const double2* __restrict__ Sm1) {
+// H(t) element (r, c) in FP64 (r, c < n)
+__device__ __forceinline__ double2 ht_element(int n, int r, int c, const double2* __restrict__ H0,
+                                              const float2* __restrict__ sig32, const double2* __restrict__ dH,
+                                              int dH_mode, double U, const double2* __restrict__ Sm1) {
+  double2 v = H0[(int64_t)r * n + c];
+  if (dH_mode == ZG_DH_MATRIX) v = cadd(v, dH[(int64_t)r * n + c]);
+  if (dH_mode == ZG_DH_HUBBARD) {
+    if (Sm1) {  // column c of S^-1 scaled by the Hubbard term of orbital c
+      const double u = U * ((double)sig32[(int64_t)c * n + c].x - 0.5);
+      const double2 sv = Sm1[(int64_t)r * n + c];
+      v.x += sv.x * u;
+      v.y += sv.y * u;
+    } else if (r == c) {
+      v.x += U * ((double)sig32[(int64_t)r * n + r].x - 0.5);
+    }
+  }
+  return v;
+}
+
+__device__ __forceinline__ void put_split(float* __restrict__ hi, float* __restrict__ lo, int64_t o, int64_t off,
+                                          float re, float im) {
+  float a, b;
+  split_tf32_r(re, a, b);
+  hi[o] = a;
+  lo[o] = b;
+  split_tf32_r(im, a, b);
+  hi[off + o] = a;
+  lo[off + o] = b;
+}
+
+// Planar TF32 hi/lo operands of the two tensor-core GEMMs (np x np blocks):
+// Ht rows [0, np) = Re H(t), rows [np, 2 np) = Im H(t); BS rows [0, np) =
+// Re sigma^T, rows [np, 2 np) = Im sigma^T.  One 32x32 tile per block: sigma
+// is read along its rows and transposed through shared memory.  HP (the
+// H(t) part): 0 = every entry, 1 = the diagonal only (the blocks on the
+// diagonal), 2 = none.  Padding (r or c >= n) is written as zero.
+template <int HP>
+__global__ void __launch_bounds__(256) k_build_operands_mixed(int n, int np, const double2* __restrict__ H0,
+                                                              const float2* __restrict__ sig32,
+                                                              const double2* __restrict__ dH, int dH_mode, double U,
+                                                              float* __restrict__ Hth, float* __restrict__ Htl,
+                                                              float* __restrict__ BSh, float* __restrict__ BSl,
+                                                              const double2* __restrict__ Sm1) {
+  __shared__ float2 tile[32][33];  // tile[k][j] = sigma[c0 + k][r0 + j]
   const int64_t nn = (int64_t)np * np;
-  const int64_t tot = nn + (h_part == 1 ? np : 0);
-  GRID_STRIDE(q, tot) {
-    const bool diag_job = q >= nn;
-    const int r = diag_job ? (int)(q - nn) : (int)(q / np);
-    const int c = diag_job ? r : (int)(q % np);
+  const int r0 = blockIdx.y * 32, c0 = blockIdx.x * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  for (int k = ty; k < 32; k += 8) {
+    const int row = c0 + k, col = r0 + tx;
+    tile[k][tx] = (row < n && col < n) ? sig32[(int64_t)row * n + col] : czero<float>();
+  }
+  __syncthreads();
+  for (int k = ty; k < 32; k += 8) {
+    const int r = r0 + k, c = c0 + tx;
+    if (r >= np || c >= np) continue;
     const int64_t o = (int64_t)r * np + c;
-    float a, b;
-    if (h_part == 0 || diag_job) {
+    const float2 sv = tile[tx][k];  // sigma[c][r]: row r of BS, K index c
+    put_split(BSh, BSl, o, nn, sv.x, sv.y);
+    if (HP == 0 || (HP == 1 && r == c)) {
       float hr = 0.f, hi = 0.f;
       if (r < n && c < n) {
-        double2 v = H0[(int64_t)r * n + c];
-        if (dH_mode == ZG_DH_MATRIX) v = cadd(v, dH[(int64_t)r * n + c]);
-        if (dH_mode == ZG_DH_HUBBARD) {
-          if (Sm1) {  // column c of S^-1 scaled by the Hubbard term of orbital c
-            const double u = U * ((double)sig32[(int64_t)c * n + c].x - 0.5);
-            const double2 sv = Sm1[(int64_t)r * n + c];
-            v.x += sv.x * u;
-            v.y += sv.y * u;
-          } else if (r == c) {
-            v.x += U * ((double)sig32[(int64_t)r * n + r].x - 0.5);
-          }
-        }
+        const double2 v = ht_element(n, r, c, H0, sig32, dH, dH_mode, U, Sm1);
         hr = (float)v.x;
         hi = (float)v.y;
       }
-      split_tf32_r(hr, a, b);
-      Hth[o] = a;
-      Htl[o] = b;
-      split_tf32_r(hi, a, b);
-      Hth[nn + o] = a;
-      Htl[nn + o] = b;
-    }
-    if (!diag_job) {
-      float sr = 0.f, si = 0.f;
-      if (r < n && c < n) {
-        const float2 sv = sig32[(int64_t)c * n + r];  // sigma[c][r]: row j = r, K index k = c
-        sr = sv.x;
-        si = sv.y;
-      }
-      split_tf32_r(sr, a, b);
-      BSh[o] = a;
-      BSl[o] = b;
-      split_tf32_r(si, a, b);
-      BSh[nn + o] = a;
-      BSl[nn + o] = b;
+      put_split(Hth, Htl, o, nn, hr, hi);
     }
   }
 }
@@ -1081,9 +1091,14 @@ int launch_build_operands_mixed(int n, int np, const double2* H0, const float2* 
                                 const double2* Sm1) {
   ZG_REQUIRE(h_part >= 0 && h_part <= 2, "bad operand part %d", h_part);
   ZG_REQUIRE(!(Sm1 && dH_mode == ZG_DH_HUBBARD && h_part == 1), "the overlap's Hubbard term changes every entry");
-  const int64_t tot = (int64_t)np * np + (h_part == 1 ? np : 0);
-  k_build_operands_mixed<<<grid_for(tot, 256, 152 * 16), 256, 0, s>>>(n, np, H0, sig32, dH, dH_mode, U, h_part, Hth,
-                                                                      Htl, BSh, BSl, Sm1);
+  const int nb = (np + 31) / 32;
+  const dim3 grid(nb, nb), block(32, 8);
+  if (h_part == 0)
+    k_build_operands_mixed<0><<<grid, block, 0, s>>>(n, np, H0, sig32, dH, dH_mode, U, Hth, Htl, BSh, BSl, Sm1);
+  else if (h_part == 1)
+    k_build_operands_mixed<1><<<grid, block, 0, s>>>(n, np, H0, sig32, dH, dH_mode, U, Hth, Htl, BSh, BSl, Sm1);
+  else
+    k_build_operands_mixed<2><<<grid, block, 0, s>>>(n, np, H0, sig32, dH, dH_mode, U, Hth, Htl, BSh, BSl, Sm1);
   ZG_CHECK_LAUNCH();
   count_launch();
   return ZG_OK;
