@@ -38,6 +38,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 
+# ncu-measured DRAM traffic of one psi H^T tensor-core launch per (workload, H(t) form)
+NCU_TRAFFIC = {("c3", "real"): 83.8e6 + 8.6e6}
+
 METRIC = "simulated fs/s at n=1024"
 WORKLOAD_DESC = {
     "c3": "n=1024 32x32 square lattice, 2 leads x 32 orbitals, 40 rank-8 Lorentzians + 30 Pade poles per lead, "
@@ -218,11 +221,18 @@ def run_ours(args):
         t_launch = g_ms / g_n / 1e3 if g_n else None
         tf32 = measure_tf32_peak()
         achieved = tc_flops / t_launch / 1e12 if t_launch else None
+        # DRAM bytes of one launch of this kernel on this workload, from the ncu
+        # capture summarised in profiles/k_gemm_tf32x3_c3.md (dram__bytes_read.sum
+        # + dram__bytes_write.sum; ncu cannot run inside the timed bench)
+        traffic = NCU_TRAFFIC.get((args.config, "real" if h_real else "complex"))
         roof = {"bound": "tensor",
                 "kernel": "k_gemm_tf32x3<256,4,16> (psi H(t)^T, tcgen05 kind::tf32, 3xTF32, %s H(t))"
                           % ("real" if h_real else "complex"),
                 "achieved": achieved, "peak": tf32, "unit": "TFLOP/s",
-                "frac": (achieved / tf32) if achieved and tf32 else None, "traffic": None,
+                "frac": (achieved / tf32) if achieved and tf32 else None, "traffic": traffic,
+                "traffic_unit": "DRAM bytes per launch (ncu capture, profiles/k_gemm_tf32x3_c3.md)",
+                "operand_bytes_per_launch": (2 * 2 * L.N * np_ + 2 * (nb32 if h_real else 2 * np_) * np_
+                                             + 2 * L.N * (nb32 if h_real else 2 * np_)) * 4,
                 "peak_source": "live cuBLAS TF32 GEMM 8192^3 (torch.matmul, allow_tf32); TF32 is not in "
                                "MEASURED_PEAKS.json (bf16 there: %s TFLOP/s)" % _peaks_file().get("bf16_tflops"),
                 "tensor_flops_per_launch": tc_flops, "algorithmic_flops_per_launch": alg_flops,
