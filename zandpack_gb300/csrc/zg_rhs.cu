@@ -84,8 +84,10 @@ __device__ __forceinline__ typename cx<T>::t load_opB(const GemmProb<T>& P, int 
   return P.opB == 0 ? P.B[(int64_t)k * P.ldb + n] : P.B[(int64_t)n * P.ldb + k];
 }
 
+// FP32: K staged 8 at a time under a 3-blocks-per-SM register budget (80
+// registers; 16 at a time needed 144 registers, one block per SM)
 template <typename T, int BN>
-__global__ void __launch_bounds__(256) k_zgemm(const __grid_constant__ GemmBatch<T> batch) {
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) k_zgemm(const __grid_constant__ GemmBatch<T> batch) {
   using C = typename cx<T>::t;
   constexpr int TX = BN / 4, TY = 256 / TX, BM = 4 * TY;
   const int tile = blockIdx.x;
@@ -99,10 +101,10 @@ __global__ void __launch_bounds__(256) k_zgemm(const __grid_constant__ GemmBatch
   const int kb1 = min(P.K, kb0 + P.kchunk);
   // K staged ZKG at a time; the next stage's global loads are issued into
   // registers before the current stage is computed, hiding their latency
-  constexpr int ZKG = 16, RA = BM * ZKG / 256, RB = BN * ZKG / 256;
+  constexpr int ZKG = sizeof(T) == 4 ? 8 : 16, RA = BM * ZKG / 256, RB = BN * ZKG / 256;
   // rows padded by one element: K-contiguous operands are stored column-wise
-  // (16 threads with consecutive k, same m), which without padding would hit
-  // one bank 16 times
+  // (ZKG threads with consecutive k, same m), which without padding would hit
+  // one bank ZKG times
   __shared__ C As[ZKG][BM + 1];
   __shared__ C Bs[ZKG][BN + 1];
   const int tid = threadIdx.x, tx = tid % TX, ty = tid / TX;
@@ -112,10 +114,10 @@ __global__ void __launch_bounds__(256) k_zgemm(const __grid_constant__ GemmBatch
 #pragma unroll
     for (int j = 0; j < 4; ++j) acc[i][j] = czero<T>();
   // element r of this thread's share of a K stage (recomputed, not kept in registers)
-#define ZG_AM(r) (P.opA == 0 ? ((tid + 256 * (r)) >> 4) : ((tid + 256 * (r)) % BM))
-#define ZG_AK(r) (P.opA == 0 ? ((tid + 256 * (r)) & 15) : ((tid + 256 * (r)) / BM))
-#define ZG_BN(r) (P.opB == 0 ? ((tid + 256 * (r)) % BN) : ((tid + 256 * (r)) >> 4))
-#define ZG_BK(r) (P.opB == 0 ? ((tid + 256 * (r)) / BN) : ((tid + 256 * (r)) & 15))
+#define ZG_AM(r) (P.opA == 0 ? ((tid + 256 * (r)) / ZKG) : ((tid + 256 * (r)) % BM))
+#define ZG_AK(r) (P.opA == 0 ? ((tid + 256 * (r)) % ZKG) : ((tid + 256 * (r)) / BM))
+#define ZG_BN(r) (P.opB == 0 ? ((tid + 256 * (r)) % BN) : ((tid + 256 * (r)) / ZKG))
+#define ZG_BK(r) (P.opB == 0 ? ((tid + 256 * (r)) / BN) : ((tid + 256 * (r)) % ZKG))
   C ra[RA], ra2[RA], rb[RB];
   const bool conjB = P.opB == 2;
 #pragma unroll
