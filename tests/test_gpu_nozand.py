@@ -183,3 +183,46 @@ def test_nozand_mixed_within_1e6_of_reference(golden_nz):
     print("\n%s mixed vs reference nozand: max|dsig| = %.2e, max|dJ| = %.2e" % (case, dsig, dJ))
     assert dsig <= 1e-6 and dJ <= 1e-6
     pr.traj.close()
+
+
+@pytest.mark.parametrize("precision", ["f64", "mixed"])
+@pytest.mark.parametrize("name", ["mini2", "mini3"])
+def test_nozand_complex_overlap_against_oracle(name, precision):
+    """A complex Hermitian overlap (S^-1 H(t) complex: the complex operand
+    forms of the tensor-core products): one RHS from a dense random state with
+    the Hubbard term on the device (mini2) or none (mini3), against the
+    oracle (pinned to the reference nozand) at 1e-12 (FP64) / 1e-5 (mixed)."""
+    from oracle import nozand_np as nz
+    from zandpack_gb300 import _lib
+    from zandpack_gb300.engine import Trajectory
+    from zandpack_gb300.layout import CompactLayout
+    from zandpack_gb300.nonorth import NonorthBasis
+    from zandpack_gb300.workloads import make_nonorth_workload
+    w = make_nonorth_workload(name, phases=True)
+    prob = nz.NonorthProblem(w.arrays, w.hbar)
+    assert np.abs(prob.Sm1.imag).max() > 1e-3
+    L = CompactLayout(NonorthBasis(w.arrays).arrays, w.hbar)
+    rng = np.random.default_rng(13)
+    y = (rng.standard_normal(L.size) + 1j * rng.standard_normal(L.size)) * 0.1
+    ys, yp, yo = L.unpack(y)
+    ys = (ys + ys.conj().transpose(0, 2, 1)) / 2
+    y = L.pack(ys, yp, yo)
+    ys, yp, yo = L.unpack(y)
+    tr = Trajectory(w.arrays, w.hbar, precision=precision, layout=L, nonorth=True)
+    tr.set_slot(tr.stages, y)
+    delta = rng.uniform(-0.3, 0.3, L.NL)
+    h = 0.011
+    tr.stage_input(0)
+    U = w.hubbard_U
+    if U is not None:
+        tr.rhs(0, 0.2, h, delta, _lib.ZG_DH_HUBBARD, U)
+        dHm = w.dH_fn()(0.2, ys)
+    else:
+        tr.rhs(0, 0.2, h, delta)
+        dHm = 0.0
+    ks, kp, ko, _, _ = prob.rhs(h, ys, yp, yo, prob.H0 + dHm, delta)
+    g = L.unpack(tr.get_slot(0))
+    tol = RTOL_RHS if precision == "f64" else 1e-5
+    for x, r, nm in zip(g, (ks, kp, ko), ("sig", "psi", "omg")):
+        assert _rel(x, r) < tol, (nm, _rel(x, r))
+    tr.close()

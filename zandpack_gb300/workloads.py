@@ -453,7 +453,7 @@ def make_workload(name: str) -> Workload:
 
 
 # ------------------------------------------------- non-orthogonal basis
-def make_nonorth_workload(name: str, s: float = 0.08) -> Workload:
+def make_nonorth_workload(name: str, s: float = 0.08, phases: bool = False) -> Workload:
     """A workload of ``name`` posed in a non-orthogonal basis, for the
     ``nozand`` path (Zandpack/mpi/nozand:259-320).
 
@@ -465,17 +465,23 @@ def make_nonorth_workload(name: str, s: float = 0.08) -> Workload:
     ``H_Ortho = S^-1/2 H' S^-1/2``, ``xi`` rows ``S^-1/2 xi'``, ``Ixi`` rows
     ``Ixi' S^-1/2``; ``nozand`` maps them back (``S^1/2`` on both sides,
     ``transform_vec_Tv/vT``).  ``DM_Ortho`` is kept: ``nozand`` starts from
-    ``S^-1/2 DM_Ortho S^-1/2``."""
+    ``S^-1/2 DM_Ortho S^-1/2``.  ``phases=True`` gives the bonds of S
+    seeded random phases (a complex Hermitian overlap, as at a k-point away
+    from Gamma)."""
     w = make_workload(name)
     A = dict(w.arrays)
     Hp = np.asarray(A["H_Ortho"])[0]
-    bonds = (np.abs(Hp) > 0) & ~np.eye(Hp.shape[0], dtype=bool)
-    S = np.eye(Hp.shape[0]) + s * bonds.astype(np.float64)
+    n = Hp.shape[0]
+    bonds = ((np.abs(Hp) > 0) & ~np.eye(n, dtype=bool)).astype(np.float64)
+    if phases:
+        up = np.triu(bonds, 1) * np.exp(1j * np.random.default_rng(2024).uniform(0, 2 * np.pi, (n, n)))
+        bonds = up + up.conj().T
+    S = np.eye(n) + s * bonds
     e, V = np.linalg.eigh(S)
     if e.min() <= 0.1:
         raise ValueError("overlap not safely positive definite (min eigenvalue %.3g)" % e.min())
-    Sm05 = (V * e ** -0.5) @ V.T
-    Sm05 = (Sm05 + Sm05.T) / 2
+    Sm05 = (V * e ** -0.5) @ V.conj().T
+    Sm05 = (Sm05 + Sm05.conj().T) / 2
     A["H_Ortho"] = (Sm05 @ Hp @ Sm05)[None].astype(np.complex128)
     A["xi"] = np.asarray(A["xi"]) @ Sm05.T
     A["Ixi"] = np.asarray(A["Ixi"]) @ Sm05
