@@ -226,3 +226,37 @@ def test_nozand_complex_overlap_against_oracle(name, precision):
     for x, r, nm in zip(g, (ks, kp, ko), ("sig", "psi", "omg")):
         assert _rel(x, r) < tol, (nm, _rel(x, r))
     tr.close()
+
+
+def test_overlap_switches_off_and_steady_state_refuses():
+    """zg_set_overlap(NULL) returns a trajectory to the orthogonal equations
+    (the same k as a trajectory that never had an overlap); the steady-state
+    entry points refuse a trajectory with an overlap set."""
+    import ctypes as C
+    from zandpack_gb300 import _lib
+    from zandpack_gb300._lib import ZGError, check, lib
+    from zandpack_gb300.engine import Trajectory
+    from zandpack_gb300.layout import CompactLayout
+    z = load_golden("mini2")
+    p = z["params"]
+    L = CompactLayout(z, p["hbar"])
+    rng = np.random.default_rng(17)
+    y = (rng.standard_normal(L.size) + 1j * rng.standard_normal(L.size)) * 0.1
+    ks = []
+    for switch in (False, True):
+        tr = Trajectory(z, p["hbar"], layout=L)
+        if switch:
+            Sm1 = np.ascontiguousarray(np.eye(L.n, dtype=np.complex128) * 1.1)
+            C0 = np.ascontiguousarray(np.ones((L.N, L.n), np.complex128))
+            check(lib().zg_set_overlap(tr._h, Sm1.ctypes.data_as(C.c_void_p), C0.ctypes.data_as(C.c_void_p)))
+            with pytest.raises(ZGError):
+                check(lib().zg_stationary_setup(tr._h, 0.0, np.zeros(_lib.ZG_MAX_LEADS).ctypes.data_as(C.c_void_p),
+                                                _lib.ZG_DH_NONE, 0.0, Sm1.ctypes.data_as(C.c_void_p),
+                                                np.zeros(L.n).ctypes.data_as(C.c_void_p)))
+            check(lib().zg_set_overlap(tr._h, None, None))
+        tr.set_slot(tr.stages, y)
+        tr.stage_input(0)
+        tr.rhs(0, 0.1, 0.01, [0.1, -0.1], _lib.ZG_DH_HUBBARD, p["hubbard_U"])
+        ks.append(tr.get_slot(0))
+        tr.close()
+    np.testing.assert_array_equal(ks[0], ks[1])
