@@ -259,6 +259,8 @@ def run_ours(args):
     tr.close()
     if args.precision == "mixed" and not args.no_f64_ref:
         out["f64_path"] = f64_reference_timing(w, dev, state, value, ms / args.steps)
+    if args.nonorth:
+        out["nozand"] = run_nonorth(args, dev)
     if rank == 0:
         if args.ensemble > 0:
             out["ensemble"] = run_ensemble(args)
@@ -459,6 +461,38 @@ def run_ensemble(args):
     return stats
 
 
+def run_nonorth(args, dev):
+    """The same workload posed in a non-orthogonal basis and propagated as the
+    reference's nozand does (overlap 1 + 0.08 x the bonds of H): attempts as
+    graph launches from its initial state, CUDA events on the trajectory's
+    stream; ms per attempt beside the orthogonal run's."""
+    import torch
+    from zandpack_gb300 import _lib
+    from zandpack_gb300.engine import Trajectory, native_bias
+    from zandpack_gb300.workloads import make_nonorth_workload
+    w = make_nonorth_workload(args.config)
+    tr = Trajectory(w.arrays, w.hbar, precision=args.precision, device=dev, nonorth=True)
+    stream = torch.cuda.ExternalStream(_lib.lib().zg_traj_stream(tr._h), device=dev)
+    tr.graph_prepare(native_bias(w.bias, tr.layout.NL), w.hubbard_U)
+    tr.set_y(tr.basis.sigma(w.arrays["DM_Ortho"]))
+    tr.graph_set(w.t0, w.stepsize, w.eps, 1e30)
+    adv = 0.0
+    for _ in range(max(3, args.warmup)):
+        tr.graph_run(1)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        recs, _, _, _ = tr.graph_run(1)
+        adv += sum(r[3] for r in recs if r[4])
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    tr.close()
+    return {"workload": "%s posed with an overlap (nozand)" % args.config, "precision": args.precision,
+            "ms_per_step": ms / args.steps, "value": adv / (ms / 1e3), "unit": "fs/s", "steps": args.steps}
+
+
 def run_steady(args):
     """The steady state (psinought) of a workload at its initial density matrix:
     GMRES on the device to a relative residual of 1e-8, as the reference's
@@ -511,6 +545,7 @@ def main():
     ap.add_argument("--slots", type=int, default=32, help="concurrent trajectories of the ensemble")
     ap.add_argument("--prep-workers", type=int, default=max(1, min(12, (os.cpu_count() or 4) - 4)),
                     help="worker processes preparing ensemble requests on the host")
+    ap.add_argument("--nonorth", type=int, default=1, help="also time the workload posed with an overlap (nozand)")
     ap.add_argument("--steady", default="c2", help="workload of the steady-state (psinought) timing ('' to skip)")
     args = ap.parse_args()
     if args.warmup < 3:
