@@ -239,6 +239,8 @@ def run_ours(args):
                 "algorithmic_tflops": alg_flops / t_launch / 1e12 if t_launch else None,
                 "ms_per_launch": t_launch * 1e3 if t_launch else None}
     roof["regions_ms_per_call"] = {k: (v[0] / v[1] if v[1] else None) for k, v in reg.items()}
+    if args.precision == "mixed":
+        roof["kernel_roofs"] = kernel_roofs(L, reg, tr.stages, peaks, tf32)
     out = {
         "metric": METRIC, "value": value, "unit": "fs/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -270,6 +272,44 @@ def run_ours(args):
         print(json.dumps(out))
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def kernel_roofs(L, reg, stages, peaks, tf32):
+    """Roofline fraction of every region of the mixed attempt: algorithmic
+    bytes (streaming regions, against the measured HBM copy rate of
+    MEASURED_PEAKS.json) or flops (against the live FP32 / cuBLAS TF32 peaks)
+    over the region's CUDA-event time per call."""
+    hbm = _peaks_file().get("hbm_gbs")
+    n, N, Ns, Nf, nc = L.n, L.N, L.Ns, L.Nf, L.nc
+    np_ = (n + 15) // 16 * 16
+    S = L.size
+    # DOP54 stage inputs read y + the nonzero k slots of their row: 1, 2, 3, 4, 5, 6, 6 slots
+    reads = [1, 2, 3, 4, 5, 6, 6][:stages]
+    stage_out = n * n + 2 * N * np_ + N * Ns + Ns * Nf  # sigma, psi hi and lo (planar), Omega
+    out = {}
+
+    def put(name, amount, unit, peak, peak_src):
+        ms, cnt = reg.get(name, (0.0, 0))
+        if not cnt or not peak:
+            return
+        t = ms / cnt / 1e3
+        ach = amount / t / (1e9 if unit == "GB/s" else 1e12)
+        out[name] = {"achieved": ach, "unit": unit, "peak": peak, "frac": ach / peak, "per_call": amount,
+                     "peak_source": peak_src}
+
+    mp = "MEASURED_PEAKS.json hbm_gbs"
+    put("combine", 8.0 * (sum(reads) * S + stages * stage_out) / stages, "GB/s", hbm, mp)
+    put("error", 8.0 * 6 * S, "GB/s", hbm, mp)
+    put("update", 8.0 * 5 * S + 16.0 * 2 * S + 8.0 * S, "GB/s", hbm, mp)
+    # psi: hi, lo, R1 (planar) in, k out, plus R2 on the sourced rows; sigma: T in, k out, T^T re-read
+    put("final", 8.0 * (4 * N * n + Ns * n) + 8.0 * 3 * n * n, "GB/s", hbm, mp)
+    fp32 = peaks[1] / 1e3 if peaks is not None else None
+    live = "live FFMA probe zg_measure_peaks"
+    put("small", 8.0 * (n * N * nc + Ns * nc * n + N * Ns * nc + Ns * Nf * nc), "TFLOP/s", fp32, live)
+    put("omega", 8.0 * (N * Ns * nc + Ns * Ns * nc + Ns * Nf * nc) + 10.0 * (N * Ns + Ns * Nf), "TFLOP/s", fp32, live)
+    # executed tensor flops of H sigma with a real H(t) (the workloads' Hamiltonians and Hubbard term)
+    put("gemm2", 3 * 2.0 * ((n + 31) // 32 * 32) * 2 * np_ * np_, "TFLOP/s", tf32, "live cuBLAS TF32")
+    return out
 
 
 def _peaks_file():
