@@ -236,6 +236,12 @@ int zg_split_tf32(const float* x, float* hi, float* lo, int64_t n, void* stream)
  * device-side wait gave up. */
 int zg_gemm_tf32x3(const float* Ah, const float* Al, const float* Bh, const float* Bl, float* D,
                    int M, int N, int K, void* stream);
+/* Self-test of the bounded device-side waits: one thread waits, with the
+ * GEMM's wait helper and a budget of `budget_cycles` SM clocks, on an
+ * mbarrier that nothing completes.  Returns ZG_ETIMEOUT when the wait gave
+ * up and reported it (the expected outcome; the context stays usable),
+ * ZG_OK if it did not. */
+int zg_wait_selftest(int device, long long budget_cycles);
 
 /* ------------------------------------------------------------------------
  * Stateless array kernels on caller device buffers (complex128), the

@@ -63,3 +63,23 @@ def test_gemm_tf32x3(M, N, K):
         ms = e0.elapsed_time(e1) / 5
         print("\nGEMM %dx%dx%d 3xTF32: %.3f ms, %.1f TFLOP/s (tensor flops %.1f)" % (
             M, N, K, ms, 2 * M * N * K / ms / 1e9, 6 * M * N * K / ms / 1e9))
+
+
+def test_bounded_wait_gives_up_and_context_survives():
+    """The bounded mbarrier wait of the tensor-core kernels, run on a barrier
+    that nothing completes with a ~1 ms budget, records its code and returns
+    (ZG_ETIMEOUT on the host); the context then still runs a GEMM."""
+    import torch
+    from zandpack_gb300 import _lib
+    from zandpack_gb300._lib import check, lib
+    assert lib().zg_wait_selftest(0, 2 * 1000 * 1000) == _lib.ZG_ETIMEOUT
+    M, N, K = 128, 128, 64
+    g = torch.Generator(device="cuda").manual_seed(5)
+    A = torch.randn(M, K, device="cuda", generator=g)
+    B = torch.randn(N, K, device="cuda", generator=g)
+    Ah, Al = _split(A)
+    Bh, Bl = _split(B)
+    D = torch.empty((M, N), device="cuda")
+    check(lib().zg_gemm_tf32x3(_p(Ah), _p(Al), _p(Bh), _p(Bl), _p(D), M, N, K, None))
+    ref = (Ah.double() + Al.double()) @ (Bh.double() + Bl.double()).T
+    assert (D.double() - ref).abs().max().item() / ref.abs().max().item() < 2e-6

@@ -85,6 +85,7 @@ _SIGS = {
     "zg_set_dH": ([_P, _P], C.c_int),
     "zg_set_dissipator": ([_P, _P], C.c_int),
     "zg_set_overlap": ([_P, _P, _P], C.c_int),
+    "zg_wait_selftest": ([C.c_int, C.c_longlong], C.c_int),
     "zg_rhs": ([_P, C.c_int, C.c_double, C.c_double, _P, C.c_int, C.c_double, _P], C.c_int),
     "zg_error_norm2": ([_P, _P], C.c_int),
     "zg_step_fourth": ([_P], C.c_int),

@@ -61,17 +61,34 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
   return ok != 0;
 }
 
-// bounded wait: true when the phase with `parity` completed, false on timeout
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err, int code) {
+// bounded wait: true when the phase with `parity` completed, false after
+// `budget` cycles (the error code is then recorded in *err)
+__device__ __forceinline__ bool mbar_wait_budget(uint32_t bar, uint32_t parity, int* err, int code,
+                                                 long long budget) {
   if (mbar_try(bar, parity)) return true;
   const long long t0 = clock64();
   while (!mbar_try(bar, parity)) {
-    if (clock64() - t0 > TC_WAIT_CYCLES) {
+    if (clock64() - t0 > budget) {
       atomicCAS(err, 0, code);
       return false;
     }
   }
   return true;
+}
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err, int code) {
+  return mbar_wait_budget(bar, parity, err, code, TC_WAIT_CYCLES);
+}
+
+// Self-test of the bounded wait: one thread waits on an mbarrier that
+// nothing arrives on, with the wait helper of the GEMM and a short budget.
+// The wait must give up, record `code` and return; nothing else is in flight.
+__global__ void k_wait_selftest(int* err, long long budget, int code) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x != 0) return;
+  const uint32_t b = smem_u32(&bar);
+  mbar_init(b, 1);
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  mbar_wait_budget(b, 0, err, code, budget);
 }
 
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, uint32_t bar, int x, int y) {
@@ -458,6 +475,31 @@ extern "C" int zg_gemm_tf32x3(const float* Ah, const float* Al, const float* Bh,
   ZG_CHECK_CUDA(cudaStreamSynchronize(s));
   if (herr != 0) {
     set_error("tensor-core GEMM wait timed out (code %d)", herr);
+    return ZG_ETIMEOUT;
+  }
+  return ZG_OK;
+}
+
+extern "C" int zg_wait_selftest(int device, long long budget_cycles) {
+  ZG_REQUIRE(budget_cycles > 0 && budget_cycles <= 4LL * 1000 * 1000 * 1000, "budget out of range");
+  ZG_CHECK_CUDA(cudaSetDevice(device));
+  int* err = nullptr;
+  ZG_CHECK_CUDA(cudaMalloc((void**)&err, sizeof(int)));
+  cudaError_t e = cudaMemset(err, 0, sizeof(int));
+  if (e == cudaSuccess) {
+    k_wait_selftest<<<1, 32>>>(err, budget_cycles, 7);
+    count_launch();
+    e = cudaGetLastError();
+  }
+  int herr = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(&herr, err, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(err);
+  if (e != cudaSuccess) {
+    set_error("%s", cudaGetErrorString(e));
+    return ZG_ECUDA;
+  }
+  if (herr != 0) {
+    set_error("bounded wait gave up as intended (code %d)", herr);
     return ZG_ETIMEOUT;
   }
   return ZG_OK;
