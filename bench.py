@@ -58,19 +58,66 @@ def _dist():
 
 
 class ClockSampler:
-    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+    """SM clocks and clock-event (throttle) reasons sampled during a region.
+
+    Reads NVML in-process (libnvidia-ml through ctypes, read-only queries) from
+    a thread every 5 ms, so that a timed region of tens of milliseconds still
+    gets several samples; falls back to ``nvidia-smi -lms 200``.  Samples go to
+    gpurun_out/bench_clocks.csv."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    # nvmlClocksEventReason bits
+    BITS = {"sw_power_cap": 0x4, "hw_slowdown": 0x8, "sw_thermal_slowdown": 0x20, "hw_thermal_slowdown": 0x40,
+            "hw_power_brake_slowdown": 0x80}
 
     def __init__(self, index=0):
         self.index = index
         self.p = None
+        self.nvml = None
+        self.rows = []
         self.path = os.path.join(HERE, "gpurun_out", "bench_clocks.csv")
 
+    def _nvml_open(self):
+        import ctypes
+        lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            return None
+        h = ctypes.c_void_p()
+        if lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(self.index), ctypes.byref(h)) != 0:
+            return None
+        mx = ctypes.c_uint()
+        if lib.nvmlDeviceGetMaxClockInfo(h, ctypes.c_int(1), ctypes.byref(mx)) != 0:
+            return None
+        reasons = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        return lib, h, mx.value, reasons
+
+    def _loop(self):
+        import ctypes
+        import time as _t
+        lib, h, mx, reasons = self.nvml
+        clk, rs = ctypes.c_uint(), ctypes.c_ulonglong()
+        while not self.stop:
+            ok = lib.nvmlDeviceGetClockInfo(h, ctypes.c_int(1), ctypes.byref(clk)) == 0
+            ok = ok and reasons(h, ctypes.byref(rs)) == 0
+            if ok:
+                self.rows.append((float(clk.value), float(mx), int(rs.value)))
+            _t.sleep(0.005)
+
     def __enter__(self):
+        import threading
+        os.makedirs(os.path.dirname(self.path), exist_ok=True)
         try:
-            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.nvml = self._nvml_open()
+        except Exception:
+            self.nvml = None
+        if self.nvml is not None:
+            self.stop = False
+            self.th = threading.Thread(target=self._loop, daemon=True)
+            self.th.start()
+            return self
+        try:
             self.f = open(self.path, "w")
             self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
                                        "--format=csv,noheader,nounits", "-lms", "200"],
@@ -80,6 +127,14 @@ class ClockSampler:
         return self
 
     def __exit__(self, *a):
+        if self.nvml is not None:
+            self.stop = True
+            self.th.join(timeout=5)
+            with open(self.path, "w") as f:
+                f.write("sm_mhz,sm_max_mhz,clocks_event_reasons\n")
+                for c, m, r in self.rows:
+                    f.write("%g,%g,0x%x\n" % (c, m, r))
+            return
         if self.p is not None:
             self.p.terminate()
             try:
@@ -89,6 +144,12 @@ class ClockSampler:
             self.f.close()
 
     def summary(self):
+        if self.nvml is not None:
+            if not self.rows:
+                return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+            reasons = sorted({k for _, _, r in self.rows for k, b in self.BITS.items() if r & b})
+            return {"sm_mhz": float(np.median([r[0] for r in self.rows])), "sm_max_mhz": max(r[1] for r in self.rows),
+                    "reasons": reasons, "samples": len(self.rows), "source": "NVML every 5 ms"}
         if self.p is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         rows = []
@@ -105,7 +166,7 @@ class ClockSampler:
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[i] for _, _, fl in rows for i, v in enumerate(fl) if v.lower() == "active"})
         return {"sm_mhz": float(np.median([r[0] for r in rows])), "sm_max_mhz": max(r[1] for r in rows),
-                "reasons": reasons, "samples": len(rows)}
+                "reasons": reasons, "samples": len(rows), "source": "nvidia-smi -lms 200"}
 
 
 def aggregate_ranks(ms, adv, device):
