@@ -191,16 +191,27 @@ def bias_value(b: dict, t: float, a: int) -> float:
     return 0.0
 
 
-def _sorted_eigh(M: np.ndarray):
-    """Hermitian eigenpairs sorted by decreasing |eigenvalue|; eigenvalues below
-    1e-12 of the largest are set to exactly zero."""
-    e, v = np.linalg.eigh(M)
+def _sort_pairs(e, v):
     order = np.argsort(-np.abs(e), kind="stable")
     e, v = e[order], v[:, order]
     if e.size:
         cut = 1e-12 * max(np.abs(e).max(), 1e-300)
         e = np.where(np.abs(e) < cut, 0.0, e)
     return e, v
+
+
+def _sorted_eigh(M: np.ndarray):
+    """Hermitian eigenpairs sorted by decreasing |eigenvalue|; eigenvalues below
+    1e-12 of the largest are set to exactly zero."""
+    e, v = np.linalg.eigh(M)
+    return _sort_pairs(e, v)
+
+
+def _sorted_eigh_stack(Ms: np.ndarray):
+    """_sorted_eigh of every matrix of a stack, in one LAPACK loop (the same
+    routine per matrix, so the same values as one call each)."""
+    es, vs = np.linalg.eigh(Ms)
+    return [_sort_pairs(es[i], vs[i]) for i in range(len(Ms))]
 
 
 def build_arrays(H: np.ndarray, coupling: list, lor: list, n_pade: int, kT: float = 0.025,
@@ -226,8 +237,9 @@ def build_arrays(H: np.ndarray, coupling: list, lor: list, n_pade: int, kT: floa
     for a in range(L):
         cen, wid, G = lor[a]
         nc = len(coupling[a])
+        lor_pairs = _sorted_eigh_stack(G[:N_L]) if N_L else []
         for x in range(N_L):
-            e, v = _sorted_eigh(G[x])
+            e, v = lor_pairs[x]
             epsx = np.array([cen[x] + 1j * wid[x]])
             fp = fermi_expanded(epsx, z, eta, beta, mu)[0]
             fm = fermi_expanded(epsx.conj(), z, eta, beta, mu)[0]
@@ -245,18 +257,24 @@ def build_arrays(H: np.ndarray, coupling: list, lor: list, n_pade: int, kT: floa
         def gamma_at(zz):
             s = wid ** 2 / ((zz - cen) ** 2 + wid ** 2)
             return np.tensordot(s, G, axes=(0, 0))
+        # Hermitian (part 0) and anti-Hermitian / i (part 1) parts of Gamma at the poles
+        Ms_p, Ms_m = [], []
         for p in range(NF):
-            for part in range(2):  # 0: B (Hermitian part), 1: C (anti-Hermitian part / i)
+            for part in range(2):
                 gp = gamma_at(poles_p[p])
                 gm = gamma_at(poles_m[p])
                 if part == 0:
-                    Mp = (gp + gp.conj().T) / 2
-                    Mm = (gm + gm.conj().T) / 2
+                    Ms_p.append((gp + gp.conj().T) / 2)
+                    Ms_m.append((gm + gm.conj().T) / 2)
                 else:
-                    Mp = (gp - gp.conj().T) / 2j
-                    Mm = (gm - gm.conj().T) / 2j
-                ep, vp = _sorted_eigh(Mp)
-                em, _ = _sorted_eigh(Mm)
+                    Ms_p.append((gp - gp.conj().T) / 2j)
+                    Ms_m.append((gm - gm.conj().T) / 2j)
+        pairs_p = _sorted_eigh_stack(np.array(Ms_p)) if NF else []
+        pairs_m = _sorted_eigh_stack(np.array(Ms_m)) if NF else []
+        for p in range(NF):
+            for part in range(2):  # 0: B (Hermitian part), 1: C (anti-Hermitian part / i)
+                ep, vp = pairs_p[2 * p + part]
+                em, _ = pairs_m[2 * p + part]
                 if part == 1:
                     ep = 1j * ep
                     em = 1j * em
