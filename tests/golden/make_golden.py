@@ -36,7 +36,7 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, HERE)
 
 import refharness  # noqa: E402
-from zandpack_gb300.workloads import make_workload, make_nonorth_workload  # noqa: E402
+from zandpack_gb300.workloads import make_kpoint_workload, make_nonorth_workload, make_workload  # noqa: E402
 from zandpack_gb300.arrays_io import write_arrays  # noqa: E402
 
 CASES = {
@@ -48,6 +48,8 @@ CASES = {
     # the same cases posed in a non-orthogonal basis, run through ``nozand``
     "nz_mini2": (1.0, 0.3, (0, 1, 9), 1),
     "nz_mini3": (1.0, 0.3, (0, 1, 9), 1),
+    # mini2 with two k-points (make_kpoint_workload)
+    "k2_mini2": (1.0, 0.3, (0, 1, 9), 1),
 }
 
 
@@ -68,7 +70,12 @@ def initial_py(w, t1, stepsize, saveevery=1):
 def make_case(name):
     t1, stepsize, keep, keep_every = CASES[name]
     nonorth = name.startswith("nz_")
-    w = make_nonorth_workload(name[3:]) if nonorth else make_workload(name)
+    if nonorth:
+        w = make_nonorth_workload(name[3:])
+    elif name.startswith("k2_"):
+        w = make_kpoint_workload(name[3:], nk=2)
+    else:
+        w = make_workload(name)
     A = w.arrays
     L = int(A["psi_shape"][1])
     nranks = L + 1
@@ -81,8 +88,7 @@ def make_case(name):
         rec = refharness.run_zand(d, nranks, keep_attempts=keep, script="nozand" if nonorth else "zand")
     roles, noT_lead = refharness.worker_roles(nranks, A)
     RK_N = 7
-    NK = 1
-    NL, NX, NOT, NO = (int(v) for v in A["psi_shape"][1:])
+    NK, NL, NX, NOT, NO = (int(v) for v in A["psi_shape"])
     out = {k: v for k, v in A.items()}
     out["params"] = np.array(json.dumps(dict(
         t0=w.t0, t1=t1, eps=w.eps, stepsize=stepsize, hbar=w.hbar, bias=w.bias,
@@ -108,8 +114,11 @@ def make_case(name):
     # saveevery=1 the first save holds [t0, t1] and later ones [t_step]
     tt = [np.asarray(times[s]).ravel() for s in steps]
     out["times"] = np.concatenate(tt)
-    out["currents"] = np.stack([np.concatenate([np.asarray(cur[a][s]).ravel() for s in steps])
+    # (NL, steps) for one k-point, (NL, steps, NK) for several
+    out["currents"] = np.stack([np.concatenate([np.asarray(cur[a][s]).reshape(-1, NK) for s in steps])
                                 for a in range(NL)])
+    if NK == 1:
+        out["currents"] = out["currents"][..., 0]
     sig = np.array(rec.sig_states)  # (nsteps, NK, NO, NO)
     out["sig_traj_idx"] = np.arange(0, len(sig), keep_every)
     out["sig_traj"] = sig[::keep_every]

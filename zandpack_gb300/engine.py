@@ -225,26 +225,61 @@ def native_bias(spec, n_leads):
     return b
 
 
+_PER_K = ("H_Ortho", "DM_Ortho", "Xpp", "Xpm", "GG_P", "GL_P", "GG_M", "GL_M", "diff_GGP_GLP", "diff_GGM_GLM",
+          "xi", "Ixi", "S^(-0.5)")
+
+
+def kpoint_arrays(arrays, k):
+    """The ``Arrays`` of k-point ``k`` alone (NK = 1): every per-k array sliced
+    to ``[k:k+1]`` (the leading NK axis, Zandpack/mpi/zand:113-124)."""
+    nk = int(np.asarray(arrays["H_Ortho"]).shape[0])
+    out = {}
+    for key in arrays.keys() if hasattr(arrays, "keys") else _PER_K:
+        v = arrays[key]
+        if key in _PER_K:
+            v = np.asarray(v)[k:k + 1]
+        elif key == "psi_shape":
+            v = np.array(v).copy()
+            v[0] = 1
+        out[key] = v
+    assert int(np.asarray(out["H_Ortho"]).shape[0]) == 1 and nk > k
+    return out
+
+
 class Propagator:
     """The ``zand`` time loop on the device (Zandpack/mpi/zand:297-430).
 
     ``bias(t, a)`` and ``dH(t, sigma)`` are the reference's callbacks; ``dH``
-    receives sigma with the k axis, shape (1, n, n), and may return 0.0.
+    receives sigma with the k axis, shape (NK, n, n), and may return 0.0.
     ``hubbard_U`` selects the built-in density-dependent term
     U * diag(Re sigma_ii - 0.5) evaluated on the device instead of ``dH``.
     ``nonorth=True`` runs the reference's ``nozand`` instead (non-orthogonal
     basis of ``arrays['S^(-0.5)']``): the state, the callbacks' sigma and the
     returned sigma are then sigma' (start from ``traj.basis.sigma(DM_Ortho)``).
+
+    Several k-points (NK > 1): one device trajectory per k-point
+    (``self.trajs``); every stage runs on all of them, the error norm is summed
+    over them and the controller is shared, as in ``zand`` where the k axis is
+    a batch axis of every array and ``TERR2_*`` sums over it.  States,
+    sigma and currents then carry the k axis (currents per step: NK x NL).
     """
 
     def __init__(self, arrays, hbar, bias: Callable, dH: Optional[Callable] = None,
                  dissipator: Optional[Callable] = None, hubbard_U: Optional[float] = None,
                  precision="f64", device=0, tableau: Tableau = DOP54, psi0=None, omg0=None,
                  dot_prod_zero_tol=1e-10, dH_depends_on_sigma=True, nonorth: bool = False):
-        self.traj = Trajectory(arrays, hbar, precision, device, psi0=psi0, omg0=omg0,
-                               dot_prod_zero_tol=dot_prod_zero_tol, nonorth=nonorth)
+        self.NK = int(np.asarray(arrays["H_Ortho"]).shape[0])
+        self.trajs = []
+        for k in range(self.NK):
+            A = arrays if self.NK == 1 else kpoint_arrays(arrays, k)
+            p0 = None if psi0 is None else np.asarray(psi0)[k:k + 1]
+            o0 = None if omg0 is None else np.asarray(omg0)[k:k + 1]
+            self.trajs.append(Trajectory(A, hbar, precision, device, psi0=p0, omg0=o0,
+                                         dot_prod_zero_tol=dot_prod_zero_tol, nonorth=nonorth))
+        self.traj = self.trajs[0]
         if tableau is not DOP54:
-            self.traj.set_tableau(tableau)
+            for tr in self.trajs:
+                tr.set_tableau(tableau)
         self.tab = tableau
         self.bias = bias
         self.dH = dH
@@ -254,28 +289,58 @@ class Propagator:
         self.NL = self.traj.layout.NL
         self.n_rhs = 0
 
+    def close(self):
+        for tr in self.trajs:
+            tr.close()
+
     def set_state(self, sig, psi=None, omg=None):
-        self.traj.set_y(sig, psi, omg)
+        if self.NK == 1:
+            self.traj.set_y(sig, psi, omg)
+            return
+        sig = np.asarray(sig)
+        for k, tr in enumerate(self.trajs):
+            tr.set_y(sig[k:k + 1], None if psi is None else np.asarray(psi)[k:k + 1],
+                     None if omg is None else np.asarray(omg)[k:k + 1])
+
+    def get_y(self):
+        """(sigma, psi, Omega) in the reference layout, with the k axis."""
+        parts = [tr.get_y() for tr in self.trajs]
+        return tuple(np.concatenate([p[i] for p in parts]) for i in range(3))
+
+    def get_sigma(self):
+        return np.concatenate([tr.get_y()[0] for tr in self.trajs]) if self.NK > 1 else self.traj.get_y()[0]
+
+    def step_fourth(self):
+        for tr in self.trajs:
+            tr.step_fourth()
 
     def _stage(self, i, t, h, want_J):
-        tr = self.traj
         ts = t + self.tab.A[i] * h
-        tr.stage_input(i)
-        mode, U = _lib.ZG_DH_NONE, 0.0
+        for tr in self.trajs:
+            tr.stage_input(i)
+        modes = [(_lib.ZG_DH_NONE, 0.0)] * self.NK
         if self.hubbard_U is not None:
-            mode, U = _lib.ZG_DH_HUBBARD, float(self.hubbard_U)
+            modes = [(_lib.ZG_DH_HUBBARD, float(self.hubbard_U))] * self.NK
         elif self.dH is not None:
-            sig = tr.stage_sigma()[None] if self.dH_depends_on_sigma else None
+            sig = (np.stack([tr.stage_sigma().copy() for tr in self.trajs])
+                   if self.dH_depends_on_sigma else None)
             dh = self.dH(ts, sig)
             if not (np.isscalar(dh) and dh == 0):
-                tr.set_dH(np.asarray(dh)[0] if np.ndim(dh) == 3 else dh)
-                mode = _lib.ZG_DH_MATRIX
+                dh = np.asarray(dh)
+                for k, tr in enumerate(self.trajs):
+                    tr.set_dH(dh[k] if dh.ndim == 3 else dh)
+                modes = [(_lib.ZG_DH_MATRIX, 0.0)] * self.NK
         if self.dissipator is not None:
-            dz = self.dissipator(ts, tr.stage_sigma()[None])
-            tr.set_dissipator(None if (np.isscalar(dz) and dz == 0) else dz)
+            dz = self.dissipator(ts, np.stack([tr.stage_sigma().copy() for tr in self.trajs]))
+            for k, tr in enumerate(self.trajs):
+                off = np.isscalar(dz) and dz == 0
+                tr.set_dissipator(None if off else (np.asarray(dz)[k] if np.ndim(dz) == 3 else dz))
         delta = [self.bias(ts, a) for a in range(self.NL)]
         self.n_rhs += 1
-        return tr.rhs(i, ts, h, delta, mode, U, currents=want_J)
+        Js = [tr.rhs(i, ts, h, delta, m, U, currents=want_J) for tr, (m, U) in zip(self.trajs, modes)]
+        if not want_J:
+            return None
+        return Js[0] if self.NK == 1 else np.array(Js)
 
     def attempt(self, t, h):
         """One attempt of all stages from the stored y; returns (TE, J at stage 0, err2 parts)."""
@@ -284,7 +349,7 @@ class Propagator:
             J = self._stage(i, t, h, want_J=(i == 0))
             if i == 0:
                 J0 = J
-        e = self.traj.error_norm2()
+        e = sum(tr.error_norm2() for tr in self.trajs)
         TE = math.sqrt(float(e.sum()))
         return TE, J0, e
 
@@ -299,7 +364,7 @@ class Propagator:
         t = float(t0)
         out = dict(times=[t], sig=[], currents=[], h_hist=[], TE_hist=[], t_attempt=[], accepted=[])
         if record_sigma:
-            out["sig"].append(self.traj.get_y()[0])
+            out["sig"].append(self.get_sigma())
         attempts = 0
         while t < t1:
             accepted = False
@@ -319,11 +384,11 @@ class Propagator:
                 if replay_h is not None and attempts < len(replay_h):
                     h = float(replay_h[attempts])
             out["currents"].append(J0)
-            self.traj.step_fourth()
+            self.step_fourth()
             t += h
             out["times"].append(t)
             if record_sigma:
-                out["sig"].append(self.traj.get_y()[0])
+                out["sig"].append(self.get_sigma())
             if on_step is not None:
                 on_step(t, h)
         return out

@@ -35,7 +35,7 @@ import numpy as np
 from .constants import HBAR
 from .pade import psd_poles, fermi_expanded
 
-__all__ = ["Workload", "make_workload", "make_nonorth_workload", "CONFIGS", "bias_value"]
+__all__ = ["Workload", "make_workload", "make_nonorth_workload", "make_kpoint_workload", "CONFIGS", "bias_value"]
 
 
 # ---------------------------------------------------------------- lattices
@@ -505,3 +505,32 @@ def make_nonorth_workload(name: str, s: float = 0.08, phases: bool = False) -> W
     A["Ixi"] = np.asarray(A["Ixi"]) @ Sm05
     A["S^(-0.5)"] = Sm05[None].astype(np.complex128)
     return dataclasses.replace(w, name=w.name + "-nonorth", arrays=A)
+
+
+# ------------------------------------------------------------ k-points
+def make_kpoint_workload(name: str, nk: int = 2, spread: float = 0.2) -> Workload:
+    """A workload of ``name`` with ``nk`` k-points (the leading NK axis of
+    every array, Zandpack/mpi/zand:113-124): k-point 0 is the named model, the
+    others add seeded random on-site energies in [-spread, spread] eV to H and
+    take their own isolated-device Fermi density matrix; the lead quantities
+    (poles, coupling coefficients, xi) are shared by all k-points."""
+    w = make_workload(name)
+    A = dict(w.arrays)
+    H0 = np.asarray(A["H_Ortho"])[0]
+    n = H0.shape[0]
+    rng = np.random.default_rng(4000 + nk)
+    Hs, DMs = [H0], [np.asarray(A["DM_Ortho"])[0]]
+    for _ in range(1, nk):
+        H = H0 + np.diag(rng.uniform(-spread, spread, n))
+        e, U = np.linalg.eigh(H)
+        f = 1.0 / (1.0 + np.exp(e / w.kT))
+        Hs.append(H)
+        DMs.append((U * f) @ U.conj().T)
+    A["H_Ortho"] = np.array(Hs, np.complex128)
+    A["DM_Ortho"] = np.array(DMs, np.complex128)
+    for k in ("Xpp", "Xpm", "GG_P", "GL_P", "GG_M", "GL_M", "diff_GGP_GLP", "diff_GGM_GLM", "xi", "Ixi"):
+        A[k] = np.repeat(np.asarray(A[k]), nk, axis=0)
+    ps = np.array(A["psi_shape"])
+    ps[0] = nk
+    A["psi_shape"] = ps
+    return dataclasses.replace(w, name="%s-k%d" % (w.name, nk), arrays=A)

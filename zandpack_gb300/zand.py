@@ -183,7 +183,8 @@ class ZandRun:
                 psi0 = np.load(save + "last_psi.npy")
                 omg0 = np.load(save + "last_omg.npy")
                 if self.nonorth:  # rows S^-1/2 psi (Zandpack/mpi/nozand:722)
-                    psi0 = np.asarray(psi0, np.complex128) @ Sm05[0].T
+                    psi0 = np.concatenate([np.asarray(psi0[k:k + 1], np.complex128) @ Sm05[k].T
+                                           for k in range(Sm05.shape[0])])
         dh_dev = getattr(B, "dH_device", None)
         hub = float(dh_dev["U"]) if isinstance(dh_dev, dict) and dh_dev.get("kind") == "hubbard" else None
         diss = getattr(B, "dissipator", None)
@@ -193,18 +194,17 @@ class ZandRun:
         self.prop = pr
         tr = pr.traj
         L = tr.layout
-        z = L.unpack(np.zeros(L.size, complex))
-        pr.set_state(sig0, z[1] if psi0 is None else psi0, z[2] if omg0 is None else omg0)
+        pr.set_state(sig0, psi0, omg0)  # psi = Omega = 0 when not loaded
         self.log("zandpack_gb300 %s: %s, precision %s, n=%d, %d live modes of %d padded, eps=%g" % (
             "nozand" if self.nonorth else "zand", self.name, self.precision, L.n, L.N, L.padded_modes, self.eps))
         occ_mask = None
         if self.dm_occ_only:
-            S05 = tr.basis.S05
+            S05 = np.concatenate([x.basis.S05 for x in pr.trajs])
             occ_mask = np.abs(S05 @ S05) > 1e-6                    # Zandpack/mpi/nozand:261-262
         self.log("Timedependent Bias:\n" + _source(B.bias))
         NL = L.NL
         currents = [[] for _ in range(NL)]
-        DM = [tr.get_y()[0]]
+        DM = [pr.get_sigma()]
         times = [t0]
         PI_holder = []
         step_count = 0
@@ -219,24 +219,24 @@ class ZandRun:
                 old_h = h
                 h = pr.tab.hnew(h, TE, self.eps)
             for a in range(NL):
-                currents[a].append(np.array([J0[a]]))
+                currents[a].append(np.array([J0[a]]) if pr.NK == 1 else np.asarray(J0)[:, a])
             if self.save_PI:
-                PI_holder.append(self._pi_from_state(L, tr))
+                PI_holder.append(np.concatenate([self._pi_from_state(x.layout, x) for x in pr.trajs]))
             # checkpoints: the state before the update, as the reference saves it
             passed = (t > self.checkpoints) * (self.checkpoint_done == 0)
             if self.save_checkpoints and passed.any():
-                sig, psi, omg = tr.get_y()
+                sig, psi, omg = pr.get_y()
                 np.save(save + "last_sig", sig)
                 np.save(save + "last_time", t)
                 np.save(save + "last_stepsize", old_h)
                 if self.nonorth:  # back to the orthogonal basis: rows S^1/2 psi'
-                    psi = psi @ tr.basis.S05[0].T
+                    psi = np.concatenate([psi[k:k + 1] @ x.basis.S05[0].T for k, x in enumerate(pr.trajs)])
                 np.save(save + "last_psi", psi)
                 np.save(save + "last_omg", omg)
                 self.checkpoint_done[np.where(passed)[0][0]] = 1
-            tr.step_fourth()
+            pr.step_fourth()
             t += h
-            DM.append(self._sigma(tr))
+            DM.append(np.concatenate([self._sigma(x) for x in pr.trajs]))
             times.append(t + 0.0)
             step_count += 1
             if np.mod(step_count, self.saveevery) == 0 and step_count >= self.saveevery:
