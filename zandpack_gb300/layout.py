@@ -60,7 +60,7 @@ class CompactLayout:
         if H0.ndim != 3 or H0.shape[1] != H0.shape[2]:
             raise LayoutError("H_Ortho must have shape (NK, NO, NO)")
         if H0.shape[0] != 1:
-            raise LayoutError("only NK = 1 (one k-point) is supported on the device path")
+            raise LayoutError("a trajectory holds one k-point (NK = 1); engine.Propagator runs one per k-point")
         self.hbar = float(hbar)
         self.H0 = H0[0]
         self.n = n = H0.shape[-1]
