@@ -97,6 +97,7 @@ struct GemmBatch {
   int nprob;
   int total_tiles;
   int bn;                 // tile width chosen by the planner (32 or 64)
+  int want_bn;            // 32: 128x32 tiles whatever the widths (0: the planner chooses)
   typename cx<T>::t* ws;  // split-K workspace
   GemmProb<T> p[ZG_MAX_GEMM];
 };

@@ -226,7 +226,7 @@ int64_t plan_zgemm_batch(GemmBatch<T>& b) {
   // tile width: 32 when every problem is at most 32 wide
   int maxN = 0;
   for (int i = 0; i < b.nprob; ++i) maxN = b.p[i].N > maxN ? b.p[i].N : maxN;
-  b.bn = maxN <= 32 ? 32 : 64;
+  b.bn = b.want_bn == 32 || maxN <= 32 ? 32 : 64;
   const int BN = b.bn, BM = 4 * (256 / (BN / 4));
   // A problem with few output tiles and a long K would serialise on a handful
   // of CTAs (the batch is then less than one wave, and its longest tile sets

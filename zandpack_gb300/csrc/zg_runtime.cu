@@ -905,16 +905,21 @@ static void gemm_prob_f32(std::vector<GemmProb<float>>& v, const float2* A, cons
 template <typename R>
 static int run_batches(zg_traj* t, std::vector<GemmProb<R>>& all, typename cx<R>::t** ws, int64_t* cap,
                        cudaStream_t s, bool plan_only) {
-  // problems at most 32 wide (the n_c-wide products) run with 128x32 tiles
+  // problems at most 32 wide (the n_c-wide products), and wide ones with a
+  // short K (the xi sigma^T rows, K = n_c), run with 128x32 tiles in one
+  // launch; the rest with 64x64 tiles
+  auto narrow_p = [](const GemmProb<R>& P) { return P.N <= 32 || P.K <= 64; };
   std::vector<GemmProb<R>> probs;
   for (int pass = 0; pass < 2; ++pass)
     for (const auto& P : all)
-      if ((P.N <= 32) == (pass == 0)) probs.push_back(P);
+      if (narrow_p(P) == (pass == 0)) probs.push_back(P);
   size_t narrow = 0;
-  for (const auto& P : all) narrow += P.N <= 32;
+  for (const auto& P : all) narrow += narrow_p(P);
   for (size_t b0 = 0; b0 < probs.size();) {
     GemmBatch<R> batch;
-    const size_t end = b0 < narrow ? narrow : probs.size();
+    const bool nar = b0 < narrow;
+    batch.want_bn = nar ? 32 : 0;
+    const size_t end = nar ? narrow : probs.size();
     batch.nprob = (int)std::min<size_t>(ZG_MAX_GEMM, end - b0);
     for (int i = 0; i < batch.nprob; ++i) batch.p[i] = probs[b0 + i];
     b0 += batch.nprob;
