@@ -331,8 +331,8 @@ int launch_set_params(const StageParams& p, StageParams* out, cudaStream_t s) {
   return ZG_OK;
 }
 
-__global__ void k_stage_prologue(const DevCtl* __restrict__ ctl, zg_bias b, double A_i, double hbar,
-                                 StageParams* __restrict__ out) {
+__device__ __forceinline__ void k_stage_prologue_body(const DevCtl* __restrict__ ctl, const zg_bias& b, double A_i,
+                                                      double hbar, StageParams* __restrict__ out) {
   const double t = ctl->t, h = ctl->h;
   const double ts = t + A_i * h;
   const int a = threadIdx.x;
@@ -354,6 +354,25 @@ __global__ void k_stage_prologue(const DevCtl* __restrict__ ctl, zg_bias b, doub
     out->finv_hb = (float)out->inv_hb;
     out->fh_hb2 = (float)out->h_hb2;
   }
+}
+
+__global__ void k_stage_prologue(const DevCtl* __restrict__ ctl, zg_bias b, double A_i, double hbar,
+                                 StageParams* __restrict__ out) {
+  k_stage_prologue_body(ctl, b, A_i, hbar, out);
+}
+
+__global__ void k_stage_prologues(const DevCtl* __restrict__ ctl, zg_bias b, StageNodes A, double hbar,
+                                  StageParams* __restrict__ out) {
+  k_stage_prologue_body(ctl, b, A.A[blockIdx.x], hbar, out + blockIdx.x);
+}
+
+int launch_stage_prologues(const DevCtl* ctl, const zg_bias& b, const StageNodes& A, int nst, double hbar,
+                           StageParams* out, cudaStream_t s) {
+  ZG_REQUIRE(nst >= 1 && nst <= ZG_MAX_STAGES, "stage count %d out of range", nst);
+  k_stage_prologues<<<nst, 32, 0, s>>>(ctl, b, A, hbar, out);
+  ZG_CHECK_LAUNCH();
+  count_launch();
+  return ZG_OK;
 }
 
 int launch_stage_prologue(const DevCtl* ctl, const zg_bias& b, double A_i, double hbar, StageParams* out,

@@ -161,6 +161,12 @@ int launch_set_params(const StageParams& p, StageParams* out, cudaStream_t s);
 // *out = h, ts = t + A_i h, hbar, delta[a] = bias(ts, a) from the device controller
 int launch_stage_prologue(const DevCtl* ctl, const zg_bias& b, double A_i, double hbar, StageParams* out,
                           cudaStream_t s);
+// the same for all stages of an attempt at once: out[i] from A[i], i < nst
+struct StageNodes {
+  double A[ZG_MAX_STAGES];
+};
+int launch_stage_prologues(const DevCtl* ctl, const zg_bias& b, const StageNodes& A, int nst, double hbar,
+                           StageParams* out, cudaStream_t s);
 // TE = sqrt(err[0]+err[1]+err[2]); accepted = TE < eps; hnew = 0.9 h (eps/TE)^(1/5);
 // an attempt that starts after done is skipped (accepted = 0)
 int launch_control(const double* err3, DevCtl* ctl, cudaStream_t s);

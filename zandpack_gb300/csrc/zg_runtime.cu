@@ -666,7 +666,7 @@ int zg_traj_create(int device, const zg_layout* Lo, int precision, zg_traj** out
   ZG_STEP(dalloc(t, &t->dH, n * n));
   ZG_STEP(dalloc(t, &t->J, L));
   ZG_STEP(dalloc(t, &t->Jpart, L * 64));
-  ZG_STEP(dalloc(t, &t->d_params, 1));
+  ZG_STEP(dalloc(t, &t->d_params, ZG_MAX_STAGES));  // one per stage in the attempt graph
   ZG_STEP(dalloc(t, &t->ctl, 1));
   ZG_STEP(dalloc(t, &t->d_recs, ZG_GRAPH_MAX_BATCH));
   {
@@ -1312,14 +1312,18 @@ extern "C" int zg_set_overlap(zg_traj* t, const double* Sm1, const double* C0) {
 // advance, then the controller and the tensor-core error flag to pinned memory.
 static int enqueue_attempt_device(zg_traj* t) {
   cudaStream_t s = t->stream;
+  // every stage's time, step size and biases at once (they depend only on the
+  // controller's t and h, which change at the end of the attempt)
+  StageNodes nodes;
+  for (int i = 0; i < t->stages; ++i) nodes.A[i] = t->A[i];
+  ZG_TRY(launch_stage_prologues(t->ctl, t->gbias, nodes, t->stages, t->hbar, t->d_params, s));
   for (int i = 0; i < t->stages; ++i) {
     ZG_TRY(zg_stage_input(t, i));
     prof_begin(t, ZG_PROF_RHS);
-    ZG_TRY(launch_stage_prologue(t->ctl, t->gbias, t->A[i], t->hbar, t->d_params, s));
     if (t->precision == ZG_PREC_F64)
-      ZG_TRY(rhs_f64(t, i, t->d_params, t->g_dH_mode, t->g_U, i == 0));
+      ZG_TRY(rhs_f64(t, i, t->d_params + i, t->g_dH_mode, t->g_U, i == 0));
     else
-      ZG_TRY(rhs_mixed(t, i, t->d_params, t->g_dH_mode, t->g_U, i == 0));
+      ZG_TRY(rhs_mixed(t, i, t->d_params + i, t->g_dH_mode, t->g_U, i == 0));
     prof_end(t, ZG_PROF_RHS);
   }
   ZG_TRY(enqueue_error(t));
