@@ -292,14 +292,16 @@ int launch_zgemm_batch(GemmBatch<T>& b, int64_t ws_capacity, cudaStream_t s) {
 }
 
 // ============================================================ RHS helpers
+// gather elements e = first, first + stride, ... of sigC and G
 template <typename T>
-__global__ void k_gathers(const RhsDev<T> d, const typename cx<T>::t* __restrict__ sig,
-                          const typename cx<T>::t* __restrict__ psi, const typename cx<T>::t* __restrict__ psi_lo,
-                          int64_t ldpsi, typename cx<T>::t* __restrict__ sigC, typename cx<T>::t* __restrict__ G,
-                          int64_t plane) {
+__device__ __forceinline__ void gathers_job(const RhsDev<T>& d, const typename cx<T>::t* __restrict__ sig,
+                                            const typename cx<T>::t* __restrict__ psi,
+                                            const typename cx<T>::t* __restrict__ psi_lo, int64_t ldpsi,
+                                            typename cx<T>::t* __restrict__ sigC, typename cx<T>::t* __restrict__ G,
+                                            int64_t plane, int64_t first, int64_t stride) {
   const int64_t ns = (int64_t)d.L * d.n * d.nc;
   const int64_t ng = (int64_t)d.N * d.L * d.nc;
-  GRID_STRIDE(e, ns + ng) {
+  for (int64_t e = first; e < ns + ng; e += stride) {
     if (e < ns) {
       const int k = (int)(e % d.nc);
       const int64_t r = e / d.nc;
@@ -327,6 +329,15 @@ __global__ void k_gathers(const RhsDev<T> d, const typename cx<T>::t* __restrict
       G[g] = v;
     }
   }
+}
+
+template <typename T>
+__global__ void k_gathers(const RhsDev<T> d, const typename cx<T>::t* __restrict__ sig,
+                          const typename cx<T>::t* __restrict__ psi, const typename cx<T>::t* __restrict__ psi_lo,
+                          int64_t ldpsi, typename cx<T>::t* __restrict__ sigC, typename cx<T>::t* __restrict__ G,
+                          int64_t plane) {
+  gathers_job<T>(d, sig, psi, psi_lo, ldpsi, sigC, G, plane, blockIdx.x * (int64_t)blockDim.x + threadIdx.x,
+                 (int64_t)gridDim.x * blockDim.x);
 }
 
 template <typename T>
@@ -1055,15 +1066,14 @@ __device__ __forceinline__ void put_split(float* __restrict__ hi, float* __restr
 // H(t) part): 0 = every entry, 1 = the diagonal only (the blocks on the
 // diagonal), 2 = none.  Padding (r or c >= n) is written as zero.
 template <int HP>
-__global__ void __launch_bounds__(256) k_build_operands_mixed(int n, int np, const double2* __restrict__ H0,
-                                                              const float2* __restrict__ sig32,
-                                                              const double2* __restrict__ dH, int dH_mode, double U,
-                                                              float* __restrict__ Hth, float* __restrict__ Htl,
-                                                              float* __restrict__ BSh, float* __restrict__ BSl,
-                                                              const double2* __restrict__ Sm1) {
+__device__ __forceinline__ void operands_tile(int bx, int by, int n, int np, const double2* __restrict__ H0,
+                                              const float2* __restrict__ sig32, const double2* __restrict__ dH,
+                                              int dH_mode, double U, float* __restrict__ Hth,
+                                              float* __restrict__ Htl, float* __restrict__ BSh,
+                                              float* __restrict__ BSl, const double2* __restrict__ Sm1) {
   __shared__ float2 tile[32][33];  // tile[k][j] = sigma[c0 + k][r0 + j]
   const int64_t nn = (int64_t)np * np;
-  const int r0 = blockIdx.y * 32, c0 = blockIdx.x * 32;
+  const int r0 = by * 32, c0 = bx * 32;
   const int tx = threadIdx.x, ty = threadIdx.y;
   for (int k = ty; k < 32; k += 8) {
     const int row = c0 + k, col = r0 + tx;
@@ -1086,6 +1096,62 @@ __global__ void __launch_bounds__(256) k_build_operands_mixed(int n, int np, con
       put_split(Hth, Htl, o, nn, hr, hi);
     }
   }
+}
+
+template <int HP>
+__global__ void __launch_bounds__(256) k_build_operands_mixed(int n, int np, const double2* __restrict__ H0,
+                                                              const float2* __restrict__ sig32,
+                                                              const double2* __restrict__ dH, int dH_mode, double U,
+                                                              float* __restrict__ Hth, float* __restrict__ Htl,
+                                                              float* __restrict__ BSh, float* __restrict__ BSl,
+                                                              const double2* __restrict__ Sm1) {
+  operands_tile<HP>(blockIdx.x, blockIdx.y, n, np, H0, sig32, dH, dH_mode, U, Hth, Htl, BSh, BSl, Sm1);
+}
+
+// The operand tiles (blocks [0, nb*nb)) and the gathers of the Omega and
+// xi sigma^T products (the remaining blocks) of a mixed stage in one launch.
+template <int HP>
+__global__ void __launch_bounds__(256) k_prep_mixed(int n, int np, int nb, const double2* __restrict__ H0,
+                                                    const float2* __restrict__ sig32, const double2* __restrict__ dH,
+                                                    int dH_mode, double U, float* __restrict__ Hth,
+                                                    float* __restrict__ Htl, float* __restrict__ BSh,
+                                                    float* __restrict__ BSl, const double2* __restrict__ Sm1,
+                                                    const RhsDev<float> d, const float2* __restrict__ psih,
+                                                    const float2* __restrict__ psil, int64_t ldpsi,
+                                                    float2* __restrict__ sigC, float2* __restrict__ G,
+                                                    int64_t plane) {
+  const int ntb = nb * nb;
+  if ((int)blockIdx.x < ntb) {
+    operands_tile<HP>(blockIdx.x % nb, blockIdx.x / nb, n, np, H0, sig32, dH, dH_mode, U, Hth, Htl, BSh, BSl, Sm1);
+  } else {
+    const int tid = threadIdx.y * 32 + threadIdx.x;
+    gathers_job<float>(d, sig32, psih, psil, ldpsi, sigC, G, plane, (int64_t)(blockIdx.x - ntb) * 256 + tid,
+                       (int64_t)(gridDim.x - ntb) * 256);
+  }
+}
+
+int launch_prep_mixed(int n, int np, const double2* H0, const float2* sig32, const double2* dH, int dH_mode,
+                      double U, int h_part, float* Hth, float* Htl, float* BSh, float* BSl, const double2* Sm1,
+                      const RhsDev<float>& d, const float2* psih, const float2* psil, int64_t ldpsi, float2* sigC,
+                      float2* G, int64_t plane, cudaStream_t s) {
+  ZG_REQUIRE(h_part >= 0 && h_part <= 2, "bad operand part %d", h_part);
+  ZG_REQUIRE(!(Sm1 && dH_mode == ZG_DH_HUBBARD && h_part == 1), "the overlap's Hubbard term changes every entry");
+  const int nb = (np + 31) / 32;
+  const int64_t tot = (int64_t)d.L * d.n * d.nc + (int64_t)d.N * d.L * d.nc;
+  const int gb = grid_for(tot, 256, 152 * 4);
+  const dim3 grid(nb * nb + gb), block(32, 8);
+  if (h_part == 0)
+    k_prep_mixed<0><<<grid, block, 0, s>>>(n, np, nb, H0, sig32, dH, dH_mode, U, Hth, Htl, BSh, BSl, Sm1, d, psih,
+                                           psil, ldpsi, sigC, G, plane);
+  else if (h_part == 1)
+    k_prep_mixed<1><<<grid, block, 0, s>>>(n, np, nb, H0, sig32, dH, dH_mode, U, Hth, Htl, BSh, BSl, Sm1, d, psih,
+                                           psil, ldpsi, sigC, G, plane);
+  else
+    k_prep_mixed<2><<<grid, block, 0, s>>>(n, np, nb, H0, sig32, dH, dH_mode, U, Hth, Htl, BSh, BSl, Sm1, d, psih,
+                                           psil, ldpsi, sigC, G, plane);
+  ZG_CHECK_LAUNCH();
+  count_launch();
+  return ZG_OK;
 }
 
 int launch_build_operands_mixed(int n, int np, const double2* H0, const float2* sig32, const double2* dH, int dH_mode,

@@ -1048,11 +1048,9 @@ static int rhs_mixed(zg_traj* t, int stage, const StageParams* p, int dH_mode, d
       t->h_offdiag_ready = true;
     }
     t->h_diag_mode = dH_mode;
-    ZG_TRY(launch_build_operands_mixed((int)n, (int)np, t->nonorth ? t->Hn0 : t->H0, sig, t->nonorth ? t->dHn : t->dH,
-                                       dH_mode, hubbard_U, h_part, t->Hth, t->Htl, t->BSh, t->BSl, s,
-                                       t->nonorth ? t->Sm1 : nullptr));
-    ZG_TRY(launch_gathers<float>(d, sig, (const float2*)psih_f, (const float2*)psil_f, np, t->sigC32, t->G32, s,
-                                 ml.plane));
+    ZG_TRY(launch_prep_mixed((int)n, (int)np, t->nonorth ? t->Hn0 : t->H0, sig, t->nonorth ? t->dHn : t->dH, dH_mode,
+                             hubbard_U, h_part, t->Hth, t->Htl, t->BSh, t->BSl, t->nonorth ? t->Sm1 : nullptr, d,
+                             (const float2*)psih_f, (const float2*)psil_f, np, t->sigC32, t->G32, ml.plane, s));
     prof_end(t, ZG_PROF_PREP);
     // tensor cores: R1 = psi H(t)^T
     prof_begin(t, ZG_PROF_GEMM);
