@@ -212,7 +212,7 @@ template <typename T>
 // (h/hbar^2)(W + W^H) replaces the lead terms (Pc is then not read)
 int launch_sigma_finalize(const RhsDev<T>& d, const StageParams* p, const typename cx<T>::t* Tm, int64_t ldT,
                           const typename cx<T>::t* Pc, const double2* dis, typename cx<T>::t* ksig, cudaStream_t s,
-                          int tmode = 0, int npl = 0, const typename cx<T>::t* W = nullptr);
+                          int tmode = 0, int npl = 0, const typename cx<T>::t* W = nullptr, bool leads = true);
 template <typename T>
 int launch_currents(const RhsDev<T>& d, const StageParams* p, const typename cx<T>::t* Pc, double* J, cudaStream_t s);
 template <typename T>
@@ -263,6 +263,15 @@ int launch_build_ht(int n, const double2* H0, const double2* sig, const double2*
 int launch_build_operands_mixed(int n, int np, const double2* H0, const float2* sig32, const double2* dH, int dH_mode,
                                 double U, int h_part, float* Hth, float* Htl, float* BSh, float* BSl, cudaStream_t s,
                                 const double2* Sm1 = nullptr);
+// the lead terms of k_sigma (after launch_sigma_finalize(..., leads = false);
+// Pc = null: none) and the psi finalisation of a mixed stage in one launch,
+// for planar psi hi/lo and planar R1 (final_mixed_ok)
+bool final_mixed_ok(const RhsDev<float>& d, const float2* psi, const float2* psi_lo, int64_t ldpsi, const float2* R1,
+                    int64_t ldR1, int64_t plane, int rmode, int npl);
+int launch_final_mixed(const RhsDev<float>& d, const StageParams* p, const float2* Pc, float2* ksig,
+                       const float2* psi, const float2* psi_lo, int64_t ldpsi, const float2* R1, int64_t ldR1,
+                       const float2* R2, const float2* ZA, const float2* ZB, float2* kpsi, int64_t plane, int rmode,
+                       int npl, const float2* R3, const float2* C0, cudaStream_t s);
 // launch_build_operands_mixed and launch_gathers<float> of a mixed stage in one launch
 int launch_prep_mixed(int n, int np, const double2* H0, const float2* sig32, const double2* dH, int dH_mode,
                       double U, int h_part, float* Hth, float* Htl, float* BSh, float* BSl, const double2* Sm1,

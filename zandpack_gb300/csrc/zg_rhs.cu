@@ -431,15 +431,14 @@ __global__ void __launch_bounds__(256) k_sigma_finalize(const RhsDev<T> d, const
 // orbital, each element once: columns j in U for every row i, then rows i in U
 // for the columns j not in U.
 template <typename T>
-__global__ void __launch_bounds__(256) k_sigma_leads(const RhsDev<T> d, const StageParams* __restrict__ pp,
-                                                     const typename cx<T>::t* __restrict__ Pc,
-                                                     typename cx<T>::t* __restrict__ ksig) {
+__device__ __forceinline__ void sigma_leads_job(const RhsDev<T>& d, const StageScalars& p,
+                                                const typename cx<T>::t* __restrict__ Pc,
+                                                typename cx<T>::t* __restrict__ ksig, int64_t first, int64_t stride) {
   using C = typename cx<T>::t;
-  const StageScalars p = load_params(pp);
   const T f = pv<T>(p.h_hb2, p.fh_hb2);
   const int n = d.n, nu = d.nu;
   const int64_t half = (int64_t)nu * n;
-  GRID_STRIDE(q, 2 * half) {
+  for (int64_t q = first; q < 2 * half; q += stride) {
     int i, j;
     if (q < half) {
       i = (int)(q / nu);
@@ -461,9 +460,17 @@ __global__ void __launch_bounds__(256) k_sigma_leads(const RhsDev<T> d, const St
 }
 
 template <typename T>
+__global__ void __launch_bounds__(256) k_sigma_leads(const RhsDev<T> d, const StageParams* __restrict__ pp,
+                                                     const typename cx<T>::t* __restrict__ Pc,
+                                                     typename cx<T>::t* __restrict__ ksig) {
+  const StageScalars p = load_params(pp);
+  sigma_leads_job<T>(d, p, Pc, ksig, blockIdx.x * (int64_t)blockDim.x + threadIdx.x, (int64_t)gridDim.x * blockDim.x);
+}
+
+template <typename T>
 int launch_sigma_finalize(const RhsDev<T>& d, const StageParams* p, const typename cx<T>::t* Tm, int64_t ldT,
                           const typename cx<T>::t* Pc, const double2* dis, typename cx<T>::t* ksig, cudaStream_t s,
-                          int tmode, int npl, const typename cx<T>::t* W) {
+                          int tmode, int npl, const typename cx<T>::t* W, bool leads) {
   ZG_REQUIRE(tmode >= 0 && tmode <= 2, "bad T layout %d", tmode);
   const int nb = (d.n + 31) / 32;
   if (dis)
@@ -472,7 +479,7 @@ int launch_sigma_finalize(const RhsDev<T>& d, const StageParams* p, const typena
     k_sigma_finalize<T, false><<<dim3(nb, nb), dim3(32, 8), 0, s>>>(d, p, Tm, ldT, dis, ksig, tmode, npl, W);
   ZG_CHECK_LAUNCH();
   count_launch();
-  if (d.nu > 0 && !W) {
+  if (d.nu > 0 && !W && leads) {
     const int64_t tot = 2 * (int64_t)d.nu * d.n;
     k_sigma_leads<T><<<grid_for(tot, 256, 152 * 8), 256, 0, s>>>(d, p, Pc, ksig);
     ZG_CHECK_LAUNCH();
@@ -681,19 +688,18 @@ __device__ __forceinline__ fvec<V> ldv(const float* p) {
 }
 
 template <int RMODE, int V>
-__global__ void __launch_bounds__(256) k_psi_finalize_v4(const RhsDev<float> d, const StageParams* __restrict__ pp,
-                                                         const float* __restrict__ ph, const float* __restrict__ pl,
-                                                         int64_t ldpsi, int64_t plane, const float* __restrict__ R1,
-                                                         int64_t ldR1, int npl, const float2* __restrict__ R2,
-                                                         const float2* __restrict__ ZA, const float2* __restrict__ ZB,
-                                                         float2* __restrict__ kpsi, const float2* __restrict__ R3,
-                                                         const float2* __restrict__ C0) {
-  const StageScalars p = load_params(pp);
+__device__ __forceinline__ void psi_v4_job(const RhsDev<float>& d, const StageScalars& p, const float* __restrict__ ph,
+                                           const float* __restrict__ pl, int64_t ldpsi, int64_t plane,
+                                           const float* __restrict__ R1, int64_t ldR1, int npl,
+                                           const float2* __restrict__ R2, const float2* __restrict__ ZA,
+                                           const float2* __restrict__ ZB, float2* __restrict__ kpsi,
+                                           const float2* __restrict__ R3, const float2* __restrict__ C0,
+                                           int64_t first, int64_t stride) {
   const float ih = p.finv_hb;
   const float h = p.fh;
   const int n = d.n, nq = n / V, nc = d.nc, L = d.L;
   const int64_t total = (int64_t)d.N * nq;
-  GRID_STRIDE(q, total) {
+  for (int64_t q = first; q < total; q += stride) {
     const int m = (int)(q / nq);
     const int i0 = (int)(q - (int64_t)m * nq) * V;
     const bool src = m < d.Ns;
@@ -744,6 +750,39 @@ __global__ void __launch_bounds__(256) k_psi_finalize_v4(const RhsDev<float> d, 
   }
 }
 
+template <int RMODE, int V>
+__global__ void __launch_bounds__(256) k_psi_finalize_v4(const RhsDev<float> d, const StageParams* __restrict__ pp,
+                                                         const float* __restrict__ ph, const float* __restrict__ pl,
+                                                         int64_t ldpsi, int64_t plane, const float* __restrict__ R1,
+                                                         int64_t ldR1, int npl, const float2* __restrict__ R2,
+                                                         const float2* __restrict__ ZA, const float2* __restrict__ ZB,
+                                                         float2* __restrict__ kpsi, const float2* __restrict__ R3,
+                                                         const float2* __restrict__ C0) {
+  const StageScalars p = load_params(pp);
+  psi_v4_job<RMODE, V>(d, p, ph, pl, ldpsi, plane, R1, ldR1, npl, R2, ZA, ZB, kpsi, R3, C0,
+                       blockIdx.x * (int64_t)blockDim.x + threadIdx.x, (int64_t)gridDim.x * blockDim.x);
+}
+
+// The lead terms of k_sigma (blocks [0, nbl), after k_sigma_finalize) and the
+// psi finalisation (the other blocks) of a mixed stage in one launch.
+template <int RMODE, int V>
+__global__ void __launch_bounds__(256) k_final_mixed(const RhsDev<float> d, const StageParams* __restrict__ pp,
+                                                     int nbl, const float2* __restrict__ Pc, float2* __restrict__ ksig,
+                                                     const float* __restrict__ ph, const float* __restrict__ pl,
+                                                     int64_t ldpsi, int64_t plane, const float* __restrict__ R1,
+                                                     int64_t ldR1, int npl, const float2* __restrict__ R2,
+                                                     const float2* __restrict__ ZA, const float2* __restrict__ ZB,
+                                                     float2* __restrict__ kpsi, const float2* __restrict__ R3,
+                                                     const float2* __restrict__ C0) {
+  const StageScalars p = load_params(pp);
+  if ((int)blockIdx.x < nbl)
+    sigma_leads_job<float>(d, p, Pc, ksig, blockIdx.x * (int64_t)blockDim.x + threadIdx.x, (int64_t)nbl * blockDim.x);
+  else
+    psi_v4_job<RMODE, V>(d, p, ph, pl, ldpsi, plane, R1, ldR1, npl, R2, ZA, ZB, kpsi, R3, C0,
+                         (blockIdx.x - nbl) * (int64_t)blockDim.x + threadIdx.x,
+                         (int64_t)(gridDim.x - nbl) * blockDim.x);
+}
+
 constexpr int kPsiV = 2;  // columns per thread of k_psi_finalize_v4
 
 template <typename T>
@@ -753,6 +792,35 @@ static bool psi_v4_ok(const RhsDev<T>& d, const void* psi, const void* psi_lo, i
   if (d.n % kPsiV || ldpsi % kPsiV || plane % kPsiV || ldR1 % kPsiV || npl % kPsiV) return false;
   auto al = [](const void* q) { return ((uintptr_t)q & (4 * kPsiV - 1)) == 0; };
   return al(psi) && al(psi_lo) && al(R1);
+}
+
+bool final_mixed_ok(const RhsDev<float>& d, const float2* psi, const float2* psi_lo, int64_t ldpsi, const float2* R1,
+                    int64_t ldR1, int64_t plane, int rmode, int npl) {
+  return psi_v4_ok<float>(d, psi, psi_lo, ldpsi, R1, ldR1, plane, rmode, npl);
+}
+
+int launch_final_mixed(const RhsDev<float>& d, const StageParams* p, const float2* Pc, float2* ksig,
+                       const float2* psi, const float2* psi_lo, int64_t ldpsi, const float2* R1, int64_t ldR1,
+                       const float2* R2, const float2* ZA, const float2* ZB, float2* kpsi, int64_t plane, int rmode,
+                       int npl, const float2* R3, const float2* C0, cudaStream_t s) {
+  ZG_REQUIRE(final_mixed_ok(d, psi, psi_lo, ldpsi, R1, ldR1, plane, rmode, npl), "operands not in the planar form");
+  ZG_REQUIRE((R3 == nullptr) == (C0 == nullptr), "R3 and C0 come together");
+  const int64_t tl = Pc && d.nu > 0 ? 2 * (int64_t)d.nu * d.n : 0;
+  const int nbl = tl ? grid_for(tl, 256, 256) : 0;
+  const int64_t total = (int64_t)d.N * (d.n / kPsiV);
+  const int grid = nbl + grid_for(total, 256, 152 * 16);
+  const float* ph = reinterpret_cast<const float*>(psi);
+  const float* plo = reinterpret_cast<const float*>(psi_lo);
+  const float* r1 = reinterpret_cast<const float*>(R1);
+  if (rmode == 1)
+    k_final_mixed<1, kPsiV><<<grid, 256, 0, s>>>(d, p, nbl, Pc, ksig, ph, plo, ldpsi, plane, r1, ldR1, npl, R2, ZA,
+                                                 ZB, kpsi, R3, C0);
+  else
+    k_final_mixed<2, kPsiV><<<grid, 256, 0, s>>>(d, p, nbl, Pc, ksig, ph, plo, ldpsi, plane, r1, ldR1, npl, R2, ZA,
+                                                 ZB, kpsi, R3, C0);
+  ZG_CHECK_LAUNCH();
+  count_launch();
+  return ZG_OK;
 }
 
 template <typename T>
@@ -1206,7 +1274,7 @@ int launch_stationary_scale(int N, int n, const double2* Xp, const int* mode_lea
                                  cx<T>::t*, cx<T>::t*, cudaStream_t, int64_t);                                        \
   template int launch_sigma_finalize<T>(const RhsDev<T>&, const StageParams*, const cx<T>::t*, int64_t,              \
                                         const cx<T>::t*, const double2*, cx<T>::t*, cudaStream_t, int, int,           \
-                                        const cx<T>::t*);                                                            \
+                                        const cx<T>::t*, bool);                                                      \
   template int launch_currents<T>(const RhsDev<T>&, const StageParams*, const cx<T>::t*, double*, cudaStream_t);     \
   template int launch_psi_finalize<T>(const RhsDev<T>&, const StageParams*, const cx<T>::t*, const cx<T>::t*,        \
                                       int64_t, const cx<T>::t*, int64_t, const cx<T>::t*, const cx<T>::t*,           \

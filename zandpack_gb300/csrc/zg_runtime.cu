@@ -1111,8 +1111,11 @@ static int rhs_mixed(zg_traj* t, int stage, const StageParams* p, int dH_mode, d
   // join: the finalisation needs T; the next stage overwrites what Omega reads
   ZG_CHECK_CUDA(cudaStreamWaitEvent(s, t->ev_join, 0));
   prof_begin(t, ZG_PROF_FINAL);
+  // the lead terms of k_sigma go with the psi finalisation into one launch when the operands allow it
+  const bool merged = final_mixed_ok(d, (const float2*)psih_f, (const float2*)psil_f, np, t->R1p, 2 * np, ml.plane,
+                                     hreal ? 1 : 2, (int)np);
   ZG_TRY(launch_sigma_finalize<float>(d, p, t->T32, 2 * np, t->Pc32, t->dis_on ? t->dis : nullptr, out, s,
-                                      hreal ? 1 : 2, (int)np, t->nonorth ? t->Wn32 : nullptr));
+                                      hreal ? 1 : 2, (int)np, t->nonorth ? t->Wn32 : nullptr, !merged));
   if (want_J) {
     if (stage == 0)  // the stage-0 input is y itself: currents from the FP64 state
     {
@@ -1124,9 +1127,15 @@ static int rhs_mixed(zg_traj* t, int stage, const StageParams* p, int dH_mode, d
     else
       ZG_TRY(launch_currents<float>(d, p, t->Pc32, t->J, s));
   }
-  ZG_TRY(launch_psi_finalize<float>(d, p, (const float2*)psih_f, (const float2*)psil_f, np, t->R1p, 2 * np,
-                                    t->R2_32, t->ZA32, t->ZB32, out + t->off_psi, s, ml.plane, hreal ? 1 : 2,
-                                    (int)np, t->nonorth ? t->R3_32 : nullptr, t->nonorth ? t->C0_32 : nullptr));
+  if (merged)
+    ZG_TRY(launch_final_mixed(d, p, t->nonorth ? nullptr : t->Pc32, out, (const float2*)psih_f,
+                              (const float2*)psil_f, np, t->R1p, 2 * np, t->R2_32, t->ZA32, t->ZB32,
+                              out + t->off_psi, ml.plane, hreal ? 1 : 2, (int)np, t->nonorth ? t->R3_32 : nullptr,
+                              t->nonorth ? t->C0_32 : nullptr, s));
+  else
+    ZG_TRY(launch_psi_finalize<float>(d, p, (const float2*)psih_f, (const float2*)psil_f, np, t->R1p, 2 * np,
+                                      t->R2_32, t->ZA32, t->ZB32, out + t->off_psi, s, ml.plane, hreal ? 1 : 2,
+                                      (int)np, t->nonorth ? t->R3_32 : nullptr, t->nonorth ? t->C0_32 : nullptr));
   prof_end(t, ZG_PROF_FINAL);
   return ZG_OK;
 }
