@@ -234,7 +234,12 @@ def kpoint_arrays(arrays, k):
     to ``[k:k+1]`` (the leading NK axis, Zandpack/mpi/zand:113-124)."""
     nk = int(np.asarray(arrays["H_Ortho"]).shape[0])
     out = {}
-    for key in arrays.keys() if hasattr(arrays, "keys") else _PER_K:
+    if hasattr(arrays, "keys"):
+        keys = list(arrays.keys())
+    else:  # a lazy Arrays mapping: the keys zand reads, plus the overlap when present
+        from .arrays_io import REQUIRED_KEYS
+        keys = list(REQUIRED_KEYS) + [k for k in ("S^(-0.5)",) if k in arrays]
+    for key in keys:
         v = arrays[key]
         if key in _PER_K:
             v = np.asarray(v)[k:k + 1]
