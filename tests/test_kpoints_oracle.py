@@ -47,3 +47,23 @@ def test_kpoint_trajectory_matches_reference(k2):
     assert np.abs(out["sig"][-1] - z["sig_final"]).max() < 1e-11
     J = np.array(out["currents"])          # (steps, NK, NL)
     assert np.abs(J.transpose(2, 0, 1) - z["currents"]).max() < 1e-10
+
+
+def test_kpoint_arrays_slices_dict_and_lazy_mapping(tmp_path):
+    """kpoint_arrays gives the NK = 1 Arrays of one k-point, from a dict or a
+    lazy ``load_dictionary`` mapping; k-point 0 of the two-k-point workload is
+    the one-k-point workload."""
+    from zandpack_gb300.arrays_io import load_dictionary, write_arrays
+    from zandpack_gb300.engine import kpoint_arrays
+    from zandpack_gb300.layout import CompactLayout
+    from zandpack_gb300.workloads import make_kpoint_workload, make_workload
+    w2, w1 = make_kpoint_workload("mini2"), make_workload("mini2")
+    write_arrays(str(tmp_path / "A"), w2.arrays)
+    lazy = load_dictionary(str(tmp_path / "A") + "/")
+    for src in (w2.arrays, lazy):
+        a0 = kpoint_arrays(src, 0)
+        for key in ("H_Ortho", "DM_Ortho", "xi", "GL_P"):
+            np.testing.assert_array_equal(np.asarray(a0[key]), np.asarray(w1.arrays[key]))
+        assert int(a0["psi_shape"][0]) == 1
+        L1 = CompactLayout(kpoint_arrays(src, 1), w2.hbar)
+        assert L1.N == CompactLayout(w1.arrays, w1.hbar).N
