@@ -272,6 +272,12 @@ int launch_final_mixed(const RhsDev<float>& d, const StageParams* p, const float
                        const float2* psi, const float2* psi_lo, int64_t ldpsi, const float2* R1, int64_t ldR1,
                        const float2* R2, const float2* ZA, const float2* ZB, float2* kpsi, int64_t plane, int rmode,
                        int npl, const float2* R3, const float2* C0, cudaStream_t s);
+// k_sigma with its lead terms and the psi finalisation in one launch (no dissipator)
+int launch_final_all_mixed(const RhsDev<float>& d, const StageParams* p, const float2* Tm, int64_t ldT, int tmode,
+                           const float2* W, const float2* Pc, float2* ksig, const float2* psi, const float2* psi_lo,
+                           int64_t ldpsi, const float2* R1, int64_t ldR1, const float2* R2, const float2* ZA,
+                           const float2* ZB, float2* kpsi, int64_t plane, int rmode, int npl, const float2* R3,
+                           const float2* C0, cudaStream_t s);
 // launch_build_operands_mixed and launch_gathers<float> of a mixed stage in one launch
 int launch_prep_mixed(int n, int np, const double2* H0, const float2* sig32, const double2* dH, int dH_mode,
                       double U, int h_part, float* Hth, float* Htl, float* BSh, float* BSl, const double2* Sm1,

@@ -382,21 +382,24 @@ __device__ __forceinline__ typename cx<T>::t load_T(const typename cx<T>::t* Tm,
 
 // DIS: a dissipator is set (a template parameter: a runtime branch would be
 // if-converted into predicated FP64 multiplies issued for every element)
+// One 32 x 32 block (bx, by) of k_sigma by 256 threads (tx < 32, ty < 8).
+// Pc (may be null): the lead terms (h/hbar^2)(P + P^H) added here to the
+// elements in a coupling row or column, after the scaling, as the separate
+// lead pass adds them.
 template <typename T, bool DIS>
-__global__ void __launch_bounds__(256) k_sigma_finalize(const RhsDev<T> d, const StageParams* __restrict__ pp,
-                                                        const typename cx<T>::t* __restrict__ Tm, int64_t ldT,
-                                                        const double2* __restrict__ dis,
-                                                        typename cx<T>::t* __restrict__ ksig, int tmode, int npl,
-                                                        const typename cx<T>::t* __restrict__ W) {
+__device__ __forceinline__ void sigma_tile_job(int bx, int by, int tx, int ty, const RhsDev<T>& d,
+                                               const StageScalars& p, const typename cx<T>::t* __restrict__ Tm,
+                                               int64_t ldT, const double2* __restrict__ dis,
+                                               typename cx<T>::t* __restrict__ ksig, int tmode, int npl,
+                                               const typename cx<T>::t* __restrict__ W,
+                                               const typename cx<T>::t* __restrict__ Pc) {
   using C = typename cx<T>::t;
   __shared__ C tile[32][33];   // tile[r][c] = T[j0 + r][i0 + c]
   __shared__ C wtile[32][33];  // the same of W (non-orthogonal basis)
-  const StageScalars p = load_params(pp);
   const T sc = pv<T>(p.h_hb, p.fh_hb);
   const T fw = pv<T>(p.h_hb2, p.fh_hb2);
   const int n = d.n;
-  const int i0 = blockIdx.y * 32, j0 = blockIdx.x * 32;
-  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int i0 = by * 32, j0 = bx * 32;
   for (int r = ty; r < 32; r += 8) {
     const int j = j0 + r, i = i0 + tx;
     const bool in = j < n && i < n;
@@ -422,9 +425,24 @@ __global__ void __launch_bounds__(256) k_sigma_finalize(const RhsDev<T> d, const
       const C wij = W[e], wji = wtile[tx][r];
       v.x += fw * (wij.x + wji.x);
       v.y += fw * (wij.y - wji.y);
+    } else if (Pc && (d.umap[i] >= 0 || d.umap[j] >= 0)) {
+      const C pij = p_full(d, Pc, i, j), pji = p_full(d, Pc, j, i);
+      v.x += fw * (pij.x + pji.x);
+      v.y += fw * (pij.y - pji.y);
     }
     ksig[e] = v;
   }
+}
+
+template <typename T, bool DIS>
+__global__ void __launch_bounds__(256) k_sigma_finalize(const RhsDev<T> d, const StageParams* __restrict__ pp,
+                                                        const typename cx<T>::t* __restrict__ Tm, int64_t ldT,
+                                                        const double2* __restrict__ dis,
+                                                        typename cx<T>::t* __restrict__ ksig, int tmode, int npl,
+                                                        const typename cx<T>::t* __restrict__ W) {
+  const StageScalars p = load_params(pp);
+  sigma_tile_job<T, DIS>(blockIdx.x, blockIdx.y, threadIdx.x, threadIdx.y, d, p, Tm, ldT, dis, ksig, tmode, npl, W,
+                         nullptr);
 }
 
 // Pass 2: + (h/hbar^2)(P + P^H) on the elements (i, j) with i or j a coupling
@@ -797,6 +815,56 @@ static bool psi_v4_ok(const RhsDev<T>& d, const void* psi, const void* psi_lo, i
 bool final_mixed_ok(const RhsDev<float>& d, const float2* psi, const float2* psi_lo, int64_t ldpsi, const float2* R1,
                     int64_t ldR1, int64_t plane, int rmode, int npl) {
   return psi_v4_ok<float>(d, psi, psi_lo, ldpsi, R1, ldR1, plane, rmode, npl);
+}
+
+// The whole mixed finalisation in one launch: k_sigma with its lead terms
+// (blocks [0, nb*nb), 32 x 32 tiles) and the psi finalisation (the other
+// blocks); no dissipator.
+template <int RMODE, int V>
+__global__ void __launch_bounds__(256) k_final_all_mixed(const RhsDev<float> d, const StageParams* __restrict__ pp,
+                                                         int nb, const float2* __restrict__ Tm, int64_t ldT, int tmode,
+                                                         const float2* __restrict__ W, const float2* __restrict__ Pc,
+                                                         float2* __restrict__ ksig, const float* __restrict__ ph,
+                                                         const float* __restrict__ pl, int64_t ldpsi, int64_t plane,
+                                                         const float* __restrict__ R1, int64_t ldR1, int npl,
+                                                         const float2* __restrict__ R2, const float2* __restrict__ ZA,
+                                                         const float2* __restrict__ ZB, float2* __restrict__ kpsi,
+                                                         const float2* __restrict__ R3, const float2* __restrict__ C0) {
+  const StageScalars p = load_params(pp);
+  const int ntb = nb * nb;
+  if ((int)blockIdx.x < ntb)
+    sigma_tile_job<float, false>(blockIdx.x % nb, blockIdx.x / nb, threadIdx.x & 31, threadIdx.x >> 5, d, p, Tm, ldT,
+                                 nullptr, ksig, tmode, npl, W, Pc);
+  else
+    psi_v4_job<RMODE, V>(d, p, ph, pl, ldpsi, plane, R1, ldR1, npl, R2, ZA, ZB, kpsi, R3, C0,
+                         (blockIdx.x - ntb) * (int64_t)blockDim.x + threadIdx.x,
+                         (int64_t)(gridDim.x - ntb) * blockDim.x);
+}
+
+int launch_final_all_mixed(const RhsDev<float>& d, const StageParams* p, const float2* Tm, int64_t ldT, int tmode,
+                           const float2* W, const float2* Pc, float2* ksig, const float2* psi, const float2* psi_lo,
+                           int64_t ldpsi, const float2* R1, int64_t ldR1, const float2* R2, const float2* ZA,
+                           const float2* ZB, float2* kpsi, int64_t plane, int rmode, int npl, const float2* R3,
+                           const float2* C0, cudaStream_t s) {
+  ZG_REQUIRE(final_mixed_ok(d, psi, psi_lo, ldpsi, R1, ldR1, plane, rmode, npl), "operands not in the planar form");
+  ZG_REQUIRE((R3 == nullptr) == (C0 == nullptr), "R3 and C0 come together");
+  ZG_REQUIRE(tmode == 1 || tmode == 2, "planar T expected");
+  const int nb = (d.n + 31) / 32;
+  const int64_t total = (int64_t)d.N * (d.n / kPsiV);
+  const int grid = nb * nb + grid_for(total, 256, 152 * 16);
+  const float* ph = reinterpret_cast<const float*>(psi);
+  const float* plo = reinterpret_cast<const float*>(psi_lo);
+  const float* r1 = reinterpret_cast<const float*>(R1);
+  const float2* P = d.nu > 0 && !W ? Pc : nullptr;
+  if (rmode == 1)
+    k_final_all_mixed<1, kPsiV><<<grid, 256, 0, s>>>(d, p, nb, Tm, ldT, tmode, W, P, ksig, ph, plo, ldpsi, plane, r1,
+                                                     ldR1, npl, R2, ZA, ZB, kpsi, R3, C0);
+  else
+    k_final_all_mixed<2, kPsiV><<<grid, 256, 0, s>>>(d, p, nb, Tm, ldT, tmode, W, P, ksig, ph, plo, ldpsi, plane, r1,
+                                                     ldR1, npl, R2, ZA, ZB, kpsi, R3, C0);
+  ZG_CHECK_LAUNCH();
+  count_launch();
+  return ZG_OK;
 }
 
 int launch_final_mixed(const RhsDev<float>& d, const StageParams* p, const float2* Pc, float2* ksig,

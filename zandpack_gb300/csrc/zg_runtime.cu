@@ -1114,8 +1114,11 @@ static int rhs_mixed(zg_traj* t, int stage, const StageParams* p, int dH_mode, d
   // the lead terms of k_sigma go with the psi finalisation into one launch when the operands allow it
   const bool merged = final_mixed_ok(d, (const float2*)psih_f, (const float2*)psil_f, np, t->R1p, 2 * np, ml.plane,
                                      hreal ? 1 : 2, (int)np);
-  ZG_TRY(launch_sigma_finalize<float>(d, p, t->T32, 2 * np, t->Pc32, t->dis_on ? t->dis : nullptr, out, s,
-                                      hreal ? 1 : 2, (int)np, t->nonorth ? t->Wn32 : nullptr, !merged));
+  // without a dissipator, k_sigma (lead terms included) and the psi finalisation share one launch
+  const bool all_in_one = merged && !t->dis_on;
+  if (!all_in_one)
+    ZG_TRY(launch_sigma_finalize<float>(d, p, t->T32, 2 * np, t->Pc32, t->dis_on ? t->dis : nullptr, out, s,
+                                        hreal ? 1 : 2, (int)np, t->nonorth ? t->Wn32 : nullptr, !merged));
   if (want_J) {
     if (stage == 0)  // the stage-0 input is y itself: currents from the FP64 state
     {
@@ -1127,7 +1130,12 @@ static int rhs_mixed(zg_traj* t, int stage, const StageParams* p, int dH_mode, d
     else
       ZG_TRY(launch_currents<float>(d, p, t->Pc32, t->J, s));
   }
-  if (merged)
+  if (all_in_one)
+    ZG_TRY(launch_final_all_mixed(d, p, t->T32, 2 * np, hreal ? 1 : 2, t->nonorth ? t->Wn32 : nullptr, t->Pc32, out,
+                                  (const float2*)psih_f, (const float2*)psil_f, np, t->R1p, 2 * np, t->R2_32,
+                                  t->ZA32, t->ZB32, out + t->off_psi, ml.plane, hreal ? 1 : 2, (int)np,
+                                  t->nonorth ? t->R3_32 : nullptr, t->nonorth ? t->C0_32 : nullptr, s));
+  else if (merged)
     ZG_TRY(launch_final_mixed(d, p, t->nonorth ? nullptr : t->Pc32, out, (const float2*)psih_f,
                               (const float2*)psil_f, np, t->R1p, 2 * np, t->R2_32, t->ZA32, t->ZB32,
                               out + t->off_psi, ml.plane, hreal ? 1 : 2, (int)np, t->nonorth ? t->R3_32 : nullptr,
