@@ -38,7 +38,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 
-OUT_DIR = "gpurun_out"  # output directory of a run, collected afterwards
+# where the clock samples of a run are written (bench_clocks.csv)
+OUT_DIR = os.environ.get("ZG_BENCH_OUT", os.path.join(HERE, "bench_out"))
 
 # ncu-measured DRAM traffic of one psi H^T tensor-core launch per (workload, H(t) form)
 NCU_TRAFFIC = {("c3", "real"): 83.8e6 + 8.6e6}
@@ -65,7 +66,7 @@ class ClockSampler:
     Reads NVML in-process (libnvidia-ml through ctypes, read-only queries) from
     a thread every 5 ms, so that a timed region of tens of milliseconds still
     gets several samples; falls back to ``nvidia-smi -lms 200``.  Samples go to
-    bench_clocks.csv in the run's output directory."""
+    bench_clocks.csv in ``$ZG_BENCH_OUT`` (default ``bench_out/``)."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -78,7 +79,7 @@ class ClockSampler:
         self.p = None
         self.nvml = None
         self.rows = []
-        self.path = os.path.join(HERE, OUT_DIR, "bench_clocks.csv")
+        self.path = os.path.join(OUT_DIR, "bench_clocks.csv")
 
     def _nvml_open(self):
         import ctypes
