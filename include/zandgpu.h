@@ -260,17 +260,40 @@ int zg_terr2_c128(const double* Y, int64_t slot_stride, int nslots, const double
  * memory while they run (for example a serving loop that reserved all of HBM
  * up front, or a host whose device memory is owned by another allocator).
  * No counterpart in the reference.  The partial sums live in a static 8 KiB
- * device array (1024 doubles) inside the library; every count is accepted, a
- * request needing more scratch than that is refused with ZG_EINVAL.  Calls
- * share the array: calls that overlap on the GPU race and must be serialised.
- * The first call on a device looks up the array's device address (with that
- * device current) and caches it; make that first call before any stream
- * capture. */
+ * device array (1024 doubles) inside the library.  The reduction's grid is
+ * capped at 608 blocks, so it never needs more than 609 of those doubles and
+ * every count the allocating entry point accepts fits; the size check before
+ * the launch (ZG_EINVAL on an oversize request) can therefore not trigger
+ * with the present grid cap.  Calls share the array: calls that overlap on
+ * the GPU race and must be serialised.  The first call on a device looks up
+ * the array's device address (with that device current) and caches it for
+ * the life of the process; the cached address does not survive a
+ * cudaDeviceReset, so a program that resets the device must not call this
+ * entry point afterwards.  Like zg_terr2_c128 it copies the result to host
+ * memory and synchronises `stream`, so it must not be called while that
+ * stream is being captured into a CUDA graph. */
 int zg_terr2_c128_noalloc(const double* Y, int64_t slot_stride, int nslots, const double* ct,
                           int64_t count, double* result, void* stream);
 /* Y[nslots-1] = sum_j ch[j] Y[j]  (step_fourth_*, mpi_funcs.py:254-259) */
 int zg_step_fourth_c128(double* Y, int64_t slot_stride, int nslots, const double* ch,
                         int64_t count, void* stream);
+/* The Omega stage combination that leaves Fermi x Fermi blocks untouched
+ * (step_omg_forward_nb_fermi_opti(Y, b, out, idx, fp_loc, fp_all),
+ * Zandpack/func_step_forward.py:112-139): a slot has shape7 = (nk, NL, NX,
+ * NOT, NL, NX, NOT); out[e] = sum_{j in idx} b[j] Y[j][e] except where
+ * fp_loc[x] and fp_all[x'] are both nonzero (x = axis 2, x' = axis 5), where
+ * out is not written.  fp_loc (NX bytes) and fp_all (NX bytes) are device
+ * arrays. */
+int zg_combine_fermi_skip_c128(const double* Y, int64_t slot_stride, int nslots, const double* b,
+                               const int32_t* idx, int nidx, double* out, const int64_t* shape7,
+                               const uint8_t* fp_loc, const uint8_t* fp_all, void* stream);
+/* The diagonal term of dOmega/dt (OuterSubtraction_hard_opti(A, B, C, out),
+ * Zandpack/mpi_funcs.py:91-102): with shape7 = (nk, na, nx, noT, NA, NX, NO)
+ * the shape of C and out, out[k,a,x,c,a',x',:] += (A[k,a,x,0] - B[k,a',x',0])
+ * * C[k,a,x,c,a',x',:].  A is (nk, na, nx, lda_c) and B (nk, NA, NX, ldb_c),
+ * all contiguous complex128 device arrays. */
+int zg_outer_subtraction_c128(const double* A, int lda_c, const double* B, int ldb_c, const double* C,
+                              double* out, const int64_t* shape7, void* stream);
 
 #ifdef __cplusplus
 }

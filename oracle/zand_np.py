@@ -77,6 +77,24 @@ def step_fourth(Y, ch):
     Y[-1] = np.tensordot(ch, Y, axes=(0, 0))
 
 
+def outer_subtraction(A, B, C, out):
+    """``OuterSubtraction_hard_opti`` (Zandpack/mpi_funcs.py:91-102):
+    out[k,a,x,c,aa,xx,:] += (A[k,a,x,0] - B[k,aa,xx,0]) * C[k,a,x,c,aa,xx,:]."""
+    d = A[..., 0][:, :, :, None, None, None, None] - B[..., 0][:, None, None, None, :, :, None]
+    out += d * C
+
+
+def combine_fermi_skip(Y, b, out, idx, fp_loc, fp_all):
+    """``step_omg_forward_nb_fermi_opti`` (Zandpack/func_step_forward.py:112-139):
+    the stage combination of Omega slots (RK, k, a, x, c, a', x', c') written
+    only where the row pole x and the column pole x' are not both Fermi poles."""
+    full = stage_combine(Y, b, idx)
+    skip = np.asarray(fp_loc, bool)[None, None, :, None, None, None, None] & \
+        np.asarray(fp_all, bool)[None, None, None, None, None, :, None]
+    skip = np.broadcast_to(skip, out.shape)
+    out[~skip] = full[~skip]
+
+
 def find_max_orbital_idx_per_lead(GG_P, GL_P, zero_tol):
     """Zandpack/mpi_splitter.py:555-580."""
     live = (np.abs(GG_P).max(axis=0) >= zero_tol) | (np.abs(GL_P).max(axis=0) >= zero_tol)
@@ -257,3 +275,68 @@ def propagate(prob, t0, t1, h, eps, bias, dH, state=None, dissipator=None, max_a
         out["sig"].append(SIGS[-1].copy())
     out["state"] = (SIGS[-1].copy(), PSIS[-1].copy(), OMGS[-1].copy())
     return out
+
+
+# ------------------------------------------------- in-process DOP stepper
+def adaptive_dop(prob, sig0, psi0, omg0, eps, t0, t1, dH, delta_func, h_guess=None, dH_given=True,
+                 fixed_mode=False, faithful_k7=True, max_steps=None):
+    """The reference's in-process ``AdaptiveDOP`` loop
+    (Zandpack/TimedependentTransport.py:3392-3560) with ``f`` = the ``zand``
+    stage body (``Problem.rhs`` with h = 1):
+
+    * ``h = (t1 - t0)/1000`` unless ``h_guess`` (:3474-3478);
+    * ``while t0 <= t1`` (:3491), attempts repeated while ``TE > eps`` (:3493);
+    * stage inputs ``y + sum_j B[i, j] k_j`` at ``t0 + A[i] h`` (:3495-3535),
+      ``k_i = h f``; ``k7 = h * k6`` (:3537) unless ``faithful_k7`` is False;
+    * ``TE = sqrt(sum |sum_j CT_j k_j|^2)`` with CT = b5 - b4 (:3410-3416),
+      ``h <- 0.9 h (eps/TE)^(1/5)`` (:3443-3444);
+    * density matrix and ``Jk(PI(psi_a, Ixi_a))`` recorded before the update
+      (:3547-3549), ``y <- y + sum_j b5_j k_j`` (:3551), ``t0 += h`` (:3553).
+    """
+    hbar = prob.hbar
+    NL = prob.NL
+    CT = _b5 - _b4
+    sig, psi, omg = (np.array(x, dtype=complex) for x in (sig0, psi0, omg0))
+    h = (t1 - t0) / 1000 if h_guess is None else float(h_guess)
+    times, dms, cur, TEs = [], [], [[] for _ in range(NL)], []
+
+    def f(t, s, p, o):
+        d = dH(t, s) if dH is not None else 0.0
+        Ht = prob.H0 + d if dH_given else np.asarray(d) + 0 * prob.H0
+        delta = [delta_func(t, a) for a in range(NL)]
+        ks, kp, ko, _, _ = prob.rhs(1.0, s, p, o, Ht, delta)
+        return ks, kp, ko
+
+    steps = 0
+    while t0 <= t1:
+        if max_steps is not None and steps >= max_steps:
+            break
+        TE = 10 * eps
+        while TE > eps:
+            ks = []
+            for i in range(RK_N):
+                if i == RK_N - 1 and faithful_k7:
+                    ks.append(tuple(h * v for v in ks[5]))
+                    break
+                y = [sig, psi, omg]
+                for j in range(i):
+                    for q in range(3):
+                        y[q] = y[q] + B[i, j] * ks[j][q]
+                ks.append(tuple(h * v for v in f(t0 + A[i] * h, *y)))
+            if fixed_mode:
+                break
+            TE = math.sqrt(sum(terr2(np.array([k[q] for k in ks]), CT) for q in range(3)))
+            TEs.append(TE)
+            with np.errstate(divide="ignore"):
+                h = float(0.9 * h * (np.float64(eps) / np.float64(TE)) ** (1 / 5))
+        dms.append(sig.copy())
+        _, J = prob.pi_and_currents(psi)
+        for a in range(NL):
+            cur[a].append(J[:, a])
+        upd = [sum(_b5[j] * ks[j][q] for j in range(RK_N)) for q in range(3)]
+        sig, psi, omg = sig + upd[0], psi + upd[1], omg + upd[2]
+        times.append(t0)
+        t0 += h
+        steps += 1
+    return dict(times=np.array(times), dm=np.array(dms), currents=[np.array(c) for c in cur], TE=TEs,
+                state=(sig, psi, omg))

@@ -43,6 +43,8 @@ CASES = {
     # name: (t1, initial stepsize, attempts whose stages are kept, keep_every)
     # the large initial steps of the small cases force rejected attempts
     "c1": (1.0, 0.01, (0, 7), 4),
+    # BASELINE config 1 over its full span, 0-50 fs (sigma kept every 40th step)
+    "c1_50fs": (50.0, 0.01, (0,), 40),
     "mini2": (2.0, 0.3, (0, 1, 12), 1),
     "mini3": (1.0, 0.3, (0, 1, 9), 1),
     # the same cases posed in a non-orthogonal basis, run through ``nozand``
@@ -75,7 +77,7 @@ def make_case(name):
     elif name.startswith("k2_"):
         w = make_kpoint_workload(name[3:], nk=2)
     else:
-        w = make_workload(name)
+        w = make_workload(name.split("_")[0])
     A = w.arrays
     L = int(A["psi_shape"][1])
     nranks = L + 1

@@ -204,3 +204,34 @@ def test_h_operands_after_a_full_dH_matrix():
         out.append([r[2] for r in recs])
         tr.close()
     assert out[0] == out[1] and len(out[0]) == 2
+
+
+def test_mixed_c1_full_span_on_reference_grid():
+    """BASELINE config 1 over 0-50 fs on the reference's own time grid (its
+    5414 step sizes replayed): the mixed-precision path stays within 1e-6 of
+    the unmodified ``zand`` in sigma and in the lead currents at every step,
+    the final time included."""
+    import os
+    from conftest import GOLDEN
+    from zandpack_gb300.engine import Propagator
+    if not os.path.exists(os.path.join(GOLDEN, "c1_50fs.npz")):
+        pytest.skip("fixture c1_50fs missing")
+    z = load_golden("c1_50fs")
+    p = z["params"]
+    bias, dH = golden_callbacks(p)
+    pr = Propagator(z, p["hbar"], bias, hubbard_U=p["hubbard_U"], precision="mixed")
+    pr.set_state(z["DM_Ortho"])
+    acc = list(z["TE_hist"] < p["eps"])
+    replay = np.concatenate([z["h_hist"], [z["times"][-1] - z["times"][-2]]])
+    out = pr.run(p["t0"], p["t1"], p["stepsize"], p["eps"], replay_h=replay, force_accept=acc)
+    pr.traj.close()
+    np.testing.assert_allclose(out["times"], z["times"], rtol=0, atol=1e-10)
+    sig = np.array(out["sig"])[:, 0][z["sig_traj_idx"] + 1]
+    dsig = np.abs(sig - z["sig_traj"][:, 0]).max()
+    dfin = np.abs(out["sig"][-1] - z["sig_final"][0]).max()
+    J = np.array(out["currents"]).T
+    dJ = np.abs(J - z["currents"]).max()
+    dJfin = np.abs(J[:, -1] - z["currents"][:, -1]).max()
+    print("\nc1 0-50 fs mixed vs reference: max|dsig| %.2e (final %.2e), max|dJ| %.2e (final %.2e)"
+          % (dsig, dfin, dJ, dJfin))
+    assert max(dsig, dfin) <= ATOL_TRAJ and dJ <= ATOL_TRAJ

@@ -72,3 +72,31 @@ def test_tableau_identities():
     assert zo.CH[-1] == 1.0 and abs(zo.CH[:-1].sum() - 1) < 1e-15
     # DOP54's last stage row equals b5 (first-same-as-last)
     assert np.allclose(zo.B[6, :6], zo.CH[:6]) and zo.CH[6] == 0.0
+
+
+def test_c1_full_span_prefix():
+    """BASELINE config 1 over 0-50 fs (``c1_50fs``: 5414 attempts of the
+    unmodified ``zand``): the oracle reproduces the first 300 attempts' error
+    norms and accept decisions and the stage derivatives of attempt 0 (the
+    whole span runs on the GPU in ``tests/test_gpu_parity.py``)."""
+    import os
+    import pytest
+    from conftest import GOLDEN, load_golden
+    if not os.path.exists(os.path.join(GOLDEN, "c1_50fs.npz")):
+        pytest.skip("fixture c1_50fs missing")
+    z = load_golden("c1_50fs")
+    p = z["params"]
+    bias, dH = golden_callbacks(p)
+    prob = zo.Problem(z, p["hbar"])
+    got = _stage_ks(prob, z, 0, bias, dH)
+    for g, name in zip(got, ("ksig", "kpsi", "komg")):
+        ref = z["%s_0" % name]
+        assert np.abs(g - ref).max() / max(np.abs(ref).max(), 1e-300) < 1e-12
+    out = zo.propagate(prob, p["t0"], p["t1"], p["stepsize"], p["eps"], bias, dH,
+                       state=(z["DM_Ortho"], None, None), max_attempts=300)
+    TE = np.array(out["TE_hist"])
+    assert len(TE) == 300
+    assert ((TE < p["eps"]) == (z["TE_hist"][:300] < p["eps"])).all()
+    np.testing.assert_allclose(TE, z["TE_hist"][:300], rtol=1e-7)
+    k = len(out["times"])
+    np.testing.assert_allclose(out["times"], z["times"][:k], rtol=0, atol=1e-9)

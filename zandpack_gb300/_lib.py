@@ -99,6 +99,8 @@ _SIGS = {
     "zg_terr2_c128": ([_P, C.c_int64, C.c_int, _P, C.c_int64, _P, _P], C.c_int),
     "zg_terr2_c128_noalloc": ([_P, C.c_int64, C.c_int, _P, C.c_int64, _P, _P], C.c_int),
     "zg_step_fourth_c128": ([_P, C.c_int64, C.c_int, _P, C.c_int64, _P], C.c_int),
+    "zg_combine_fermi_skip_c128": ([_P, C.c_int64, C.c_int, _P, _P, C.c_int, _P, _P, _P, _P, _P], C.c_int),
+    "zg_outer_subtraction_c128": ([_P, C.c_int, _P, C.c_int, _P, _P, _P, _P], C.c_int),
 }
 
 _lib = None

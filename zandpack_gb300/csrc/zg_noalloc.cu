@@ -36,7 +36,10 @@ static double* g_noalloc_addr[ZG_NOALLOC_MAX_DEVICES] = {};
 
 // Device address of the static scratch array on the current device.  The name
 // g_noalloc_scratch in host code is only a host-side stand-in, so the address
-// is looked up once per device (with that device current) and cached.
+// is looked up once per device (with that device current) and cached for the
+// life of the process.  The cache does not survive cudaDeviceReset (the module
+// is loaded again afterwards and the array may move): a program that resets
+// the device must not call zg_terr2_c128_noalloc after the reset.
 static int noalloc_scratch(double** out) {
   int dev = 0;
   ZG_CHECK_CUDA(cudaGetDevice(&dev));

@@ -6,24 +6,27 @@
 //
 // A is M x K and B is N x K, both row-major with K contiguous (K-major), FP32
 // arrays whose values are exact TF32 numbers (zg_split_tf32 produces them).
-// Complex products use the real embedding of the complex operand (built by
-// k_build_operands_mixed in zg_rhs.cu), so this kernel only sees real matrices.
+// Complex products are real GEMMs on planar operands (the real-part rows,
+// then the imaginary-part rows; k_build_operands_mixed and the stage input in
+// zg_rhs.cu / zg_flat.cu write them), so this kernel only sees real matrices.
 //
-// One CTA computes a BM x BN tile (BM = 128 lanes of TMEM, BN fp32 columns):
-//   * one elected thread of warp 8 streams K-blocks of 32 elements (one
-//     128-byte swizzle row) of Ahi, Alo, Bhi, Blo into a STAGES-deep ring of
-//     shared-memory buffers with TMA (cp.async.bulk.tensor, SWIZZLE_128B);
-//   * one elected thread of warp 9 issues tcgen05.mma (kind::tf32, M=128,
-//     N=BN, K=8) for the three products of a K-block into one of NACC TMEM
-//     accumulator buffers and commits to the smem buffer's "empty" barrier
-//     and to the TMEM buffer's "full" barrier;
-//   * warps 0-7 read each K-block's partial sum from TMEM (tcgen05.ld
-//     32x32b; warps w and w+4 share TMEM lane quarter w and take one half of
-//     the columns each), add it into FP32 registers and release the buffer.
+// One CTA computes a BM x BN tile (BM = 128 TMEM lanes, BN = 256 or 128 fp32
+// columns) with NDW = 4 * BN / 64 drain warps followed by two more warps:
+//   * warp NDW, one elected thread: streams K blocks of Ahi, Alo, Bhi, Blo
+//     with TMA (cp.async.bulk.tensor) into a STAGES-deep ring of shared-memory
+//     buffers.  BN = 256: four stages of 16 floats along K (64-byte rows,
+//     SWIZZLE_64B); BN = 128: three stages of 32 floats (SWIZZLE_128B);
+//   * warp NDW + 1, one elected thread: owns the TMEM allocation and issues
+//     tcgen05.mma (kind::tf32, M = 128, N = BN, K = 8) for the three products
+//     of every K block into one of NACC = 512 / BN TMEM accumulator buffers
+//     (all 512 columns), committing to the ring stage's "empty" barrier and,
+//     after each K = 32 group, to the TMEM buffer's "full" barrier;
+//   * warps 0 .. NDW-1: read each K = 32 group's partial sum from TMEM
+//     (tcgen05.ld 32x32b; warp w takes TMEM lane quarter w % 4 and the 64
+//     columns w / 4), add it into FP32 registers and release the buffer.
 // The tensor core truncates inside its accumulation, so a single accumulator
-// over K = 2048 drifts by ~1e-5 relative; per-K-block partials summed with
-// round-to-nearest keep the product at ~1e-7.  Eight drain warps and four
-// accumulator buffers keep the drain off the MMA issue path.
+// over K = 2048 drifts by ~1e-5 relative; per-group partials summed with
+// round-to-nearest keep the product at ~1e-7.
 // Every wait on an mbarrier is bounded by a clock64 budget; on timeout the
 // thread records an error code in *err and stops issuing, the MMA thread
 // waits for its own MMAs, the producer for its copies in flight, and TMEM is

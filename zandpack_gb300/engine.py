@@ -99,6 +99,18 @@ class Trajectory:
         args = [np.ascontiguousarray(x, np.float64) for x in (tab.A, Bz, tab.CT, tab.CH)]
         check(lib().zg_set_tableau(self._h, tab.RK_N, *[_ptr(a) for a in args]))
         self.stages = tab.RK_N
+        self._tab_args = args
+
+    def set_error_weights(self, CT):
+        """Replace the error weights CT of the current tableau (the stages, the
+        stage rows and the update weights stay)."""
+        if getattr(self, "_tab_args", None) is None:
+            self.set_tableau(DOP54)
+        A, Bz, _, CH = self._tab_args
+        CT = np.ascontiguousarray(CT, np.float64)
+        assert CT.shape == (self.stages,)
+        check(lib().zg_set_tableau(self._h, self.stages, _ptr(A), _ptr(Bz), _ptr(CT), _ptr(CH)))
+        self._tab_args = [A, Bz, CT, CH]
 
     # ------------------------------------------------------------- state
     def set_slot(self, slot, y):

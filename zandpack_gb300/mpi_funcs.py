@@ -18,13 +18,39 @@ def abs2(x):
 
 
 def MM(A, B, OUT):
-    """``np.matmul(A, B, out=OUT)`` (Zandpack/mpi_funcs.py:24-25); device
-    tensors go through ``torch.matmul``."""
+    """``np.matmul(A, B, out=OUT)`` (Zandpack/mpi_funcs.py:24-25) on CUDA
+    tensors.  ``zand`` calls it in two forms.  The stage combination
+    ``MM(SIGS[idx].transpose(..., 0), B[i, idx], out)`` (Zandpack/mpi/zand:
+    306-313), a product with a vector whose left operand is a set of
+    Runge-Kutta slots viewed slot-axis-last, runs on this library's combination
+    kernel (``zg_combine_c128``).  Every other form is a plain complex GEMM of
+    the worker's stage body, which this package replaces as a whole (``zg_rhs``);
+    it goes to ``torch.matmul`` (cuBLAS), as a library GEMM."""
     torch = _dev._torch()
-    if isinstance(A, torch.Tensor):
-        torch.matmul(A, B, out=OUT)
-    else:
-        np.matmul(A, B, out=OUT)
+    for name, x in (("A", A), ("OUT", OUT)):
+        if not (isinstance(x, torch.Tensor) and x.is_cuda):
+            raise _lib_invalid("%s must be a CUDA tensor" % name)
+    if np.ndim(B) == 1 and A.dim() >= 2 and A.shape[-1] == len(B):
+        slots = A.movedim(-1, 0)
+        bh = B.detach().cpu().numpy() if isinstance(B, torch.Tensor) else np.asarray(B)
+        if (slots.is_contiguous() and A.dtype == torch.complex128 and OUT.is_contiguous()
+                and OUT.dtype == torch.complex128 and tuple(OUT.shape) == tuple(A.shape[:-1])
+                and not np.any(np.imag(bh))):
+            b = _dev.host_f64(np.real(bh))
+            ns = slots.shape[0]
+            count = OUT.numel()
+            idx = np.arange(ns, dtype=np.int32)
+            check(lib().zg_combine_c128(_dev.ptr(slots), count, ns, b.ctypes.data_as(C.c_void_p),
+                                        idx.ctypes.data_as(C.c_void_p), ns, _dev.ptr(OUT), count,
+                                        _dev.stream_of(OUT)))
+            return
+    Bd = B if isinstance(B, torch.Tensor) else torch.as_tensor(np.asarray(B), device=A.device).to(A.dtype)
+    torch.matmul(A, Bd, out=OUT)
+
+
+def _lib_invalid(msg):
+    from ._lib import ZGInvalid
+    return ZGInvalid(1, msg)
 
 
 _multiply = np.multiply
@@ -86,7 +112,17 @@ def step_fourth_omg(Y3, CH):
 
 def OuterSubtraction_hard_opti(A, B, C_, out):
     """out[k,a,x,c,aa,xx,:] += (A[k,a,x,0] - B[k,aa,xx,0]) * C[k,a,x,c,aa,xx,:]
-    (Zandpack/mpi_funcs.py:91-102), broadcast on the device."""
-    a = A[..., 0][:, :, :, None, None, None, None]
-    b = B[..., 0][:, None, None, None, :, :, None]
-    out += (a - b) * C_
+    (Zandpack/mpi_funcs.py:91-102), in one pass of ``zg_outer_subtraction_c128``."""
+    A = _dev.as_c128(A, "A")
+    B = _dev.as_c128(B, "B")
+    C_ = _dev.as_c128(C_, "C")
+    out = _dev.as_c128(out, "out")
+    if A.dim() != 4 or B.dim() != 4 or C_.dim() != 7 or tuple(out.shape) != tuple(C_.shape):
+        raise AssertionError("OuterSubtraction_hard_opti: A (nk,na,nx,*), B (nk,NA,NX,*), C and out 7-D alike")
+    nk, na, nx, noT, NA, NX, NO = C_.shape
+    if tuple(A.shape[:3]) != (nk, na, nx) or tuple(B.shape[:3]) != (nk, NA, NX):
+        raise AssertionError("OuterSubtraction_hard_opti: A/B do not match C")
+    shape = np.array(C_.shape, np.int64)
+    check(lib().zg_outer_subtraction_c128(_dev.ptr(A), int(A.shape[3]), _dev.ptr(B), int(B.shape[3]),
+                                          _dev.ptr(C_), _dev.ptr(out), shape.ctypes.data_as(C.c_void_p),
+                                          _dev.stream_of(out)))
