@@ -282,7 +282,8 @@ int launch_final_all_mixed(const RhsDev<float>& d, const StageParams* p, const f
 int launch_prep_mixed(int n, int np, const double2* H0, const float2* sig32, const double2* dH, int dH_mode,
                       double U, int h_part, float* Hth, float* Htl, float* BSh, float* BSl, const double2* Sm1,
                       const RhsDev<float>& d, const float2* psih, const float2* psil, int64_t ldpsi, float2* sigC,
-                      float2* G, int64_t plane, cudaStream_t s);
+                      float2* G, int64_t plane, cudaStream_t s, float* sigEh = nullptr, float* sigEl = nullptr,
+                      int ldx = 0);
 // Lead currents in FP64 from the FP64 state: J_a = 2 Re sum_{m in a} sum_k psi[m][C_a[k]] IXI[m][k] / hbar^2
 // row ranges per lead: sourced rows [s[a], s[a+1]), free rows [f[a], f[a+1])
 struct CurRows {

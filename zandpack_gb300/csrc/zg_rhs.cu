@@ -298,7 +298,9 @@ __device__ __forceinline__ void gathers_job(const RhsDev<T>& d, const typename c
                                             const typename cx<T>::t* __restrict__ psi,
                                             const typename cx<T>::t* __restrict__ psi_lo, int64_t ldpsi,
                                             typename cx<T>::t* __restrict__ sigC, typename cx<T>::t* __restrict__ G,
-                                            int64_t plane, int64_t first, int64_t stride) {
+                                            int64_t plane, int64_t first, int64_t stride,
+                                            float* __restrict__ sigEh = nullptr, float* __restrict__ sigEl = nullptr,
+                                            int ldx = 0) {
   const int64_t ns = (int64_t)d.L * d.n * d.nc;
   const int64_t ng = (int64_t)d.N * d.L * d.nc;
   for (int64_t e = first; e < ns + ng; e += stride) {
@@ -306,7 +308,27 @@ __device__ __forceinline__ void gathers_job(const RhsDev<T>& d, const typename c
       const int k = (int)(e % d.nc);
       const int64_t r = e / d.nc;
       const int i = (int)(r % d.n), a = (int)(r / d.n);
-      sigC[e] = sig[(int64_t)i * d.n + d.lead_cols[a * d.nc + k]];
+      const typename cx<T>::t v = sig[(int64_t)i * d.n + d.lead_cols[a * d.nc + k]];
+      sigC[e] = v;
+      if (sigEh) {
+        // B' of the xi sigma^T product on the tensor cores: rows 2i, 2i+1 of
+        // lead a hold (Re, -Im) and (Im, Re) of sigma[i][C_a[k]], TF32 hi/lo
+        const float x = (float)v.x, y = (float)v.y;
+        uint32_t hx, hy, lx, ly;
+        asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(hx) : "f"(x));
+        asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(hy) : "f"(y));
+        asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(lx) : "f"(x - __uint_as_float(hx)));
+        asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(ly) : "f"(y - __uint_as_float(hy)));
+        const int64_t o0 = ((int64_t)a * 2 * d.n + 2 * i) * ldx + 2 * k, o1 = o0 + ldx;
+        sigEh[o0] = __uint_as_float(hx);
+        sigEh[o0 + 1] = -__uint_as_float(hy);
+        sigEh[o1] = __uint_as_float(hy);
+        sigEh[o1 + 1] = __uint_as_float(hx);
+        sigEl[o0] = __uint_as_float(lx);
+        sigEl[o0 + 1] = -__uint_as_float(ly);
+        sigEl[o1] = __uint_as_float(ly);
+        sigEl[o1 + 1] = __uint_as_float(lx);
+      }
     } else {
       const int64_t g = e - ns;
       const int k = (int)(g % d.nc);
@@ -1255,21 +1277,22 @@ __global__ void __launch_bounds__(256) k_prep_mixed(int n, int np, int nb, const
                                                     const RhsDev<float> d, const float2* __restrict__ psih,
                                                     const float2* __restrict__ psil, int64_t ldpsi,
                                                     float2* __restrict__ sigC, float2* __restrict__ G,
-                                                    int64_t plane) {
+                                                    int64_t plane, float* __restrict__ sigEh,
+                                                    float* __restrict__ sigEl, int ldx) {
   const int ntb = nb * nb;
   if ((int)blockIdx.x < ntb) {
     operands_tile<HP>(blockIdx.x % nb, blockIdx.x / nb, n, np, H0, sig32, dH, dH_mode, U, Hth, Htl, BSh, BSl, Sm1);
   } else {
     const int tid = threadIdx.y * 32 + threadIdx.x;
     gathers_job<float>(d, sig32, psih, psil, ldpsi, sigC, G, plane, (int64_t)(blockIdx.x - ntb) * 256 + tid,
-                       (int64_t)(gridDim.x - ntb) * 256);
+                       (int64_t)(gridDim.x - ntb) * 256, sigEh, sigEl, ldx);
   }
 }
 
 int launch_prep_mixed(int n, int np, const double2* H0, const float2* sig32, const double2* dH, int dH_mode,
                       double U, int h_part, float* Hth, float* Htl, float* BSh, float* BSl, const double2* Sm1,
                       const RhsDev<float>& d, const float2* psih, const float2* psil, int64_t ldpsi, float2* sigC,
-                      float2* G, int64_t plane, cudaStream_t s) {
+                      float2* G, int64_t plane, cudaStream_t s, float* sigEh, float* sigEl, int ldx) {
   ZG_REQUIRE(h_part >= 0 && h_part <= 2, "bad operand part %d", h_part);
   ZG_REQUIRE(!(Sm1 && dH_mode == ZG_DH_HUBBARD && h_part == 1), "the overlap's Hubbard term changes every entry");
   const int nb = (np + 31) / 32;
@@ -1278,13 +1301,13 @@ int launch_prep_mixed(int n, int np, const double2* H0, const float2* sig32, con
   const dim3 grid(nb * nb + gb), block(32, 8);
   if (h_part == 0)
     k_prep_mixed<0><<<grid, block, 0, s>>>(n, np, nb, H0, sig32, dH, dH_mode, U, Hth, Htl, BSh, BSl, Sm1, d, psih,
-                                           psil, ldpsi, sigC, G, plane);
+                                           psil, ldpsi, sigC, G, plane, sigEh, sigEl, ldx);
   else if (h_part == 1)
     k_prep_mixed<1><<<grid, block, 0, s>>>(n, np, nb, H0, sig32, dH, dH_mode, U, Hth, Htl, BSh, BSl, Sm1, d, psih,
-                                           psil, ldpsi, sigC, G, plane);
+                                           psil, ldpsi, sigC, G, plane, sigEh, sigEl, ldx);
   else
     k_prep_mixed<2><<<grid, block, 0, s>>>(n, np, nb, H0, sig32, dH, dH_mode, U, Hth, Htl, BSh, BSl, Sm1, d, psih,
-                                           psil, ldpsi, sigC, G, plane);
+                                           psil, ldpsi, sigC, G, plane, sigEh, sigEl, ldx);
   ZG_CHECK_LAUNCH();
   count_launch();
   return ZG_OK;

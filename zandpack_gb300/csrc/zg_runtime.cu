@@ -3,16 +3,19 @@
 // right-hand side in the FP64 and the mixed-precision form, and the
 // extern "C" entry points declared in zandgpu.h.
 #include <stdarg.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <math.h>
 
 #include <algorithm>
 #include <cmath>
+#include <memory>
 #include <mutex>
 #include <vector>
 
 #include "zg_kernels.cuh"
+#include "zg_tcx.cuh"
 
 namespace zg {
 
@@ -213,6 +216,17 @@ struct zg_traj {
   float2* ws32 = nullptr;
   int64_t ws64_cap = 0, ws32_cap = 0;
   TcGemm gT, gR1;
+  // mixed path: the PI partials, Omega xi and xi sigma^T products on the
+  // tensor cores (zg_tcx.cu): problem table, the B' operand stack and the A
+  // operand of xi sigma^T (constants, TF32 hi/lo), the per-stage B' of
+  // xi sigma^T (embedded sigma columns, written by the operand kernel),
+  // split-K partials and slice counters
+  bool tcx_on = false;
+  TcxBatch* tcx = nullptr;
+  int tcx_grid = 0, ldx = 0;
+  float *tcxBh = nullptr, *tcxBl = nullptr, *XIh = nullptr, *XIl = nullptr, *sigEh = nullptr, *sigEl = nullptr,
+        *tcx_ws = nullptr;
+  int* tcx_cnt = nullptr;
   // stage parameters read by the RHS kernels, and the device-side controller
   StageParams* d_params = nullptr;
   DevCtl* ctl = nullptr;
@@ -380,8 +394,10 @@ static void free_traj(zg_traj* t) {
                   t->conv64, t->sig64, t->tc_err, t->ws64, t->ws32, t->dis, t->ucols, t->umap,
                   t->st_V, t->st_Vc, t->st_W, t->st_lam, t->st_delta,
                   t->Sm1, t->Hn0, t->dHn, t->SmR, t->SmT, t->C0, t->Qcat, t->Wn, t->Zcat, t->R3,
-                  t->SmR32, t->SmT32, t->C0_32, t->Qcat32, t->Wn32, t->Zcat32, t->R3_32};
+                  t->SmR32, t->SmT32, t->C0_32, t->Qcat32, t->Wn32, t->Zcat32, t->R3_32,
+                  t->tcxBh, t->tcxBl, t->XIh, t->XIl, t->sigEh, t->sigEl, t->tcx_ws, t->tcx_cnt};
   for (void* p : ptrs) dfree(t, p);
+  delete t->tcx;
   if (t->stream2) {
     cudaStreamSynchronize(t->stream2);
     cudaStreamDestroy(t->stream2);
@@ -474,6 +490,181 @@ static void to_f32(const double2* a, float2* b, size_t n) {
   for (size_t i = 0; i < n; ++i) b[i] = make_float2((float)a[i].x, (float)a[i].y);
 }
 
+// The products of the mixed stage that run on the tensor cores (zg_tcx.cu):
+// PI partials (A = the planar psi parts, transposed in shared memory), the
+// Omega xi products (A = the raw Omega blocks of the stage input) and the
+// xi sigma^T rows (A = xi, B' = the embedded sigma columns of the lead).  The
+// B' operands of the first two kinds are constants: the real embedding of
+// IXI (PI) and XIS (Omega xi) over each problem's mode range, zero outside it,
+// stacked along K.  Leaves t->tcx_on false (the SIMT batch then runs) when a
+// shape does not suit TMA (odd block widths, misaligned blocks) or the
+// coupling width exceeds the kernels.
+static int build_tcx(zg_traj* t, const zg_layout* Lo) {
+  const int64_t n = t->n, N = t->N, Ns = t->Ns, Nf = t->Nf, L = t->L, nc = t->nc, np = t->np;
+  const int bn = tcx_bn_for((int)(2 * nc));
+  const MixedLayout& ml = t->ml;
+  const float* psih = (const float*)(t->stage32 + ml.st_psih);
+  const float* psil = (const float*)(t->stage32 + ml.st_psil);
+  const float* omA = (const float*)(t->stage32 + ml.st_om);
+  const float* omB = omA + 2 * N * Ns;
+  auto al16 = [](const void* q) { return ((uintptr_t)q & 15) == 0; };
+  if (bn == 0 || Ns % 2 || Nf % 2 || !al16(omA) || !al16(omB) || Ns == 0) return ZG_OK;
+  cudaStream_t s = t->stream;
+  const int ndw = tcx_ndw(bn);
+  const int kchunk = 256;
+  std::unique_ptr<TcxBatch> B(new TcxBatch());
+  memset(B.get(), 0, sizeof(TcxBatch));
+  // ---- B' stack of the PI and Omega xi problems
+  struct Blk { int kind, a, cls; int64_t r0, r1, q0, q1, koff; };  // kind 0 PI, 1 ZA, 2 ZB
+  std::vector<Blk> blk;
+  int64_t kstack = 0;
+  auto add = [&](int kind, int a, int cls, int64_t r0, int64_t r1) {
+    if (r1 <= r0) return;
+    Blk b;
+    b.kind = kind; b.a = a; b.cls = cls; b.r0 = r0; b.r1 = r1;
+    b.q0 = r0 / 16 * 16;
+    b.q1 = (r1 + 15) / 16 * 16;
+    b.koff = kstack;
+    kstack += 2 * (b.q1 - b.q0);
+    blk.push_back(b);
+  };
+  for (int a = 0; a < L; ++a) {
+    add(0, a, 0, t->s_start[a], t->s_start[a + 1]);
+    add(0, a, 1, t->f_start[a], t->f_start[a + 1]);
+  }
+  for (int b = 0; b < L; ++b) add(1, b, 0, t->s_start[b], t->s_start[b + 1]);
+  for (int b = 0; b < L; ++b) add(2, b, 0, t->f_start[b] - Ns, t->f_start[b + 1] - Ns);
+  if ((int)blk.size() + L > ZG_TCX_PROBS || kstack == 0) return ZG_OK;
+  std::vector<float> Bh((size_t)bn * kstack, 0.f);
+  const double2* IXI = (const double2*)Lo->IXI;
+  const double2* XIS = (const double2*)Lo->XIS;
+  const double2* XI = (const double2*)Lo->XI;
+  for (const Blk& b : blk) {
+    const double2* val = b.kind == 0 ? IXI : XIS;
+    for (int64_t r = b.r0; r < b.r1; ++r) {
+      const int64_t m = b.kind == 2 ? r + Ns : r;  // OmB columns are free modes
+      const int64_t j = b.koff + 2 * (r - b.q0);
+      for (int64_t k = 0; k < nc; ++k) {
+        const double2 v = val[m * nc + k];
+        Bh[(size_t)(2 * k) * kstack + j] = (float)v.x;
+        Bh[(size_t)(2 * k) * kstack + j + 1] = (float)-v.y;
+        Bh[(size_t)(2 * k + 1) * kstack + j] = (float)v.y;
+        Bh[(size_t)(2 * k + 1) * kstack + j + 1] = (float)v.x;
+      }
+    }
+  }
+  ZG_TRY(dalloc(t, &t->tcxBh, Bh.size()));
+  ZG_TRY(dalloc(t, &t->tcxBl, Bh.size()));
+  ZG_CHECK_CUDA(cudaMemcpyAsync(t->tcxBl, Bh.data(), Bh.size() * sizeof(float), cudaMemcpyHostToDevice, s));
+  ZG_TRY(launch_split_tf32(t->tcxBl, t->tcxBh, t->tcxBl, (int64_t)Bh.size(), s));
+  // ---- A of xi sigma^T (xi, interleaved) and the per-stage B' (embedded sigma columns)
+  const int ldx = (int)((2 * nc + 31) / 32 * 32);
+  t->ldx = ldx;
+  std::vector<float> Xh((size_t)N * ldx, 0.f);
+  for (int64_t m = 0; m < N; ++m)
+    for (int64_t k = 0; k < nc; ++k) {
+      Xh[(size_t)m * ldx + 2 * k] = (float)XI[m * nc + k].x;
+      Xh[(size_t)m * ldx + 2 * k + 1] = (float)XI[m * nc + k].y;
+    }
+  ZG_TRY(dalloc(t, &t->XIh, Xh.size()));
+  ZG_TRY(dalloc(t, &t->XIl, Xh.size()));
+  ZG_CHECK_CUDA(cudaMemcpyAsync(t->XIl, Xh.data(), Xh.size() * sizeof(float), cudaMemcpyHostToDevice, s));
+  ZG_TRY(launch_split_tf32(t->XIl, t->XIh, t->XIl, (int64_t)Xh.size(), s));
+  const int64_t nE = L * 2 * n * ldx;
+  ZG_TRY(dalloc(t, &t->sigEh, nE));
+  ZG_TRY(dalloc(t, &t->sigEl, nE));
+  ZG_CHECK_CUDA(cudaMemsetAsync(t->sigEh, 0, nE * sizeof(float), s));
+  ZG_CHECK_CUDA(cudaMemsetAsync(t->sigEl, 0, nE * sizeof(float), s));
+  // products that get no problem keep zero blocks (an empty class or lead)
+  ZG_CHECK_CUDA(cudaMemsetAsync(t->Pc32, 0, 2 * L * n * nc * sizeof(float2), s));
+  ZG_CHECK_CUDA(cudaMemsetAsync(t->ZA32, 0, L * N * nc * sizeof(float2), s));
+  ZG_CHECK_CUDA(cudaMemsetAsync(t->ZB32, 0, L * std::max<int64_t>(Ns, 1) * nc * sizeof(float2), s));
+  // ---- tensor maps
+  CUtensorMap* mp = B->maps;
+  ZG_TRY(make_tmap_f32_box(&mp[0], psih, 2 * N, np, np, 16, 128, false));
+  ZG_TRY(make_tmap_f32_box(&mp[1], psil, 2 * N, np, np, 16, 128, false));
+  ZG_TRY(make_tmap_f32_box(&mp[2], omA, N, 2 * Ns, 2 * Ns, 128, 32, true));
+  if (Nf > 0) ZG_TRY(make_tmap_f32_box(&mp[3], omB, Ns, 2 * Nf, 2 * Nf, 128, 32, true));
+  ZG_TRY(make_tmap_f32_box(&mp[4], t->XIh, N, 2 * nc, ldx, 128, 32, true));
+  ZG_TRY(make_tmap_f32_box(&mp[5], t->XIl, N, 2 * nc, ldx, 128, 32, true));
+  ZG_TRY(make_tmap_f32_box(&mp[6], t->tcxBh, bn, kstack, kstack, bn, 32, true));
+  ZG_TRY(make_tmap_f32_box(&mp[7], t->tcxBl, bn, kstack, kstack, bn, 32, true));
+  ZG_TRY(make_tmap_f32_box(&mp[8], t->sigEh, L * 2 * n, 2 * nc, ldx, bn, 32, true));
+  ZG_TRY(make_tmap_f32_box(&mp[9], t->sigEl, L * 2 * n, 2 * nc, ldx, bn, 32, true));
+  // ---- problems
+  int np_ = 0, items = 0;
+  int64_t ws_need = 0, cnt_need = 0;
+  std::vector<int64_t> ws_off, cnt_off;
+  auto prob = [&](TcxProb P) {
+    P.nsplit = (P.K + P.kchunk - 1) / P.kchunk;
+    P.item_begin = items;
+    items += P.tiles_m * P.tiles_n * P.nsplit;
+    ws_off.push_back(P.nsplit > 1 ? ws_need : -1);
+    if (P.nsplit > 1) ws_need += (int64_t)P.tiles_m * P.tiles_n * P.nsplit * 128 * bn;
+    cnt_off.push_back(cnt_need);
+    cnt_need += (int64_t)P.tiles_m * P.tiles_n * ndw;
+    B->p[np_++] = P;
+  };
+  for (const Blk& b : blk) {
+    TcxProb P;
+    memset(&P, 0, sizeof(P));
+    P.mapB = 6;
+    P.b_row0 = 0;
+    P.b_k0 = (int)b.koff;
+    P.a_k0 = (int)(2 * b.q0);
+    P.K = (int)(2 * (b.q1 - b.q0));
+    P.kchunk = std::min(P.K, kchunk);
+    P.Nv = (int)(2 * nc);
+    P.ldd = 2 * nc;
+    P.tiles_n = 1;
+    if (b.kind == 0) {
+      P.amode = 2; P.mapA = 0; P.a_row0 = 0; P.a_plane = (int)N; P.M = (int)n;
+      P.D = (float*)(t->Pc32 + ((int64_t)(b.cls * L + b.a) * n) * nc);
+    } else if (b.kind == 1) {
+      P.amode = 1; P.mapA = 2; P.M = (int)N;
+      P.D = (float*)(t->ZA32 + (int64_t)b.a * N * nc);
+    } else {
+      P.amode = 1; P.mapA = 3; P.M = (int)Ns;
+      P.D = (float*)(t->ZB32 + (int64_t)b.a * Ns * nc);
+    }
+    P.tiles_m = (P.M + 127) / 128;
+    prob(P);
+  }
+  for (int a = 0; a < L; ++a) {
+    const int64_t r0 = t->s_start[a], r1 = t->s_start[a + 1];
+    if (r1 <= r0) continue;
+    TcxProb P;
+    memset(&P, 0, sizeof(P));
+    P.amode = 0; P.mapA = 4; P.mapB = 8;
+    P.a_row0 = (int)r0; P.a_k0 = 0;
+    P.b_row0 = (int)(a * 2 * n); P.b_k0 = 0;
+    P.M = (int)(r1 - r0); P.Nv = (int)(2 * n);
+    P.K = ldx; P.kchunk = ldx;
+    P.tiles_m = (P.M + 127) / 128;
+    P.tiles_n = (int)((2 * n + bn - 1) / bn);
+    P.D = (float*)(t->R2_32 + r0 * n);
+    P.ldd = 2 * n;
+    prob(P);
+  }
+  if (ws_need > 0) ZG_TRY(dalloc(t, &t->tcx_ws, ws_need));
+  ZG_TRY(dalloc(t, &t->tcx_cnt, std::max<int64_t>(cnt_need, 1)));
+  ZG_CHECK_CUDA(cudaMemsetAsync(t->tcx_cnt, 0, std::max<int64_t>(cnt_need, 1) * sizeof(int), s));
+  for (int i = 0; i < np_; ++i) {
+    B->p[i].ws = ws_off[i] >= 0 ? t->tcx_ws + ws_off[i] : nullptr;
+    B->p[i].counters = t->tcx_cnt + cnt_off[i];
+  }
+  B->nprob = np_;
+  B->nitems = items;
+  B->bn = bn;
+  B->err = t->tc_err;
+  int sms = 0;
+  ZG_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, t->dev));
+  t->tcx_grid = std::max(1, std::min(items, sms));
+  t->tcx = B.release();
+  t->tcx_on = true;
+  return ZG_OK;
+}
+
 static int create_mixed(zg_traj* t, const zg_layout* Lo, const std::vector<double2>& U, const std::vector<double2>& V) {
   const int64_t n = t->n, N = t->N, Ns = t->Ns, Nf = t->Nf, L = t->L, nc = t->nc;
   const int64_t np = (n + 15) / 16 * 16;
@@ -542,6 +733,7 @@ static int create_mixed(zg_traj* t, const zg_layout* Lo, const std::vector<doubl
                          (int)nb32, (int)np, t->tc_err));
   ZG_TRY(tc_gemm_prepare(t->gR1c, psih, psil, t->Hth, t->Htl, np, np, (float*)t->R1p, 2 * np, (int)(2 * N),
                          (int)(2 * np), (int)np, t->tc_err));
+  if (getenv("ZG_SIMT_PRODUCTS") == nullptr) ZG_TRY(build_tcx(t, Lo));
   ZG_CHECK_CUDA(cudaStreamSynchronize(s));
   return ZG_OK;
 }
@@ -1050,7 +1242,8 @@ static int rhs_mixed(zg_traj* t, int stage, const StageParams* p, int dH_mode, d
     t->h_diag_mode = dH_mode;
     ZG_TRY(launch_prep_mixed((int)n, (int)np, t->nonorth ? t->Hn0 : t->H0, sig, t->nonorth ? t->dHn : t->dH, dH_mode,
                              hubbard_U, h_part, t->Hth, t->Htl, t->BSh, t->BSl, t->nonorth ? t->Sm1 : nullptr, d,
-                             (const float2*)psih_f, (const float2*)psil_f, np, t->sigC32, t->G32, ml.plane, s));
+                             (const float2*)psih_f, (const float2*)psil_f, np, t->sigC32, t->G32, ml.plane, s,
+                             t->tcx_on ? t->sigEh : nullptr, t->tcx_on ? t->sigEl : nullptr, t->ldx));
     prof_end(t, ZG_PROF_PREP);
     // tensor cores: R1 = psi H(t)^T
     prof_begin(t, ZG_PROF_GEMM);
@@ -1069,9 +1262,10 @@ static int rhs_mixed(zg_traj* t, int stage, const StageParams* p, int dH_mode, d
     prof_end(t, ZG_PROF_OMEGA, s2);
     ZG_CHECK_CUDA(cudaEventRecord(t->ev_join, s2));
   }
-  // SIMT FP32: PI partials, xi sigma^T rows, Omega xi
+  // PI partials, xi sigma^T rows, Omega xi: on the tensor cores (t->tcx), else
+  // as the SIMT FP32 batch
   std::vector<GemmProb<float>> probs;
-  for (int a = 0; a < L; ++a) {
+  for (int a = 0; a < L && !t->tcx_on; ++a) {
     int64_t r0 = t->s_start[a], r1 = t->s_start[a + 1];
     gemm_prob_f32(probs, (const float2*)(psih_f + r0 * np), (const float2*)(psil_f + r0 * np), np, 1,
                   t->IXI32 + r0 * nc, nc, 0, t->Pc32 + ((0 * L + a) * n) * nc, nc, (int)n, (int)nc, (int)(r1 - r0),
@@ -1102,7 +1296,10 @@ static int rhs_mixed(zg_traj* t, int stage, const StageParams* p, int dH_mode, d
     return run_batches<float>(t, probs2, &t->ws32, &t->ws32_cap, s, true);
   }
   prof_begin(t, ZG_PROF_SMALL);
-  ZG_TRY(run_batches<float>(t, probs, &t->ws32, &t->ws32_cap, s, false));
+  if (t->tcx_on)
+    ZG_TRY(tcx_launch(*t->tcx, t->tcx_grid, s));
+  else
+    ZG_TRY(run_batches<float>(t, probs, &t->ws32, &t->ws32_cap, s, false));
   if (t->nonorth) {
     ZG_TRY(launch_nonorth_gather<float>(d, t->Pc32, t->ZA32, t->ZB32, t->Qcat32, t->Zcat32, s));
     ZG_TRY(run_batches<float>(t, probs2, &t->ws32, &t->ws32_cap, s, false));

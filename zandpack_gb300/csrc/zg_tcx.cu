@@ -1,0 +1,417 @@
+// Complex products of the mixed-precision right-hand side on the tcgen05
+// tensor cores: the PI partials psi^T IXI (Zandpack/mpi/zand:91-110,363-366),
+// the Omega xi products (:770-778) and the xi sigma^T rows (:760-768).
+//
+// Every product is C = A B^T with complex A (M x K) and B (Nc x K).  On the
+// tensor core it is the real GEMM
+//
+//   D (M x 2Nc) = A' (M x 2K) B'^T,   A'[m][2k], A'[m][2k+1] = Re, Im A[m][k]
+//   B'[2c][2k] = Re B[c][k],   B'[2c][2k+1] = -Im B[c][k]
+//   B'[2c+1][2k] = Im B[c][k], B'[2c+1][2k+1] = Re B[c][k]
+//
+// so that D[m][2c], D[m][2c+1] = Re, Im C[m][c]: A' is the interleaved
+// complex storage itself and D is the interleaved complex result.  Products
+// are 3xTF32 (Ahi.Bhi + Ahi.Blo + Alo.Bhi) with FP32 accumulation, each K
+// block of 32 floats accumulated alone in TMEM and added into FP32 registers
+// with round-to-nearest (the tensor core truncates inside its accumulation).
+//
+// The A operand reaches shared memory in one of three forms (per problem):
+//   0: hi and lo parts, K-major (constants split once);
+//   1: raw FP32, K-major (the Omega blocks of the stage input): converter
+//      warps split each element into hi and lo in place;
+//   2: the planar TF32 hi/lo parts of psi (rows = modes, columns = orbitals),
+//      loaded as 16-mode x 128-orbital boxes: converter warps transpose and
+//      interleave them into K-major A' rows (one orbital per row), so the
+//      reduction over modes needs no transposed copy of psi in HBM.
+// B' always arrives pre-split (constants, or built by the stage's operand
+// kernel).
+//
+// One persistent CTA per SM walks a static list of work items (problem,
+// 128-row tile, BN-column tile, K chunk).  Warp roles:
+//   warp 0      one thread: TMA loads into a 2-stage ring;
+//   warp 1      one thread: tcgen05.mma issue, owns the TMEM allocation;
+//   warps 2-5   converters (forms 1 and 2; form 0 passes through);
+//   warps 6..   drain: TMEM -> registers, per-item sums, epilogue.
+// Split-K items write FP32 partial tiles; the last drain warp to finish a
+// 32-row slice of a tile (an atomic counter per slice) adds the partials in a
+// fixed order and writes the result, so results are deterministic.  Waits on mbarriers are bounded like
+// those of the 3xTF32 GEMM (zg_tc.cu): on timeout the error code is recorded,
+// in-flight copies and MMAs are waited for (bounded) and TMEM is freed.
+#include "zg_tc_ptx.cuh"
+#include "zg_tcx.cuh"
+
+namespace zg {
+
+template <int BN>
+struct TcxCfg {
+  static constexpr int STAGES = 2;
+  static constexpr int A_BYTES = 128 * 32 * 4;   // one 128 x 32-float K-major tile
+  static constexpr int RAW_BYTES = 4 * 16 * 128 * 4;  // four 16-mode x 128-orbital planes (form 2)
+  static constexpr int B_BYTES = BN * 32 * 4;
+  // stage: A hi | A lo | raw planes | B hi | B lo
+  static constexpr int OFF_AL = A_BYTES, OFF_RAW = 2 * A_BYTES, OFF_BH = 2 * A_BYTES + RAW_BYTES,
+                       OFF_BL = OFF_BH + B_BYTES;
+  static constexpr int STAGE_BYTES = OFF_BL + B_BYTES;
+  static constexpr int BAR_OFF = STAGES * STAGE_BYTES;
+  static constexpr int SMEM = BAR_OFF + 256 + 1024;
+  static constexpr int NACC = BN <= 128 ? 4 : 2;  // TMEM accumulator buffers of BN columns
+  static constexpr uint32_t TMEM_COLS = NACC * BN <= 256 ? (NACC * BN <= 128 ? 128 : 256) : 512;
+  static constexpr int DCOLS = BN % 64 == 0 ? 64 : 32;
+  static constexpr int NDW = 4 * (BN / DCOLS);
+  static constexpr int NCONV = 4;
+  static constexpr int W_DRAIN = 2 + NCONV;
+  static constexpr int THREADS = 32 * (W_DRAIN + NDW);
+  static_assert(BN % 32 == 0 && BN >= 32 && BN <= 256, "BN");
+  static_assert(SMEM <= 232448, "shared memory");
+};
+
+struct TcxItem {
+  int prob, tm, tn, split;
+};
+
+__device__ __forceinline__ TcxItem tcx_item(const TcxBatch& b, int w) {
+  int p = 0;
+  while (p + 1 < b.nprob && w >= b.p[p + 1].item_begin) ++p;
+  const TcxProb& P = b.p[p];
+  int r = w - P.item_begin;
+  TcxItem it;
+  it.prob = p;
+  it.split = r % P.nsplit;
+  r /= P.nsplit;
+  it.tn = r % P.tiles_n;
+  it.tm = r / P.tiles_n;
+  return it;
+}
+
+// K blocks (of 32 floats) of an item
+__device__ __forceinline__ void tcx_kblocks(const TcxProb& P, int split, int& kb0, int& nkb) {
+  const int total = P.K / 32;
+  const int per = P.kchunk / 32;
+  kb0 = split * per;
+  nkb = min(per, total - kb0);
+}
+
+__device__ __forceinline__ uint32_t tf32_rna(float x) {
+  uint32_t h;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(x));
+  return h;
+}
+
+template <int BN>
+__global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_constant__ TcxBatch batch) {
+  using C = TcxCfg<BN>;
+  constexpr int STAGES = C::STAGES, NACC = C::NACC, NDW = C::NDW;
+  extern __shared__ uint8_t smem_raw[];
+  const uint32_t raw = smem_u32(smem_raw);
+  const uint32_t pad = (1024u - (raw & 1023u)) & 1023u;
+  uint8_t* smem = smem_raw + pad;
+  const uint32_t sbase = raw + pad;
+  const uint32_t bar_full = sbase + C::BAR_OFF;        // STAGES: TMA landed
+  const uint32_t bar_conv = bar_full + 8 * STAGES;     // STAGES: converters done
+  const uint32_t bar_empty = bar_conv + 8 * STAGES;    // STAGES: MMAs read the stage
+  const uint32_t bar_tfull = bar_empty + 8 * STAGES;   // NACC
+  const uint32_t bar_tempty = bar_tfull + 8 * NACC;    // NACC
+  const uint32_t bar_done = bar_tempty + 8 * NACC;
+  uint32_t* tmem_slot = (uint32_t*)(smem + C::BAR_OFF + 24 * STAGES + 16 * NACC + 8);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int* err = batch.err;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(bar_full + 8 * s, 1);
+      mbar_init(bar_conv + 8 * s, 32 * C::NCONV);
+      mbar_init(bar_empty + 8 * s, 1);
+    }
+    for (int b = 0; b < NACC; ++b) {
+      mbar_init(bar_tfull + 8 * b, 1);
+      mbar_init(bar_tempty + 8 * b, 32 * NDW);
+    }
+    mbar_init(bar_done, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(C::TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+  const int nitems = batch.nitems;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---------------- TMA producer
+      int issued[STAGES];
+      for (int s = 0; s < STAGES; ++s) issued[s] = 0;
+      bool ok = true;
+      int kb_global = 0;
+      for (int w = blockIdx.x; w < nitems && ok; w += gridDim.x) {
+        const TcxItem it = tcx_item(batch, w);
+        const TcxProb& P = batch.p[it.prob];
+        int kb0, nkb;
+        tcx_kblocks(P, it.split, kb0, nkb);
+        for (int q = 0; q < nkb; ++q, ++kb_global) {
+          const int s = kb_global % STAGES;
+          const uint32_t ph = (uint32_t)(kb_global / STAGES) & 1u;
+          ok = mbar_wait(bar_empty + 8 * s, ph ^ 1u, err, 11);
+          if (!ok) break;
+          const uint32_t st = sbase + s * C::STAGE_BYTES;
+          const uint32_t fb = bar_full + 8 * s;
+          const int kx = (kb0 + q) * 32;  // K float offset inside the problem
+          const int bytes_a = P.amode == 0 ? 2 * C::A_BYTES : P.amode == 1 ? C::A_BYTES : C::RAW_BYTES;
+          mbar_expect_tx(fb, bytes_a + 2 * C::B_BYTES);
+          const CUtensorMap* mA = &batch.maps[P.mapA];
+          if (P.amode == 0) {
+            tma_load_2d(st, mA, fb, P.a_k0 + kx, P.a_row0 + it.tm * 128);
+            tma_load_2d(st + C::OFF_AL, mA + 1, fb, P.a_k0 + kx, P.a_row0 + it.tm * 128);
+          } else if (P.amode == 1) {
+            tma_load_2d(st, mA, fb, P.a_k0 + kx, P.a_row0 + it.tm * 128);
+          } else {
+            // planes: rows = modes (16 per K block), columns = 128 orbitals
+            const int x = P.a_row0 + it.tm * 128, mode = (P.a_k0 + kx) / 2;
+            const uint32_t rb = st + C::OFF_RAW;
+            tma_load_2d(rb, mA, fb, x, mode);
+            tma_load_2d(rb + 8192, mA, fb, x, P.a_plane + mode);
+            tma_load_2d(rb + 16384, mA + 1, fb, x, mode);
+            tma_load_2d(rb + 24576, mA + 1, fb, x, P.a_plane + mode);
+          }
+          const CUtensorMap* mB = &batch.maps[P.mapB];
+          tma_load_2d(st + C::OFF_BH, mB, fb, P.b_k0 + kx, P.b_row0 + it.tn * BN);
+          tma_load_2d(st + C::OFF_BL, mB + 1, fb, P.b_k0 + kx, P.b_row0 + it.tn * BN);
+          issued[s] = kb_global / STAGES + 1;
+        }
+      }
+      if (!ok) {
+        for (int s = 0; s < STAGES; ++s)
+          if (issued[s] > 0) mbar_wait(bar_full + 8 * s, (uint32_t)(issued[s] - 1) & 1u, err, 14);
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---------------- MMA issuer: one TMEM buffer per K block
+      constexpr uint32_t idesc = idesc_tf32(128, BN);
+      bool ok = true;
+      int kb_global = 0;
+      for (int w = blockIdx.x; w < nitems && ok; w += gridDim.x) {
+        const TcxItem it = tcx_item(batch, w);
+        int kb0, nkb;
+        tcx_kblocks(batch.p[it.prob], it.split, kb0, nkb);
+        for (int q = 0; q < nkb; ++q, ++kb_global) {
+          const int b = kb_global % NACC;
+          if (!mbar_wait(bar_tempty + 8 * b, ((uint32_t)(kb_global / NACC) & 1u) ^ 1u, err, 15)) {
+            ok = false;
+            break;
+          }
+          const int s = kb_global % STAGES;
+          if (!mbar_wait(bar_conv + 8 * s, (uint32_t)(kb_global / STAGES) & 1u, err, 12)) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t st = sbase + s * C::STAGE_BYTES;
+          const uint32_t aH = st, aL = st + C::OFF_AL, bH = st + C::OFF_BH, bL = st + C::OFF_BL;
+          const uint32_t d = tmem + (uint32_t)(b * BN);
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const uint32_t off = j * 32;
+            umma_tf32(d, umma_desc_k<32>(aH + off), umma_desc_k<32>(bH + off), idesc, j == 0 ? 0u : 1u);
+            umma_tf32(d, umma_desc_k<32>(aH + off), umma_desc_k<32>(bL + off), idesc, 1u);
+            umma_tf32(d, umma_desc_k<32>(aL + off), umma_desc_k<32>(bH + off), idesc, 1u);
+          }
+          umma_commit(bar_empty + 8 * s);
+          umma_commit(bar_tfull + 8 * b);
+        }
+      }
+      umma_commit(bar_done);
+      mbar_wait(bar_done, 0, err, 16);
+    }
+  } else if (warp < C::W_DRAIN) {
+    // ---------------- converters (128 threads)
+    const int ct = threadIdx.x - 64;
+    bool ok = true;
+    int kb_global = 0;
+    for (int w = blockIdx.x; w < nitems && ok; w += gridDim.x) {
+      const TcxItem it = tcx_item(batch, w);
+      const TcxProb& P = batch.p[it.prob];
+      int kb0, nkb;
+      tcx_kblocks(P, it.split, kb0, nkb);
+      for (int q = 0; q < nkb; ++q, ++kb_global) {
+        const int s = kb_global % STAGES;
+        ok = __all_sync(0xffffffffu, mbar_wait(bar_full + 8 * s, (uint32_t)(kb_global / STAGES) & 1u, err, 13));
+        if (!ok) break;
+        uint8_t* st = smem + s * C::STAGE_BYTES;
+        if (P.amode == 1) {
+          // split in place: A hi overwrites the raw tile, A lo goes to its own tile
+          float4* ah = reinterpret_cast<float4*>(st);
+          float4* al = reinterpret_cast<float4*>(st + C::OFF_AL);
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            const int c = ct + 128 * j;
+            const float4 v = ah[c];
+            float4 h, l;
+            h.x = __uint_as_float(tf32_rna(v.x)); l.x = __uint_as_float(tf32_rna(v.x - h.x));
+            h.y = __uint_as_float(tf32_rna(v.y)); l.y = __uint_as_float(tf32_rna(v.y - h.y));
+            h.z = __uint_as_float(tf32_rna(v.z)); l.z = __uint_as_float(tf32_rna(v.z - h.z));
+            h.w = __uint_as_float(tf32_rna(v.w)); l.w = __uint_as_float(tf32_rna(v.w - h.w));
+            ah[c] = h;
+            al[c] = l;
+          }
+        } else if (P.amode == 2) {
+          // row ct of A' (orbital ct of the tile): modes 0..15 as (re, im) pairs,
+          // 128-byte rows in the SWIZZLE_128B pattern (16-byte chunk c of row r
+          // at chunk c ^ (r % 8))
+          const float* rp = reinterpret_cast<const float*>(st + C::OFF_RAW);
+#pragma unroll
+          for (int part = 0; part < 2; ++part) {  // 0: hi, 1: lo
+            const float* re = rp + part * 4096;
+            const float* im = re + 2048;
+            uint8_t* dst = st + (part ? C::OFF_AL : 0) + ct * 128;
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+              const float4 v = make_float4(re[(2 * c) * 128 + ct], im[(2 * c) * 128 + ct], re[(2 * c + 1) * 128 + ct],
+                                           im[(2 * c + 1) * 128 + ct]);
+              *reinterpret_cast<float4*>(dst + ((c ^ (ct & 7)) << 4)) = v;
+            }
+          }
+        }
+        // generic-proxy writes to shared memory, read next by the tensor core
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_arrive(bar_conv + 8 * s);
+      }
+    }
+  } else {
+    // ---------------- drain warps: TMEM lane quarter (warp % 4), columns part * DCOLS
+    const int dw = warp - C::W_DRAIN;
+    const int quarter = warp & 3, part = dw >> 2;
+    const int row_in_tile = quarter * 32 + lane;
+    const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
+    float acc[C::DCOLS];
+    bool ok = true;
+    int kb_global = 0;
+    for (int w = blockIdx.x; w < nitems && ok; w += gridDim.x) {
+      const TcxItem it = tcx_item(batch, w);
+      const TcxProb& P = batch.p[it.prob];
+      int kb0, nkb;
+      tcx_kblocks(P, it.split, kb0, nkb);
+#pragma unroll
+      for (int i = 0; i < C::DCOLS; ++i) acc[i] = 0.f;
+      for (int q = 0; q < nkb; ++q, ++kb_global) {
+        const int b = kb_global % NACC;
+        ok = __all_sync(0xffffffffu, mbar_wait(bar_tfull + 8 * b, (uint32_t)(kb_global / NACC) & 1u, err, 17));
+        if (!ok) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t t0 = tmem + lane_base + (uint32_t)(b * BN + part * C::DCOLS);
+#pragma unroll
+        for (int c = 0; c < C::DCOLS; c += 32) {
+          uint32_t r0[32];
+          TC_LD32(r0, t0 + c);
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+          for (int i = 0; i < 32; ++i) acc[c + i] += __uint_as_float(r0[i]);
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        mbar_arrive(bar_tempty + 8 * b);
+      }
+      if (!ok) break;
+      // ---- epilogue of the item
+      const int row = it.tm * 128 + row_in_tile;
+      const int col0 = it.tn * BN + part * C::DCOLS;
+      if (P.nsplit == 1) {
+        if (row < P.M) {
+          float* dst = P.D + (long long)row * P.ldd + col0;
+#pragma unroll
+          for (int i = 0; i < C::DCOLS; ++i)
+            if (col0 + i < P.Nv) dst[i] = acc[i];
+        }
+        continue;
+      }
+      // split K: every drain warp writes its 32-row slice of the partial tile;
+      // the warp that completes a slice last (one counter per slice) adds the
+      // partials in split order and writes the result
+      const int tile = it.tm * P.tiles_n + it.tn;
+      const int slice = tile * NDW + dw;
+      const long long tile_ws = (long long)tile * P.nsplit * (128 * BN);
+      const long long my = (long long)row_in_tile * BN + part * C::DCOLS;
+      float* wsp = P.ws + tile_ws + (long long)it.split * (128 * BN) + my;
+#pragma unroll
+      for (int i = 0; i < C::DCOLS; i += 4)
+        __stcg(reinterpret_cast<float4*>(wsp + i), make_float4(acc[i], acc[i + 1], acc[i + 2], acc[i + 3]));
+      __threadfence();
+      __syncwarp();
+      int prev = 0;
+      if (lane == 0) prev = atomicAdd(P.counters + slice, 1);
+      prev = __shfl_sync(0xffffffffu, prev, 0);
+      if (prev == P.nsplit - 1) {
+        __threadfence();
+        if (row < P.M) {
+          const float* src = P.ws + tile_ws + my;
+          float* dst = P.D + (long long)row * P.ldd + col0;
+#pragma unroll 1
+          for (int i = 0; i < C::DCOLS; i += 4) {
+            float4 sum = __ldcg(reinterpret_cast<const float4*>(src + i));
+            for (int sp = 1; sp < P.nsplit; ++sp) {
+              const float4 v = __ldcg(reinterpret_cast<const float4*>(src + (long long)sp * (128 * BN) + i));
+              sum.x += v.x; sum.y += v.y; sum.z += v.z; sum.w += v.w;
+            }
+            const float sv[4] = {sum.x, sum.y, sum.z, sum.w};
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+              if (col0 + i + e < P.Nv) dst[i + e] = sv[e];
+          }
+        }
+        __syncwarp();
+        if (lane == 0) P.counters[slice] = 0;  // ready for the next launch
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(C::TMEM_COLS) : "memory");
+  }
+}
+
+// ---------------------------------------------------------------- host side
+int make_tmap_f32_box(CUtensorMap* map, const float* base, int64_t rows, int64_t cols, int64_t ld, int box_rows,
+                      int box_cols, bool swizzle128);
+
+template <int BN>
+static int launch_tcx_bn(const TcxBatch& b, int grid, cudaStream_t s) {
+  using C = TcxCfg<BN>;
+  static std::atomic<bool> configured[64];
+  int dev = 0;
+  ZG_CHECK_CUDA(cudaGetDevice(&dev));
+  if (dev < 64 && !configured[dev].load()) {
+    ZG_CHECK_CUDA(cudaFuncSetAttribute(k_tcx<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
+    configured[dev] = true;
+  }
+  k_tcx<BN><<<grid, C::THREADS, C::SMEM, s>>>(b);
+  ZG_CHECK_LAUNCH();
+  count_launch();
+  return ZG_OK;
+}
+
+int tcx_bn_for(int ncols) {
+  if (ncols <= 32) return 32;
+  if (ncols <= 64) return 64;
+  if (ncols <= 128) return 128;
+  if (ncols <= 192) return 192;
+  return 0;
+}
+
+int tcx_launch(const TcxBatch& b, int grid, cudaStream_t s) {
+  if (b.nitems == 0) return ZG_OK;
+  switch (b.bn) {
+    case 32: return launch_tcx_bn<32>(b, grid, s);
+    case 64: return launch_tcx_bn<64>(b, grid, s);
+    case 128: return launch_tcx_bn<128>(b, grid, s);
+    case 192: return launch_tcx_bn<192>(b, grid, s);
+    default: set_error("complex tensor-core product: no kernel for %d columns", b.bn); return ZG_EINVAL;
+  }
+}
+
+}  // namespace zg

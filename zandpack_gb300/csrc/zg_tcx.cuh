@@ -1,0 +1,47 @@
+// Problem table of the complex tensor-core products (zg_tcx.cu).
+#pragma once
+#include <cuda.h>
+
+#include "zg_kernels.cuh"
+
+namespace zg {
+
+#define ZG_TCX_MAPS 12
+#define ZG_TCX_PROBS (5 * ZG_MAX_LEADS)
+
+// One complex product D (M x Nv real columns, row stride ldd floats) =
+// A' B'^T over K floats (a multiple of 32), in items of kchunk floats.
+struct TcxProb {
+  int amode;          // 0: A hi/lo (maps mapA, mapA+1); 1: raw FP32 A (map mapA); 2: planar psi hi/lo planes
+  int mapA, mapB;     // tensor-map indices (B: hi at mapB, lo at mapB + 1)
+  int a_row0;         // forms 0/1: first A row; form 2: first orbital (x coordinate)
+  int a_k0;           // first K float of A (form 2: 2 x the first mode)
+  int a_plane;        // form 2: row offset of the imaginary plane
+  int b_row0, b_k0;   // first row and K float of B'
+  int M, Nv, K, kchunk, nsplit, tiles_m, tiles_n;
+  int item_begin;     // first work item of this problem
+  float* D;
+  long long ldd;
+  float* ws;          // split-K partial tiles (nsplit > 1): [tile][split][128][BN]
+  int* counters;      // one per 32-row slice of a tile and drain warp, zero between launches
+};
+
+struct TcxBatch {
+  CUtensorMap maps[ZG_TCX_MAPS];
+  TcxProb p[ZG_TCX_PROBS];
+  int nprob, nitems, bn;
+  int* err;
+};
+
+// BN of the kernel for products with `ncols` real output columns per tile
+// (0 when none fits)
+int tcx_bn_for(int ncols);
+// number of drain warps of the BN kernel (counters per tile)
+inline int tcx_ndw(int bn) { return 4 * (bn / (bn % 64 == 0 ? 64 : 32)); }
+int tcx_launch(const TcxBatch& b, int grid, cudaStream_t s);
+// rows x cols fp32 row-major (row stride ld floats); box = box_cols x box_rows;
+// swizzle128: the 128-byte swizzle of a 32-float K-major row, else no swizzle
+int make_tmap_f32_box(CUtensorMap* map, const float* base, int64_t rows, int64_t cols, int64_t ld, int box_rows,
+                      int box_cols, bool swizzle128);
+
+}  // namespace zg
