@@ -511,7 +511,6 @@ static int build_tcx(zg_traj* t, const zg_layout* Lo) {
   if (bn == 0 || Ns % 2 || Nf % 2 || !al16(omA) || !al16(omB) || Ns == 0) return ZG_OK;
   cudaStream_t s = t->stream;
   const int ndw = tcx_ndw(bn);
-  const int kchunk = 256;
   std::unique_ptr<TcxBatch> B(new TcxBatch());
   memset(B.get(), 0, sizeof(TcxBatch));
   // ---- B' stack of the PI and Omega xi problems
@@ -591,20 +590,8 @@ static int build_tcx(zg_traj* t, const zg_layout* Lo) {
   ZG_TRY(make_tmap_f32_box(&mp[7], t->tcxBl, bn, kstack, kstack, bn, 32, true));
   ZG_TRY(make_tmap_f32_box(&mp[8], t->sigEh, L * 2 * n, 2 * nc, ldx, bn, 32, true));
   ZG_TRY(make_tmap_f32_box(&mp[9], t->sigEl, L * 2 * n, 2 * nc, ldx, bn, 32, true));
-  // ---- problems
-  int np_ = 0, items = 0;
-  int64_t ws_need = 0, cnt_need = 0;
-  std::vector<int64_t> ws_off, cnt_off;
-  auto prob = [&](TcxProb P) {
-    P.nsplit = (P.K + P.kchunk - 1) / P.kchunk;
-    P.item_begin = items;
-    items += P.tiles_m * P.tiles_n * P.nsplit;
-    ws_off.push_back(P.nsplit > 1 ? ws_need : -1);
-    if (P.nsplit > 1) ws_need += (int64_t)P.tiles_m * P.tiles_n * P.nsplit * 128 * bn;
-    cnt_off.push_back(cnt_need);
-    cnt_need += (int64_t)P.tiles_m * P.tiles_n * ndw;
-    B->p[np_++] = P;
-  };
+  // ---- problems (K chunks set below, once the total work is known)
+  std::vector<TcxProb> probs;
   for (const Blk& b : blk) {
     TcxProb P;
     memset(&P, 0, sizeof(P));
@@ -613,7 +600,6 @@ static int build_tcx(zg_traj* t, const zg_layout* Lo) {
     P.b_k0 = (int)b.koff;
     P.a_k0 = (int)(2 * b.q0);
     P.K = (int)(2 * (b.q1 - b.q0));
-    P.kchunk = std::min(P.K, kchunk);
     P.Nv = (int)(2 * nc);
     P.ldd = 2 * nc;
     P.tiles_n = 1;
@@ -628,7 +614,7 @@ static int build_tcx(zg_traj* t, const zg_layout* Lo) {
       P.D = (float*)(t->ZB32 + (int64_t)b.a * Ns * nc);
     }
     P.tiles_m = (P.M + 127) / 128;
-    prob(P);
+    probs.push_back(P);
   }
   for (int a = 0; a < L; ++a) {
     const int64_t r0 = t->s_start[a], r1 = t->s_start[a + 1];
@@ -639,27 +625,80 @@ static int build_tcx(zg_traj* t, const zg_layout* Lo) {
     P.a_row0 = (int)r0; P.a_k0 = 0;
     P.b_row0 = (int)(a * 2 * n); P.b_k0 = 0;
     P.M = (int)(r1 - r0); P.Nv = (int)(2 * n);
-    P.K = ldx; P.kchunk = ldx;
+    P.K = ldx;
     P.tiles_m = (P.M + 127) / 128;
     P.tiles_n = (int)((2 * n + bn - 1) / bn);
     P.D = (float*)(t->R2_32 + r0 * n);
     P.ldd = 2 * n;
-    prob(P);
+    probs.push_back(P);
+  }
+  int sms = 0;
+  ZG_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, t->dev));
+  const int grid = std::max(1, std::min(sms, ZG_TCX_GRID));
+  // K chunk: about the average work of a CTA, so that no item outlasts the
+  // others by much and split-K partials stay few
+  int64_t total_kb = 0;
+  for (const TcxProb& P : probs) total_kb += (int64_t)P.tiles_m * P.tiles_n * (P.K / 32);
+  int chunk_kb = (int)std::min<int64_t>(64, std::max<int64_t>(8, (total_kb + grid - 1) / grid));
+  std::vector<int> item_kb;
+  for (;;) {
+    int items = 0;
+    item_kb.clear();
+    for (TcxProb& P : probs) {
+      P.kchunk = std::min(P.K, 32 * chunk_kb);
+      P.nsplit = (P.K + P.kchunk - 1) / P.kchunk;
+      P.item_begin = items;
+      items += P.tiles_m * P.tiles_n * P.nsplit;
+      for (int w = 0; w < P.tiles_m * P.tiles_n * P.nsplit; ++w) {
+        const int split = w % P.nsplit;
+        item_kb.push_back(std::min(P.kchunk, P.K - split * P.kchunk) / 32);
+      }
+    }
+    if (items <= ZG_TCX_ITEMS) break;
+    if (chunk_kb >= 1024) return ZG_OK;  // too many tiles for the item table: the SIMT batch runs
+    chunk_kb *= 2;
+  }
+  const int nitems = (int)item_kb.size();
+  // longest first onto the least loaded CTA
+  std::vector<int> order(nitems);
+  for (int i = 0; i < nitems; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return item_kb[x] > item_kb[y]; });
+  std::vector<int64_t> load(grid, 0);
+  std::vector<std::vector<int>> per(grid);
+  for (int w : order) {
+    int c = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+    load[c] += item_kb[w] + 2;  // + the item's epilogue
+    per[c].push_back(w);
+  }
+  int used = 0, pos = 0;
+  for (int c = 0; c < grid; ++c) {
+    if (per[c].empty()) continue;
+    B->cta_off[used++] = (unsigned short)pos;
+    for (int w : per[c]) B->items[pos++] = (unsigned short)w;
+  }
+  B->cta_off[used] = (unsigned short)pos;
+  int64_t ws_need = 0, cnt_need = 0;
+  std::vector<int64_t> ws_off, cnt_off;
+  for (const TcxProb& P : probs) {
+    ws_off.push_back(P.nsplit > 1 ? ws_need : -1);
+    if (P.nsplit > 1) ws_need += (int64_t)P.tiles_m * P.tiles_n * P.nsplit * 128 * bn;
+    cnt_off.push_back(cnt_need);
+    cnt_need += (int64_t)P.tiles_m * P.tiles_n * ndw;
   }
   if (ws_need > 0) ZG_TRY(dalloc(t, &t->tcx_ws, ws_need));
   ZG_TRY(dalloc(t, &t->tcx_cnt, std::max<int64_t>(cnt_need, 1)));
   ZG_CHECK_CUDA(cudaMemsetAsync(t->tcx_cnt, 0, std::max<int64_t>(cnt_need, 1) * sizeof(int), s));
+  const int np_ = (int)probs.size();
   for (int i = 0; i < np_; ++i) {
+    B->p[i] = probs[i];
     B->p[i].ws = ws_off[i] >= 0 ? t->tcx_ws + ws_off[i] : nullptr;
     B->p[i].counters = t->tcx_cnt + cnt_off[i];
   }
   B->nprob = np_;
-  B->nitems = items;
+  B->nitems = nitems;
   B->bn = bn;
   B->err = t->tc_err;
-  int sms = 0;
-  ZG_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, t->dev));
-  t->tcx_grid = std::max(1, std::min(items, sms));
+  t->tcx_grid = used;
   t->tcx = B.release();
   t->tcx_on = true;
   return ZG_OK;

@@ -26,8 +26,8 @@
 // B' always arrives pre-split (constants, or built by the stage's operand
 // kernel).
 //
-// One persistent CTA per SM walks a static list of work items (problem,
-// 128-row tile, BN-column tile, K chunk).  Warp roles:
+// One persistent CTA per SM walks its list of work items (problem, 128-row
+// tile, BN-column tile, K chunk), assigned longest first on the host.  Warp roles:
 //   warp 0      one thread: TMA loads into a 2-stage ring;
 //   warp 1      one thread: tcgen05.mma issue, owns the TMEM allocation;
 //   warps 2-5   converters (forms 1 and 2; form 0 passes through);
@@ -139,7 +139,7 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
-  const int nitems = batch.nitems;
+  const int wbeg = batch.cta_off[blockIdx.x], wend = batch.cta_off[blockIdx.x + 1];
 
   if (warp == 0) {
     if (lane == 0) {
@@ -148,7 +148,8 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
       for (int s = 0; s < STAGES; ++s) issued[s] = 0;
       bool ok = true;
       int kb_global = 0;
-      for (int w = blockIdx.x; w < nitems && ok; w += gridDim.x) {
+      for (int wi = wbeg; wi < wend && ok; ++wi) {
+        const int w = batch.items[wi];
         const TcxItem it = tcx_item(batch, w);
         const TcxProb& P = batch.p[it.prob];
         int kb0, nkb;
@@ -195,7 +196,8 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
       constexpr uint32_t idesc = idesc_tf32(128, BN);
       bool ok = true;
       int kb_global = 0;
-      for (int w = blockIdx.x; w < nitems && ok; w += gridDim.x) {
+      for (int wi = wbeg; wi < wend && ok; ++wi) {
+        const int w = batch.items[wi];
         const TcxItem it = tcx_item(batch, w);
         int kb0, nkb;
         tcx_kblocks(batch.p[it.prob], it.split, kb0, nkb);
@@ -233,7 +235,8 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
     const int ct = threadIdx.x - 64;
     bool ok = true;
     int kb_global = 0;
-    for (int w = blockIdx.x; w < nitems && ok; w += gridDim.x) {
+    for (int wi = wbeg; wi < wend && ok; ++wi) {
+        const int w = batch.items[wi];
       const TcxItem it = tcx_item(batch, w);
       const TcxProb& P = batch.p[it.prob];
       int kb0, nkb;
@@ -291,7 +294,8 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
     float acc[C::DCOLS];
     bool ok = true;
     int kb_global = 0;
-    for (int w = blockIdx.x; w < nitems && ok; w += gridDim.x) {
+    for (int wi = wbeg; wi < wend && ok; ++wi) {
+        const int w = batch.items[wi];
       const TcxItem it = tcx_item(batch, w);
       const TcxProb& P = batch.p[it.prob];
       int kb0, nkb;
@@ -347,19 +351,28 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
       if (prev == P.nsplit - 1) {
         __threadfence();
         if (row < P.M) {
+          // every load of one partial slice in flight at once
           const float* src = P.ws + tile_ws + my;
-          float* dst = P.D + (long long)row * P.ldd + col0;
-#pragma unroll 1
-          for (int i = 0; i < C::DCOLS; i += 4) {
-            float4 sum = __ldcg(reinterpret_cast<const float4*>(src + i));
-            for (int sp = 1; sp < P.nsplit; ++sp) {
-              const float4 v = __ldcg(reinterpret_cast<const float4*>(src + (long long)sp * (128 * BN) + i));
-              sum.x += v.x; sum.y += v.y; sum.z += v.z; sum.w += v.w;
+          float4 sum[C::DCOLS / 4];
+#pragma unroll
+          for (int i = 0; i < C::DCOLS / 4; ++i) sum[i] = __ldcg(reinterpret_cast<const float4*>(src) + i);
+          for (int sp = 1; sp < P.nsplit; ++sp) {
+            const float4* q = reinterpret_cast<const float4*>(src + (long long)sp * (128 * BN));
+            float4 v[C::DCOLS / 4];
+#pragma unroll
+            for (int i = 0; i < C::DCOLS / 4; ++i) v[i] = __ldcg(q + i);
+#pragma unroll
+            for (int i = 0; i < C::DCOLS / 4; ++i) {
+              sum[i].x += v[i].x; sum[i].y += v[i].y; sum[i].z += v[i].z; sum[i].w += v[i].w;
             }
-            const float sv[4] = {sum.x, sum.y, sum.z, sum.w};
+          }
+          float* dst = P.D + (long long)row * P.ldd + col0;
+#pragma unroll
+          for (int i = 0; i < C::DCOLS / 4; ++i) {
+            const float sv[4] = {sum[i].x, sum[i].y, sum[i].z, sum[i].w};
 #pragma unroll
             for (int e = 0; e < 4; ++e)
-              if (col0 + i + e < P.Nv) dst[i + e] = sv[e];
+              if (col0 + 4 * i + e < P.Nv) dst[4 * i + e] = sv[e];
           }
         }
         __syncwarp();

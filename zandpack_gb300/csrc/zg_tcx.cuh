@@ -26,9 +26,16 @@ struct TcxProb {
   int* counters;      // one per 32-row slice of a tile and drain warp, zero between launches
 };
 
+#define ZG_TCX_ITEMS 3072
+#define ZG_TCX_GRID 160
+
 struct TcxBatch {
   CUtensorMap maps[ZG_TCX_MAPS];
   TcxProb p[ZG_TCX_PROBS];
+  // work items of CTA c: items[cta_off[c] .. cta_off[c + 1]) (a longest-first
+  // assignment made on the host; item w is decoded against p[].item_begin)
+  unsigned short items[ZG_TCX_ITEMS];
+  unsigned short cta_off[ZG_TCX_GRID + 1];
   int nprob, nitems, bn;
   int* err;
 };
