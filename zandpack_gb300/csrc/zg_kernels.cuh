@@ -279,11 +279,19 @@ int launch_final_all_mixed(const RhsDev<float>& d, const StageParams* p, const f
                            const float2* ZB, float2* kpsi, int64_t plane, int rmode, int npl, const float2* R3,
                            const float2* C0, cudaStream_t s);
 // launch_build_operands_mixed and launch_gathers<float> of a mixed stage in one launch
+// Per-stage operands of the tensor-core products (zg_tcx.cu) written by the
+// stage's gathers: the embedded sigma columns of the xi sigma^T product, and
+// the psi gathers of the Omega sources as A rows (Gt, [lead][mode]) and as
+// embedded conjugate B' rows (Gc, [lead][2 mode + 0/1]); TF32 hi/lo, rows of
+// ldx floats.  Null pointers: not written.
+struct TcxOperands {
+  float *sigEh = nullptr, *sigEl = nullptr, *Gth = nullptr, *Gtl = nullptr, *Gch = nullptr, *Gcl = nullptr;
+  int ldx = 0;
+};
 int launch_prep_mixed(int n, int np, const double2* H0, const float2* sig32, const double2* dH, int dH_mode,
                       double U, int h_part, float* Hth, float* Htl, float* BSh, float* BSl, const double2* Sm1,
                       const RhsDev<float>& d, const float2* psih, const float2* psil, int64_t ldpsi, float2* sigC,
-                      float2* G, int64_t plane, cudaStream_t s, float* sigEh = nullptr, float* sigEl = nullptr,
-                      int ldx = 0);
+                      float2* G, int64_t plane, cudaStream_t s, const TcxOperands& op = TcxOperands());
 // Lead currents in FP64 from the FP64 state: J_a = 2 Re sum_{m in a} sum_k psi[m][C_a[k]] IXI[m][k] / hbar^2
 // row ranges per lead: sourced rows [s[a], s[a+1]), free rows [f[a], f[a+1])
 struct CurRows {

@@ -299,8 +299,10 @@ __device__ __forceinline__ void gathers_job(const RhsDev<T>& d, const typename c
                                             const typename cx<T>::t* __restrict__ psi_lo, int64_t ldpsi,
                                             typename cx<T>::t* __restrict__ sigC, typename cx<T>::t* __restrict__ G,
                                             int64_t plane, int64_t first, int64_t stride,
-                                            float* __restrict__ sigEh = nullptr, float* __restrict__ sigEl = nullptr,
-                                            int ldx = 0) {
+                                            const TcxOperands op = TcxOperands()) {
+  float* __restrict__ sigEh = op.sigEh;
+  float* __restrict__ sigEl = op.sigEl;
+  const int ldx = op.ldx;
   const int64_t ns = (int64_t)d.L * d.n * d.nc;
   const int64_t ng = (int64_t)d.N * d.L * d.nc;
   for (int64_t e = first; e < ns + ng; e += stride) {
@@ -343,6 +345,18 @@ __device__ __forceinline__ void gathers_job(const RhsDev<T>& d, const typename c
         if (psi_lo) {
           const T* pl = reinterpret_cast<const T*>(psi_lo);
           v = cadd(v, cx<T>::make(pl[o], pl[o + plane]));
+          if (op.Gth) {
+            // the Omega sources on the tensor cores: A rows (psi on lead a's
+            // columns) and the embedded conjugate B' rows (Re, Im) / (-Im, Re),
+            // from the TF32 hi/lo parts of psi as they are
+            const float hr = (float)ph[o], hi = (float)ph[o + plane], lr = (float)pl[o], li = (float)pl[o + plane];
+            const int64_t ot = ((int64_t)a * d.N + m) * ldx + 2 * k;
+            op.Gth[ot] = hr; op.Gth[ot + 1] = hi;
+            op.Gtl[ot] = lr; op.Gtl[ot + 1] = li;
+            const int64_t oc = ((int64_t)a * 2 * d.N + 2 * m) * ldx + 2 * k, oc1 = oc + ldx;
+            op.Gch[oc] = hr; op.Gch[oc + 1] = hi; op.Gch[oc1] = -hi; op.Gch[oc1 + 1] = hr;
+            op.Gcl[oc] = lr; op.Gcl[oc + 1] = li; op.Gcl[oc1] = -li; op.Gcl[oc1 + 1] = lr;
+          }
         }
       } else {
         v = psi[o];
@@ -1277,22 +1291,21 @@ __global__ void __launch_bounds__(256) k_prep_mixed(int n, int np, int nb, const
                                                     const RhsDev<float> d, const float2* __restrict__ psih,
                                                     const float2* __restrict__ psil, int64_t ldpsi,
                                                     float2* __restrict__ sigC, float2* __restrict__ G,
-                                                    int64_t plane, float* __restrict__ sigEh,
-                                                    float* __restrict__ sigEl, int ldx) {
+                                                    int64_t plane, const TcxOperands op) {
   const int ntb = nb * nb;
   if ((int)blockIdx.x < ntb) {
     operands_tile<HP>(blockIdx.x % nb, blockIdx.x / nb, n, np, H0, sig32, dH, dH_mode, U, Hth, Htl, BSh, BSl, Sm1);
   } else {
     const int tid = threadIdx.y * 32 + threadIdx.x;
     gathers_job<float>(d, sig32, psih, psil, ldpsi, sigC, G, plane, (int64_t)(blockIdx.x - ntb) * 256 + tid,
-                       (int64_t)(gridDim.x - ntb) * 256, sigEh, sigEl, ldx);
+                       (int64_t)(gridDim.x - ntb) * 256, op);
   }
 }
 
 int launch_prep_mixed(int n, int np, const double2* H0, const float2* sig32, const double2* dH, int dH_mode,
                       double U, int h_part, float* Hth, float* Htl, float* BSh, float* BSl, const double2* Sm1,
                       const RhsDev<float>& d, const float2* psih, const float2* psil, int64_t ldpsi, float2* sigC,
-                      float2* G, int64_t plane, cudaStream_t s, float* sigEh, float* sigEl, int ldx) {
+                      float2* G, int64_t plane, cudaStream_t s, const TcxOperands& op) {
   ZG_REQUIRE(h_part >= 0 && h_part <= 2, "bad operand part %d", h_part);
   ZG_REQUIRE(!(Sm1 && dH_mode == ZG_DH_HUBBARD && h_part == 1), "the overlap's Hubbard term changes every entry");
   const int nb = (np + 31) / 32;
@@ -1301,13 +1314,13 @@ int launch_prep_mixed(int n, int np, const double2* H0, const float2* sig32, con
   const dim3 grid(nb * nb + gb), block(32, 8);
   if (h_part == 0)
     k_prep_mixed<0><<<grid, block, 0, s>>>(n, np, nb, H0, sig32, dH, dH_mode, U, Hth, Htl, BSh, BSl, Sm1, d, psih,
-                                           psil, ldpsi, sigC, G, plane, sigEh, sigEl, ldx);
+                                           psil, ldpsi, sigC, G, plane, op);
   else if (h_part == 1)
     k_prep_mixed<1><<<grid, block, 0, s>>>(n, np, nb, H0, sig32, dH, dH_mode, U, Hth, Htl, BSh, BSl, Sm1, d, psih,
-                                           psil, ldpsi, sigC, G, plane, sigEh, sigEl, ldx);
+                                           psil, ldpsi, sigC, G, plane, op);
   else
     k_prep_mixed<2><<<grid, block, 0, s>>>(n, np, nb, H0, sig32, dH, dH_mode, U, Hth, Htl, BSh, BSl, Sm1, d, psih,
-                                           psil, ldpsi, sigC, G, plane, sigEh, sigEl, ldx);
+                                           psil, ldpsi, sigC, G, plane, op);
   ZG_CHECK_LAUNCH();
   count_launch();
   return ZG_OK;

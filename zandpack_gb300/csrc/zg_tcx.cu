@@ -162,10 +162,15 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
           const uint32_t st = sbase + s * C::STAGE_BYTES;
           const uint32_t fb = bar_full + 8 * s;
           const int kx = (kb0 + q) * 32;  // K float offset inside the problem
-          const int bytes_a = P.amode == 0 ? 2 * C::A_BYTES : P.amode == 1 ? C::A_BYTES : C::RAW_BYTES;
+          const bool seg2 = kx >= P.kseg;
+          const int bytes_a = P.amode == 0 || seg2 ? 2 * C::A_BYTES : P.amode == 1 ? C::A_BYTES : C::RAW_BYTES;
           mbar_expect_tx(fb, bytes_a + 2 * C::B_BYTES);
-          const CUtensorMap* mA = &batch.maps[P.mapA];
-          if (P.amode == 0) {
+          const CUtensorMap* mA = &batch.maps[seg2 ? P.mapA2 : P.mapA];
+          if (seg2) {
+            const int k2 = kx - P.kseg;
+            tma_load_2d(st, mA, fb, k2, P.a_row0_2 + it.tm * 128);
+            tma_load_2d(st + C::OFF_AL, mA + 1, fb, k2, P.a_row0_2 + it.tm * 128);
+          } else if (P.amode == 0) {
             tma_load_2d(st, mA, fb, P.a_k0 + kx, P.a_row0 + it.tm * 128);
             tma_load_2d(st + C::OFF_AL, mA + 1, fb, P.a_k0 + kx, P.a_row0 + it.tm * 128);
           } else if (P.amode == 1) {
@@ -179,9 +184,11 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
             tma_load_2d(rb + 16384, mA + 1, fb, x, mode);
             tma_load_2d(rb + 24576, mA + 1, fb, x, P.a_plane + mode);
           }
-          const CUtensorMap* mB = &batch.maps[P.mapB];
-          tma_load_2d(st + C::OFF_BH, mB, fb, P.b_k0 + kx, P.b_row0 + it.tn * BN);
-          tma_load_2d(st + C::OFF_BL, mB + 1, fb, P.b_k0 + kx, P.b_row0 + it.tn * BN);
+          const CUtensorMap* mB = &batch.maps[seg2 ? P.mapB2 : P.mapB];
+          const int bx = seg2 ? kx - P.kseg : P.b_k0 + kx;
+          const int by = (seg2 ? P.b_row0_2 : P.b_row0) + it.tn * BN;
+          tma_load_2d(st + C::OFF_BH, mB, fb, bx, by);
+          tma_load_2d(st + C::OFF_BL, mB + 1, fb, bx, by);
           issued[s] = kb_global / STAGES + 1;
         }
       }
@@ -246,7 +253,8 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
         ok = __all_sync(0xffffffffu, mbar_wait(bar_full + 8 * s, (uint32_t)(kb_global / STAGES) & 1u, err, 13));
         if (!ok) break;
         uint8_t* st = smem + s * C::STAGE_BYTES;
-        if (P.amode == 1) {
+        const int amode = (kb0 + q) * 32 >= P.kseg ? 0 : P.amode;
+        if (amode == 1) {
           // split in place: A hi overwrites the raw tile, A lo goes to its own tile
           float4* ah = reinterpret_cast<float4*>(st);
           float4* al = reinterpret_cast<float4*>(st + C::OFF_AL);
@@ -262,7 +270,7 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
             ah[c] = h;
             al[c] = l;
           }
-        } else if (P.amode == 2) {
+        } else if (amode == 2) {
           // row ct of A' (orbital ct of the tile): modes 0..15 as (re, im) pairs,
           // 128-byte rows in the SWIZZLE_128B pattern (16-byte chunk c of row r
           // at chunk c ^ (r % 8))
@@ -323,6 +331,32 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
       // ---- epilogue of the item
       const int row = it.tm * 128 + row_in_tile;
       const int col0 = it.tn * BN + part * C::DCOLS;
+      if (P.epi == 1) {
+        // the Omega derivative (Zandpack/mpi/zand:782-809; the diagonal term
+        // is Zandpack/mpi_funcs.py:91-102): h (sources) + (i h/hbar)(X+ - X-) Omega
+        if (row < P.M) {
+          const StageParams* pp = batch.params;
+          const float h = pp->fh, sc = pp->fh_hb;
+          const int m = P.row_mode0 + row;
+          float2 xp = batch.Xp[m];
+          xp.x += pp->fdelta[P.la];
+          const float db = pp->fdelta[P.lb];
+          const float2* in = P.om_in + (long long)row * P.ld_om;
+          float2* out = batch.om_out_base + P.om_out_off + (long long)row * P.ld_om;
+#pragma unroll
+          for (int c2 = 0; c2 < C::DCOLS / 2; ++c2) {
+            const int col = (col0 >> 1) + c2;
+            if (2 * col >= P.Nv) continue;
+            float2 xm = batch.Xm[P.col_mode0 + col];
+            xm.x += db;
+            const float2 dx = make_float2(xp.x - xm.x, xp.y - xm.y);
+            const float2 om = in[col];
+            const float2 dd = make_float2(dx.x * om.x - dx.y * om.y, dx.x * om.y + dx.y * om.x);
+            out[col] = make_float2(acc[2 * c2] * h - sc * dd.y, acc[2 * c2 + 1] * h + sc * dd.x);
+          }
+        }
+        continue;
+      }
       if (P.nsplit == 1) {
         if (row < P.M) {
           float* dst = P.D + (long long)row * P.ldd + col0;

@@ -24,6 +24,18 @@ struct TcxProb {
   long long ldd;
   float* ws;          // split-K partial tiles (nsplit > 1): [tile][split][128][BN]
   int* counters;      // one per 32-row slice of a tile and drain warp, zero between launches
+  // a second operand pair for the K floats from kseg on (form 0 only):
+  // A from map mapA2 at row a_row0_2, B' from map mapB2 at row b_row0_2,
+  // both from K float 0
+  int kseg, mapA2, mapB2, a_row0_2, b_row0_2;
+  // epi 1: the Omega derivative of a block of Omega instead of a plain store:
+  // out = h D + (i h/hbar)(X+_m + delta_la - X-_l - delta_lb) Omega_in, with
+  // D = the source terms, row m = row_mode0 + row, column l = col_mode0 + col
+  // (complex columns), Omega_in at om_in and out at om_out_base + om_out_off,
+  // both with row stride ld_om complex
+  int epi, ld_om, row_mode0, col_mode0, la, lb;
+  const float2* om_in;
+  long long om_out_off;
 };
 
 #define ZG_TCX_ITEMS 3072
@@ -38,6 +50,11 @@ struct TcxBatch {
   unsigned short cta_off[ZG_TCX_GRID + 1];
   int nprob, nitems, bn;
   int* err;
+  // epilogue 1: stage parameters, X+ and X- of the modes (complex64), output base
+  const StageParams* params;
+  const float2* Xp;
+  const float2* Xm;
+  float2* om_out_base;
 };
 
 // BN of the kernel for products with `ncols` real output columns per tile
