@@ -591,16 +591,16 @@ static int build_tcx(zg_traj* t, const zg_layout* Lo) {
   ZG_CHECK_CUDA(cudaMemsetAsync(t->ZB32, 0, L * std::max<int64_t>(Ns, 1) * nc * sizeof(float2), s));
   // ---- tensor maps
   CUtensorMap* mp = B->maps;
-  ZG_TRY(make_tmap_f32_box(&mp[0], psih, 2 * N, np, np, 16, 128, false));
-  ZG_TRY(make_tmap_f32_box(&mp[1], psil, 2 * N, np, np, 16, 128, false));
-  ZG_TRY(make_tmap_f32_box(&mp[2], omA, N, 2 * Ns, 2 * Ns, 128, 32, true));
-  if (Nf > 0) ZG_TRY(make_tmap_f32_box(&mp[3], omB, Ns, 2 * Nf, 2 * Nf, 128, 32, true));
-  ZG_TRY(make_tmap_f32_box(&mp[4], t->XIh, N, 2 * nc, ldx, 128, 32, true));
-  ZG_TRY(make_tmap_f32_box(&mp[5], t->XIl, N, 2 * nc, ldx, 128, 32, true));
-  ZG_TRY(make_tmap_f32_box(&mp[6], t->tcxBh, bn, kstack, kstack, bn, 32, true));
-  ZG_TRY(make_tmap_f32_box(&mp[7], t->tcxBl, bn, kstack, kstack, bn, 32, true));
-  ZG_TRY(make_tmap_f32_box(&mp[8], t->sigEh, L * 2 * n, 2 * nc, ldx, bn, 32, true));
-  ZG_TRY(make_tmap_f32_box(&mp[9], t->sigEl, L * 2 * n, 2 * nc, ldx, bn, 32, true));
+  ZG_TRY(tcx_map(*B, 0, psih, 2 * N, np, np, 16, 128, false));
+  ZG_TRY(tcx_map(*B, 1, psil, 2 * N, np, np, 16, 128, false));
+  ZG_TRY(tcx_map(*B, 2, omA, N, 2 * Ns, 2 * Ns, 128, 32, true));
+  if (Nf > 0) ZG_TRY(tcx_map(*B, 3, omB, Ns, 2 * Nf, 2 * Nf, 128, 32, true));
+  ZG_TRY(tcx_map(*B, 4, t->XIh, N, 2 * nc, ldx, 128, 32, true));
+  ZG_TRY(tcx_map(*B, 5, t->XIl, N, 2 * nc, ldx, 128, 32, true));
+  ZG_TRY(tcx_map(*B, 6, t->tcxBh, bn, kstack, kstack, bn, 32, true));
+  ZG_TRY(tcx_map(*B, 7, t->tcxBl, bn, kstack, kstack, bn, 32, true));
+  ZG_TRY(tcx_map(*B, 8, t->sigEh, L * 2 * n, 2 * nc, ldx, bn, 32, true));
+  ZG_TRY(tcx_map(*B, 9, t->sigEl, L * 2 * n, 2 * nc, ldx, bn, 32, true));
   // ---- problems (K chunks set below, once the total work is known)
   std::vector<TcxProb> probs;
   for (const Blk& b : blk) {
@@ -611,6 +611,7 @@ static int build_tcx(zg_traj* t, const zg_layout* Lo) {
     P.b_k0 = (int)b.koff;
     P.a_k0 = (int)(2 * b.q0);
     P.K = (int)(2 * (b.q1 - b.q0));
+    P.kseg = P.K;  // one operand pair
     P.Nv = (int)(2 * nc);
     P.ldd = 2 * nc;
     P.tiles_n = 1;
@@ -637,6 +638,7 @@ static int build_tcx(zg_traj* t, const zg_layout* Lo) {
     P.b_row0 = (int)(a * 2 * n); P.b_k0 = 0;
     P.M = (int)(r1 - r0); P.Nv = (int)(2 * n);
     P.K = ldx;
+    P.kseg = P.K;
     P.tiles_m = (P.M + 127) / 128;
     P.tiles_n = (int)((2 * n + bn - 1) / bn);
     P.D = (float*)(t->R2_32 + r0 * n);
@@ -709,6 +711,7 @@ static int build_tcx(zg_traj* t, const zg_layout* Lo) {
   B->nitems = nitems;
   B->bn = bn;
   B->err = t->tc_err;
+  ZG_TRY(tcx_validate(*B));
   t->tcx_grid = used;
   t->tcx = B.release();
   t->tcx_on = true;
@@ -762,14 +765,14 @@ static int build_omega_tc(zg_traj* t, const std::vector<double2>& U, const std::
   std::unique_ptr<TcxBatch> B(new TcxBatch());
   memset(B.get(), 0, sizeof(TcxBatch));
   CUtensorMap* mp = B->maps;
-  ZG_TRY(make_tmap_f32_box(&mp[0], t->Gth, L * N, 2 * nc, ldx, 128, 32, true));
-  ZG_TRY(make_tmap_f32_box(&mp[1], t->Gtl, L * N, 2 * nc, ldx, 128, 32, true));
-  ZG_TRY(make_tmap_f32_box(&mp[2], t->Uh, 2 * N, 2 * nc, ldx, bn, 32, true));
-  ZG_TRY(make_tmap_f32_box(&mp[3], t->Ul, 2 * N, 2 * nc, ldx, bn, 32, true));
-  ZG_TRY(make_tmap_f32_box(&mp[4], t->Vh, N, 2 * nc, ldx, 128, 32, true));
-  ZG_TRY(make_tmap_f32_box(&mp[5], t->Vl, N, 2 * nc, ldx, 128, 32, true));
-  ZG_TRY(make_tmap_f32_box(&mp[6], t->Gch, L * 2 * N, 2 * nc, ldx, bn, 32, true));
-  ZG_TRY(make_tmap_f32_box(&mp[7], t->Gcl, L * 2 * N, 2 * nc, ldx, bn, 32, true));
+  ZG_TRY(tcx_map(*B, 0, t->Gth, L * N, 2 * nc, ldx, 128, 32, true));
+  ZG_TRY(tcx_map(*B, 1, t->Gtl, L * N, 2 * nc, ldx, 128, 32, true));
+  ZG_TRY(tcx_map(*B, 2, t->Uh, 2 * N, 2 * nc, ldx, bn, 32, true));
+  ZG_TRY(tcx_map(*B, 3, t->Ul, 2 * N, 2 * nc, ldx, bn, 32, true));
+  ZG_TRY(tcx_map(*B, 4, t->Vh, N, 2 * nc, ldx, 128, 32, true));
+  ZG_TRY(tcx_map(*B, 5, t->Vl, N, 2 * nc, ldx, 128, 32, true));
+  ZG_TRY(tcx_map(*B, 6, t->Gch, L * 2 * N, 2 * nc, ldx, bn, 32, true));
+  ZG_TRY(tcx_map(*B, 7, t->Gcl, L * 2 * N, 2 * nc, ldx, bn, 32, true));
   const float2* omA = t->stage32 + t->ml.st_om;
   const float2* omB = omA + N * Ns;
   std::vector<TcxProb> probs;
@@ -845,6 +848,7 @@ static int build_omega_tc(zg_traj* t, const std::vector<double2>& U, const std::
   B->params = t->d_params;
   B->Xp = t->Xp32;
   B->Xm = t->Xm32;
+  ZG_TRY(tcx_validate(*B));
   t->tco_grid = used;
   t->tco = B.release();
   t->tco_on = true;

@@ -442,6 +442,64 @@ static int launch_tcx_bn(const TcxBatch& b, int grid, cudaStream_t s) {
   return ZG_OK;
 }
 
+int tcx_map(TcxBatch& b, int i, const void* base, int64_t rows, int64_t cols, int64_t ld, int box_rows,
+            int box_cols, bool swizzle128) {
+  ZG_REQUIRE(i >= 0 && i < ZG_TCX_MAPS, "tensor map index %d", i);
+  ZG_TRY(make_tmap_f32_box(&b.maps[i], (const float*)base, rows, cols, ld, box_rows, box_cols, swizzle128));
+  b.box_cols[i] = box_cols;
+  b.box_rows[i] = box_rows;
+  return ZG_OK;
+}
+
+int tcx_validate(const TcxBatch& b) {
+  ZG_REQUIRE(b.nprob > 0 && b.nprob <= ZG_TCX_PROBS, "problem count %d", b.nprob);
+  ZG_REQUIRE(b.nitems > 0 && b.nitems <= ZG_TCX_ITEMS, "item count %d", b.nitems);
+  ZG_REQUIRE(tcx_bn_for(b.bn) == b.bn, "no kernel for BN %d", b.bn);
+  auto has = [&](int m, int cols, int rows) {
+    return m >= 0 && m + 1 < ZG_TCX_MAPS + 1 && b.box_cols[m] == cols && b.box_rows[m] == rows;
+  };
+  int items = 0;
+  for (int i = 0; i < b.nprob; ++i) {
+    const TcxProb& P = b.p[i];
+    ZG_REQUIRE(P.K > 0 && P.K % 32 == 0 && P.kseg >= 0 && P.kseg <= P.K && P.kseg % 32 == 0,
+               "problem %d: K %d, split point %d", i, P.K, P.kseg);
+    ZG_REQUIRE(P.kchunk > 0 && P.kchunk % 32 == 0 && P.nsplit == (P.K + P.kchunk - 1) / P.kchunk,
+               "problem %d: K chunk %d, %d splits", i, P.kchunk, P.nsplit);
+    ZG_REQUIRE(P.tiles_m > 0 && P.tiles_n > 0 && P.M > 0 && P.M <= 128 * P.tiles_m && P.Nv > 0 &&
+                   P.Nv <= b.bn * P.tiles_n,
+               "problem %d: tiles", i);
+    ZG_REQUIRE(P.item_begin == items, "problem %d: item range", i);
+    items += P.tiles_m * P.tiles_n * P.nsplit;
+    if (P.kseg > 0) {
+      if (P.amode == 2)
+        ZG_REQUIRE(has(P.mapA, 128, 16) && has(P.mapA + 1, 128, 16), "problem %d: planar A maps", i);
+      else if (P.amode == 1)
+        ZG_REQUIRE(has(P.mapA, 32, 128), "problem %d: raw A map", i);
+      else
+        ZG_REQUIRE(P.amode == 0 && has(P.mapA, 32, 128) && has(P.mapA + 1, 32, 128), "problem %d: A maps", i);
+      ZG_REQUIRE(has(P.mapB, 32, b.bn) && has(P.mapB + 1, 32, b.bn), "problem %d: B maps", i);
+      ZG_REQUIRE(P.a_k0 % 32 == 0 && P.b_k0 % 32 == 0, "problem %d: K offsets", i);
+    }
+    if (P.kseg < P.K) {
+      ZG_REQUIRE(has(P.mapA2, 32, 128) && has(P.mapA2 + 1, 32, 128), "problem %d: second A maps", i);
+      ZG_REQUIRE(has(P.mapB2, 32, b.bn) && has(P.mapB2 + 1, 32, b.bn), "problem %d: second B maps", i);
+    }
+    if (P.epi == 1) {
+      ZG_REQUIRE(P.nsplit == 1 && P.om_in && b.params && b.Xp && b.Xm && P.ld_om > 0, "problem %d: Omega epilogue", i);
+    } else {
+      ZG_REQUIRE(P.D && P.ldd >= P.Nv, "problem %d: output", i);
+      ZG_REQUIRE(P.nsplit == 1 || (P.ws && P.counters), "problem %d: split-K scratch", i);
+    }
+  }
+  ZG_REQUIRE(items == b.nitems, "item total %d, table %d", items, b.nitems);
+  ZG_REQUIRE(b.cta_off[0] == 0, "item lists");
+  int c = 0;
+  while (c < ZG_TCX_GRID && b.cta_off[c + 1] > b.cta_off[c]) ++c;
+  ZG_REQUIRE(b.cta_off[c] == b.nitems, "item lists cover %d of %d items", (int)b.cta_off[c], b.nitems);
+  for (int w = 0; w < b.nitems; ++w) ZG_REQUIRE(b.items[w] < b.nitems, "item %d", w);
+  return ZG_OK;
+}
+
 int tcx_bn_for(int ncols) {
   if (ncols <= 32) return 32;
   if (ncols <= 64) return 64;

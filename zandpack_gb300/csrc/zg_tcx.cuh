@@ -55,6 +55,8 @@ struct TcxBatch {
   const float2* Xp;
   const float2* Xm;
   float2* om_out_base;
+  // box of each tensor map (columns x rows; 0: map not set), for tcx_validate
+  int box_cols[ZG_TCX_MAPS], box_rows[ZG_TCX_MAPS];
 };
 
 // BN of the kernel for products with `ncols` real output columns per tile
@@ -63,6 +65,15 @@ int tcx_bn_for(int ncols);
 // number of drain warps of the BN kernel (counters per tile)
 inline int tcx_ndw(int bn) { return 4 * (bn / (bn % 64 == 0 ? 64 : 32)); }
 int tcx_launch(const TcxBatch& b, int grid, cudaStream_t s);
+// tensor map `i` of a batch over a rows x cols fp32 array (row stride ld),
+// with its box recorded for tcx_validate
+int tcx_map(TcxBatch& b, int i, const void* base, int64_t rows, int64_t cols, int64_t ld, int box_rows,
+            int box_cols, bool swizzle128);
+// host checks before any launch: every map a problem reads is set and has the
+// box the kernel expects for its role (so the expected transaction bytes
+// match the copies), K split points and chunks are whole K blocks, split-K
+// problems have their scratch, and the item lists are consistent
+int tcx_validate(const TcxBatch& b);
 // rows x cols fp32 row-major (row stride ld floats); box = box_cols x box_rows;
 // swizzle128: the 128-byte swizzle of a 32-float K-major row, else no swizzle
 int make_tmap_f32_box(CUtensorMap* map, const float* base, int64_t rows, int64_t cols, int64_t ld, int box_rows,
