@@ -224,12 +224,10 @@ struct zg_traj {
   bool tcx_on = false;
   TcxBatch* tcx = nullptr;
   TcxOperands tcx_ops;
-  // the Omega derivative on the tensor cores (epilogue 1 of zg_tcx.cu): its
-  // problem table, the constant operands U' (embedded) and V (TF32 hi/lo), and
-  // the per-stage psi gathers Gt (A rows) and Gc (embedded conjugate B' rows)
+  // the Omega derivative in the same batch (epilogue 1 of zg_tcx.cu): the
+  // constant operands U' (embedded) and V (TF32 hi/lo), and the per-stage psi
+  // gathers Gt (A rows) and Gc (embedded conjugate B' rows)
   bool tco_on = false;
-  TcxBatch* tco = nullptr;
-  int tco_grid = 0;
   float *Uh = nullptr, *Ul = nullptr, *Vh = nullptr, *Vl = nullptr, *Gth = nullptr, *Gtl = nullptr, *Gch = nullptr,
         *Gcl = nullptr;
   int tcx_grid = 0, ldx = 0;
@@ -408,7 +406,6 @@ static void free_traj(zg_traj* t) {
                   t->Uh, t->Ul, t->Vh, t->Vl, t->Gth, t->Gtl, t->Gch, t->Gcl};
   for (void* p : ptrs) dfree(t, p);
   delete t->tcx;
-  delete t->tco;
   if (t->stream2) {
     cudaStreamSynchronize(t->stream2);
     cudaStreamDestroy(t->stream2);
@@ -510,7 +507,7 @@ static void to_f32(const double2* a, float2* b, size_t n) {
 // stacked along K.  Leaves t->tcx_on false (the SIMT batch then runs) when a
 // shape does not suit TMA (odd block widths, misaligned blocks) or the
 // coupling width exceeds the kernels.
-static int build_tcx(zg_traj* t, const zg_layout* Lo) {
+static int build_tcx(zg_traj* t, const zg_layout* Lo, const std::vector<double2>& U, const std::vector<double2>& V) {
   const int64_t n = t->n, N = t->N, Ns = t->Ns, Nf = t->Nf, L = t->L, nc = t->nc, np = t->np;
   const int bn = tcx_bn_for((int)(2 * nc));
   const MixedLayout& ml = t->ml;
@@ -645,6 +642,88 @@ static int build_tcx(zg_traj* t, const zg_layout* Lo) {
     P.ldd = 2 * n;
     probs.push_back(P);
   }
+  // ---- the Omega derivative: one problem per block of Omega (rows of one
+  // class and lead a, columns of lead b) in tiles of 128 rows x bn/2 complex
+  // columns.  Source terms (Zandpack/mpi/zand:784-801) as two K segments of
+  // n_c complex:
+  //   term 1 (OmA blocks): psi[m] on lead b's columns . U[l]   (U = dGM Ixi)
+  //   term 2 (sourced rows): V[m] . conj(psi[l] on lead a's columns)
+  // (A rows Gt[b][m] and V[m]; B' rows the embeddings of U and of conj psi),
+  // the diagonal term in the kernel's epilogue.
+  bool omega_tc = (int)probs.size() + 3 * L * L <= ZG_TCX_PROBS;
+  if (omega_tc) {
+    std::vector<float> Vf((size_t)N * ldx, 0.f), Uf((size_t)2 * N * ldx, 0.f);
+    for (int64_t m = 0; m < N; ++m)
+      for (int64_t k = 0; k < nc; ++k) {
+        const double2 v = V[m * nc + k], u = U[m * nc + k];
+        Vf[(size_t)m * ldx + 2 * k] = (float)v.x;
+        Vf[(size_t)m * ldx + 2 * k + 1] = (float)v.y;
+        Uf[(size_t)(2 * m) * ldx + 2 * k] = (float)u.x;
+        Uf[(size_t)(2 * m) * ldx + 2 * k + 1] = (float)-u.y;
+        Uf[(size_t)(2 * m + 1) * ldx + 2 * k] = (float)u.y;
+        Uf[(size_t)(2 * m + 1) * ldx + 2 * k + 1] = (float)u.x;
+      }
+    ZG_TRY(dalloc(t, &t->Vh, Vf.size()));
+    ZG_TRY(dalloc(t, &t->Vl, Vf.size()));
+    ZG_TRY(dalloc(t, &t->Uh, Uf.size()));
+    ZG_TRY(dalloc(t, &t->Ul, Uf.size()));
+    ZG_CHECK_CUDA(cudaMemcpyAsync(t->Vl, Vf.data(), Vf.size() * sizeof(float), cudaMemcpyHostToDevice, s));
+    ZG_CHECK_CUDA(cudaMemcpyAsync(t->Ul, Uf.data(), Uf.size() * sizeof(float), cudaMemcpyHostToDevice, s));
+    ZG_TRY(launch_split_tf32(t->Vl, t->Vh, t->Vl, (int64_t)Vf.size(), s));
+    ZG_TRY(launch_split_tf32(t->Ul, t->Uh, t->Ul, (int64_t)Uf.size(), s));
+    const int64_t ng = L * N * ldx, nG = L * 2 * N * ldx;
+    ZG_TRY(dalloc(t, &t->Gth, ng));
+    ZG_TRY(dalloc(t, &t->Gtl, ng));
+    ZG_TRY(dalloc(t, &t->Gch, nG));
+    ZG_TRY(dalloc(t, &t->Gcl, nG));
+    for (float* q : {t->Gth, t->Gtl}) ZG_CHECK_CUDA(cudaMemsetAsync(q, 0, ng * sizeof(float), s));
+    for (float* q : {t->Gch, t->Gcl}) ZG_CHECK_CUDA(cudaMemsetAsync(q, 0, nG * sizeof(float), s));
+    ZG_TRY(tcx_map(*B, 10, t->Gth, L * N, 2 * nc, ldx, 128, 32, true));
+    ZG_TRY(tcx_map(*B, 11, t->Gtl, L * N, 2 * nc, ldx, 128, 32, true));
+    ZG_TRY(tcx_map(*B, 12, t->Uh, 2 * N, 2 * nc, ldx, bn, 32, true));
+    ZG_TRY(tcx_map(*B, 13, t->Ul, 2 * N, 2 * nc, ldx, bn, 32, true));
+    ZG_TRY(tcx_map(*B, 14, t->Vh, N, 2 * nc, ldx, 128, 32, true));
+    ZG_TRY(tcx_map(*B, 15, t->Vl, N, 2 * nc, ldx, 128, 32, true));
+    ZG_TRY(tcx_map(*B, 16, t->Gch, L * 2 * N, 2 * nc, ldx, bn, 32, true));
+    ZG_TRY(tcx_map(*B, 17, t->Gcl, L * 2 * N, 2 * nc, ldx, bn, 32, true));
+    const float2* oA = t->stage32 + ml.st_om;
+    const float2* oB = oA + N * Ns;
+    // kind 0: OmA rows sourced of a (both terms); 1: OmA rows free of a (term 1);
+    // 2: OmB rows sourced of a, columns free of b (term 2)
+    for (int a = 0; a < L; ++a)
+      for (int b = 0; b < L; ++b)
+        for (int kind = 0; kind < 3; ++kind) {
+          const int64_t r0 = kind == 1 ? t->f_start[a] : t->s_start[a];
+          const int64_t r1 = kind == 1 ? t->f_start[a + 1] : t->s_start[a + 1];
+          const int64_t c0 = kind == 2 ? t->f_start[b] : t->s_start[b];
+          const int64_t c1 = kind == 2 ? t->f_start[b + 1] : t->s_start[b + 1];
+          if (r1 <= r0 || c1 <= c0) continue;
+          TcxProb P;
+          memset(&P, 0, sizeof(P));
+          P.amode = 0;
+          P.epi = 1;
+          P.M = (int)(r1 - r0);
+          P.Nv = (int)(2 * (c1 - c0));
+          P.tiles_m = (int)((r1 - r0 + 127) / 128);
+          P.tiles_n = (int)((2 * (c1 - c0) + bn - 1) / bn);
+          P.mapA = 10; P.a_row0 = (int)(b * N + r0); P.a_k0 = 0;  // term 1: Gt[b][m]
+          P.mapB = 12; P.b_row0 = (int)(2 * c0); P.b_k0 = 0;       // U' rows 2l
+          P.mapA2 = 14; P.a_row0_2 = (int)r0;                      // term 2: V[m]
+          P.mapB2 = 16; P.b_row0_2 = (int)(a * 2 * N + 2 * c0);    // Gc[a] rows 2l
+          if (kind == 0) { P.kseg = ldx; P.K = 2 * ldx; }
+          else if (kind == 1) { P.kseg = ldx; P.K = ldx; }
+          else { P.kseg = 0; P.K = ldx; }
+          P.ld_om = (int)(kind == 2 ? Nf : Ns);
+          const int64_t lc0 = kind == 2 ? c0 - Ns : c0;  // local column in OmA / OmB
+          P.om_in = (kind == 2 ? oB : oA) + r0 * P.ld_om + lc0;
+          P.om_out_off = (kind == 2 ? t->off_omB : t->off_omA) + r0 * P.ld_om + lc0;
+          P.row_mode0 = (int)r0;
+          P.col_mode0 = (int)c0;
+          P.la = a;
+          P.lb = b;
+          probs.push_back(P);
+        }
+  }
   int sms = 0;
   ZG_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, t->dev));
   const int grid = std::max(1, std::min(sms, ZG_TCX_GRID));
@@ -658,13 +737,14 @@ static int build_tcx(zg_traj* t, const zg_layout* Lo) {
     int items = 0;
     item_kb.clear();
     for (TcxProb& P : probs) {
-      P.kchunk = std::min(P.K, 32 * chunk_kb);
+      P.kchunk = P.epi == 1 ? P.K : std::min(P.K, 32 * chunk_kb);  // Omega blocks: whole K per tile
       P.nsplit = (P.K + P.kchunk - 1) / P.kchunk;
       P.item_begin = items;
       items += P.tiles_m * P.tiles_n * P.nsplit;
       for (int w = 0; w < P.tiles_m * P.tiles_n * P.nsplit; ++w) {
         const int split = w % P.nsplit;
-        item_kb.push_back(std::min(P.kchunk, P.K - split * P.kchunk) / 32);
+        // an Omega tile also moves its block of Omega in and out (about two K blocks)
+        item_kb.push_back(std::min(P.kchunk, P.K - split * P.kchunk) / 32 + (P.epi == 1 ? 2 : 0));
       }
     }
     if (items <= ZG_TCX_ITEMS) break;
@@ -693,6 +773,11 @@ static int build_tcx(zg_traj* t, const zg_layout* Lo) {
   int64_t ws_need = 0, cnt_need = 0;
   std::vector<int64_t> ws_off, cnt_off;
   for (const TcxProb& P : probs) {
+    if (P.epi == 1) {
+      ws_off.push_back(-1);
+      cnt_off.push_back(0);
+      continue;
+    }
     ws_off.push_back(P.nsplit > 1 ? ws_need : -1);
     if (P.nsplit > 1) ws_need += (int64_t)P.tiles_m * P.tiles_n * P.nsplit * 128 * bn;
     cnt_off.push_back(cnt_need);
@@ -705,8 +790,11 @@ static int build_tcx(zg_traj* t, const zg_layout* Lo) {
   for (int i = 0; i < np_; ++i) {
     B->p[i] = probs[i];
     B->p[i].ws = ws_off[i] >= 0 ? t->tcx_ws + ws_off[i] : nullptr;
-    B->p[i].counters = t->tcx_cnt + cnt_off[i];
+    B->p[i].counters = probs[i].epi == 1 ? nullptr : t->tcx_cnt + cnt_off[i];
   }
+  B->params = t->d_params;
+  B->Xp = t->Xp32;
+  B->Xm = t->Xm32;
   B->nprob = np_;
   B->nitems = nitems;
   B->bn = bn;
@@ -718,144 +806,13 @@ static int build_tcx(zg_traj* t, const zg_layout* Lo) {
   t->tcx_ops.sigEh = t->sigEh;
   t->tcx_ops.sigEl = t->sigEl;
   t->tcx_ops.ldx = ldx;
-  return ZG_OK;
-}
-
-// The Omega derivative on the tensor cores: one problem per block of Omega
-// (rows of one class and lead a, columns of lead b), 128 x 64 complex tiles.
-// Source terms (Zandpack/mpi/zand:784-801) as two K segments of n_c complex:
-//   term 1 (OmA blocks): psi[m] on lead b's columns . U[l]   (U = dGM Ixi)
-//   term 2 (sourced rows): V[m] . conj(psi[l] on lead a's columns)
-// (A rows Gt[b][m] and V[m]; B' rows the embeddings of U and of conj psi),
-// then the diagonal term in the epilogue.  Needs the products' layout checks
-// (build_tcx) to have passed.
-static int build_omega_tc(zg_traj* t, const std::vector<double2>& U, const std::vector<double2>& V) {
-  if (!t->tcx_on) return ZG_OK;
-  const int64_t N = t->N, Ns = t->Ns, Nf = t->Nf, L = t->L, nc = t->nc;
-  const int ldx = t->ldx;
-  const int bn = 128;  // 64 complex columns per tile
-  cudaStream_t s = t->stream;
-  // constants: V (A of term 2) interleaved, U' (B' of term 1) embedded
-  std::vector<float> Vf((size_t)N * ldx, 0.f), Uf((size_t)2 * N * ldx, 0.f);
-  for (int64_t m = 0; m < N; ++m)
-    for (int64_t k = 0; k < nc; ++k) {
-      const double2 v = V[m * nc + k], u = U[m * nc + k];
-      Vf[(size_t)m * ldx + 2 * k] = (float)v.x;
-      Vf[(size_t)m * ldx + 2 * k + 1] = (float)v.y;
-      Uf[(size_t)(2 * m) * ldx + 2 * k] = (float)u.x;
-      Uf[(size_t)(2 * m) * ldx + 2 * k + 1] = (float)-u.y;
-      Uf[(size_t)(2 * m + 1) * ldx + 2 * k] = (float)u.y;
-      Uf[(size_t)(2 * m + 1) * ldx + 2 * k + 1] = (float)u.x;
-    }
-  ZG_TRY(dalloc(t, &t->Vh, Vf.size()));
-  ZG_TRY(dalloc(t, &t->Vl, Vf.size()));
-  ZG_TRY(dalloc(t, &t->Uh, Uf.size()));
-  ZG_TRY(dalloc(t, &t->Ul, Uf.size()));
-  ZG_CHECK_CUDA(cudaMemcpyAsync(t->Vl, Vf.data(), Vf.size() * sizeof(float), cudaMemcpyHostToDevice, s));
-  ZG_CHECK_CUDA(cudaMemcpyAsync(t->Ul, Uf.data(), Uf.size() * sizeof(float), cudaMemcpyHostToDevice, s));
-  ZG_TRY(launch_split_tf32(t->Vl, t->Vh, t->Vl, (int64_t)Vf.size(), s));
-  ZG_TRY(launch_split_tf32(t->Ul, t->Uh, t->Ul, (int64_t)Uf.size(), s));
-  const int64_t ng = L * N * ldx, nG = L * 2 * N * ldx;
-  ZG_TRY(dalloc(t, &t->Gth, ng));
-  ZG_TRY(dalloc(t, &t->Gtl, ng));
-  ZG_TRY(dalloc(t, &t->Gch, nG));
-  ZG_TRY(dalloc(t, &t->Gcl, nG));
-  for (float* q : {t->Gth, t->Gtl}) ZG_CHECK_CUDA(cudaMemsetAsync(q, 0, ng * sizeof(float), s));
-  for (float* q : {t->Gch, t->Gcl}) ZG_CHECK_CUDA(cudaMemsetAsync(q, 0, nG * sizeof(float), s));
-  std::unique_ptr<TcxBatch> B(new TcxBatch());
-  memset(B.get(), 0, sizeof(TcxBatch));
-  CUtensorMap* mp = B->maps;
-  ZG_TRY(tcx_map(*B, 0, t->Gth, L * N, 2 * nc, ldx, 128, 32, true));
-  ZG_TRY(tcx_map(*B, 1, t->Gtl, L * N, 2 * nc, ldx, 128, 32, true));
-  ZG_TRY(tcx_map(*B, 2, t->Uh, 2 * N, 2 * nc, ldx, bn, 32, true));
-  ZG_TRY(tcx_map(*B, 3, t->Ul, 2 * N, 2 * nc, ldx, bn, 32, true));
-  ZG_TRY(tcx_map(*B, 4, t->Vh, N, 2 * nc, ldx, 128, 32, true));
-  ZG_TRY(tcx_map(*B, 5, t->Vl, N, 2 * nc, ldx, 128, 32, true));
-  ZG_TRY(tcx_map(*B, 6, t->Gch, L * 2 * N, 2 * nc, ldx, bn, 32, true));
-  ZG_TRY(tcx_map(*B, 7, t->Gcl, L * 2 * N, 2 * nc, ldx, bn, 32, true));
-  const float2* omA = t->stage32 + t->ml.st_om;
-  const float2* omB = omA + N * Ns;
-  std::vector<TcxProb> probs;
-  // kind 0: OmA rows sourced of a (both terms); 1: OmA rows free of a (term 1);
-  // 2: OmB rows sourced of a, columns free of b (term 2)
-  for (int a = 0; a < L; ++a)
-    for (int b = 0; b < L; ++b)
-      for (int kind = 0; kind < 3; ++kind) {
-        const int64_t r0 = kind == 1 ? t->f_start[a] : t->s_start[a], r1 = kind == 1 ? t->f_start[a + 1] : t->s_start[a + 1];
-        const int64_t c0 = kind == 2 ? t->f_start[b] : t->s_start[b], c1 = kind == 2 ? t->f_start[b + 1] : t->s_start[b + 1];
-        if (r1 <= r0 || c1 <= c0) continue;
-        TcxProb P;
-        memset(&P, 0, sizeof(P));
-        P.amode = 0;
-        P.epi = 1;
-        P.M = (int)(r1 - r0);
-        P.Nv = (int)(2 * (c1 - c0));
-        P.tiles_m = (int)((r1 - r0 + 127) / 128);
-        P.tiles_n = (int)((2 * (c1 - c0) + bn - 1) / bn);
-        P.mapA = 0; P.a_row0 = (int)(b * N + r0); P.a_k0 = 0;   // term 1: Gt[b][m]
-        P.mapB = 2; P.b_row0 = (int)(2 * c0); P.b_k0 = 0;        // U' rows 2l
-        P.mapA2 = 4; P.a_row0_2 = (int)r0;                       // term 2: V[m]
-        P.mapB2 = 6; P.b_row0_2 = (int)(a * 2 * N + 2 * c0);     // Gc[a] rows 2l
-        if (kind == 0) { P.kseg = ldx; P.K = 2 * ldx; }
-        else if (kind == 1) { P.kseg = ldx; P.K = ldx; }
-        else { P.kseg = 0; P.K = ldx; }
-        P.kchunk = P.K;
-        P.nsplit = 1;
-        P.ld_om = (int)(kind == 2 ? Nf : Ns);
-        const int64_t lc0 = kind == 2 ? c0 - Ns : c0;  // local column in OmA / OmB
-        P.om_in = (kind == 2 ? omB : omA) + r0 * P.ld_om + lc0;
-        P.om_out_off = (kind == 2 ? t->off_omB : t->off_omA) + r0 * P.ld_om + lc0;
-        P.row_mode0 = (int)r0;
-        P.col_mode0 = (int)c0;
-        P.la = a;
-        P.lb = b;
-        probs.push_back(P);
-      }
-  if (probs.empty() || (int)probs.size() > ZG_TCX_PROBS) return ZG_OK;
-  int sms = 0;
-  ZG_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, t->dev));
-  const int grid = std::max(1, std::min(sms, ZG_TCX_GRID));
-  std::vector<int> item_kb;
-  int items = 0;
-  for (TcxProb& P : probs) {
-    P.item_begin = items;
-    items += P.tiles_m * P.tiles_n;
-    for (int w = 0; w < P.tiles_m * P.tiles_n; ++w) item_kb.push_back(P.K / 32 + 4);  // + the epilogue's Omega traffic
+  if (omega_tc) {
+    t->tco_on = true;
+    t->tcx_ops.Gth = t->Gth;
+    t->tcx_ops.Gtl = t->Gtl;
+    t->tcx_ops.Gch = t->Gch;
+    t->tcx_ops.Gcl = t->Gcl;
   }
-  if (items > ZG_TCX_ITEMS) return ZG_OK;
-  std::vector<int> order(items);
-  for (int i = 0; i < items; ++i) order[i] = i;
-  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return item_kb[x] > item_kb[y]; });
-  std::vector<int64_t> load(grid, 0);
-  std::vector<std::vector<int>> per(grid);
-  for (int w : order) {
-    int c = (int)(std::min_element(load.begin(), load.end()) - load.begin());
-    load[c] += item_kb[w];
-    per[c].push_back(w);
-  }
-  int used = 0, pos = 0;
-  for (int c = 0; c < grid; ++c) {
-    if (per[c].empty()) continue;
-    B->cta_off[used++] = (unsigned short)pos;
-    for (int w : per[c]) B->items[pos++] = (unsigned short)w;
-  }
-  B->cta_off[used] = (unsigned short)pos;
-  for (size_t i = 0; i < probs.size(); ++i) B->p[i] = probs[i];
-  B->nprob = (int)probs.size();
-  B->nitems = items;
-  B->bn = bn;
-  B->err = t->tc_err;
-  B->params = t->d_params;
-  B->Xp = t->Xp32;
-  B->Xm = t->Xm32;
-  ZG_TRY(tcx_validate(*B));
-  t->tco_grid = used;
-  t->tco = B.release();
-  t->tco_on = true;
-  t->tcx_ops.Gth = t->Gth;
-  t->tcx_ops.Gtl = t->Gtl;
-  t->tcx_ops.Gch = t->Gch;
-  t->tcx_ops.Gcl = t->Gcl;
   return ZG_OK;
 }
 
@@ -928,8 +885,7 @@ static int create_mixed(zg_traj* t, const zg_layout* Lo, const std::vector<doubl
   ZG_TRY(tc_gemm_prepare(t->gR1c, psih, psil, t->Hth, t->Htl, np, np, (float*)t->R1p, 2 * np, (int)(2 * N),
                          (int)(2 * np), (int)np, t->tc_err));
   if (getenv("ZG_SIMT_PRODUCTS") == nullptr) {
-    ZG_TRY(build_tcx(t, Lo));
-    ZG_TRY(build_omega_tc(t, U, V));
+    ZG_TRY(build_tcx(t, Lo, U, V));
   }
   ZG_CHECK_CUDA(cudaStreamSynchronize(s));
   return ZG_OK;
@@ -1455,14 +1411,9 @@ static int rhs_mixed(zg_traj* t, int stage, const StageParams* p, int dH_mode, d
     ZG_TRY(tc_gemm_launch(gT, s2));
     prof_end(t, ZG_PROF_GEMM2, s2);
     prof_begin(t, ZG_PROF_OMEGA, s2);
-    if (t->tco_on) {
-      t->tco->om_out_base = out;
-      t->tco->params = p;
-      ZG_TRY(tcx_launch(*t->tco, t->tco_grid, s2));
-    } else {
+    if (!t->tco_on)  // else the Omega derivative runs in the tensor-core batch below
       ZG_TRY(launch_omega<float>(d, p, t->tiles, t->ntiles, t->G32, omA, omB, out + t->off_omA, out + t->off_omB,
                                  s2));
-    }
     prof_end(t, ZG_PROF_OMEGA, s2);
     ZG_CHECK_CUDA(cudaEventRecord(t->ev_join, s2));
   }
@@ -1500,8 +1451,11 @@ static int rhs_mixed(zg_traj* t, int stage, const StageParams* p, int dH_mode, d
     return run_batches<float>(t, probs2, &t->ws32, &t->ws32_cap, s, true);
   }
   prof_begin(t, ZG_PROF_SMALL);
-  if (t->tcx_on)
+  if (t->tcx_on) {
+    t->tcx->om_out_base = out;
+    t->tcx->params = p;
     ZG_TRY(tcx_launch(*t->tcx, t->tcx_grid, s));
+  }
   else
     ZG_TRY(run_batches<float>(t, probs, &t->ws32, &t->ws32_cap, s, false));
   if (t->nonorth) {

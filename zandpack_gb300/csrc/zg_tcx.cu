@@ -53,11 +53,18 @@ struct TcxCfg {
                        OFF_BL = OFF_BH + B_BYTES;
   static constexpr int STAGE_BYTES = OFF_BL + B_BYTES;
   static constexpr int BAR_OFF = STAGES * STAGE_BYTES;
-  static constexpr int SMEM = BAR_OFF + 256 + 1024;
-  static constexpr int NACC = BN <= 128 ? 4 : 2;  // TMEM accumulator buffers of BN columns
+  static constexpr int NACC_ = BN <= 128 ? 4 : 2;
+  static constexpr int NDW_ = 4 * (BN / (BN % 64 == 0 ? 64 : 32));
+  // epilogue staging: per drain warp a 32-row x 16-float tile (rows padded to
+  // 20 floats), so that global loads and stores run along rows; kept when it fits
+  static constexpr int STG_OFF = BAR_OFF + 256;
+  static constexpr int STG_WARP_FLOATS = 32 * 20;
+  static constexpr bool STAGED = STG_OFF + NDW_ * STG_WARP_FLOATS * 4 + 1024 <= 232448;
+  static constexpr int SMEM = STG_OFF + (STAGED ? NDW_ * STG_WARP_FLOATS * 4 : 0) + 1024;
+  static constexpr int NACC = NACC_;  // TMEM accumulator buffers of BN columns
   static constexpr uint32_t TMEM_COLS = NACC * BN <= 256 ? (NACC * BN <= 128 ? 128 : 256) : 512;
   static constexpr int DCOLS = BN % 64 == 0 ? 64 : 32;
-  static constexpr int NDW = 4 * (BN / DCOLS);
+  static constexpr int NDW = NDW_;
   static constexpr int NCONV = 4;
   static constexpr int W_DRAIN = 2 + NCONV;
   static constexpr int THREADS = 32 * (W_DRAIN + NDW);
@@ -331,6 +338,51 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
       // ---- epilogue of the item
       const int row = it.tm * 128 + row_in_tile;
       const int col0 = it.tn * BN + part * C::DCOLS;
+      if constexpr (C::STAGED) {
+        if (P.epi == 1 || P.nsplit == 1) {
+          // 16 columns at a time through the warp's staging tile: lane r writes
+          // its row, then each lane takes one complex column of 4 rows per pass
+          float* stg = reinterpret_cast<float*>(smem + C::STG_OFF) + dw * C::STG_WARP_FLOATS;
+          const int rs = lane >> 3, cs = lane & 7;
+          const StageParams* pp = batch.params;
+#pragma unroll
+          for (int ch = 0; ch < C::DCOLS / 16; ++ch) {
+            float4* wv = reinterpret_cast<float4*>(stg + lane * 20);
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+              wv[j] = make_float4(acc[16 * ch + 4 * j], acc[16 * ch + 4 * j + 1], acc[16 * ch + 4 * j + 2],
+                                  acc[16 * ch + 4 * j + 3]);
+            __syncwarp();
+#pragma unroll 2
+            for (int itr = 0; itr < 8; ++itr) {
+              const int rr = itr * 4 + rs;
+              const int r = it.tm * 128 + quarter * 32 + rr;
+              const int col = (col0 >> 1) + ch * 8 + cs;  // complex column
+              const float2 v = *reinterpret_cast<const float2*>(stg + rr * 20 + 2 * cs);
+              if (r < P.M && 2 * col < P.Nv) {
+                if (P.epi == 1) {
+                  // the Omega derivative (Zandpack/mpi/zand:782-809; the diagonal
+                  // term is Zandpack/mpi_funcs.py:91-102):
+                  // h (sources) + (i h/hbar)(X+ - X-) Omega
+                  float2 xp = batch.Xp[P.row_mode0 + r];
+                  xp.x += pp->fdelta[P.la];
+                  float2 xm = batch.Xm[P.col_mode0 + col];
+                  xm.x += pp->fdelta[P.lb];
+                  const float2 dx = make_float2(xp.x - xm.x, xp.y - xm.y);
+                  const float2 om = P.om_in[(long long)r * P.ld_om + col];
+                  const float2 dd = make_float2(dx.x * om.x - dx.y * om.y, dx.x * om.y + dx.y * om.x);
+                  batch.om_out_base[P.om_out_off + (long long)r * P.ld_om + col] =
+                      make_float2(v.x * pp->fh - pp->fh_hb * dd.y, v.y * pp->fh + pp->fh_hb * dd.x);
+                } else {
+                  *reinterpret_cast<float2*>(P.D + (long long)r * P.ldd + 2 * col) = v;
+                }
+              }
+            }
+            __syncwarp();
+          }
+          continue;
+        }
+      }
       if (P.epi == 1) {
         // the Omega derivative (Zandpack/mpi/zand:782-809; the diagonal term
         // is Zandpack/mpi_funcs.py:91-102): h (sources) + (i h/hbar)(X+ - X-) Omega

@@ -6,7 +6,7 @@
 
 namespace zg {
 
-#define ZG_TCX_MAPS 12
+#define ZG_TCX_MAPS 18
 #define ZG_TCX_PROBS (5 * ZG_MAX_LEADS)
 
 // One complex product D (M x Nv real columns, row stride ldd floats) =
