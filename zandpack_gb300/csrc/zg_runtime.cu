@@ -609,6 +609,7 @@ static int build_tcx(zg_traj* t, const zg_layout* Lo, const std::vector<double2>
     P.a_k0 = (int)(2 * b.q0);
     P.K = (int)(2 * (b.q1 - b.q0));
     P.kseg = P.K;  // one operand pair
+    P.om_map = -1;
     P.Nv = (int)(2 * nc);
     P.ldd = 2 * nc;
     P.tiles_n = 1;
@@ -636,6 +637,7 @@ static int build_tcx(zg_traj* t, const zg_layout* Lo, const std::vector<double2>
     P.M = (int)(r1 - r0); P.Nv = (int)(2 * n);
     P.K = ldx;
     P.kseg = P.K;
+    P.om_map = -1;
     P.tiles_m = (P.M + 127) / 128;
     P.tiles_n = (int)((2 * n + bn - 1) / bn);
     P.D = (float*)(t->R2_32 + r0 * n);
@@ -688,6 +690,12 @@ static int build_tcx(zg_traj* t, const zg_layout* Lo, const std::vector<double2>
     ZG_TRY(tcx_map(*B, 17, t->Gcl, L * 2 * N, 2 * nc, ldx, bn, 32, true));
     const float2* oA = t->stage32 + ml.st_om;
     const float2* oB = oA + N * Ns;
+    // blocks of Omega_in prefetched by the kernel (when its shared memory has room)
+    const bool tiles_ok = tcx_has_omega_tile(bn);
+    if (tiles_ok) {
+      ZG_TRY(tcx_map(*B, 18, oA, N, 2 * Ns, 2 * Ns, 128, bn, false));
+      if (Nf > 0) ZG_TRY(tcx_map(*B, 19, oB, Ns, 2 * Nf, 2 * Nf, 128, bn, false));
+    }
     // kind 0: OmA rows sourced of a (both terms); 1: OmA rows free of a (term 1);
     // 2: OmB rows sourced of a, columns free of b (term 2)
     for (int a = 0; a < L; ++a)
@@ -721,6 +729,10 @@ static int build_tcx(zg_traj* t, const zg_layout* Lo, const std::vector<double2>
           P.col_mode0 = (int)c0;
           P.la = a;
           P.lb = b;
+          // TMA needs the block's first float column on a 16-byte boundary
+          P.om_map = tiles_ok && lc0 % 2 == 0 ? (kind == 2 ? 19 : 18) : -1;
+          P.om_x0 = (int)(2 * lc0);
+          P.om_y0 = (int)r0;
           probs.push_back(P);
         }
   }

@@ -60,7 +60,11 @@ struct TcxCfg {
   static constexpr int STG_OFF = BAR_OFF + 256;
   static constexpr int STG_WARP_FLOATS = 32 * 20;
   static constexpr bool STAGED = STG_OFF + NDW_ * STG_WARP_FLOATS * 4 + 1024 <= 232448;
-  static constexpr int SMEM = STG_OFF + (STAGED ? NDW_ * STG_WARP_FLOATS * 4 : 0) + 1024;
+  // the Omega tile of an item with epilogue 1 (128 rows x BN floats)
+  static constexpr int OMT_OFF = STG_OFF + (STAGED ? NDW_ * STG_WARP_FLOATS * 4 : 0);
+  static constexpr int OMT_BYTES = 128 * BN * 4;
+  static constexpr bool HAS_OMT = STAGED && OMT_OFF + OMT_BYTES + 1024 <= 232448;
+  static constexpr int SMEM = OMT_OFF + (HAS_OMT ? OMT_BYTES : 0) + 1024;
   static constexpr int NACC = NACC_;  // TMEM accumulator buffers of BN columns
   static constexpr uint32_t TMEM_COLS = NACC * BN <= 256 ? (NACC * BN <= 128 ? 128 : 256) : 512;
   static constexpr int DCOLS = BN % 64 == 0 ? 64 : 32;
@@ -119,6 +123,8 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
   const uint32_t bar_tfull = bar_empty + 8 * STAGES;   // NACC
   const uint32_t bar_tempty = bar_tfull + 8 * NACC;    // NACC
   const uint32_t bar_done = bar_tempty + 8 * NACC;
+  const uint32_t bar_omt_full = sbase + C::BAR_OFF + 160;   // the Omega tile landed
+  const uint32_t bar_omt_empty = sbase + C::BAR_OFF + 168;  // the drain warps read it
   uint32_t* tmem_slot = (uint32_t*)(smem + C::BAR_OFF + 24 * STAGES + 16 * NACC + 8);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int* err = batch.err;
@@ -134,6 +140,8 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
       mbar_init(bar_tempty + 8 * b, 32 * NDW);
     }
     mbar_init(bar_done, 1);
+    mbar_init(bar_omt_full, 1);
+    mbar_init(bar_omt_empty, 32 * NDW);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
@@ -309,12 +317,26 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
     float acc[C::DCOLS];
     bool ok = true;
     int kb_global = 0;
+    int nom = 0;             // Omega tiles prefetched so far (all drain threads count them)
+    bool omt_pending = false;  // lane 0 of drain warp 0: a tile load not yet waited for
     for (int wi = wbeg; wi < wend && ok; ++wi) {
         const int w = batch.items[wi];
       const TcxItem it = tcx_item(batch, w);
       const TcxProb& P = batch.p[it.prob];
       int kb0, nkb;
       tcx_kblocks(P, it.split, kb0, nkb);
+      const bool omt = C::HAS_OMT && P.epi == 1 && P.om_map >= 0;
+      if (omt && dw == 0 && lane == 0) {
+        // the block of Omega_in for this tile, loaded while its MMAs run; the
+        // buffer is free once every drain thread has read the previous tile
+        bool free_ok = nom == 0 || mbar_wait(bar_omt_empty, (uint32_t)(nom - 1) & 1u, err, 18);
+        if (free_ok) {
+          mbar_expect_tx(bar_omt_full, C::OMT_BYTES);
+          tma_load_2d(sbase + C::OMT_OFF, &batch.maps[P.om_map], bar_omt_full, P.om_x0 + it.tn * BN,
+                      P.om_y0 + it.tm * 128);
+          omt_pending = true;
+        }
+      }
 #pragma unroll
       for (int i = 0; i < C::DCOLS; ++i) acc[i] = 0.f;
       for (int q = 0; q < nkb; ++q, ++kb_global) {
@@ -345,6 +367,12 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
           float* stg = reinterpret_cast<float*>(smem + C::STG_OFF) + dw * C::STG_WARP_FLOATS;
           const int rs = lane >> 3, cs = lane & 7;
           const StageParams* pp = batch.params;
+          const float* omt_s = reinterpret_cast<const float*>(smem + C::OMT_OFF);
+          if (omt) {
+            ok = __all_sync(0xffffffffu, mbar_wait(bar_omt_full, (uint32_t)nom & 1u, err, 19));
+            if (!ok) break;
+            if (dw == 0 && lane == 0) omt_pending = false;
+          }
 #pragma unroll
           for (int ch = 0; ch < C::DCOLS / 16; ++ch) {
             float4* wv = reinterpret_cast<float4*>(stg + lane * 20);
@@ -369,7 +397,9 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
                   float2 xm = batch.Xm[P.col_mode0 + col];
                   xm.x += pp->fdelta[P.lb];
                   const float2 dx = make_float2(xp.x - xm.x, xp.y - xm.y);
-                  const float2 om = P.om_in[(long long)r * P.ld_om + col];
+                  const float2 om =
+                      omt ? *reinterpret_cast<const float2*>(omt_s + (quarter * 32 + rr) * BN + 2 * (col - it.tn * (BN / 2)))
+                          : P.om_in[(long long)r * P.ld_om + col];
                   const float2 dd = make_float2(dx.x * om.x - dx.y * om.y, dx.x * om.y + dx.y * om.x);
                   batch.om_out_base[P.om_out_off + (long long)r * P.ld_om + col] =
                       make_float2(v.x * pp->fh - pp->fh_hb * dd.y, v.y * pp->fh + pp->fh_hb * dd.x);
@@ -379,6 +409,10 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
               }
             }
             __syncwarp();
+          }
+          if (omt) {
+            mbar_arrive(bar_omt_empty);
+            ++nom;
           }
           continue;
         }
@@ -465,6 +499,8 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
         if (lane == 0) P.counters[slice] = 0;  // ready for the next launch
       }
     }
+    // a tile load still in flight (only after a timed-out wait): wait for it
+    if (omt_pending) mbar_wait(bar_omt_full, (uint32_t)nom & 1u, err, 20);
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
@@ -538,6 +574,10 @@ int tcx_validate(const TcxBatch& b) {
     }
     if (P.epi == 1) {
       ZG_REQUIRE(P.nsplit == 1 && P.om_in && b.params && b.Xp && b.Xm && P.ld_om > 0, "problem %d: Omega epilogue", i);
+      if (P.om_map >= 0)
+        ZG_REQUIRE(tcx_has_omega_tile(b.bn) && P.om_map < ZG_TCX_MAPS && b.box_cols[P.om_map] == b.bn &&
+                       b.box_rows[P.om_map] == 128 && P.om_x0 % 4 == 0 && P.om_x0 >= 0 && P.om_y0 >= 0,
+                   "problem %d: Omega tile map", i);
     } else {
       ZG_REQUIRE(P.D && P.ldd >= P.Nv, "problem %d: output", i);
       ZG_REQUIRE(P.nsplit == 1 || (P.ws && P.counters), "problem %d: split-K scratch", i);
@@ -550,6 +590,16 @@ int tcx_validate(const TcxBatch& b) {
   ZG_REQUIRE(b.cta_off[c] == b.nitems, "item lists cover %d of %d items", (int)b.cta_off[c], b.nitems);
   for (int w = 0; w < b.nitems; ++w) ZG_REQUIRE(b.items[w] < b.nitems, "item %d", w);
   return ZG_OK;
+}
+
+bool tcx_has_omega_tile(int bn) {
+  switch (bn) {
+    case 32: return TcxCfg<32>::HAS_OMT;
+    case 64: return TcxCfg<64>::HAS_OMT;
+    case 128: return TcxCfg<128>::HAS_OMT;
+    case 192: return TcxCfg<192>::HAS_OMT;
+    default: return false;
+  }
 }
 
 int tcx_bn_for(int ncols) {

@@ -6,7 +6,7 @@
 
 namespace zg {
 
-#define ZG_TCX_MAPS 18
+#define ZG_TCX_MAPS 20
 #define ZG_TCX_PROBS (5 * ZG_MAX_LEADS)
 
 // One complex product D (M x Nv real columns, row stride ldd floats) =
@@ -36,6 +36,10 @@ struct TcxProb {
   int epi, ld_om, row_mode0, col_mode0, la, lb;
   const float2* om_in;
   long long om_out_off;
+  // epi 1: the block of Omega_in is prefetched into shared memory with TMA
+  // through map om_map (box BN floats x 128 rows, no swizzle) from float
+  // column om_x0 and row om_y0 of that map; om_map < 0: read from om_in
+  int om_map, om_x0, om_y0;
 };
 
 #define ZG_TCX_ITEMS 3072
@@ -64,6 +68,8 @@ struct TcxBatch {
 int tcx_bn_for(int ncols);
 // number of drain warps of the BN kernel (counters per tile)
 inline int tcx_ndw(int bn) { return 4 * (bn / (bn % 64 == 0 ? 64 : 32)); }
+// whether the BN kernel prefetches Omega tiles into shared memory (it fits)
+bool tcx_has_omega_tile(int bn);
 int tcx_launch(const TcxBatch& b, int grid, cudaStream_t s);
 // tensor map `i` of a batch over a rows x cols fp32 array (row stride ld),
 // with its box recorded for tcx_validate
