@@ -58,7 +58,8 @@ struct TcxCfg {
   // epilogue staging: per drain warp a 32-row x 16-float tile (rows padded to
   // 20 floats), so that global loads and stores run along rows; kept when it fits
   static constexpr int STG_OFF = BAR_OFF + 256;
-  static constexpr int STG_WARP_FLOATS = 32 * 20;
+  static constexpr int STG_LD = 36;                 // staging row stride (floats): 32 + 4 against bank conflicts
+  static constexpr int STG_WARP_FLOATS = 32 * STG_LD;
   static constexpr bool STAGED = STG_OFF + NDW_ * STG_WARP_FLOATS * 4 + 1024 <= 232448;
   // the Omega tile of an item with epilogue 1 (128 rows x BN floats)
   static constexpr int OMT_OFF = STG_OFF + (STAGED ? NDW_ * STG_WARP_FLOATS * 4 : 0);
@@ -362,47 +363,63 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
       const int col0 = it.tn * BN + part * C::DCOLS;
       if constexpr (C::STAGED) {
         if (P.epi == 1 || P.nsplit == 1) {
-          // 16 columns at a time through the warp's staging tile: lane r writes
-          // its row, then each lane takes one complex column of 4 rows per pass
+          // 32 columns at a time through the warp's staging tile: lane r writes
+          // its row, then each pass stores two rows of 16 complex columns
           float* stg = reinterpret_cast<float*>(smem + C::STG_OFF) + dw * C::STG_WARP_FLOATS;
-          const int rs = lane >> 3, cs = lane & 7;
-          const StageParams* pp = batch.params;
+          const int rs = lane >> 4, cs = lane & 15;
           const float* omt_s = reinterpret_cast<const float*>(smem + C::OMT_OFF);
-          if (omt) {
-            ok = __all_sync(0xffffffffu, mbar_wait(bar_omt_full, (uint32_t)nom & 1u, err, 19));
-            if (!ok) break;
-            if (dw == 0 && lane == 0) omt_pending = false;
+          float fh = 0.f, fhh = 0.f;
+          float2 xp_own = make_float2(0.f, 0.f), xmv[C::DCOLS / 32];
+          if (P.epi == 1) {
+            // X+ of this lane's row (shared across lanes below) and X- of its
+            // column in each 32-column chunk, loaded once per item
+            const StageParams* pp = batch.params;
+            fh = pp->fh;
+            fhh = pp->fh_hb;
+            if (row < P.M) xp_own = batch.Xp[P.row_mode0 + row];
+            xp_own.x += pp->fdelta[P.la];
+            const float db = pp->fdelta[P.lb];
+#pragma unroll
+            for (int ch = 0; ch < C::DCOLS / 32; ++ch) {
+              const int col = (col0 >> 1) + ch * 16 + cs;
+              xmv[ch] = 2 * col < P.Nv ? batch.Xm[P.col_mode0 + col] : make_float2(0.f, 0.f);
+              xmv[ch].x += db;
+            }
+            if (omt) {
+              ok = __all_sync(0xffffffffu, mbar_wait(bar_omt_full, (uint32_t)nom & 1u, err, 19));
+              if (!ok) break;
+              if (dw == 0 && lane == 0) omt_pending = false;
+            }
           }
 #pragma unroll
-          for (int ch = 0; ch < C::DCOLS / 16; ++ch) {
-            float4* wv = reinterpret_cast<float4*>(stg + lane * 20);
+          for (int ch = 0; ch < C::DCOLS / 32; ++ch) {
+            float4* wv = reinterpret_cast<float4*>(stg + lane * C::STG_LD);
 #pragma unroll
-            for (int j = 0; j < 4; ++j)
-              wv[j] = make_float4(acc[16 * ch + 4 * j], acc[16 * ch + 4 * j + 1], acc[16 * ch + 4 * j + 2],
-                                  acc[16 * ch + 4 * j + 3]);
+            for (int j = 0; j < 8; ++j)
+              wv[j] = make_float4(acc[32 * ch + 4 * j], acc[32 * ch + 4 * j + 1], acc[32 * ch + 4 * j + 2],
+                                  acc[32 * ch + 4 * j + 3]);
             __syncwarp();
-#pragma unroll 2
-            for (int itr = 0; itr < 8; ++itr) {
-              const int rr = itr * 4 + rs;
+            const int col = (col0 >> 1) + ch * 16 + cs;  // complex column
+#pragma unroll 4
+            for (int itr = 0; itr < 16; ++itr) {
+              const int rr = itr * 2 + rs;
               const int r = it.tm * 128 + quarter * 32 + rr;
-              const int col = (col0 >> 1) + ch * 8 + cs;  // complex column
-              const float2 v = *reinterpret_cast<const float2*>(stg + rr * 20 + 2 * cs);
+              const float2 v = *reinterpret_cast<const float2*>(stg + rr * C::STG_LD + 2 * cs);
+              const float2 xp = make_float2(__shfl_sync(0xffffffffu, xp_own.x, rr),
+                                            __shfl_sync(0xffffffffu, xp_own.y, rr));
               if (r < P.M && 2 * col < P.Nv) {
                 if (P.epi == 1) {
                   // the Omega derivative (Zandpack/mpi/zand:782-809; the diagonal
                   // term is Zandpack/mpi_funcs.py:91-102):
                   // h (sources) + (i h/hbar)(X+ - X-) Omega
-                  float2 xp = batch.Xp[P.row_mode0 + r];
-                  xp.x += pp->fdelta[P.la];
-                  float2 xm = batch.Xm[P.col_mode0 + col];
-                  xm.x += pp->fdelta[P.lb];
-                  const float2 dx = make_float2(xp.x - xm.x, xp.y - xm.y);
+                  const float2 dx = make_float2(xp.x - xmv[ch].x, xp.y - xmv[ch].y);
                   const float2 om =
-                      omt ? *reinterpret_cast<const float2*>(omt_s + (quarter * 32 + rr) * BN + 2 * (col - it.tn * (BN / 2)))
+                      omt ? *reinterpret_cast<const float2*>(omt_s + (quarter * 32 + rr) * BN +
+                                                             2 * (col - it.tn * (BN / 2)))
                           : P.om_in[(long long)r * P.ld_om + col];
                   const float2 dd = make_float2(dx.x * om.x - dx.y * om.y, dx.x * om.y + dx.y * om.x);
                   batch.om_out_base[P.om_out_off + (long long)r * P.ld_om + col] =
-                      make_float2(v.x * pp->fh - pp->fh_hb * dd.y, v.y * pp->fh + pp->fh_hb * dd.x);
+                      make_float2(v.x * fh - fhh * dd.y, v.y * fh + fhh * dd.x);
                 } else {
                   *reinterpret_cast<float2*>(P.D + (long long)r * P.ldd + 2 * col) = v;
                 }
