@@ -214,6 +214,9 @@ def run_ours(args):
     # one attempt = one launch of the captured attempt graph (controller on the device)
     tr.graph_prepare(bias, w.hubbard_U)
     tr.set_y(w.arrays["DM_Ortho"])
+    # measured choice of the small-product / dOmega kernels for this workload class
+    from zandpack_gb300 import autotune
+    kernels = autotune.choose(tr, dev)
     tr.graph_set(w.t0, w.stepsize, w.eps, 1e30)
 
     def attempts(k):
@@ -312,7 +315,8 @@ def run_ours(args):
         "config": {"workload": "%s: %s" % (args.config, WORKLOAD_DESC.get(args.config, "")),
                    "precision": args.precision, "layout": L.summary(),
                    "l2": "inputs larger than L2: %d state slots x %.0f MB" % (tr.stages + 1, L.size * 16 / 1e6),
-                   "parallelism": "replicas" if ws > 1 else "single"},
+                   "parallelism": "replicas" if ws > 1 else "single",
+                   "kernels": kernels},
         "rhs_evals_per_s": tr.stages * args.steps * ws / (ms / 1e3),
         "simulated_fs": adv_total,
         "t_h_after": list(state),

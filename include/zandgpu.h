@@ -214,6 +214,29 @@ int zg_graph_set(zg_traj* t, double time, double h, double eps, double t1);
  * (each may be NULL) the controller after the batch. */
 int zg_graph_run(zg_traj* t, int count, zg_attempt_rec* recs, int* nrec, double* time, double* h, int* done);
 
+/* Which kernels compute the mixed path's small products (the PI partials,
+ * Omega xi, xi sigma^T) and dOmega/dt:
+ *   ZG_IMPL_SIMT         FP32 SIMT kernels for both (dOmega/dt on the
+ *                        trajectory's second stream);
+ *   ZG_IMPL_TC_PRODUCTS  the products on the tensor cores, dOmega/dt SIMT on
+ *                        the second stream;
+ *   ZG_IMPL_TC_ALL       both in one tensor-core launch.
+ * zg_set_impl selects one (ZG_EINVAL when the trajectory's shapes do not
+ * allow it; the FP64 path ignores it); zg_get_impl reads the current choice
+ * and, in *avail, a bit mask of the implementations the trajectory supports.
+ * zg_tune times one right-hand side of each supported implementation
+ * (CUDA events, `reps` evaluations each, after one untimed evaluation) on the
+ * current state, keeps the fastest and returns its index and the
+ * milliseconds per evaluation of each (ms[ZG_IMPL_COUNT], -1 where not
+ * supported).  It overwrites k slot 0 and drops a captured attempt graph.
+ * These replace no reference interface: they choose among this library's
+ * kernels for the reference's Q_np / Omega stage terms
+ * (Zandpack/mpi/zand:91-110,770-809). */
+enum { ZG_IMPL_SIMT = 0, ZG_IMPL_TC_PRODUCTS = 1, ZG_IMPL_TC_ALL = 2, ZG_IMPL_COUNT = 3 };
+int zg_set_impl(zg_traj* t, int impl);
+int zg_get_impl(const zg_traj* t, int* impl, int* avail);
+int zg_tune(zg_traj* t, int reps, int* best, double* ms);
+
 /* Measurement.  With profiling on, CUDA events on the trajectory's stream
  * bracket each region; zg_profile_read returns accumulated milliseconds and
  * counts per region (indices ZG_PROF_*).  zg_profile(t, 1) also resets them. */

@@ -16,6 +16,8 @@ ZG_PREC_F64, ZG_PREC_MIXED = 0, 1
 ZG_DH_NONE, ZG_DH_MATRIX, ZG_DH_HUBBARD = 0, 1, 2
 ZG_MAX_LEADS = 16
 ZG_MAX_STAGES = 13
+ZG_IMPL_SIMT, ZG_IMPL_TC_PRODUCTS, ZG_IMPL_TC_ALL, ZG_IMPL_COUNT = 0, 1, 2, 3
+IMPL_NAMES = ["simt", "tc_products", "tc_all"]
 PROF_REGIONS = ["gemm", "omega", "final", "combine", "error", "update", "rhs", "prep", "small", "gemm2"]
 
 _NAMES = {ZG_EINVAL: "EINVAL", ZG_ENOMEM: "ENOMEM", ZG_ECUDA: "ECUDA", ZG_ETIMEOUT: "ETIMEOUT",
@@ -99,6 +101,9 @@ _SIGS = {
     "zg_terr2_c128": ([_P, C.c_int64, C.c_int, _P, C.c_int64, _P, _P], C.c_int),
     "zg_terr2_c128_noalloc": ([_P, C.c_int64, C.c_int, _P, C.c_int64, _P, _P], C.c_int),
     "zg_step_fourth_c128": ([_P, C.c_int64, C.c_int, _P, C.c_int64, _P], C.c_int),
+    "zg_set_impl": ([_P, C.c_int], C.c_int),
+    "zg_get_impl": ([_P, C.POINTER(C.c_int), C.POINTER(C.c_int)], C.c_int),
+    "zg_tune": ([_P, C.c_int, C.POINTER(C.c_int), _P], C.c_int),
     "zg_combine_fermi_skip_c128": ([_P, C.c_int64, C.c_int, _P, _P, C.c_int, _P, _P, _P, _P, _P], C.c_int),
     "zg_outer_subtraction_c128": ([_P, C.c_int, _P, C.c_int, _P, _P, _P, _P], C.c_int),
 }

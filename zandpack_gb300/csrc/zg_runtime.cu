@@ -222,7 +222,10 @@ struct zg_traj {
   // xi sigma^T (embedded sigma columns, written by the operand kernel),
   // split-K partials and slice counters
   bool tcx_on = false;
-  TcxBatch* tcx = nullptr;
+  TcxBatch* tcx = nullptr;      // the products alone
+  TcxBatch* tcx_all = nullptr;  // the products and the Omega derivative
+  int tcx_grid_all = 0;
+  int prod_impl = 0;            // ZG_IMPL_*: which kernels compute the products and dOmega/dt
   TcxOperands tcx_ops;
   // the Omega derivative in the same batch (epilogue 1 of zg_tcx.cu): the
   // constant operands U' (embedded) and V (TF32 hi/lo), and the per-stage psi
@@ -406,6 +409,7 @@ static void free_traj(zg_traj* t) {
                   t->Uh, t->Ul, t->Vh, t->Vl, t->Gth, t->Gtl, t->Gch, t->Gcl};
   for (void* p : ptrs) dfree(t, p);
   delete t->tcx;
+  delete t->tcx_all;
   if (t->stream2) {
     cudaStreamSynchronize(t->stream2);
     cudaStreamDestroy(t->stream2);
@@ -739,55 +743,32 @@ static int build_tcx(zg_traj* t, const zg_layout* Lo, const std::vector<double2>
   int sms = 0;
   ZG_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, t->dev));
   const int grid = std::max(1, std::min(sms, ZG_TCX_GRID));
-  // K chunk: about the average work of a CTA, so that no item outlasts the
-  // others by much and split-K partials stay few
+  // K chunk: about the average work of a CTA over the products, so that no
+  // item outlasts the others by much and split-K partials stay few (the same
+  // chunks in both batches below, so that they share the split-K scratch)
   int64_t total_kb = 0;
-  for (const TcxProb& P : probs) total_kb += (int64_t)P.tiles_m * P.tiles_n * (P.K / 32);
-  int chunk_kb = (int)std::min<int64_t>(64, std::max<int64_t>(8, (total_kb + grid - 1) / grid));
-  std::vector<int> item_kb;
+  for (const TcxProb& P : probs)
+    if (P.epi == 0) total_kb += (int64_t)P.tiles_m * P.tiles_n * (P.K / 32);
+  const int chunk_kb0 = (int)std::min<int64_t>(64, std::max<int64_t>(8, (total_kb + grid - 1) / grid));
+  int chunk_kb = chunk_kb0;
   for (;;) {
     int items = 0;
-    item_kb.clear();
     for (TcxProb& P : probs) {
       P.kchunk = P.epi == 1 ? P.K : std::min(P.K, 32 * chunk_kb);  // Omega blocks: whole K per tile
       P.nsplit = (P.K + P.kchunk - 1) / P.kchunk;
-      P.item_begin = items;
       items += P.tiles_m * P.tiles_n * P.nsplit;
-      for (int w = 0; w < P.tiles_m * P.tiles_n * P.nsplit; ++w) {
-        const int split = w % P.nsplit;
-        // an Omega tile also moves its block of Omega in and out (about two K blocks)
-        item_kb.push_back(std::min(P.kchunk, P.K - split * P.kchunk) / 32 + (P.epi == 1 ? 2 : 0));
-      }
     }
     if (items <= ZG_TCX_ITEMS) break;
-    if (chunk_kb >= 1024) return ZG_OK;  // too many tiles for the item table: the SIMT batch runs
+    if (chunk_kb >= 1024) return ZG_OK;  // too many tiles for the item table: the SIMT kernels run
     chunk_kb *= 2;
   }
-  const int nitems = (int)item_kb.size();
-  // longest first onto the least loaded CTA
-  std::vector<int> order(nitems);
-  for (int i = 0; i < nitems; ++i) order[i] = i;
-  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return item_kb[x] > item_kb[y]; });
-  std::vector<int64_t> load(grid, 0);
-  std::vector<std::vector<int>> per(grid);
-  for (int w : order) {
-    int c = (int)(std::min_element(load.begin(), load.end()) - load.begin());
-    load[c] += item_kb[w] + 2;  // + the item's epilogue
-    per[c].push_back(w);
-  }
-  int used = 0, pos = 0;
-  for (int c = 0; c < grid; ++c) {
-    if (per[c].empty()) continue;
-    B->cta_off[used++] = (unsigned short)pos;
-    for (int w : per[c]) B->items[pos++] = (unsigned short)w;
-  }
-  B->cta_off[used] = (unsigned short)pos;
+  // split-K scratch and slice counters of the products (shared by both batches)
   int64_t ws_need = 0, cnt_need = 0;
   std::vector<int64_t> ws_off, cnt_off;
   for (const TcxProb& P : probs) {
     if (P.epi == 1) {
       ws_off.push_back(-1);
-      cnt_off.push_back(0);
+      cnt_off.push_back(-1);
       continue;
     }
     ws_off.push_back(P.nsplit > 1 ? ws_need : -1);
@@ -798,33 +779,69 @@ static int build_tcx(zg_traj* t, const zg_layout* Lo, const std::vector<double2>
   if (ws_need > 0) ZG_TRY(dalloc(t, &t->tcx_ws, ws_need));
   ZG_TRY(dalloc(t, &t->tcx_cnt, std::max<int64_t>(cnt_need, 1)));
   ZG_CHECK_CUDA(cudaMemsetAsync(t->tcx_cnt, 0, std::max<int64_t>(cnt_need, 1) * sizeof(int), s));
-  const int np_ = (int)probs.size();
-  for (int i = 0; i < np_; ++i) {
-    B->p[i] = probs[i];
-    B->p[i].ws = ws_off[i] >= 0 ? t->tcx_ws + ws_off[i] : nullptr;
-    B->p[i].counters = probs[i].epi == 1 ? nullptr : t->tcx_cnt + cnt_off[i];
+  for (size_t i = 0; i < probs.size(); ++i) {
+    probs[i].ws = ws_off[i] >= 0 ? t->tcx_ws + ws_off[i] : nullptr;
+    probs[i].counters = cnt_off[i] >= 0 ? t->tcx_cnt + cnt_off[i] : nullptr;
   }
   B->params = t->d_params;
   B->Xp = t->Xp32;
   B->Xm = t->Xm32;
-  B->nprob = np_;
-  B->nitems = nitems;
   B->bn = bn;
   B->err = t->tc_err;
-  ZG_TRY(tcx_validate(*B));
-  t->tcx_grid = used;
+  // one batch with the products alone, one with the products and the Omega
+  // blocks: the problem list, item numbering and the longest-first item lists
+  auto finish = [&](TcxBatch& Bt, bool with_omega, int* grid_used) -> int {
+    int np_ = 0, items = 0;
+    std::vector<int> item_kb;
+    for (const TcxProb& P0 : probs) {
+      if (P0.epi == 1 && !with_omega) continue;
+      TcxProb P = P0;
+      P.item_begin = items;
+      items += P.tiles_m * P.tiles_n * P.nsplit;
+      for (int w = 0; w < P.tiles_m * P.tiles_n * P.nsplit; ++w) {
+        const int split = w % P.nsplit;
+        // an Omega tile also moves its block of Omega in and out (about two K blocks)
+        item_kb.push_back(std::min(P.kchunk, P.K - split * P.kchunk) / 32 + (P.epi == 1 ? 2 : 0));
+      }
+      Bt.p[np_++] = P;
+    }
+    Bt.nprob = np_;
+    Bt.nitems = items;
+    std::vector<int> order(items);
+    for (int i = 0; i < items; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return item_kb[x] > item_kb[y]; });
+    std::vector<int64_t> load(grid, 0);
+    std::vector<std::vector<int>> per(grid);
+    for (int w : order) {
+      int c = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+      load[c] += item_kb[w] + 2;  // + the item's epilogue
+      per[c].push_back(w);
+    }
+    int used = 0, pos = 0;
+    for (int c = 0; c < grid; ++c) {
+      if (per[c].empty()) continue;
+      Bt.cta_off[used++] = (unsigned short)pos;
+      for (int w : per[c]) Bt.items[pos++] = (unsigned short)w;
+    }
+    Bt.cta_off[used] = (unsigned short)pos;
+    for (int c = used + 1; c <= ZG_TCX_GRID; ++c) Bt.cta_off[c] = 0;
+    *grid_used = used;
+    return tcx_validate(Bt);
+  };
+  std::unique_ptr<TcxBatch> Bm;
+  if (omega_tc) {
+    Bm.reset(new TcxBatch(*B));
+    ZG_TRY(finish(*Bm, true, &t->tcx_grid_all));
+  }
+  ZG_TRY(finish(*B, false, &t->tcx_grid));
   t->tcx = B.release();
+  t->tcx_all = Bm.release();
   t->tcx_on = true;
+  t->prod_impl = ZG_IMPL_TC_PRODUCTS;
   t->tcx_ops.sigEh = t->sigEh;
   t->tcx_ops.sigEl = t->sigEl;
   t->tcx_ops.ldx = ldx;
-  if (omega_tc) {
-    t->tco_on = true;
-    t->tcx_ops.Gth = t->Gth;
-    t->tcx_ops.Gtl = t->Gtl;
-    t->tcx_ops.Gch = t->Gch;
-    t->tcx_ops.Gcl = t->Gcl;
-  }
+  if (omega_tc) t->tco_on = true;
   return ZG_OK;
 }
 
@@ -1392,6 +1409,7 @@ static int rhs_mixed(zg_traj* t, int stage, const StageParams* p, int dH_mode, d
   float2* out = t->kslot(stage);
   cudaStream_t s = t->stream;
   const int64_t n = t->n, N = t->N, Ns = t->Ns, Nf = t->Nf, L = t->L, nc = t->nc, np = t->np;
+  const int impl = t->prod_impl;
   if (!plan_only) {
     prof_begin(t, ZG_PROF_PREP);
     // H(t) = H0 + dH changes only on the diagonal unless dH is a full matrix
@@ -1405,10 +1423,19 @@ static int rhs_mixed(zg_traj* t, int stage, const StageParams* p, int dH_mode, d
       t->h_offdiag_ready = true;
     }
     t->h_diag_mode = dH_mode;
+    // operands of the tensor-core kernels the chosen implementation runs
+    TcxOperands ops;
+    if (impl >= ZG_IMPL_TC_PRODUCTS) {
+      ops.sigEh = t->tcx_ops.sigEh;
+      ops.sigEl = t->tcx_ops.sigEl;
+      ops.ldx = t->tcx_ops.ldx;
+    }
+    if (impl == ZG_IMPL_TC_ALL) {
+      ops.Gth = t->Gth; ops.Gtl = t->Gtl; ops.Gch = t->Gch; ops.Gcl = t->Gcl;
+    }
     ZG_TRY(launch_prep_mixed((int)n, (int)np, t->nonorth ? t->Hn0 : t->H0, sig, t->nonorth ? t->dHn : t->dH, dH_mode,
                              hubbard_U, h_part, t->Hth, t->Htl, t->BSh, t->BSl, t->nonorth ? t->Sm1 : nullptr, d,
-                             (const float2*)psih_f, (const float2*)psil_f, np, t->sigC32, t->G32, ml.plane, s,
-                             t->tcx_ops));
+                             (const float2*)psih_f, (const float2*)psil_f, np, t->sigC32, t->G32, ml.plane, s, ops));
     prof_end(t, ZG_PROF_PREP);
     // tensor cores: R1 = psi H(t)^T
     prof_begin(t, ZG_PROF_GEMM);
@@ -1423,7 +1450,7 @@ static int rhs_mixed(zg_traj* t, int stage, const StageParams* p, int dH_mode, d
     ZG_TRY(tc_gemm_launch(gT, s2));
     prof_end(t, ZG_PROF_GEMM2, s2);
     prof_begin(t, ZG_PROF_OMEGA, s2);
-    if (!t->tco_on)  // else the Omega derivative runs in the tensor-core batch below
+    if (impl != ZG_IMPL_TC_ALL)  // else the Omega derivative runs in the tensor-core batch below
       ZG_TRY(launch_omega<float>(d, p, t->tiles, t->ntiles, t->G32, omA, omB, out + t->off_omA, out + t->off_omB,
                                  s2));
     prof_end(t, ZG_PROF_OMEGA, s2);
@@ -1432,7 +1459,7 @@ static int rhs_mixed(zg_traj* t, int stage, const StageParams* p, int dH_mode, d
   // PI partials, xi sigma^T rows, Omega xi: on the tensor cores (t->tcx), else
   // as the SIMT FP32 batch
   std::vector<GemmProb<float>> probs;
-  for (int a = 0; a < L && !t->tcx_on; ++a) {
+  for (int a = 0; a < L && (plan_only || impl == ZG_IMPL_SIMT); ++a) {
     int64_t r0 = t->s_start[a], r1 = t->s_start[a + 1];
     gemm_prob_f32(probs, (const float2*)(psih_f + r0 * np), (const float2*)(psil_f + r0 * np), np, 1,
                   t->IXI32 + r0 * nc, nc, 0, t->Pc32 + ((0 * L + a) * n) * nc, nc, (int)n, (int)nc, (int)(r1 - r0),
@@ -1463,10 +1490,11 @@ static int rhs_mixed(zg_traj* t, int stage, const StageParams* p, int dH_mode, d
     return run_batches<float>(t, probs2, &t->ws32, &t->ws32_cap, s, true);
   }
   prof_begin(t, ZG_PROF_SMALL);
-  if (t->tcx_on) {
-    t->tcx->om_out_base = out;
-    t->tcx->params = p;
-    ZG_TRY(tcx_launch(*t->tcx, t->tcx_grid, s));
+  if (impl != ZG_IMPL_SIMT) {
+    TcxBatch* b = impl == ZG_IMPL_TC_ALL ? t->tcx_all : t->tcx;
+    b->om_out_base = out;
+    b->params = p;
+    ZG_TRY(tcx_launch(*b, impl == ZG_IMPL_TC_ALL ? t->tcx_grid_all : t->tcx_grid, s));
   }
   else
     ZG_TRY(run_batches<float>(t, probs, &t->ws32, &t->ws32_cap, s, false));
@@ -1986,6 +2014,83 @@ int zg_stationary_precond(zg_traj* t, const double* r_dev, double* out_dev) {
   gemm_prob_f64(p2, t->st_W, n, 0, t->st_V, n, 1, (double2*)out_dev, n, (int)N, (int)n, (int)n);
   ZG_TRY(run_batches<double>(t, p2, &t->ws64, &t->ws64_cap, s, false));
   ZG_CHECK_CUDA(cudaStreamSynchronize(s));
+  return ZG_OK;
+}
+
+static int impl_mask(const zg_traj* t) {
+  if (t->precision != ZG_PREC_MIXED) return 1 << ZG_IMPL_SIMT;
+  return (1 << ZG_IMPL_SIMT) | (t->tcx_on ? 1 << ZG_IMPL_TC_PRODUCTS : 0) | (t->tcx_all ? 1 << ZG_IMPL_TC_ALL : 0);
+}
+
+int zg_set_impl(zg_traj* t, int impl) {
+  ZG_REQUIRE(t, "null argument");
+  ZG_REQUIRE(impl >= 0 && impl < ZG_IMPL_COUNT && (impl_mask(t) >> impl & 1),
+             "implementation %d not available for this trajectory (mask %d)", impl, impl_mask(t));
+  if (t->prod_impl != impl) {
+    drop_graph(t);
+    t->prod_impl = impl;
+  }
+  return ZG_OK;
+}
+
+int zg_get_impl(const zg_traj* t, int* impl, int* avail) {
+  ZG_REQUIRE(t, "null argument");
+  if (impl) *impl = t->prod_impl;
+  if (avail) *avail = impl_mask(t);
+  return ZG_OK;
+}
+
+int zg_tune(zg_traj* t, int reps, int* best, double* ms) {
+  ZG_REQUIRE(t && reps >= 1 && reps <= 1000, "bad arguments");
+  ZG_REQUIRE(!t->capturing, "zg_tune during graph capture");
+  ZG_CHECK_CUDA(cudaSetDevice(t->dev));
+  const int mask = impl_mask(t);
+  double times[ZG_IMPL_COUNT];
+  for (int i = 0; i < ZG_IMPL_COUNT; ++i) times[i] = -1.0;
+  if (t->precision != ZG_PREC_MIXED) {
+    if (best) *best = t->prod_impl;
+    if (ms) for (int i = 0; i < ZG_IMPL_COUNT; ++i) ms[i] = times[i];
+    return ZG_OK;
+  }
+  StageParams p;
+  memset(&p, 0, sizeof(p));
+  p.h = 1e-3; p.ts = 0.0; p.hbar = t->hbar;
+  derive_params(p);
+  cudaEvent_t e0, e1;
+  ZG_CHECK_CUDA(cudaEventCreate(&e0));
+  ZG_CHECK_CUDA(cudaEventCreate(&e1));
+  int st = ZG_OK;
+  int choice = t->prod_impl;
+  double tbest = 1e300;
+  for (int impl = 0; impl < ZG_IMPL_COUNT && st == ZG_OK; ++impl) {
+    if (!(mask >> impl & 1)) continue;
+    st = zg_set_impl(t, impl);
+    if (st == ZG_OK) st = zg_stage_input(t, 0);
+    if (st == ZG_OK) st = launch_set_params(p, t->d_params, t->stream);
+    if (st == ZG_OK) st = rhs_mixed(t, 0, t->d_params, ZG_DH_NONE, 0.0, false);  // untimed
+    if (st != ZG_OK) break;
+    cudaEventRecord(e0, t->stream);
+    for (int r = 0; r < reps && st == ZG_OK; ++r) st = rhs_mixed(t, 0, t->d_params, ZG_DH_NONE, 0.0, false);
+    cudaEventRecord(e1, t->stream);
+    if (cudaEventSynchronize(e1) != cudaSuccess) {
+      set_error("tuning run failed: %s", cudaGetErrorString(cudaGetLastError()));
+      st = ZG_ECUDA;
+      break;
+    }
+    float el = 0.f;
+    cudaEventElapsedTime(&el, e0, e1);
+    times[impl] = el / reps;
+    if (times[impl] < tbest) {
+      tbest = times[impl];
+      choice = impl;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st != ZG_OK) return st;
+  ZG_TRY(zg_set_impl(t, choice));
+  if (best) *best = choice;
+  if (ms) for (int i = 0; i < ZG_IMPL_COUNT; ++i) ms[i] = times[i];
   return ZG_OK;
 }
 

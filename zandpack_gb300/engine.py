@@ -167,6 +167,27 @@ class Trajectory:
                            float(hubbard_U), Jp))
         return self._J.copy() if currents else None
 
+    # ------------------------------------------------ kernel implementation
+    def set_impl(self, impl):
+        """Kernels of the mixed path's small products and dOmega/dt:
+        ``_lib.ZG_IMPL_*`` (``zg_set_impl``)."""
+        check(lib().zg_set_impl(self._h, int(impl)))
+
+    def get_impl(self):
+        """(current implementation, list of the supported ones)."""
+        impl, avail = C.c_int(), C.c_int()
+        check(lib().zg_get_impl(self._h, C.byref(impl), C.byref(avail)))
+        return impl.value, [i for i in range(_lib.ZG_IMPL_COUNT) if avail.value >> i & 1]
+
+    def tune(self, reps=5):
+        """Time one right-hand side of every supported implementation and keep
+        the fastest (``zg_tune``); returns (choice, ms per RHS per implementation,
+        None where unsupported).  Overwrites k slot 0."""
+        best = C.c_int()
+        ms = np.zeros(_lib.ZG_IMPL_COUNT)
+        check(lib().zg_tune(self._h, int(reps), C.byref(best), _ptr(ms)))
+        return best.value, [None if m < 0 else float(m) for m in ms]
+
     def error_norm2(self):
         e = np.zeros(3)
         check(lib().zg_error_norm2(self._h, _ptr(e)))
