@@ -237,6 +237,8 @@ def run_ours(args):
     state0 = (t0_, h0_)
     peaks = np.zeros(2)
     _lib.check(_lib.lib().zg_measure_peaks(dev, peaks.ctypes.data_as(ctypes.c_void_p)))
+    dmma = ctypes.c_double()
+    _lib.check(_lib.lib().zg_measure_fp64_mma(dev, ctypes.byref(dmma)))
     _lib.check(_lib.lib().zg_profile(tr._h, 1))
     tr.graph_run(0)  # recapture with the profiling event nodes before the timed region
     n0 = _lib.lib().zg_launch_count()
@@ -324,7 +326,7 @@ def run_ours(args):
         "e2e": e2e,
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
-        "peaks_live_gflops": {"fp64": peaks[0], "fp32": peaks[1]},
+        "peaks_live_gflops": {"fp64": peaks[0], "fp32": peaks[1], "fp64_mma": dmma.value},
     }
     tr.close()
     if args.precision == "mixed" and not args.no_f64_ref:

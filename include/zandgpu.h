@@ -247,6 +247,10 @@ int zg_profile(zg_traj* t, int enable);
 int zg_profile_read(zg_traj* t, double* ms, long long* count);
 /* Live FP64 and FP32 FMA throughput of `device` in GFLOP/s (out[0], out[1]). */
 int zg_measure_peaks(int device, double* out);
+/* Live FP64 tensor-core (mma.sync m8n8k4, DMMA) throughput of `device` in
+ * GFLOP/s, beside the DFMA rate of zg_measure_peaks: the FP64 path's GEMMs
+ * run on DFMA, and this probe records whether DMMA would be faster. */
+int zg_measure_fp64_mma(int device, double* gflops);
 
 /* ------------------------------------------------------------------------
  * Tensor-core building blocks of the mixed-precision path (device pointers).

@@ -83,3 +83,16 @@ def test_bounded_wait_gives_up_and_context_survives():
     check(lib().zg_gemm_tf32x3(_p(Ah), _p(Al), _p(Bh), _p(Bl), _p(D), M, N, K, None))
     ref = (Ah.double() + Al.double()) @ (Bh.double() + Bl.double()).T
     assert (D.double() - ref).abs().max().item() / ref.abs().max().item() < 2e-6
+
+
+def test_fp64_tensor_core_probe():
+    """The DMMA (mma.sync m8n8k4 f64) probe runs and reports a rate beside
+    the DFMA one (both printed for the record)."""
+    import ctypes as C
+    from zandpack_gb300 import _lib
+    g = C.c_double()
+    _lib.check(_lib.lib().zg_measure_fp64_mma(0, C.byref(g)))
+    peaks = np.zeros(2)
+    _lib.check(_lib.lib().zg_measure_peaks(0, peaks.ctypes.data_as(C.c_void_p)))
+    print("\nFP64: DMMA %.1f GFLOP/s, DFMA %.1f GFLOP/s" % (g.value, peaks[0]))
+    assert g.value > 0 and peaks[0] > 0

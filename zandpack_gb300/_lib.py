@@ -95,6 +95,7 @@ _SIGS = {
     "zg_profile": ([_P, C.c_int], C.c_int),
     "zg_profile_read": ([_P, _P, _P], C.c_int),
     "zg_measure_peaks": ([C.c_int, _P], C.c_int),
+    "zg_measure_fp64_mma": ([C.c_int, C.POINTER(C.c_double)], C.c_int),
     "zg_split_tf32": ([_P, _P, _P, C.c_int64, _P], C.c_int),
     "zg_gemm_tf32x3": ([_P, _P, _P, _P, _P, C.c_int, C.c_int, C.c_int, _P], C.c_int),
     "zg_combine_c128": ([_P, C.c_int64, C.c_int, _P, _P, C.c_int, _P, C.c_int64, _P], C.c_int),

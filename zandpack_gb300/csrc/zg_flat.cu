@@ -461,6 +461,57 @@ __global__ void __launch_bounds__(256) k_fma_peak(T* out, T a, T b, int iters) {
   if (s == (T)1.2345) out[0] = s;
 }
 
+// FP64 tensor-core probe: mma.sync m8n8k4 (DMMA) in four independent
+// accumulator chains per warp; registers only.
+__global__ void __launch_bounds__(256) k_dmma_peak(double* out, int iters) {
+  double a = 1e-3 * (threadIdx.x & 7), b = 0.999;
+  double c[4][2];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) c[j][0] = c[j][1] = (double)j;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0, %1}, {%2}, {%3}, {%0, %1};"
+                   : "+d"(c[j][0]), "+d"(c[j][1])
+                   : "d"(a), "d"(b));
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) s += c[j][0] + c[j][1];
+  if (s == 1.2345) out[0] = s;
+}
+
+int measure_dmma(double* gflops) {
+  int dev = 0, sms = 0;
+  ZG_CHECK_CUDA(cudaGetDevice(&dev));
+  ZG_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  double* d = nullptr;
+  ZG_CHECK_CUDA(cudaMalloc(&d, 16));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const int blocks = sms * 8, thr = 256, iters = 4096;
+  double best = 0.0;
+  for (int rep = 0; rep < 3; ++rep) {
+    cudaEventRecord(e0);
+    k_dmma_peak<<<blocks, thr>>>(d, iters);
+    cudaEventRecord(e1);
+    cudaError_t err = cudaEventSynchronize(e1);
+    if (err != cudaSuccess) { cudaFree(d); set_error("DMMA probe: %s", cudaGetErrorString(err)); return ZG_ECUDA; }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    // 512 flops per m8n8k4 MMA of a warp, four per iteration
+    const double gf = 512.0 * 4.0 * iters * (double)blocks * (thr / 32) / (ms * 1e6);
+    best = gf > best ? gf : best;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(d);
+  ZG_CHECK_LAUNCH();
+  *gflops = best;
+  return ZG_OK;
+}
+
 int measure_peaks(double* out) {
   int dev = 0, sms = 0;
   ZG_CHECK_CUDA(cudaGetDevice(&dev));

@@ -303,6 +303,7 @@ int launch_currents64(int n, int L, int nc, const CurRows& rows, const int* lead
                       const double2* IXI, double hbar, double* part, double* J, cudaStream_t s);
 
 // out[0] = FP64 FMA rate, out[1] = FP32 FMA rate, GFLOP/s (2 flops per FMA)
+int measure_dmma(double* gflops);
 int measure_peaks(double* out);
 
 }  // namespace zg

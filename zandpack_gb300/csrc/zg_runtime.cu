@@ -2123,6 +2123,12 @@ int zg_profile_read(zg_traj* t, double* ms, long long* count) {
   return ZG_OK;
 }
 
+int zg_measure_fp64_mma(int device, double* gflops) {
+  ZG_REQUIRE(gflops, "null argument");
+  ZG_CHECK_CUDA(cudaSetDevice(device));
+  return measure_dmma(gflops);
+}
+
 int zg_measure_peaks(int device, double* out) {
   ZG_REQUIRE(out, "null argument");
   ZG_CHECK_CUDA(cudaSetDevice(device));
