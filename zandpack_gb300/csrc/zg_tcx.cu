@@ -44,37 +44,43 @@ namespace zg {
 
 template <int BN>
 struct TcxCfg {
-  static constexpr int STAGES = 2;
   static constexpr int A_BYTES = 128 * 32 * 4;   // one 128 x 32-float K-major tile
   static constexpr int RAW_BYTES = 4 * 16 * 128 * 4;  // four 16-mode x 128-orbital planes (form 2)
   static constexpr int B_BYTES = BN * 32 * 4;
-  // stage: A hi | A lo | raw planes | B hi | B lo
-  static constexpr int OFF_AL = A_BYTES, OFF_RAW = 2 * A_BYTES, OFF_BH = 2 * A_BYTES + RAW_BYTES,
-                       OFF_BL = OFF_BH + B_BYTES;
+  // stage: A region (A hi | A lo; the raw tile of form 1 and the planes of
+  // form 2 land here and are converted in place) | B hi | B lo
+  static constexpr int OFF_AL = A_BYTES, OFF_BH = 2 * A_BYTES, OFF_BL = OFF_BH + B_BYTES;
   static constexpr int STAGE_BYTES = OFF_BL + B_BYTES;
-  static constexpr int BAR_OFF = STAGES * STAGE_BYTES;
-  static constexpr int NACC_ = BN <= 128 ? 4 : 2;
-  static constexpr int NDW_ = 4 * (BN / (BN % 64 == 0 ? 64 : 32));
-  // epilogue staging: per drain warp a 32-row x 16-float tile (rows padded to
-  // 20 floats), so that global loads and stores run along rows; kept when it fits
-  static constexpr int STG_OFF = BAR_OFF + 256;
-  static constexpr int STG_LD = 36;                 // staging row stride (floats): 32 + 4 against bank conflicts
-  static constexpr int STG_WARP_FLOATS = 32 * STG_LD;
-  static constexpr bool STAGED = STG_OFF + NDW_ * STG_WARP_FLOATS * 4 + 1024 <= 232448;
-  // the Omega tile of an item with epilogue 1 (128 rows x BN floats)
-  static constexpr int OMT_OFF = STG_OFF + (STAGED ? NDW_ * STG_WARP_FLOATS * 4 : 0);
-  static constexpr int OMT_BYTES = 128 * BN * 4;
-  static constexpr bool HAS_OMT = STAGED && OMT_OFF + OMT_BYTES + 1024 <= 232448;
-  static constexpr int SMEM = OMT_OFF + (HAS_OMT ? OMT_BYTES : 0) + 1024;
-  static constexpr int NACC = NACC_;  // TMEM accumulator buffers of BN columns
-  static constexpr uint32_t TMEM_COLS = NACC * BN <= 256 ? (NACC * BN <= 128 ? 128 : 256) : 512;
+  static constexpr int NACC = BN <= 128 ? 4 : 2;  // TMEM accumulator buffers of BN columns
   static constexpr int DCOLS = BN % 64 == 0 ? 64 : 32;
-  static constexpr int NDW = NDW_;
+  static constexpr int NDW = 4 * (BN / DCOLS);
+  // epilogue staging: per drain warp a 32-row x 32-float tile (rows padded to
+  // 36 floats), so that global loads and stores run along rows; and the Omega
+  // tile of an item with epilogue 1 (128 rows x BN floats)
+  static constexpr int STG_LD = 36;
+  static constexpr int STG_WARP_FLOATS = 32 * STG_LD;
+  static constexpr int STG_BYTES = NDW * STG_WARP_FLOATS * 4;
+  static constexpr int OMT_BYTES = 128 * BN * 4;
+  static constexpr int LIMIT = 232448 - 1024;  // dynamic shared memory less the alignment slack
+  static constexpr int fit(int stages, bool stg, bool omt) {
+    return stages * STAGE_BYTES + 256 + (stg ? STG_BYTES : 0) + (omt ? OMT_BYTES : 0) <= LIMIT;
+  }
+  // the deepest ring that fits with staging and the Omega tile, else with
+  // staging alone, else two stages with what fits
+  static constexpr int STAGES = fit(4, true, true) ? 4 : fit(3, true, true) ? 3 : fit(3, true, false) ? 3 : 2;
+  static constexpr bool STAGED = fit(STAGES, true, false);
+  static constexpr bool HAS_OMT = STAGED && fit(STAGES, true, true);
+  static constexpr int BAR_OFF = STAGES * STAGE_BYTES;
+  static constexpr int STG_OFF = BAR_OFF + 256;
+  static constexpr int OMT_OFF = STG_OFF + (STAGED ? STG_BYTES : 0);
+  static constexpr int SMEM = OMT_OFF + (HAS_OMT ? OMT_BYTES : 0) + 1024;
+  static constexpr uint32_t TMEM_COLS = NACC * BN <= 256 ? (NACC * BN <= 128 ? 128 : 256) : 512;
   static constexpr int NCONV = 4;
   static constexpr int W_DRAIN = 2 + NCONV;
   static constexpr int THREADS = 32 * (W_DRAIN + NDW);
   static_assert(BN % 32 == 0 && BN >= 32 && BN <= 256, "BN");
   static_assert(SMEM <= 232448, "shared memory");
+  static_assert(STAGES <= 4, "barrier area");
 };
 
 struct TcxItem {
@@ -124,8 +130,9 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
   const uint32_t bar_tfull = bar_empty + 8 * STAGES;   // NACC
   const uint32_t bar_tempty = bar_tfull + 8 * NACC;    // NACC
   const uint32_t bar_done = bar_tempty + 8 * NACC;
-  const uint32_t bar_omt_full = sbase + C::BAR_OFF + 160;   // the Omega tile landed
-  const uint32_t bar_omt_empty = sbase + C::BAR_OFF + 168;  // the drain warps read it
+  const uint32_t bar_omt_full = sbase + C::BAR_OFF + 192;   // the Omega tile landed
+  const uint32_t bar_omt_empty = sbase + C::BAR_OFF + 200;  // the drain warps read it
+  const uint32_t bar_cread = sbase + C::BAR_OFF + 208;      // converters read a form-2 stage
   uint32_t* tmem_slot = (uint32_t*)(smem + C::BAR_OFF + 24 * STAGES + 16 * NACC + 8);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int* err = batch.err;
@@ -143,6 +150,7 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
     mbar_init(bar_done, 1);
     mbar_init(bar_omt_full, 1);
     mbar_init(bar_omt_empty, 32 * NDW);
+    mbar_init(bar_cread, 32 * C::NCONV);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
@@ -194,7 +202,7 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
           } else {
             // planes: rows = modes (16 per K block), columns = 128 orbitals
             const int x = P.a_row0 + it.tm * 128, mode = (P.a_k0 + kx) / 2;
-            const uint32_t rb = st + C::OFF_RAW;
+            const uint32_t rb = st;  // the A region; converted in place
             tma_load_2d(rb, mA, fb, x, mode);
             tma_load_2d(rb + 8192, mA, fb, x, P.a_plane + mode);
             tma_load_2d(rb + 16384, mA + 1, fb, x, mode);
@@ -258,6 +266,7 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
     const int ct = threadIdx.x - 64;
     bool ok = true;
     int kb_global = 0;
+    int nform2 = 0;  // form-2 stages converted (phase of bar_cread)
     for (int wi = wbeg; wi < wend && ok; ++wi) {
         const int w = batch.items[wi];
       const TcxItem it = tcx_item(batch, w);
@@ -287,21 +296,31 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
             al[c] = l;
           }
         } else if (amode == 2) {
-          // row ct of A' (orbital ct of the tile): modes 0..15 as (re, im) pairs,
-          // 128-byte rows in the SWIZZLE_128B pattern (16-byte chunk c of row r
-          // at chunk c ^ (r % 8))
-          const float* rp = reinterpret_cast<const float*>(st + C::OFF_RAW);
+          // row ct of A' (orbital ct of the tile): modes 0..15 as (re, im)
+          // pairs, 128-byte rows in the SWIZZLE_128B pattern (16-byte chunk c
+          // of row r at chunk c ^ (r % 8)).  The planes occupy the same 32 KB:
+          // every converter thread reads its values first, all of them meet at
+          // an mbarrier (bounded wait), then the rows are written in place.
+          const float* rp = reinterpret_cast<const float*>(st);
+          float4 v[2][8];
 #pragma unroll
           for (int part = 0; part < 2; ++part) {  // 0: hi, 1: lo
             const float* re = rp + part * 4096;
             const float* im = re + 2048;
+#pragma unroll
+            for (int c = 0; c < 8; ++c)
+              v[part][c] = make_float4(re[(2 * c) * 128 + ct], im[(2 * c) * 128 + ct], re[(2 * c + 1) * 128 + ct],
+                                       im[(2 * c + 1) * 128 + ct]);
+          }
+          mbar_arrive(bar_cread);
+          ok = __all_sync(0xffffffffu, mbar_wait(bar_cread, (uint32_t)nform2 & 1u, err, 21));
+          ++nform2;
+          if (!ok) break;
+#pragma unroll
+          for (int part = 0; part < 2; ++part) {
             uint8_t* dst = st + (part ? C::OFF_AL : 0) + ct * 128;
 #pragma unroll
-            for (int c = 0; c < 8; ++c) {
-              const float4 v = make_float4(re[(2 * c) * 128 + ct], im[(2 * c) * 128 + ct], re[(2 * c + 1) * 128 + ct],
-                                           im[(2 * c + 1) * 128 + ct]);
-              *reinterpret_cast<float4*>(dst + ((c ^ (ct & 7)) << 4)) = v;
-            }
+            for (int c = 0; c < 8; ++c) *reinterpret_cast<float4*>(dst + ((c ^ (ct & 7)) << 4)) = v[part][c];
           }
         }
         // generic-proxy writes to shared memory, read next by the tensor core
