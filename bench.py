@@ -18,10 +18,12 @@ stream.  ``e2e`` repeats it through the public C ABI with the initial state
 uploaded from pinned host memory and every attempt's record plus sigma after
 every accepted step read back, as ``zand`` records them.
 
-``--impl reference`` times the CPU restatement of the reference (the oracle,
-NumPy/BLAS on all host cores) on the same workload; its step is one stage of
-the attempt (stage combination + right-hand side), its simulated time is the
-attempt's advance shared evenly over the attempt's stages.
+``--impl reference`` times the CPU restatement of the reference (the oracle
+port, NumPy/BLAS on all host cores) on the same workload; its step is one
+attempt of its own controller from the initial state (seven stage
+combinations and right-hand sides, the error norm and the update), and fs/s
+is its own simulated advance over the wall time.  ``cpu_baseline`` in our
+line is the same measurement on two attempts.
 """
 from __future__ import annotations
 
@@ -41,7 +43,10 @@ sys.path.insert(0, HERE)
 # where the clock samples of a run are written (bench_clocks.csv)
 OUT_DIR = os.environ.get("ZG_BENCH_OUT", os.path.join(HERE, "bench_out"))
 
-# ncu-measured DRAM traffic of one psi H^T tensor-core launch per (workload, H(t) form)
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
+# the psi H^T tensor-core GEMM per (workload, H(t) form), taken from a separate
+# ncu capture of that launch (ncu cannot run inside the timed region); reported
+# with its source, never as a measurement of this run
 NCU_TRAFFIC = {("c3", "real"): 83.8e6 + 8.6e6}
 
 METRIC = "simulated fs/s at n=1024"
@@ -280,36 +285,11 @@ def run_ours(args):
                 "peak_source": "live DFMA probe zg_measure_peaks (FP64 is not in MEASURED_PEAKS.json)",
                 "algorithmic_flops_per_launch": gemm_f}
     else:
-        # psi H(t)^T on tcgen05, planar operands, three TF32 products: A = (Re psi; Im psi)
-        # (2N x np), B = the rows of Re H (real H(t): nb32 of them) or of (Re H; Im H) (2 np)
-        np_ = (L.n + 15) // 16 * 16
-        nb32 = (L.n + 31) // 32 * 32
-        h_real = not np.any(np.asarray(w.arrays["H_Ortho"]).imag)  # the Hubbard term is real
-        tc_flops = 3 * 2 * (2 * L.N) * (nb32 if h_real else 2 * np_) * np_
-        alg_flops = 8 * L.N * L.n * L.n if not h_real else 4 * L.N * L.n * L.n
-        t_launch = g_ms / g_n / 1e3 if g_n else None
         tf32 = measure_tf32_peak()
-        achieved = tc_flops / t_launch / 1e12 if t_launch else None
-        # DRAM bytes of one launch of this kernel on this workload, from the ncu
-        # capture summarised in profiles/k_gemm_tf32x3_c3.md (dram__bytes_read.sum
-        # + dram__bytes_write.sum; ncu cannot run inside the timed bench)
-        traffic = NCU_TRAFFIC.get((args.config, "real" if h_real else "complex"))
-        roof = {"bound": "tensor",
-                "kernel": "k_gemm_tf32x3<256,4,16> (psi H(t)^T, tcgen05 kind::tf32, 3xTF32, %s H(t))"
-                          % ("real" if h_real else "complex"),
-                "achieved": achieved, "peak": tf32, "unit": "TFLOP/s",
-                "frac": (achieved / tf32) if achieved and tf32 else None, "traffic": traffic,
-                "traffic_unit": "DRAM bytes per launch (ncu capture, profiles/k_gemm_tf32x3_c3.md)",
-                "operand_bytes_per_launch": (2 * 2 * L.N * np_ + 2 * (nb32 if h_real else 2 * np_) * np_
-                                             + 2 * L.N * (nb32 if h_real else 2 * np_)) * 4,
-                "peak_source": "live cuBLAS TF32 GEMM 8192^3 (torch.matmul, allow_tf32); TF32 is not in "
-                               "MEASURED_PEAKS.json (bf16 there: %s TFLOP/s)" % _peaks_file().get("bf16_tflops"),
-                "tensor_flops_per_launch": tc_flops, "algorithmic_flops_per_launch": alg_flops,
-                "algorithmic_tflops": alg_flops / t_launch / 1e12 if t_launch else None,
-                "ms_per_launch": t_launch * 1e3 if t_launch else None}
+        roof = mixed_roofline(args, w, L, reg, tr.stages, peaks, tf32, kernels["impl"])
     roof["regions_ms_per_call"] = {k: (v[0] / v[1] if v[1] else None) for k, v in reg.items()}
     if args.precision == "mixed":
-        roof["kernel_roofs"] = kernel_roofs(L, reg, tr.stages, peaks, tf32)
+        roof["kernel_roofs"] = kernel_roofs(L, reg, tr.stages, peaks, tf32, kernels["impl"])
     out = {
         "metric": METRIC, "value": value, "unit": "fs/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -344,7 +324,63 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
-def kernel_roofs(L, reg, stages, peaks, tf32):
+def mixed_roofline(args, w, L, reg, stages, peaks, tf32, impl):
+    """Roofline of the region that takes the most time per right-hand side,
+    against MEASURED_PEAKS.json: the psi H^T tensor-core GEMM on algorithmic
+    flops (8 N n^2, SURVEY's count for a dense complex H(t)) against the bf16
+    burst peak; the streaming regions on algorithmic bytes against the
+    measured HBM copy rate."""
+    pk = _peaks_file()
+    bf16, hbm = pk.get("bf16_tflops"), pk.get("hbm_gbs")
+    n, N, Ns, Nf, nc, NL = L.n, L.N, L.Ns, L.Nf, L.nc, L.NL
+    np_ = (n + 15) // 16 * 16
+    nb32 = (n + 31) // 32 * 32
+    h_real = not np.any(np.asarray(w.arrays["H_Ortho"]).imag)  # the Hubbard term is real
+    per_rhs = {k: (v[0] / v[1] if v[1] else 0.0) for k, v in reg.items()}
+    om = N * Ns + Ns * Nf
+    cands = {
+        "gemm": ("tensor", "k_gemm_tf32x3<256,4,16> (psi H(t)^T, tcgen05 kind::tf32, 3xTF32, %s H(t))"
+                 % ("real" if h_real else "complex"), 8.0 * N * n * n, bf16, "TFLOP/s",
+                 "MEASURED_PEAKS.json bf16_tflops (burst)"),
+        # the small products read psi's hi/lo planes and the Omega blocks and write PI, Omega xi, xi sigma^T
+        "small": ("hbm", "k_tcx (PI partials, Omega xi, xi sigma^T%s on tcgen05)" % (
+                  " and dOmega/dt" if impl == "tc_all" else "") if impl != "simt" else "k_zgemm<float> SIMT batch",
+                  16.0 * N * np_ + 8.0 * om + 8.0 * (2 * NL * n * nc + NL * N * nc + NL * Ns * nc + Ns * n)
+                  + (16.0 * om if impl == "tc_all" else 0.0), hbm, "GB/s", "MEASURED_PEAKS.json hbm_gbs"),
+        "omega": ("hbm", "k_omega<float> (dOmega/dt, SIMT)", 16.0 * om, hbm, "GB/s", "MEASURED_PEAKS.json hbm_gbs"),
+        "final": ("hbm", "k_final_all_mixed (k_sigma and k_psi finalisation)",
+                  8.0 * (4 * N * n + Ns * n) + 8.0 * 3 * n * n, hbm, "GB/s", "MEASURED_PEAKS.json hbm_gbs"),
+    }
+    name = max((k for k in cands if per_rhs.get(k, 0.0) > 0), key=lambda k: per_rhs[k])
+    bound, kernel, amount, peak, unit, src = cands[name]
+    t = per_rhs[name] / 1e3
+    achieved = amount / t / (1e12 if unit == "TFLOP/s" else 1e9)
+    roof = {"bound": bound, "kernel": kernel, "region": name, "achieved": achieved, "peak": peak, "unit": unit,
+            "frac": achieved / peak if peak else None, "peak_source": src,
+            "algorithmic_%s_per_launch" % ("flops" if unit == "TFLOP/s" else "bytes"): amount,
+            "ms_per_launch": per_rhs[name], "traffic": None,
+            "regions_share_of_rhs": {k: v / sum(per_rhs[x] for x in cands) for k, v in per_rhs.items() if k in cands}}
+    # psi H(t)^T beside it: executed 3xTF32 work against live cuBLAS TF32, and its ncu traffic
+    g = per_rhs.get("gemm", 0.0) / 1e3
+    tc_flops = 3 * 2 * (2 * N) * (nb32 if h_real else 2 * np_) * np_
+    if g > 0:
+        roof["psi_HT"] = {"algorithmic_tflops": 8.0 * N * n * n / g / 1e12,
+                          "frac_of_bf16_burst": 8.0 * N * n * n / g / 1e12 / bf16 if bf16 else None,
+                          "executed_tf32_tflops": tc_flops / g / 1e12, "live_cublas_tf32_tflops": tf32,
+                          "frac_executed_of_tf32": tc_flops / g / 1e12 / tf32 if tf32 else None,
+                          "ms_per_launch": g * 1e3}
+        traffic = NCU_TRAFFIC.get((args.config, "real" if h_real else "complex"))
+        if traffic is not None:
+            roof["psi_HT"]["traffic"] = traffic
+            roof["psi_HT"]["traffic_source"] = ("dram__bytes_read.sum + dram__bytes_write.sum of one launch, "
+                                                "separate ncu capture at this workload (not this run)")
+            if name == "gemm":
+                roof["traffic"] = traffic
+                roof["traffic_source"] = roof["psi_HT"]["traffic_source"]
+    return roof
+
+
+def kernel_roofs(L, reg, stages, peaks, tf32, impl="simt"):
     """Roofline fraction of every region of the mixed attempt: algorithmic
     bytes (streaming regions, against the measured HBM copy rate of
     MEASURED_PEAKS.json) or flops (against the live FP32 / cuBLAS TF32 peaks)
@@ -375,8 +411,13 @@ def kernel_roofs(L, reg, stages, peaks, tf32):
     put("final", 8.0 * (4 * N * n + Ns * n) + 8.0 * 3 * n * n, "GB/s", hbm, mp)
     fp32 = peaks[1] / 1e3 if peaks is not None else None
     live = "live FFMA probe zg_measure_peaks"
-    put("small", 8.0 * (n * N * nc + Ns * nc * n + N * Ns * nc + Ns * Nf * nc), "TFLOP/s", fp32, live)
-    put("omega", 8.0 * (N * Ns * nc + Ns * Ns * nc + Ns * Nf * nc) + 10.0 * (N * Ns + Ns * Nf), "TFLOP/s", fp32, live)
+    om = N * Ns + Ns * Nf
+    if impl == "simt":
+        put("small", 8.0 * (n * N * nc + Ns * nc * n + N * Ns * nc + Ns * Nf * nc), "TFLOP/s", fp32, live)
+    else:  # on the tensor cores: bytes of psi's planes, the Omega blocks and the products
+        put("small", 16.0 * N * np_ + 8.0 * om + 8.0 * (2 * L.NL * n * nc + L.NL * N * nc + L.NL * Ns * nc + Ns * n)
+            + (16.0 * om if impl == "tc_all" else 0.0), "GB/s", hbm, mp)
+    put("omega", 16.0 * om, "GB/s", hbm, mp)
     # executed tensor flops of H sigma with a real H(t) (the workloads' Hamiltonians and Hubbard term)
     put("gemm2", 3 * 2.0 * ((n + 31) // 32 * 32) * 2 * np_ * np_, "TFLOP/s", tf32, "live cuBLAS TF32")
     return out
@@ -414,30 +455,38 @@ def measure_tf32_peak():
         torch.backends.cuda.matmul.allow_tf32 = old
 
 
-def f64_reference_timing(w, dev, state, mixed_value, mixed_ms):
-    """The plain FP64 device path on the same workload and controller state:
-    one warm-up and two timed attempts (the same step size), for the
-    mixed/FP64 ratio of the target specification."""
+def f64_reference_timing(w, dev, state, mixed_value, mixed_ms, attempts=6):
+    """The plain FP64 device path on the same workload, at the mixed run's
+    controller state: one warm-up and `attempts` timed attempts, each a launch
+    of the FP64 attempt graph (the mixed run's launch mode) with the step size
+    reset to the mixed run's before every attempt, for the mixed/FP64 ratio of
+    the target specification."""
     import torch
     from zandpack_gb300 import _lib
-    from zandpack_gb300.engine import Propagator
-    pr = Propagator(w.arrays, w.hbar, w.bias_fn(), hubbard_U=w.hubbard_U, precision="f64", device=dev)
-    pr.set_state(w.arrays["DM_Ortho"])
+    from zandpack_gb300.engine import Trajectory, native_bias
+    tr = Trajectory(w.arrays, w.hbar, precision="f64", device=dev)
+    tr.graph_prepare(native_bias(w.bias, tr.layout.NL), w.hubbard_U)
+    tr.set_y(w.arrays["DM_Ortho"])
     t, h = state
-    stream = torch.cuda.ExternalStream(_lib.lib().zg_traj_stream(pr.traj._h), device=dev)
-    pr.attempt(t, h)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for _ in range(2):
-        pr.attempt(t, h)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / 2
-    pr.traj.close()
-    return {"ms_per_step": ms, "value_same_h": mixed_value * mixed_ms / ms, "unit": "fs/s",
-            "mixed_over_f64": ms / mixed_ms,
-            "note": "FP64 attempt time at the mixed run's step size; value_same_h = mixed value x time ratio"}
+    stream = torch.cuda.ExternalStream(_lib.lib().zg_traj_stream(tr._h), device=dev)
+    tr.graph_set(t, h, w.eps, 1e30)
+    tr.graph_run(1)
+    times = []
+    for _ in range(attempts):
+        tr.graph_set(t, h, w.eps, 1e30)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        tr.graph_run(1)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    tr.close()
+    ms = float(np.median(times))
+    return {"ms_per_step": ms, "ms_per_step_min_max": [min(times), max(times)], "attempts": attempts,
+            "value_same_h": mixed_value * mixed_ms / ms, "unit": "fs/s", "mixed_over_f64": ms / mixed_ms,
+            "note": "median FP64 attempt (graph launch) at the mixed run's step size; "
+                    "value_same_h = mixed value x time ratio"}
 
 
 def run_e2e(tr, w, args, state0, pinned, stream):
@@ -532,20 +581,23 @@ def _oracle_stages(w, nstages, warm_stages=0):
 
 
 def cpu_baseline(args, w, adv_per_attempt):
-    """Oracle (NumPy restatement of the reference) on a bounded sample: two
-    stages of the same workload; simulated time uses the GPU run's mean advance
-    per attempt so both arms follow the same controller trajectory."""
-    nst = 2
+    """The reference arm's measurement on a bounded sample: the oracle port
+    (NumPy restatement of the reference's stage body and controller, BLAS on
+    the host cores) runs one warm-up attempt and two timed attempts of its own
+    controller from the initial state (~20 s); fs/s = its own simulated
+    advance / wall.  The same protocol as ``--impl reference``, whose step is
+    one attempt too."""
     try:
-        wall, _, done = _oracle_stages(w, nst, 0)
+        wall, sim, done = _oracle_stages(w, 14, 7)
     except MemoryError:
         return {"value": None, "unit": "fs/s", "cores": os.cpu_count(), "kind": "port",
                 "sample": "oracle out of host memory"}
-    per_stage = wall / done
-    return {"value": adv_per_attempt / (7 * per_stage), "unit": "fs/s", "cores": os.cpu_count(), "kind": "port",
-            "sample": "%d stages (combination + RHS) of %s from the initial state, NumPy/BLAS default threads; "
-                      "fs per attempt taken from the GPU run (%.4g fs)" % (done, args.config, adv_per_attempt),
-            "s_per_rhs": per_stage}
+    return {"value": sim / wall if wall > 0 else None, "unit": "fs/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": "2 attempts (14 stages: stage combination + RHS, error norm, update) of %s after one warm-up "
+                      "attempt, the oracle's own controller from the initial state; NumPy/BLAS default threads. "
+                      "The port, not the unmodified zand (numba and mpi4py are absent on the GPU box)" % args.config,
+            "s_per_rhs": wall / done, "simulated_fs": sim,
+            "gpu_fs_per_attempt_for_reference": adv_per_attempt}
 
 
 def run_ensemble(args):
@@ -622,21 +674,28 @@ def run_steady(args):
 
 
 def run_reference(args):
+    """The reference arm: the oracle port (the reference's stage body and
+    controller restated in NumPy, pinned to the unmodified zand's outputs) on
+    the host cores.  A step is one Dormand-Prince attempt of its own controller
+    from the initial state, like a step of our arm; `--warmup` attempts are
+    untimed."""
     ws, rank = _dist()
     if rank != 0:
         return
     from zandpack_gb300.workloads import make_workload
     w = make_workload(args.config)
-    # warm-up stages then timed stages; each "step" is one stage of an attempt
-    wall, sim, done = _oracle_stages(w, args.steps, args.warmup)
+    wall, sim, done = _oracle_stages(w, 7 * args.steps, 7 * args.warmup)
     value = sim / wall if wall > 0 else None
     out = {"impl": "reference", "metric": METRIC, "value": value, "unit": "fs/s", "n_gpus": ws,
-           "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall / done * 1e3,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
            "config": {"workload": "%s: %s" % (args.config, WORKLOAD_DESC.get(args.config, "")),
                       "precision": "f64", "layout": "reference padded (NL, NX, NOT)"},
            "cpu_baseline": {"value": value, "unit": "fs/s", "cores": os.cpu_count(), "kind": "port",
-                            "sample": "%d stages of the reference controller (oracle restatement, NumPy/BLAS)" % done},
+                            "sample": "%d attempts (%d stages) of the oracle port's controller after %d warm-up "
+                                      "attempts, NumPy/BLAS on the host cores; the port, not the unmodified zand "
+                                      "(numba and mpi4py are absent on the GPU box)" % (args.steps, done, args.warmup),
+                            "s_per_rhs": wall / done},
            "e2e": {"value": value, "unit": "fs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
 
