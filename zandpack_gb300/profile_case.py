@@ -18,6 +18,8 @@ def main():
     ap.add_argument("--attempts", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=1)
     ap.add_argument("--regions", action="store_true", help="print CUDA-event times per region of the timed attempts")
+    ap.add_argument("--impl", default=None, choices=["simt", "tc_products", "tc_all"],
+                    help="kernels of the small products and dOmega/dt (default: the trajectory's)")
     ap.add_argument("--nonorth", action="store_true",
                     help="the workload posed in a non-orthogonal basis, propagated as nozand does")
     args = ap.parse_args()
@@ -31,6 +33,9 @@ def main():
     w = make_nonorth_workload(args.config) if args.nonorth else make_workload(args.config)
     pr = Propagator(w.arrays, w.hbar, w.bias_fn(), hubbard_U=w.hubbard_U, precision=args.precision,
                     nonorth=args.nonorth)
+    if args.impl is not None:
+        from ._lib import IMPL_NAMES
+        pr.traj.set_impl(IMPL_NAMES.index(args.impl))
     sig0 = w.arrays["DM_Ortho"]
     pr.set_state(pr.traj.basis.sigma(sig0) if args.nonorth else sig0)
     t, h = w.t0, w.stepsize
