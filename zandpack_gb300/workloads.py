@@ -408,12 +408,14 @@ CONFIGS = {
 C4_SIZES = [(64, (8, 8)), (128, (16, 8)), (256, (16, 16)), (384, (24, 16)), (512, (32, 16))]
 
 
-def c4_requests(count=512, rate=50.0, seed=1004, t_span=2.0):
+def c4_requests(count=512, rate=50.0, seed=1004, t_span="pulse"):
     """Requests of the serving ensemble: Poisson arrivals at ``rate`` per
     second, device sizes n in {64,128,256,384,512} as 1D chains (n_c = 1) or
     2D lattices (8x8, 16x8, 16x16, 24x16, 32x16, n_c = W), 2-3 leads, 16-32
     Lorentzians of rank min(4, n_c), 20-40 Pade poles, Gaussian pulses with
-    amplitude U[0.1, 1] V and width U[2, 20] fs, propagated over ``t_span`` fs."""
+    amplitude U[0.1, 1] V and width U[2, 20] fs centred at one width.  Each is
+    propagated over its pulse, to centre + 3 widths (``t_span="pulse"``), or
+    over ``t_span`` fs when that is a number."""
     rng = np.random.default_rng(seed)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, count))
     out = []
@@ -423,7 +425,8 @@ def c4_requests(count=512, rate=50.0, seed=1004, t_span=2.0):
                         geom="1d" if rng.random() < 0.5 else "2d", leads=int(rng.integers(2, 4)),
                         n_l=int(rng.integers(16, 33)), n_f=int(rng.integers(20, 41)),
                         amp=float(rng.uniform(0.1, 1.0)), width=float(rng.uniform(2.0, 20.0)),
-                        seed=int(rng.integers(2 ** 31)), t1=float(t_span)))
+                        seed=int(rng.integers(2 ** 31)), t1=0.0))
+        out[-1]["t1"] = 4.0 * out[-1]["width"] if t_span == "pulse" else float(t_span)
     return out
 
 
