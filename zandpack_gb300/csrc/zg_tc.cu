@@ -20,13 +20,14 @@
 //     tcgen05.mma (kind::tf32, M = 128, N = BN, K = 8) for the three products
 //     of every K block into one of NACC = 512 / BN TMEM accumulator buffers
 //     (all 512 columns), committing to the ring stage's "empty" barrier and,
-//     after each K = 32 group, to the TMEM buffer's "full" barrier;
-//   * warps 0 .. NDW-1: read each K = 32 group's partial sum from TMEM
+//     after each K = TC_BK group, to the TMEM buffer's "full" barrier;
+//   * warps 0 .. NDW-1: read each K = TC_BK group's partial sum from TMEM
 //     (tcgen05.ld 32x32b; warp w takes TMEM lane quarter w % 4 and the 64
 //     columns w / 4), add it into FP32 registers and release the buffer.
 // The tensor core truncates inside its accumulation, so a single accumulator
-// over K = 2048 drifts by ~1e-5 relative; per-group partials summed with
-// round-to-nearest keep the product at ~1e-7.
+// over K = 2048 drifts by ~1e-5 relative; per-group partials (TC_BK = 64
+// floats) summed with round-to-nearest keep the product within 2e-6 (groups of
+// 32 measured 2.5% slower at n = 1024 for no accuracy the tests need).
 // Every wait on an mbarrier is bounded by a clock64 budget; on timeout the
 // thread records an error code in *err and stops issuing, the MMA thread
 // waits for its own MMAs, the producer for its copies in flight, and TMEM is
@@ -50,7 +51,7 @@ __global__ void k_wait_selftest(int* err, long long budget, int code) {
 }
 
 // BK: K elements per shared-memory stage (32 or 16); a TMEM accumulation
-// group always spans K = 32 (KPG stages), so the drain granularity and hence
+// group always spans K = TC_BK (KPG stages), so the drain granularity and hence
 // the accuracy do not depend on BK.
 template <int BN, int STAGES, int BK>
 struct TcCfg {
@@ -73,7 +74,7 @@ struct TcCfg {
 // Warp roles (32 * (NDW + 2) threads): warps 0..NDW-1 drain the accumulators
 // (TMEM lane quarter = warp % 4, 64-column part = warp / 4), warp NDW lane 0
 // loads with TMA, warp NDW+1 lane 0 issues MMAs and that warp owns the TMEM
-// allocation.  Each K-block of 32 is accumulated alone in one of NACC TMEM
+// allocation.  Each K group of TC_BK is accumulated alone in one of NACC TMEM
 // buffers and added into FP32 registers (round to nearest), so the tensor
 // core's truncating accumulation never spans more than 12 instructions.
 template <int BN, int STAGES, int BK>
@@ -97,7 +98,7 @@ __global__ void __launch_bounds__(TcCfg<BN, STAGES, BK>::THREADS, 1)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * BN;
   const int nk = (K + BK - 1) / BK;       // shared-memory stages of BK
-  const int ng = (nk + KPG - 1) / KPG;    // TMEM accumulation groups of K = 32
+  const int ng = (nk + KPG - 1) / KPG;    // TMEM accumulation groups of K = TC_BK
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -180,7 +181,7 @@ __global__ void __launch_bounds__(TcCfg<BN, STAGES, BK>::THREADS, 1)
           umma_commit(bar_empty + 8 * s);  // frees the smem buffer once these MMAs have read it
         }
         if (!ok) break;
-        umma_commit(bar_tfull + 8 * b);  // hands the group's K = 32 sum to the drain warps
+        umma_commit(bar_tfull + 8 * b);  // hands the group's K = TC_BK sum to the drain warps
       }
       umma_commit(bar_done);
       mbar_wait(bar_done, 0, err, 6);  // every MMA issued above has completed
