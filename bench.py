@@ -286,10 +286,10 @@ def run_ours(args):
                 "algorithmic_flops_per_launch": gemm_f}
     else:
         tf32 = measure_tf32_peak()
-        roof = mixed_roofline(args, w, L, reg, tr.stages, peaks, tf32, kernels["impl"])
+        roof = mixed_roofline(args, w, L, reg, tr.stages, peaks, tf32, kernels["impl"].split("/")[0])
     roof["regions_ms_per_call"] = {k: (v[0] / v[1] if v[1] else None) for k, v in reg.items()}
     if args.precision == "mixed":
-        roof["kernel_roofs"] = kernel_roofs(L, reg, tr.stages, peaks, tf32, kernels["impl"])
+        roof["kernel_roofs"] = kernel_roofs(L, reg, tr.stages, peaks, tf32, kernels["impl"].split("/")[0])
     out = {
         "metric": METRIC, "value": value, "unit": "fs/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,

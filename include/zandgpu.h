@@ -224,17 +224,25 @@ int zg_graph_run(zg_traj* t, int count, zg_attempt_rec* recs, int* nrec, double*
  * zg_set_impl selects one (ZG_EINVAL when the trajectory's shapes do not
  * allow it; the FP64 path ignores it); zg_get_impl reads the current choice
  * and, in *avail, a bit mask of the implementations the trajectory supports.
- * zg_tune times one right-hand side of each supported implementation
- * (CUDA events, `reps` evaluations each, after one untimed evaluation) on the
- * current state, keeps the fastest and returns its index and the
- * milliseconds per evaluation of each (ms[ZG_IMPL_COUNT], -1 where not
- * supported).  It overwrites k slot 0 and drops a captured attempt graph.
+ * The second stream (H(t) sigma, and dOmega/dt unless ZG_IMPL_TC_ALL) forks
+ * off before psi H(t)^T (ZG_SCHED_EARLY) or after it (ZG_SCHED_LATE, the
+ * default): zg_set_schedule / zg_get_schedule.
+ * zg_tune times one right-hand side of every supported implementation under
+ * both schedules (CUDA events, `reps` evaluations each, after one untimed
+ * evaluation) on the current state, keeps the fastest and returns it as
+ * *best = impl + ZG_IMPL_COUNT * schedule, and the milliseconds per
+ * evaluation of each in ms[ZG_IMPL_COUNT * ZG_SCHED_COUNT] (same index, -1
+ * where not supported).  It overwrites k slot 0 and drops a captured attempt
+ * graph.
  * These replace no reference interface: they choose among this library's
  * kernels for the reference's Q_np / Omega stage terms
  * (Zandpack/mpi/zand:91-110,770-809). */
 enum { ZG_IMPL_SIMT = 0, ZG_IMPL_TC_PRODUCTS = 1, ZG_IMPL_TC_ALL = 2, ZG_IMPL_COUNT = 3 };
+enum { ZG_SCHED_LATE = 0, ZG_SCHED_EARLY = 1, ZG_SCHED_COUNT = 2 };
 int zg_set_impl(zg_traj* t, int impl);
 int zg_get_impl(const zg_traj* t, int* impl, int* avail);
+int zg_set_schedule(zg_traj* t, int sched);
+int zg_get_schedule(const zg_traj* t, int* sched);
 int zg_tune(zg_traj* t, int reps, int* best, double* ms);
 
 /* Measurement.  With profiling on, CUDA events on the trajectory's stream

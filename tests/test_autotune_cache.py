@@ -15,6 +15,7 @@ class _FakeTraj:
         self.avail = avail
         self.best = best
         self.impl = _lib.ZG_IMPL_SIMT
+        self.sched = _lib.ZG_SCHED_LATE
         self.tuned = 0
 
     def get_impl(self):
@@ -24,10 +25,13 @@ class _FakeTraj:
         assert i in self.avail
         self.impl = i
 
+    def set_schedule(self, s):
+        self.sched = s
+
     def tune(self, reps=5):
         self.tuned += 1
-        self.impl = self.best
-        return self.best, [1.0 if i in self.avail else None for i in range(_lib.ZG_IMPL_COUNT)]
+        self.impl, self.sched = self.best, _lib.ZG_SCHED_EARLY
+        return (self.best, _lib.ZG_SCHED_EARLY), {(i, s): 1.0 for i in self.avail for s in (0, 1)}
 
 
 def test_measure_once_then_reuse(tmp_path, monkeypatch):
@@ -36,14 +40,15 @@ def test_measure_once_then_reuse(tmp_path, monkeypatch):
     path = str(tmp_path / "tune.json")
     a = _FakeTraj([0, 1, 2], best=2)
     e = autotune.choose(a, path=path)
-    assert e["measured"] and e["impl"] == "tc_all" and a.tuned == 1
+    assert e["measured"] and e["impl"] == "tc_all/early" and a.tuned == 1
     stored = json.load(open(path))
     key = autotune.class_key(a.layout, "mixed", "GB300")
-    assert stored[key]["impl"] == "tc_all"
+    assert stored[key]["impl"] == "tc_all/early"
     monkeypatch.setattr(autotune, "_MEM", {})  # a new process reads the file
     b = _FakeTraj([0, 1, 2], best=0)
     e = autotune.choose(b, path=path)
     assert not e["measured"] and b.tuned == 0 and b.impl == _lib.ZG_IMPL_TC_ALL
+    assert b.sched == _lib.ZG_SCHED_EARLY
     # a class member that cannot run the stored choice is measured again
     c = _FakeTraj([0, 1], best=1)
     e = autotune.choose(c, path=path)

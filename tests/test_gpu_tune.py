@@ -41,10 +41,10 @@ def test_every_implementation_against_oracle(case):
     _, avail = tr.get_impl()
     assert _lib.ZG_IMPL_SIMT in avail and _lib.ZG_IMPL_TC_PRODUCTS in avail
     outs = {}
+    mode = _lib.ZG_DH_HUBBARD if w.hubbard_U is not None else _lib.ZG_DH_NONE
     for impl in avail:
         tr.set_impl(impl)
         tr.stage_input(0)
-        mode = _lib.ZG_DH_HUBBARD if w.hubbard_U is not None else _lib.ZG_DH_NONE
         tr.rhs(0, t, h, delta, mode, w.hubbard_U or 0.0)
         got = L.unpack(tr.get_slot(0))
         for name, g, r, sc in zip(("sigma", "psi", "Omega"), got, ref, scales):
@@ -52,8 +52,15 @@ def test_every_implementation_against_oracle(case):
             print("\n%s %s %s: %.2e" % (case, _lib.IMPL_NAMES[impl], name, err))
             assert err < 2e-5, (case, impl, name, err)
         outs[impl] = tr.get_slot(0)
-    best, ms = tr.tune(3)
-    print("\n%s tuned: %s, ms per RHS %s" % (case, _lib.IMPL_NAMES[best], ms))
-    assert best in avail and all((m is not None) == (i in avail) for i, m in enumerate(ms))
-    assert tr.get_impl()[0] == best
+    for impl in avail:  # the early fork gives the same numbers
+        tr.set_impl(impl)
+        tr.set_schedule(_lib.ZG_SCHED_EARLY)
+        tr.stage_input(0)
+        tr.rhs(0, t, h, delta, mode, w.hubbard_U or 0.0)
+        assert np.array_equal(tr.get_slot(0), outs[impl])
+        tr.set_schedule(_lib.ZG_SCHED_LATE)
+    (best, sched), times = tr.tune(3)
+    print("\n%s tuned: %s/%s, ms per RHS %s" % (case, _lib.IMPL_NAMES[best], _lib.SCHED_NAMES[sched], times))
+    assert best in avail and {i for i, _ in times} == set(avail)
+    assert tr.get_impl()[0] == best and tr.get_schedule() == sched
     tr.close()

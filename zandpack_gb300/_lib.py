@@ -18,6 +18,8 @@ ZG_MAX_LEADS = 16
 ZG_MAX_STAGES = 13
 ZG_IMPL_SIMT, ZG_IMPL_TC_PRODUCTS, ZG_IMPL_TC_ALL, ZG_IMPL_COUNT = 0, 1, 2, 3
 IMPL_NAMES = ["simt", "tc_products", "tc_all"]
+ZG_SCHED_LATE, ZG_SCHED_EARLY, ZG_SCHED_COUNT = 0, 1, 2
+SCHED_NAMES = ["late", "early"]
 PROF_REGIONS = ["gemm", "omega", "final", "combine", "error", "update", "rhs", "prep", "small", "gemm2"]
 
 _NAMES = {ZG_EINVAL: "EINVAL", ZG_ENOMEM: "ENOMEM", ZG_ECUDA: "ECUDA", ZG_ETIMEOUT: "ETIMEOUT",
@@ -105,6 +107,8 @@ _SIGS = {
     "zg_set_impl": ([_P, C.c_int], C.c_int),
     "zg_get_impl": ([_P, C.POINTER(C.c_int), C.POINTER(C.c_int)], C.c_int),
     "zg_tune": ([_P, C.c_int, C.POINTER(C.c_int), _P], C.c_int),
+    "zg_set_schedule": ([_P, C.c_int], C.c_int),
+    "zg_get_schedule": ([_P, C.POINTER(C.c_int)], C.c_int),
     "zg_combine_fermi_skip_c128": ([_P, C.c_int64, C.c_int, _P, _P, C.c_int, _P, _P, _P, _P, _P], C.c_int),
     "zg_outer_subtraction_c128": ([_P, C.c_int, _P, C.c_int, _P, _P, _P, _P], C.c_int),
 }

@@ -3,7 +3,8 @@
 The mixed-precision path can compute its small complex products (the PI
 partials, Omega xi, xi sigma^T) and dOmega/dt with FP32 SIMT kernels, with the
 products on the tensor cores, or with both on the tensor cores in one launch
-(``zg_set_impl``).  Which is fastest depends on the shapes (orbitals n, modes
+(``zg_set_impl``), and fork its second stream before or after psi H^T
+(``zg_set_schedule``).  Which is fastest depends on the shapes (orbitals n, modes
 N, sourced modes Ns, coupling width n_c, leads) and on the GPU, so it is
 measured: ``zg_tune`` times one right-hand side of each, and the winner is
 stored in a JSON file keyed by those shapes and the device name, so that later
@@ -60,23 +61,38 @@ def device_name(device=0):
     return torch.cuda.get_device_name(device).replace("|", "/")
 
 
+def _name(impl, sched):
+    return "%s/%s" % (_lib.IMPL_NAMES[impl], _lib.SCHED_NAMES[sched])
+
+
+def _parse(name):
+    impl, sched = name.split("/")
+    return _lib.IMPL_NAMES.index(impl), _lib.SCHED_NAMES.index(sched)
+
+
 def choose(traj, device=0, reps=5, path=None, retune=False):
-    """Set the trajectory's kernels from the cache, measuring (and storing)
-    the class's choice first when it is not there.  Returns the entry:
-    {"impl": name, "ms": {name: ms per RHS}, "measured": bool}."""
+    """Set the trajectory's kernels and stream schedule from the cache,
+    measuring (and storing) the class's choice first when it is not there.
+    Returns the entry: {"impl": "<kernels>/<schedule>", "ms": {name: ms per
+    RHS}, "measured": bool}."""
     if traj.precision != "mixed":
-        return {"impl": _lib.IMPL_NAMES[_lib.ZG_IMPL_SIMT], "ms": {}, "measured": False}
+        return {"impl": _name(_lib.ZG_IMPL_SIMT, _lib.ZG_SCHED_LATE), "ms": {}, "measured": False}
     path = path or cache_path()
     key = class_key(traj.layout, traj.precision, device_name(device))
     _, avail = traj.get_impl()
     entry = None if retune else (_MEM.get(key) or _load(path).get(key))
-    if entry is not None and _lib.IMPL_NAMES.index(entry["impl"]) in avail:
-        traj.set_impl(_lib.IMPL_NAMES.index(entry["impl"]))
-        _MEM[key] = entry
-        return dict(entry, measured=False)
-    best, ms = traj.tune(reps)
-    entry = {"impl": _lib.IMPL_NAMES[best],
-             "ms": {_lib.IMPL_NAMES[i]: m for i, m in enumerate(ms) if m is not None}}
+    if entry is not None:
+        try:
+            impl, sched = _parse(entry["impl"])
+        except (ValueError, KeyError):
+            impl = -1
+        if impl in avail:
+            traj.set_impl(impl)
+            traj.set_schedule(sched)
+            _MEM[key] = entry
+            return dict(entry, measured=False)
+    (impl, sched), times = traj.tune(reps)
+    entry = {"impl": _name(impl, sched), "ms": {_name(i, s): m for (i, s), m in sorted(times.items())}}
     _MEM[key] = entry
     try:
         _store(path, key, entry)

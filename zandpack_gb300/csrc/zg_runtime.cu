@@ -226,6 +226,7 @@ struct zg_traj {
   TcxBatch* tcx_all = nullptr;  // the products and the Omega derivative
   int tcx_grid_all = 0;
   int prod_impl = 0;            // ZG_IMPL_*: which kernels compute the products and dOmega/dt
+  int sched = 0;                // ZG_SCHED_*: where the second stream forks off
   TcxOperands tcx_ops;
   // the Omega derivative in the same batch (epilogue 1 of zg_tcx.cu): the
   // constant operands U' (embedded) and V (TF32 hi/lo), and the per-stage psi
@@ -1437,15 +1438,22 @@ static int rhs_mixed(zg_traj* t, int stage, const StageParams* p, int dH_mode, d
                              hubbard_U, h_part, t->Hth, t->Htl, t->BSh, t->BSl, t->nonorth ? t->Sm1 : nullptr, d,
                              (const float2*)psih_f, (const float2*)psil_f, np, t->sigC32, t->G32, ml.plane, s, ops));
     prof_end(t, ZG_PROF_PREP);
+    // fork: T = H(t) sigma (tensor cores) and then the Omega derivative run on
+    // the second stream, beside psi H(t)^T and the products (ZG_SCHED_EARLY)
+    // or beside the products alone (ZG_SCHED_LATE)
+    cudaStream_t s2 = t->stream2;
+    if (t->sched == ZG_SCHED_EARLY) {
+      ZG_CHECK_CUDA(cudaEventRecord(t->ev_fork, s));
+      ZG_CHECK_CUDA(cudaStreamWaitEvent(s2, t->ev_fork, 0));
+    }
     // tensor cores: R1 = psi H(t)^T
     prof_begin(t, ZG_PROF_GEMM);
     ZG_TRY(tc_gemm_launch(gR1, s));
     prof_end(t, ZG_PROF_GEMM);
-    // fork: T = H(t) sigma (tensor cores) and then the Omega derivative run on
-    // the second stream, concurrently with the SIMT products below
-    cudaStream_t s2 = t->stream2;
-    ZG_CHECK_CUDA(cudaEventRecord(t->ev_fork, s));
-    ZG_CHECK_CUDA(cudaStreamWaitEvent(s2, t->ev_fork, 0));
+    if (t->sched == ZG_SCHED_LATE) {
+      ZG_CHECK_CUDA(cudaEventRecord(t->ev_fork, s));
+      ZG_CHECK_CUDA(cudaStreamWaitEvent(s2, t->ev_fork, 0));
+    }
     prof_begin(t, ZG_PROF_GEMM2, s2);
     ZG_TRY(tc_gemm_launch(gT, s2));
     prof_end(t, ZG_PROF_GEMM2, s2);
@@ -2033,6 +2041,22 @@ int zg_set_impl(zg_traj* t, int impl) {
   return ZG_OK;
 }
 
+int zg_set_schedule(zg_traj* t, int sched) {
+  ZG_REQUIRE(t, "null argument");
+  ZG_REQUIRE(sched == ZG_SCHED_LATE || sched == ZG_SCHED_EARLY, "schedule %d", sched);
+  if (t->sched != sched) {
+    drop_graph(t);
+    t->sched = sched;
+  }
+  return ZG_OK;
+}
+
+int zg_get_schedule(const zg_traj* t, int* sched) {
+  ZG_REQUIRE(t && sched, "null argument");
+  *sched = t->sched;
+  return ZG_OK;
+}
+
 int zg_get_impl(const zg_traj* t, int* impl, int* avail) {
   ZG_REQUIRE(t, "null argument");
   if (impl) *impl = t->prod_impl;
@@ -2045,11 +2069,12 @@ int zg_tune(zg_traj* t, int reps, int* best, double* ms) {
   ZG_REQUIRE(!t->capturing, "zg_tune during graph capture");
   ZG_CHECK_CUDA(cudaSetDevice(t->dev));
   const int mask = impl_mask(t);
-  double times[ZG_IMPL_COUNT];
-  for (int i = 0; i < ZG_IMPL_COUNT; ++i) times[i] = -1.0;
+  constexpr int NV = ZG_IMPL_COUNT * ZG_SCHED_COUNT;
+  double times[NV];
+  for (int i = 0; i < NV; ++i) times[i] = -1.0;
   if (t->precision != ZG_PREC_MIXED) {
-    if (best) *best = t->prod_impl;
-    if (ms) for (int i = 0; i < ZG_IMPL_COUNT; ++i) ms[i] = times[i];
+    if (best) *best = t->prod_impl + ZG_IMPL_COUNT * t->sched;
+    if (ms) for (int i = 0; i < NV; ++i) ms[i] = times[i];
     return ZG_OK;
   }
   StageParams p;
@@ -2060,11 +2085,13 @@ int zg_tune(zg_traj* t, int reps, int* best, double* ms) {
   ZG_CHECK_CUDA(cudaEventCreate(&e0));
   ZG_CHECK_CUDA(cudaEventCreate(&e1));
   int st = ZG_OK;
-  int choice = t->prod_impl;
+  int choice = t->prod_impl + ZG_IMPL_COUNT * t->sched;
   double tbest = 1e300;
-  for (int impl = 0; impl < ZG_IMPL_COUNT && st == ZG_OK; ++impl) {
+  for (int v = 0; v < NV && st == ZG_OK; ++v) {
+    const int impl = v % ZG_IMPL_COUNT, sched = v / ZG_IMPL_COUNT;
     if (!(mask >> impl & 1)) continue;
     st = zg_set_impl(t, impl);
+    if (st == ZG_OK) st = zg_set_schedule(t, sched);
     if (st == ZG_OK) st = zg_stage_input(t, 0);
     if (st == ZG_OK) st = launch_set_params(p, t->d_params, t->stream);
     if (st == ZG_OK) st = rhs_mixed(t, 0, t->d_params, ZG_DH_NONE, 0.0, false);  // untimed
@@ -2079,18 +2106,19 @@ int zg_tune(zg_traj* t, int reps, int* best, double* ms) {
     }
     float el = 0.f;
     cudaEventElapsedTime(&el, e0, e1);
-    times[impl] = el / reps;
-    if (times[impl] < tbest) {
-      tbest = times[impl];
-      choice = impl;
+    times[v] = el / reps;
+    if (times[v] < tbest) {
+      tbest = times[v];
+      choice = v;
     }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (st != ZG_OK) return st;
-  ZG_TRY(zg_set_impl(t, choice));
+  ZG_TRY(zg_set_impl(t, choice % ZG_IMPL_COUNT));
+  ZG_TRY(zg_set_schedule(t, choice / ZG_IMPL_COUNT));
   if (best) *best = choice;
-  if (ms) for (int i = 0; i < ZG_IMPL_COUNT; ++i) ms[i] = times[i];
+  if (ms) for (int i = 0; i < NV; ++i) ms[i] = times[i];
   return ZG_OK;
 }
 

@@ -179,14 +179,27 @@ class Trajectory:
         check(lib().zg_get_impl(self._h, C.byref(impl), C.byref(avail)))
         return impl.value, [i for i in range(_lib.ZG_IMPL_COUNT) if avail.value >> i & 1]
 
+    def set_schedule(self, sched):
+        """Where the second stream forks off: ``_lib.ZG_SCHED_*`` (``zg_set_schedule``)."""
+        check(lib().zg_set_schedule(self._h, int(sched)))
+
+    def get_schedule(self):
+        v = C.c_int()
+        check(lib().zg_get_schedule(self._h, C.byref(v)))
+        return v.value
+
     def tune(self, reps=5):
-        """Time one right-hand side of every supported implementation and keep
-        the fastest (``zg_tune``); returns (choice, ms per RHS per implementation,
-        None where unsupported).  Overwrites k slot 0."""
+        """Time one right-hand side of every supported implementation under both
+        stream schedules and keep the fastest (``zg_tune``); returns
+        ((impl, schedule), {(impl, schedule): ms per RHS}) over the supported ones.
+        Overwrites k slot 0."""
         best = C.c_int()
-        ms = np.zeros(_lib.ZG_IMPL_COUNT)
+        nv = _lib.ZG_IMPL_COUNT * _lib.ZG_SCHED_COUNT
+        ms = np.zeros(nv)
         check(lib().zg_tune(self._h, int(reps), C.byref(best), _ptr(ms)))
-        return best.value, [None if m < 0 else float(m) for m in ms]
+        n = _lib.ZG_IMPL_COUNT
+        times = {(v % n, v // n): float(ms[v]) for v in range(nv) if ms[v] >= 0}
+        return (best.value % n, best.value // n), times
 
     def error_norm2(self):
         e = np.zeros(3)
