@@ -318,7 +318,8 @@ def run_ours(args):
             out["ensemble"] = run_ensemble(args)
         if args.steady:
             out["steady_state"] = run_steady(args)
-        out["cpu_baseline"] = cpu_baseline(args, w, adv_total / (args.steps * ws))
+        if args.cpu:
+            out["cpu_baseline"] = cpu_baseline(args, w, adv_total / (args.steps * ws))
         print(json.dumps(out))
     if ws > 1:
         torch.distributed.destroy_process_group()
@@ -715,6 +716,8 @@ def main():
     ap.add_argument("--ensemble-fs", default="pulse",
                     help="simulated span per ensemble trajectory: 'pulse' (its pulse centre + 3 widths) or fs")
     ap.add_argument("--slots", type=int, default=32, help="concurrent trajectories of the ensemble")
+    ap.add_argument("--cpu", type=int, default=1,
+                    help="time the CPU baseline (the oracle port; 0 for workloads too large for host memory, c5)")
     ap.add_argument("--capacity", action="store_true",
                     help="also serve the ensemble with every request present at t = 0")
     ap.add_argument("--prep-workers", type=int, default=max(1, min(12, (os.cpu_count() or 4) - 4)),
