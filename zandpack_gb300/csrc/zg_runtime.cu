@@ -757,11 +757,17 @@ static int build_tcx(zg_traj* t, const zg_layout* Lo, const std::vector<double2>
     for (TcxProb& P : probs) {
       P.kchunk = P.epi == 1 ? P.K : std::min(P.K, 32 * chunk_kb);  // Omega blocks: whole K per tile
       P.nsplit = (P.K + P.kchunk - 1) / P.kchunk;
-      items += P.tiles_m * P.tiles_n * P.nsplit;
+      if (P.epi == 0) items += P.tiles_m * P.tiles_n * P.nsplit;
     }
     if (items <= ZG_TCX_ITEMS) break;
     if (chunk_kb >= 1024) return ZG_OK;  // too many tiles for the item table: the SIMT kernels run
     chunk_kb *= 2;
+  }
+  // the batch with the Omega blocks too needs its items in the table as well
+  if (omega_tc) {
+    int all = 0;
+    for (const TcxProb& P : probs) all += P.tiles_m * P.tiles_n * P.nsplit;
+    if (all > ZG_TCX_ITEMS) omega_tc = false;
   }
   // split-K scratch and slice counters of the products (shared by both batches)
   int64_t ws_need = 0, cnt_need = 0;

@@ -42,7 +42,7 @@ struct TcxProb {
   int om_map, om_x0, om_y0;
 };
 
-#define ZG_TCX_ITEMS 3072
+#define ZG_TCX_ITEMS 6144
 #define ZG_TCX_GRID 160
 
 struct TcxBatch {
