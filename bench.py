@@ -328,7 +328,7 @@ def run_ours(args):
 def mixed_roofline(args, w, L, reg, stages, peaks, tf32, impl):
     """Roofline of the region that takes the most time per right-hand side,
     against MEASURED_PEAKS.json: the psi H^T tensor-core GEMM on algorithmic
-    flops (8 N n^2, SURVEY's count for a dense complex H(t)) against the bf16
+    flops (8 N n^2, the count for a dense complex H(t)) against the bf16
     burst peak; the streaming regions on algorithmic bytes against the
     measured HBM copy rate."""
     pk = _peaks_file()

@@ -43,7 +43,7 @@ CASES = {
     # name: (t1, initial stepsize, attempts whose stages are kept, keep_every)
     # the large initial steps of the small cases force rejected attempts
     "c1": (1.0, 0.01, (0, 7), 4),
-    # BASELINE config 1 over its full span, 0-50 fs (sigma kept every 40th step)
+    # the n=20 chain over its full span, 0-50 fs (sigma kept every 40th step)
     "c1_50fs": (50.0, 0.01, (0,), 40),
     "mini2": (2.0, 0.3, (0, 1, 12), 1),
     "mini3": (1.0, 0.3, (0, 1, 9), 1),

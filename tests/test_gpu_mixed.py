@@ -207,7 +207,7 @@ def test_h_operands_after_a_full_dH_matrix():
 
 
 def test_mixed_c1_full_span_on_reference_grid():
-    """BASELINE config 1 over 0-50 fs on the reference's own time grid (its
+    """The n=20 chain over 0-50 fs on the reference's own time grid (its
     5414 step sizes replayed): the mixed-precision path stays within 1e-6 of
     the unmodified ``zand`` in sigma and in the lead currents at every step,
     the final time included."""

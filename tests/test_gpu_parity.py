@@ -155,7 +155,7 @@ def test_array_kernels(count):
 
 
 def test_c1_full_span_matches_reference():
-    """BASELINE config 1 over its whole span, 0-50 fs: the unmodified ``zand``
+    """The n=20 chain over its whole span, 0-50 fs: the unmodified ``zand``
     took 5414 attempts (``c1_50fs``).  The FP64 device path must take the same
     attempts with the same accept decisions, land on the same time grid, and
     give the reference's sigma (every 40th step and the last) and currents."""

@@ -75,7 +75,7 @@ def test_tableau_identities():
 
 
 def test_c1_full_span_prefix():
-    """BASELINE config 1 over 0-50 fs (``c1_50fs``: 5414 attempts of the
+    """The n=20 chain over 0-50 fs (``c1_50fs``: 5414 attempts of the
     unmodified ``zand``): the oracle reproduces the first 300 attempts' error
     norms and accept decisions and the stage derivatives of attempt 0 (the
     whole span runs on the GPU in ``tests/test_gpu_parity.py``)."""

@@ -21,39 +21,37 @@ from .arrays_io import flexload
 __all__ = ["natural_keys", "combine_currents", "rectified_charge", "combine_dm", "herm_insert_tril", "combine_pi"]
 
 
-def atoi(text):
-    return int(text) if text.isdigit() else text
-
-
 def natural_keys(text):
     """Sort key: the digit groups of ``text`` compared as integers
     (Zandpack/mpi_tools.py:13-17)."""
-    return [atoi(c) for c in re.split(r"(\d+)", text)]
+    return [int(part) if part.isdigit() else part for part in re.split(r"(\d+)", text)]
 
 
-def _sorted(d, pred):
-    return sorted((v for v in os.listdir(d) if pred(v)), key=natural_keys)
+def _step_files(d, keep):
+    """The names in directory ``d`` for which ``keep(name)`` holds, in natural order."""
+    return sorted(filter(keep, os.listdir(d)), key=natural_keys)
+
+
+def _read_all(d, names, load=np.load):
+    return [load(os.path.join(d, name)) for name in names]
 
 
 def combine_currents(dirs, n=2):
     """(T, [J_0, ..., J_{n-1}]) over the save directories ``dirs``
     (Zandpack/mpi_tools.py:19-49): every ``current_<lead>_<step>`` file of a
-    lead stacked in natural order, the ``times*`` files concatenated with the
-    last entry of each directory dropped (the time after the last step)."""
-    C = [[] for _ in range(n)]
-    T = []
-    count = 0
+    lead stacked in natural order, and the ``times*`` files concatenated with
+    as many trailing entries dropped as there are directories (the time after
+    the last step), as the reference does."""
+    leads = [[] for _ in range(n)]
+    times = []
     for d in dirs:
-        for ff in _sorted(d, lambda v: "current_" in v):
-            vals = ff.split("_")
-            if len(vals) != 2:
-                C[int(vals[1])].append(flexload(os.path.join(d, ff)))
-        for ff in _sorted(d, lambda v: "times" in v):
-            T.append(np.load(os.path.join(d, ff)))
-        count += 1
-    CC = [np.vstack(C[i]) for i in range(n)]
-    T = np.hstack(T)[:-count]
-    return T, CC
+        for name in _step_files(d, lambda v: "current_" in v):
+            fields = name.split("_")
+            if len(fields) != 2:  # current_<lead>_<step>
+                leads[int(fields[1])].append(flexload(os.path.join(d, name)))
+        times.extend(_read_all(d, _step_files(d, lambda v: "times" in v)))
+    T = np.hstack(times)
+    return T[:T.shape[0] - len(dirs)], [np.vstack(rows) for rows in leads]
 
 
 def rectified_charge(dirs, n=2, wgts=(0.5, -0.5), idx=0):
@@ -99,42 +97,33 @@ def combine_dm(dirs, times_label="DMt", insert_tril=False, split=None, split_ran
     ``lossy_dm_arc`` the archive itself is returned.  ``insert_tril`` restores
     the lower triangle of ``dm_triu_only`` files; ``split``/``split_rank``
     read one of ``split`` contiguous shares of the files."""
-    DM, T = [], []
+    mats, times = [], []
     for d in dirs:
-        names = os.listdir(d)
-        arc = _lossy_archive(d, names)
-        files = _sorted(d, lambda v: "DM" in v and "DMt" not in v)
-        if not (len(files) > 0 and prefer_full):
+        dm_names = _step_files(d, lambda v: "DM" in v and "DMt" not in v)
+        if not dm_names or not prefer_full:
+            archive = _lossy_archive(d, os.listdir(d))
             if lossy_dm_arc:
-                return arc
-            dm = arc["dm"].transpose(3, 0, 1, 2).copy()
-            if insert_tril:
-                herm_insert_tril(dm)
-            return arc["tdm"], dm
-        tfiles = _sorted(d, lambda v: times_label in v)
+                return archive
+            dm = archive["dm"].transpose(3, 0, 1, 2).copy()
+            return archive["tdm"], herm_insert_tril(dm) if insert_tril else dm
+        t_names = _step_files(d, lambda v: times_label in v)
         if split is not None and split_rank is not None:
-            assert split < len(files)
-            idx = np.array_split(np.arange(len(files)), split)[split_rank]
-            files = [files[i] for i in idx]
-            tfiles = [tfiles[i] for i in idx]
-        for ff in files:
-            dm = flexload(os.path.join(d, ff))
-            if insert_tril:
-                herm_insert_tril(dm)
-            DM.append(dm)
-        for ff in tfiles:
-            T.append(np.load(os.path.join(d, ff)))
-    return np.hstack(T), np.vstack(DM)
+            assert split < len(dm_names)
+            share = np.array_split(np.arange(len(dm_names)), split)[split_rank]
+            dm_names = [dm_names[i] for i in share]
+            t_names = [t_names[i] for i in share]
+        for dm in _read_all(d, dm_names, flexload):
+            mats.append(herm_insert_tril(dm) if insert_tril else dm)
+        times.extend(_read_all(d, t_names))
+    return np.hstack(times), np.vstack(mats)
 
 
 def combine_pi(dirs, times_label="DMt"):
     """(T, PI): the saved ``PIa`` arrays and time files of ``dirs``
     (Zandpack/mpi_tools.py:120-144); ``.npz`` archives (``compress_mat``) are
     read as well."""
-    DM, T = [], []
+    pis, times = [], []
     for d in dirs:
-        for ff in _sorted(d, lambda v: "PIa" in v):
-            DM.append(flexload(os.path.join(d, ff)))
-        for ff in _sorted(d, lambda v: times_label in v):
-            T.append(np.load(os.path.join(d, ff)))
-    return np.hstack(T), np.vstack(DM)
+        pis.extend(_read_all(d, _step_files(d, lambda v: "PIa" in v), flexload))
+        times.extend(_read_all(d, _step_files(d, lambda v: times_label in v)))
+    return np.hstack(times), np.vstack(pis)
