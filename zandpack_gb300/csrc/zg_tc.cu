@@ -25,9 +25,12 @@
 //     (tcgen05.ld 32x32b; warp w takes TMEM lane quarter w % 4 and the 64
 //     columns w / 4), add it into FP32 registers and release the buffer.
 // The tensor core truncates inside its accumulation, so a single accumulator
-// over K = 2048 drifts by ~1e-5 relative; per-group partials (TC_BK = 64
-// floats) summed with round-to-nearest keep the product within 2e-6 (groups of
-// 32 measured 2.5% slower at n = 1024 for no accuracy the tests need).
+// over K = 2048 drifts by ~1e-5 relative; per-group partials (TC_BK = 32
+// floats) summed with round-to-nearest keep the product within 2e-6.  Groups
+// of 64 are 2.5% faster at n = 1024, but their truncation bias accumulates
+// along a trajectory: over 10 fs of the n = 1024 lattice (269 steps) the
+// mixed path's sigma drifts from the FP64 one by 3.1e-7 and its currents by
+// 1.5e-6, against 1.8e-7 and 6.1e-7 with groups of 32.
 // Every wait on an mbarrier is bounded by a clock64 budget; on timeout the
 // thread records an error code in *err and stops issuing, the MMA thread
 // waits for its own MMAs, the producer for its copies in flight, and TMEM is

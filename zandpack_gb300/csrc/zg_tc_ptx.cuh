@@ -10,7 +10,7 @@
 namespace zg {
 
 #define TC_BM 128
-#define TC_BK 64  // K floats accumulated alone in TMEM before the drain adds them
+#define TC_BK 32  // K floats accumulated alone in TMEM before the drain adds them
 #define TC_WAIT_CYCLES (4LL * 1000 * 1000 * 1000)  // ~2 s at 2 GHz
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {

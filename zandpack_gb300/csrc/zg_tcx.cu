@@ -168,6 +168,17 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
   if (warp == 0) {
     if (lane == 0) {
       // ---------------- TMA producer
+      // the descriptors of every map the problems read, into the descriptor cache
+      for (int i = 0; i < batch.nprob; ++i) {
+        const TcxProb& P = batch.p[i];
+        const int ids[7] = {P.mapA, P.mapB, P.kseg < P.K ? P.mapA2 : -1, P.kseg < P.K ? P.mapB2 : -1, P.om_map, -1, -1};
+        for (int j = 0; j < 5; ++j) {
+          if (ids[j] < 0 || ids[j] + 1 >= ZG_TCX_MAPS + 1) continue;
+          asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&batch.maps[ids[j]]) : "memory");
+          if (j < 4 && ids[j] + 1 < ZG_TCX_MAPS)
+            asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&batch.maps[ids[j] + 1]) : "memory");
+        }
+      }
       int issued[STAGES];
       for (int s = 0; s < STAGES; ++s) issued[s] = 0;
       bool ok = true;
@@ -381,7 +392,13 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
       const int row = it.tm * 128 + row_in_tile;
       const int col0 = it.tn * BN + part * C::DCOLS;
       if constexpr (C::STAGED) {
-        if (P.epi == 1 || P.nsplit == 1) {
+        {
+          // split K: this item's partial tile goes to its slot of the scratch
+          // (row-major 128 x BN), written through the staging like the result
+          const int tile = it.tm * P.tiles_n + it.tn;
+          const bool part_out = P.epi == 0 && P.nsplit > 1;
+          float* ws_tile = part_out ? P.ws + (long long)tile * P.nsplit * (128 * BN) : nullptr;
+          float* ws_mine = part_out ? ws_tile + (long long)it.split * (128 * BN) : nullptr;
           // 32 columns at a time through the warp's staging tile: lane r writes
           // its row, then each pass stores two rows of 16 complex columns
           float* stg = reinterpret_cast<float*>(smem + C::STG_OFF) + dw * C::STG_WARP_FLOATS;
@@ -439,6 +456,9 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
                   const float2 dd = make_float2(dx.x * om.x - dx.y * om.y, dx.x * om.y + dx.y * om.x);
                   batch.om_out_base[P.om_out_off + (long long)r * P.ld_om + col] =
                       make_float2(v.x * fh - fhh * dd.y, v.y * fh + fhh * dd.x);
+                } else if (part_out) {
+                  __stcg(reinterpret_cast<float2*>(ws_mine + (quarter * 32 + rr) * BN + 2 * (col - it.tn * (BN / 2))),
+                         v);
                 } else {
                   *reinterpret_cast<float2*>(P.D + (long long)r * P.ldd + 2 * col) = v;
                 }
@@ -449,6 +469,42 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
           if (omt) {
             mbar_arrive(bar_omt_empty);
             ++nom;
+          }
+          if (part_out) {
+            // the warp that completes this 32-row slice last (one counter per
+            // slice; one release fence before the count, one acquire after)
+            // adds the partials in split order and writes the result
+            const int slice = tile * NDW + dw;
+            __syncwarp();
+            int prev = 0;
+            if (lane == 0) {
+              __threadfence();
+              prev = atomicAdd(P.counters + slice, 1);
+              if (prev == P.nsplit - 1) __threadfence();
+            }
+            prev = __shfl_sync(0xffffffffu, prev, 0);
+            if (prev == P.nsplit - 1) {
+#pragma unroll
+              for (int ch = 0; ch < C::DCOLS / 32; ++ch) {
+                const int col = (col0 >> 1) + ch * 16 + cs;
+                const int lc = 2 * (col - it.tn * (BN / 2));
+#pragma unroll 2
+                for (int itr = 0; itr < 16; ++itr) {
+                  const int rr = itr * 2 + rs;
+                  const int r = it.tm * 128 + quarter * 32 + rr;
+                  const float* src = ws_tile + (quarter * 32 + rr) * BN + lc;
+                  float2 sum = __ldcg(reinterpret_cast<const float2*>(src));
+                  for (int sp = 1; sp < P.nsplit; ++sp) {
+                    const float2 q = __ldcg(reinterpret_cast<const float2*>(src + (long long)sp * (128 * BN)));
+                    sum.x += q.x;
+                    sum.y += q.y;
+                  }
+                  if (r < P.M && 2 * col < P.Nv) *reinterpret_cast<float2*>(P.D + (long long)r * P.ldd + 2 * col) = sum;
+                }
+              }
+              __syncwarp();
+              if (lane == 0) P.counters[slice] = 0;  // ready for the next launch
+            }
           }
           continue;
         }
@@ -499,13 +555,15 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
 #pragma unroll
       for (int i = 0; i < C::DCOLS; i += 4)
         __stcg(reinterpret_cast<float4*>(wsp + i), make_float4(acc[i], acc[i + 1], acc[i + 2], acc[i + 3]));
-      __threadfence();
       __syncwarp();
       int prev = 0;
-      if (lane == 0) prev = atomicAdd(P.counters + slice, 1);
+      if (lane == 0) {
+        __threadfence();
+        prev = atomicAdd(P.counters + slice, 1);
+        if (prev == P.nsplit - 1) __threadfence();
+      }
       prev = __shfl_sync(0xffffffffu, prev, 0);
       if (prev == P.nsplit - 1) {
-        __threadfence();
         if (row < P.M) {
           // every load of one partial slice in flight at once
           const float* src = P.ws + tile_ws + my;
