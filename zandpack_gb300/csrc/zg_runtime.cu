@@ -224,6 +224,7 @@ struct zg_traj {
   bool tcx_on = false;
   TcxBatch* tcx = nullptr;      // the products alone
   TcxBatch* tcx_all = nullptr;  // the products and the Omega derivative
+  int* tcx_claim = nullptr;     // item claim counters of the two batches
   int tcx_grid_all = 0;
   int prod_impl = 0;            // ZG_IMPL_*: which kernels compute the products and dOmega/dt
   int sched = 0;                // ZG_SCHED_*: where the second stream forks off
@@ -406,7 +407,7 @@ static void free_traj(zg_traj* t) {
                   t->st_V, t->st_Vc, t->st_W, t->st_lam, t->st_delta,
                   t->Sm1, t->Hn0, t->dHn, t->SmR, t->SmT, t->C0, t->Qcat, t->Wn, t->Zcat, t->R3,
                   t->SmR32, t->SmT32, t->C0_32, t->Qcat32, t->Wn32, t->Zcat32, t->R3_32,
-                  t->tcxBh, t->tcxBl, t->XIh, t->XIl, t->sigEh, t->sigEl, t->tcx_ws, t->tcx_cnt,
+                  t->tcxBh, t->tcxBl, t->XIh, t->XIl, t->sigEh, t->sigEl, t->tcx_ws, t->tcx_cnt, t->tcx_claim,
                   t->Uh, t->Ul, t->Vh, t->Vl, t->Gth, t->Gtl, t->Gch, t->Gcl};
   for (void* p : ptrs) dfree(t, p);
   delete t->tcx;
@@ -797,50 +798,47 @@ static int build_tcx(zg_traj* t, const zg_layout* Lo, const std::vector<double2>
   B->err = t->tc_err;
   // one batch with the products alone, one with the products and the Omega
   // blocks: the problem list, item numbering and the longest-first item lists
-  auto finish = [&](TcxBatch& Bt, bool with_omega, int* grid_used) -> int {
+  // CTAs claim items at run time, most expensive first; the estimate is the
+  // item's traffic through shared memory in KB: per K block the A tile (raw
+  // FP32 Omega: 16 KB; hi and lo parts or the four psi planes: 32 KB) and B'
+  // hi and lo (bn / 4 KB), then the stored tile (bn / 2 KB) and, for split
+  // K, the partial re-read by the reduction, for an Omega tile its block of
+  // Omega_in
+  auto item_cost = [&](const TcxProb& P, int split) -> int64_t {
+    const int64_t nkb = std::min(P.kchunk, P.K - split * P.kchunk) / 32;
+    const int64_t tile = bn / 2;
+    return nkb * ((P.amode == 1 ? 16 : 32) + bn / 4) + tile * (1 + (P.nsplit > 1) + (P.epi == 1));
+  };
+  // two claim counters per batch, zero between launches
+  ZG_TRY(dalloc(t, &t->tcx_claim, 4));
+  ZG_CHECK_CUDA(cudaMemsetAsync(t->tcx_claim, 0, 4 * sizeof(int), s));
+  auto finish = [&](TcxBatch& Bt, bool with_omega, int* claim, int* grid_used) -> int {
     int np_ = 0, items = 0;
-    std::vector<int> item_kb;
+    std::vector<int64_t> cost;
     for (const TcxProb& P0 : probs) {
       if (P0.epi == 1 && !with_omega) continue;
       TcxProb P = P0;
       P.item_begin = items;
       items += P.tiles_m * P.tiles_n * P.nsplit;
-      for (int w = 0; w < P.tiles_m * P.tiles_n * P.nsplit; ++w) {
-        const int split = w % P.nsplit;
-        // an Omega tile also moves its block of Omega in and out (about two K blocks)
-        item_kb.push_back(std::min(P.kchunk, P.K - split * P.kchunk) / 32 + (P.epi == 1 ? 2 : 0));
-      }
+      for (int w = 0; w < P.tiles_m * P.tiles_n * P.nsplit; ++w) cost.push_back(item_cost(P, w % P.nsplit));
       Bt.p[np_++] = P;
     }
     Bt.nprob = np_;
     Bt.nitems = items;
     std::vector<int> order(items);
     for (int i = 0; i < items; ++i) order[i] = i;
-    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return item_kb[x] > item_kb[y]; });
-    std::vector<int64_t> load(grid, 0);
-    std::vector<std::vector<int>> per(grid);
-    for (int w : order) {
-      int c = (int)(std::min_element(load.begin(), load.end()) - load.begin());
-      load[c] += item_kb[w] + 2;  // + the item's epilogue
-      per[c].push_back(w);
-    }
-    int used = 0, pos = 0;
-    for (int c = 0; c < grid; ++c) {
-      if (per[c].empty()) continue;
-      Bt.cta_off[used++] = (unsigned short)pos;
-      for (int w : per[c]) Bt.items[pos++] = (unsigned short)w;
-    }
-    Bt.cta_off[used] = (unsigned short)pos;
-    for (int c = used + 1; c <= ZG_TCX_GRID; ++c) Bt.cta_off[c] = 0;
-    *grid_used = used;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cost[x] > cost[y]; });
+    for (int i = 0; i < items; ++i) Bt.items[i] = (unsigned short)order[i];
+    Bt.claim = claim;
+    *grid_used = std::min(grid, items);
     return tcx_validate(Bt);
   };
   std::unique_ptr<TcxBatch> Bm;
   if (omega_tc) {
     Bm.reset(new TcxBatch(*B));
-    ZG_TRY(finish(*Bm, true, &t->tcx_grid_all));
+    ZG_TRY(finish(*Bm, true, t->tcx_claim + 2, &t->tcx_grid_all));
   }
-  ZG_TRY(finish(*B, false, &t->tcx_grid));
+  ZG_TRY(finish(*B, false, t->tcx_claim, &t->tcx_grid));
   t->tcx = B.release();
   t->tcx_all = Bm.release();
   t->tcx_on = true;

@@ -26,8 +26,11 @@
 // B' always arrives pre-split (constants, or built by the stage's operand
 // kernel).
 //
-// One persistent CTA per SM walks its list of work items (problem, 128-row
-// tile, BN-column tile, K chunk), assigned longest first on the host.  Warp roles:
+// One persistent CTA per SM claims work items (problem, 128-row tile,
+// BN-column tile, K chunk) from a global counter, most expensive first, so
+// that the CTAs finish together whatever the items cost; the producer claims
+// and passes each item to the other roles through a small queue in shared
+// memory.  Warp roles:
 //   warp 0      one thread: TMA loads into a 2-stage ring;
 //   warp 1      one thread: tcgen05.mma issue, owns the TMEM allocation;
 //   warps 2-5   converters (forms 1 and 2; form 0 passes through);
@@ -37,6 +40,8 @@
 // fixed order and writes the result, so results are deterministic.  Waits on mbarriers are bounded like
 // those of the 3xTF32 GEMM (zg_tc.cu): on timeout the error code is recorded,
 // in-flight copies and MMAs are waited for (bounded) and TMEM is freed.
+#include <vector>
+
 #include "zg_tc_ptx.cuh"
 #include "zg_tcx.cuh"
 
@@ -62,8 +67,12 @@ struct TcxCfg {
   static constexpr int STG_BYTES = NDW * STG_WARP_FLOATS * 4;
   static constexpr int OMT_BYTES = 128 * BN * 4;
   static constexpr int LIMIT = 232448 - 1024;  // dynamic shared memory less the alignment slack
+  // barriers (first 256 bytes), then the item queue: QLEN "full" and "empty"
+  // barriers and the item numbers
+  static constexpr int BAR_AREA = 512;
+  static constexpr int QLEN = 8;
   static constexpr int fit(int stages, bool stg, bool omt) {
-    return stages * STAGE_BYTES + 256 + (stg ? STG_BYTES : 0) + (omt ? OMT_BYTES : 0) <= LIMIT;
+    return stages * STAGE_BYTES + BAR_AREA + (stg ? STG_BYTES : 0) + (omt ? OMT_BYTES : 0) <= LIMIT;
   }
   // the deepest ring that fits with staging and the Omega tile, else with
   // staging alone, else two stages with what fits
@@ -71,7 +80,7 @@ struct TcxCfg {
   static constexpr bool STAGED = fit(STAGES, true, false);
   static constexpr bool HAS_OMT = STAGED && fit(STAGES, true, true);
   static constexpr int BAR_OFF = STAGES * STAGE_BYTES;
-  static constexpr int STG_OFF = BAR_OFF + 256;
+  static constexpr int STG_OFF = BAR_OFF + BAR_AREA;
   static constexpr int OMT_OFF = STG_OFF + (STAGED ? STG_BYTES : 0);
   static constexpr int SMEM = OMT_OFF + (HAS_OMT ? OMT_BYTES : 0) + 1024;
   static constexpr uint32_t TMEM_COLS = NACC * BN <= 256 ? (NACC * BN <= 128 ? 128 : 256) : 512;
@@ -133,6 +142,9 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
   const uint32_t bar_omt_full = sbase + C::BAR_OFF + 192;   // the Omega tile landed
   const uint32_t bar_omt_empty = sbase + C::BAR_OFF + 200;  // the drain warps read it
   const uint32_t bar_cread = sbase + C::BAR_OFF + 208;      // converters read a form-2 stage
+  const uint32_t bar_qfull = sbase + C::BAR_OFF + 256;      // QLEN: the producer wrote an item number
+  const uint32_t bar_qempty = bar_qfull + 8 * C::QLEN;      // QLEN: every role read it
+  volatile int* q_ids = reinterpret_cast<volatile int*>(smem + C::BAR_OFF + 256 + 16 * C::QLEN);
   uint32_t* tmem_slot = (uint32_t*)(smem + C::BAR_OFF + 24 * STAGES + 16 * NACC + 8);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int* err = batch.err;
@@ -151,6 +163,10 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
     mbar_init(bar_omt_full, 1);
     mbar_init(bar_omt_empty, 32 * NDW);
     mbar_init(bar_cread, 32 * C::NCONV);
+    for (int q = 0; q < C::QLEN; ++q) {
+      mbar_init(bar_qfull + 8 * q, 1);
+      mbar_init(bar_qempty + 8 * q, 1 + C::NCONV + NDW);  // MMA thread, lane 0 of each warp
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
@@ -163,7 +179,6 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
-  const int wbeg = batch.cta_off[blockIdx.x], wend = batch.cta_off[blockIdx.x + 1];
 
   if (warp == 0) {
     if (lane == 0) {
@@ -183,8 +198,19 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
       for (int s = 0; s < STAGES; ++s) issued[s] = 0;
       bool ok = true;
       int kb_global = 0;
-      for (int wi = wbeg; wi < wend && ok; ++wi) {
-        const int w = batch.items[wi];
+      // items are claimed one ahead: the claim of the next item (an atomic
+      // round trip) runs while this item's loads are issued
+      int idx = atomicAdd(batch.claim, 1);
+      for (int seq = 0; ok; ++seq) {
+        // pass the claimed item on once the queue has room (-1: none left)
+        const int slot = seq % C::QLEN;
+        ok = mbar_wait(bar_qempty + 8 * slot, ((uint32_t)(seq / C::QLEN) & 1u) ^ 1u, err, 22);
+        if (!ok) break;
+        const int w = idx < batch.nitems ? (int)batch.items[idx] : -1;
+        if (w >= 0) idx = atomicAdd(batch.claim, 1);
+        q_ids[slot] = w;
+        mbar_arrive(bar_qfull + 8 * slot);
+        if (w < 0) break;
         const TcxItem it = tcx_item(batch, w);
         const TcxProb& P = batch.p[it.prob];
         int kb0, nkb;
@@ -231,6 +257,14 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
         for (int s = 0; s < STAGES; ++s)
           if (issued[s] > 0) mbar_wait(bar_full + 8 * s, (uint32_t)(issued[s] - 1) & 1u, err, 14);
       }
+      // this CTA claims no more; the last CTA to get here zeroes the counters
+      // for the next launch (every claim of every CTA precedes its count)
+      __threadfence();
+      if (atomicAdd(batch.claim + 1, 1) == (int)gridDim.x - 1) {
+        __threadfence();
+        atomicExch(batch.claim, 0);
+        atomicExch(batch.claim + 1, 0);
+      }
     }
   } else if (warp == 1) {
     if (lane == 0) {
@@ -238,8 +272,13 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
       constexpr uint32_t idesc = idesc_tf32(128, BN);
       bool ok = true;
       int kb_global = 0;
-      for (int wi = wbeg; wi < wend && ok; ++wi) {
-        const int w = batch.items[wi];
+      for (int seq = 0; ok; ++seq) {
+        const int slot = seq % C::QLEN;
+        ok = mbar_wait(bar_qfull + 8 * slot, (uint32_t)(seq / C::QLEN) & 1u, err, 23);
+        if (!ok) break;
+        const int w = q_ids[slot];
+        mbar_arrive(bar_qempty + 8 * slot);
+        if (w < 0) break;
         const TcxItem it = tcx_item(batch, w);
         int kb0, nkb;
         tcx_kblocks(batch.p[it.prob], it.split, kb0, nkb);
@@ -278,8 +317,14 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
     bool ok = true;
     int kb_global = 0;
     int nform2 = 0;  // form-2 stages converted (phase of bar_cread)
-    for (int wi = wbeg; wi < wend && ok; ++wi) {
-        const int w = batch.items[wi];
+    for (int seq = 0; ok; ++seq) {
+      const int slot = seq % C::QLEN;
+      ok = __all_sync(0xffffffffu, mbar_wait(bar_qfull + 8 * slot, (uint32_t)(seq / C::QLEN) & 1u, err, 24));
+      if (!ok) break;
+      const int w = q_ids[slot];
+      __syncwarp();
+      if (lane == 0) mbar_arrive(bar_qempty + 8 * slot);
+      if (w < 0) break;
       const TcxItem it = tcx_item(batch, w);
       const TcxProb& P = batch.p[it.prob];
       int kb0, nkb;
@@ -350,8 +395,14 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
     int kb_global = 0;
     int nom = 0;             // Omega tiles prefetched so far (all drain threads count them)
     bool omt_pending = false;  // lane 0 of drain warp 0: a tile load not yet waited for
-    for (int wi = wbeg; wi < wend && ok; ++wi) {
-        const int w = batch.items[wi];
+    for (int seq = 0; ok; ++seq) {
+      const int slot = seq % C::QLEN;
+      ok = __all_sync(0xffffffffu, mbar_wait(bar_qfull + 8 * slot, (uint32_t)(seq / C::QLEN) & 1u, err, 25));
+      if (!ok) break;
+      const int w = q_ids[slot];
+      __syncwarp();
+      if (lane == 0) mbar_arrive(bar_qempty + 8 * slot);
+      if (w < 0) break;
       const TcxItem it = tcx_item(batch, w);
       const TcxProb& P = batch.p[it.prob];
       int kb0, nkb;
@@ -678,11 +729,13 @@ int tcx_validate(const TcxBatch& b) {
     }
   }
   ZG_REQUIRE(items == b.nitems, "item total %d, table %d", items, b.nitems);
-  ZG_REQUIRE(b.cta_off[0] == 0, "item lists");
-  int c = 0;
-  while (c < ZG_TCX_GRID && b.cta_off[c + 1] > b.cta_off[c]) ++c;
-  ZG_REQUIRE(b.cta_off[c] == b.nitems, "item lists cover %d of %d items", (int)b.cta_off[c], b.nitems);
-  for (int w = 0; w < b.nitems; ++w) ZG_REQUIRE(b.items[w] < b.nitems, "item %d", w);
+  ZG_REQUIRE(b.claim != nullptr, "item claim counters");
+  // the claim order is a permutation of the items
+  std::vector<char> seen(b.nitems, 0);
+  for (int w = 0; w < b.nitems; ++w) {
+    ZG_REQUIRE(b.items[w] < b.nitems && !seen[b.items[w]], "item %d in the claim order", w);
+    seen[b.items[w]] = 1;
+  }
   return ZG_OK;
 }
 

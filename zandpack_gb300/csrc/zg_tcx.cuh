@@ -48,10 +48,13 @@ struct TcxProb {
 struct TcxBatch {
   CUtensorMap maps[ZG_TCX_MAPS];
   TcxProb p[ZG_TCX_PROBS];
-  // work items of CTA c: items[cta_off[c] .. cta_off[c + 1]) (a longest-first
-  // assignment made on the host; item w is decoded against p[].item_begin)
+  // work items in the order CTAs claim them (most expensive first, ordered on
+  // the host; item w is decoded against p[].item_begin).  A CTA claims its
+  // next item when it is ready to load it: claim[0] counts the claims and
+  // claim[1] the CTAs that are done; the last CTA zeroes both, so they are
+  // zero between launches
   unsigned short items[ZG_TCX_ITEMS];
-  unsigned short cta_off[ZG_TCX_GRID + 1];
+  int* claim;
   int nprob, nitems, bn;
   int* err;
   // epilogue 1: stage parameters, X+ and X- of the modes (complex64), output base
