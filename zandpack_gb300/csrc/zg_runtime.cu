@@ -745,18 +745,22 @@ static int build_tcx(zg_traj* t, const zg_layout* Lo, const std::vector<double2>
   int sms = 0;
   ZG_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, t->dev));
   const int grid = std::max(1, std::min(sms, ZG_TCX_GRID));
-  // K chunk: about the average work of a CTA over the products, so that no
-  // item outlasts the others by much and split-K partials stay few (the same
-  // chunks in both batches below, so that they share the split-K scratch)
+  // K chunks: at most about half the average work of a CTA over the products,
+  // so that the CTAs, claiming the items most expensive first, end close
+  // together, while split-K partials stay few; each problem's K is cut into
+  // equal chunks (the same chunks in both batches below, so that they share
+  // the split-K scratch)
   int64_t total_kb = 0;
   for (const TcxProb& P : probs)
     if (P.epi == 0) total_kb += (int64_t)P.tiles_m * P.tiles_n * (P.K / 32);
-  const int chunk_kb0 = (int)std::min<int64_t>(64, std::max<int64_t>(8, (total_kb + grid - 1) / grid));
+  const int chunk_kb0 = (int)std::min<int64_t>(64, std::max<int64_t>(8, (total_kb + 2 * grid - 1) / (2 * grid)));
   int chunk_kb = chunk_kb0;
   for (;;) {
     int items = 0;
     for (TcxProb& P : probs) {
-      P.kchunk = P.epi == 1 ? P.K : std::min(P.K, 32 * chunk_kb);  // Omega blocks: whole K per tile
+      const int kb = P.K / 32;
+      const int ns = (kb + chunk_kb - 1) / chunk_kb;
+      P.kchunk = P.epi == 1 ? P.K : 32 * ((kb + ns - 1) / ns);  // Omega blocks: whole K per tile
       P.nsplit = (P.K + P.kchunk - 1) / P.kchunk;
       if (P.epi == 0) items += P.tiles_m * P.tiles_n * P.nsplit;
     }

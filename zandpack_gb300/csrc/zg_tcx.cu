@@ -56,7 +56,10 @@ struct TcxCfg {
   // form 2 land here and are converted in place) | B hi | B lo
   static constexpr int OFF_AL = A_BYTES, OFF_BH = 2 * A_BYTES, OFF_BL = OFF_BH + B_BYTES;
   static constexpr int STAGE_BYTES = OFF_BL + B_BYTES;
-  static constexpr int NACC = BN <= 128 ? 4 : 2;  // TMEM accumulator buffers of BN columns
+  // TMEM accumulator buffers of BN columns: as many as fit in the 512
+  // columns (at most 8), so that the MMAs run ahead while the drain warps
+  // finish an item's epilogue
+  static constexpr int NACC = 512 / BN < 8 ? 512 / BN : 8;
   static constexpr int DCOLS = BN % 64 == 0 ? 64 : 32;
   static constexpr int NDW = 4 * (BN / DCOLS);
   // epilogue staging: per drain warp a 32-row x 32-float tile (rows padded to
@@ -67,8 +70,8 @@ struct TcxCfg {
   static constexpr int STG_BYTES = NDW * STG_WARP_FLOATS * 4;
   static constexpr int OMT_BYTES = 128 * BN * 4;
   static constexpr int LIMIT = 232448 - 1024;  // dynamic shared memory less the alignment slack
-  // barriers (first 256 bytes), then the item queue: QLEN "full" and "empty"
-  // barriers and the item numbers
+  // barriers and the TMEM address (first 264 bytes), then at byte 320 the
+  // item queue: QLEN "full" and "empty" barriers and the item numbers
   static constexpr int BAR_AREA = 512;
   static constexpr int QLEN = 8;
   static constexpr int fit(int stages, bool stg, bool omt) {
@@ -89,7 +92,7 @@ struct TcxCfg {
   static constexpr int THREADS = 32 * (W_DRAIN + NDW);
   static_assert(BN % 32 == 0 && BN >= 32 && BN <= 256, "BN");
   static_assert(SMEM <= 232448, "shared memory");
-  static_assert(STAGES <= 4, "barrier area");
+  static_assert(STAGES <= 4 && 24 * STAGES + 16 * NACC + 12 <= 240, "barrier area");
 };
 
 struct TcxItem {
@@ -139,12 +142,12 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
   const uint32_t bar_tfull = bar_empty + 8 * STAGES;   // NACC
   const uint32_t bar_tempty = bar_tfull + 8 * NACC;    // NACC
   const uint32_t bar_done = bar_tempty + 8 * NACC;
-  const uint32_t bar_omt_full = sbase + C::BAR_OFF + 192;   // the Omega tile landed
-  const uint32_t bar_omt_empty = sbase + C::BAR_OFF + 200;  // the drain warps read it
-  const uint32_t bar_cread = sbase + C::BAR_OFF + 208;      // converters read a form-2 stage
-  const uint32_t bar_qfull = sbase + C::BAR_OFF + 256;      // QLEN: the producer wrote an item number
+  const uint32_t bar_omt_full = sbase + C::BAR_OFF + 240;   // the Omega tile landed
+  const uint32_t bar_omt_empty = sbase + C::BAR_OFF + 248;  // the drain warps read it
+  const uint32_t bar_cread = sbase + C::BAR_OFF + 256;      // converters read a form-2 stage
+  const uint32_t bar_qfull = sbase + C::BAR_OFF + 320;      // QLEN: the producer wrote an item number
   const uint32_t bar_qempty = bar_qfull + 8 * C::QLEN;      // QLEN: every role read it
-  volatile int* q_ids = reinterpret_cast<volatile int*>(smem + C::BAR_OFF + 256 + 16 * C::QLEN);
+  volatile int* q_ids = reinterpret_cast<volatile int*>(smem + C::BAR_OFF + 320 + 16 * C::QLEN);
   uint32_t* tmem_slot = (uint32_t*)(smem + C::BAR_OFF + 24 * STAGES + 16 * NACC + 8);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int* err = batch.err;
@@ -198,8 +201,9 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
       for (int s = 0; s < STAGES; ++s) issued[s] = 0;
       bool ok = true;
       int kb_global = 0;
-      // items are claimed one ahead: the claim of the next item (an atomic
-      // round trip) runs while this item's loads are issued
+      // the next item is claimed while the last K blocks of the current one
+      // are issued, so that the atomic's round trip overlaps the loads in
+      // flight but no CTA holds an item it is far from starting
       int idx = atomicAdd(batch.claim, 1);
       for (int seq = 0; ok; ++seq) {
         // pass the claimed item on once the queue has room (-1: none left)
@@ -207,7 +211,6 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
         ok = mbar_wait(bar_qempty + 8 * slot, ((uint32_t)(seq / C::QLEN) & 1u) ^ 1u, err, 22);
         if (!ok) break;
         const int w = idx < batch.nitems ? (int)batch.items[idx] : -1;
-        if (w >= 0) idx = atomicAdd(batch.claim, 1);
         q_ids[slot] = w;
         mbar_arrive(bar_qfull + 8 * slot);
         if (w < 0) break;
@@ -220,6 +223,7 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
           const uint32_t ph = (uint32_t)(kb_global / STAGES) & 1u;
           ok = mbar_wait(bar_empty + 8 * s, ph ^ 1u, err, 11);
           if (!ok) break;
+          if (q == max(0, nkb - 2)) idx = atomicAdd(batch.claim, 1);
           const uint32_t st = sbase + s * C::STAGE_BYTES;
           const uint32_t fb = bar_full + 8 * s;
           const int kx = (kb0 + q) * 32;  // K float offset inside the problem
@@ -535,22 +539,33 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
             }
             prev = __shfl_sync(0xffffffffu, prev, 0);
             if (prev == P.nsplit - 1) {
-#pragma unroll
+              // the 16 row pairs of a 32-column chunk in flight at once, one
+              // split after the other (partials added in split order)
+#pragma unroll 1
               for (int ch = 0; ch < C::DCOLS / 32; ++ch) {
                 const int col = (col0 >> 1) + ch * 16 + cs;
                 const int lc = 2 * (col - it.tn * (BN / 2));
-#pragma unroll 2
-                for (int itr = 0; itr < 16; ++itr) {
-                  const int rr = itr * 2 + rs;
-                  const int r = it.tm * 128 + quarter * 32 + rr;
-                  const float* src = ws_tile + (quarter * 32 + rr) * BN + lc;
-                  float2 sum = __ldcg(reinterpret_cast<const float2*>(src));
-                  for (int sp = 1; sp < P.nsplit; ++sp) {
-                    const float2 q = __ldcg(reinterpret_cast<const float2*>(src + (long long)sp * (128 * BN)));
-                    sum.x += q.x;
-                    sum.y += q.y;
+                const float* src = ws_tile + (quarter * 32 + rs) * BN + lc;
+                float2 sum[16];
+#pragma unroll
+                for (int itr = 0; itr < 16; ++itr)
+                  sum[itr] = __ldcg(reinterpret_cast<const float2*>(src + itr * 2 * BN));
+                for (int sp = 1; sp < P.nsplit; ++sp) {
+                  const float* sps = src + (long long)sp * (128 * BN);
+                  float2 q[16];
+#pragma unroll
+                  for (int itr = 0; itr < 16; ++itr) q[itr] = __ldcg(reinterpret_cast<const float2*>(sps + itr * 2 * BN));
+#pragma unroll
+                  for (int itr = 0; itr < 16; ++itr) {
+                    sum[itr].x += q[itr].x;
+                    sum[itr].y += q[itr].y;
                   }
-                  if (r < P.M && 2 * col < P.Nv) *reinterpret_cast<float2*>(P.D + (long long)r * P.ldd + 2 * col) = sum;
+                }
+#pragma unroll
+                for (int itr = 0; itr < 16; ++itr) {
+                  const int r = it.tm * 128 + quarter * 32 + itr * 2 + rs;
+                  if (r < P.M && 2 * col < P.Nv)
+                    *reinterpret_cast<float2*>(P.D + (long long)r * P.ldd + 2 * col) = sum[itr];
                 }
               }
               __syncwarp();
