@@ -47,7 +47,7 @@
 
 namespace zg {
 
-template <int BN>
+template <int BN, bool OMG>
 struct TcxCfg {
   static constexpr int A_BYTES = 128 * 32 * 4;   // one 128 x 32-float K-major tile
   static constexpr int RAW_BYTES = 4 * 16 * 128 * 4;  // four 16-mode x 128-orbital planes (form 2)
@@ -79,9 +79,11 @@ struct TcxCfg {
   }
   // the deepest ring that fits with staging and the Omega tile, else with
   // staging alone, else two stages with what fits
-  static constexpr int STAGES = fit(4, true, true) ? 4 : fit(3, true, true) ? 3 : fit(3, true, false) ? 3 : 2;
+  // (OMG: the kernel of batches with Omega blocks; without them the room of
+  // the Omega tile can hold another stage)
+  static constexpr int STAGES = fit(4, true, OMG) ? 4 : fit(3, true, OMG) ? 3 : fit(3, true, false) ? 3 : 2;
   static constexpr bool STAGED = fit(STAGES, true, false);
-  static constexpr bool HAS_OMT = STAGED && fit(STAGES, true, true);
+  static constexpr bool HAS_OMT = OMG && STAGED && fit(STAGES, true, true);
   static constexpr int BAR_OFF = STAGES * STAGE_BYTES;
   static constexpr int STG_OFF = BAR_OFF + BAR_AREA;
   static constexpr int OMT_OFF = STG_OFF + (STAGED ? STG_BYTES : 0);
@@ -127,9 +129,9 @@ __device__ __forceinline__ uint32_t tf32_rna(float x) {
   return h;
 }
 
-template <int BN>
-__global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_constant__ TcxBatch batch) {
-  using C = TcxCfg<BN>;
+template <int BN, bool OMG>
+__global__ void __launch_bounds__(TcxCfg<BN, OMG>::THREADS, 1) k_tcx(const __grid_constant__ TcxBatch batch) {
+  using C = TcxCfg<BN, OMG>;
   constexpr int STAGES = C::STAGES, NACC = C::NACC, NDW = C::NDW;
   extern __shared__ uint8_t smem_raw[];
   const uint32_t raw = smem_u32(smem_raw);
@@ -674,17 +676,17 @@ __global__ void __launch_bounds__(TcxCfg<BN>::THREADS, 1) k_tcx(const __grid_con
 int make_tmap_f32_box(CUtensorMap* map, const float* base, int64_t rows, int64_t cols, int64_t ld, int box_rows,
                       int box_cols, bool swizzle128);
 
-template <int BN>
+template <int BN, bool OMG>
 static int launch_tcx_bn(const TcxBatch& b, int grid, cudaStream_t s) {
-  using C = TcxCfg<BN>;
+  using C = TcxCfg<BN, OMG>;
   static std::atomic<bool> configured[64];
   int dev = 0;
   ZG_CHECK_CUDA(cudaGetDevice(&dev));
   if (dev < 64 && !configured[dev].load()) {
-    ZG_CHECK_CUDA(cudaFuncSetAttribute(k_tcx<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
+    ZG_CHECK_CUDA(cudaFuncSetAttribute(k_tcx<BN, OMG>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
     configured[dev] = true;
   }
-  k_tcx<BN><<<grid, C::THREADS, C::SMEM, s>>>(b);
+  k_tcx<BN, OMG><<<grid, C::THREADS, C::SMEM, s>>>(b);
   ZG_CHECK_LAUNCH();
   count_launch();
   return ZG_OK;
@@ -756,10 +758,10 @@ int tcx_validate(const TcxBatch& b) {
 
 bool tcx_has_omega_tile(int bn) {
   switch (bn) {
-    case 32: return TcxCfg<32>::HAS_OMT;
-    case 64: return TcxCfg<64>::HAS_OMT;
-    case 128: return TcxCfg<128>::HAS_OMT;
-    case 192: return TcxCfg<192>::HAS_OMT;
+    case 32: return TcxCfg<32, true>::HAS_OMT;
+    case 64: return TcxCfg<64, true>::HAS_OMT;
+    case 128: return TcxCfg<128, true>::HAS_OMT;
+    case 192: return TcxCfg<192, true>::HAS_OMT;
     default: return false;
   }
 }
@@ -774,11 +776,17 @@ int tcx_bn_for(int ncols) {
 
 int tcx_launch(const TcxBatch& b, int grid, cudaStream_t s) {
   if (b.nitems == 0) return ZG_OK;
-  switch (b.bn) {
-    case 32: return launch_tcx_bn<32>(b, grid, s);
-    case 64: return launch_tcx_bn<64>(b, grid, s);
-    case 128: return launch_tcx_bn<128>(b, grid, s);
-    case 192: return launch_tcx_bn<192>(b, grid, s);
+  bool om = false;  // Omega blocks in the batch: the kernel with room for their tiles
+  for (int i = 0; i < b.nprob; ++i) om = om || b.p[i].epi == 1;
+  switch (b.bn * 2 + (om ? 1 : 0)) {
+    case 64: return launch_tcx_bn<32, false>(b, grid, s);
+    case 65: return launch_tcx_bn<32, true>(b, grid, s);
+    case 128: return launch_tcx_bn<64, false>(b, grid, s);
+    case 129: return launch_tcx_bn<64, true>(b, grid, s);
+    case 256: return launch_tcx_bn<128, false>(b, grid, s);
+    case 257: return launch_tcx_bn<128, true>(b, grid, s);
+    case 384: return launch_tcx_bn<192, false>(b, grid, s);
+    case 385: return launch_tcx_bn<192, true>(b, grid, s);
     default: set_error("complex tensor-core product: no kernel for %d columns", b.bn); return ZG_EINVAL;
   }
 }
