@@ -60,7 +60,9 @@ struct TcxCfg {
   // columns (at most 8), so that the MMAs run ahead while the drain warps
   // finish an item's epilogue
   static constexpr int NACC = 512 / BN < 8 ? 512 / BN : 8;
-  static constexpr int DCOLS = BN % 64 == 0 ? 64 : 32;
+  // columns per drain warp: 32 for the BN = 64 kernel with Omega blocks, whose
+  // epilogues (the Omega derivative of every tile) then have eight warps
+  static constexpr int DCOLS = (OMG && BN == 64) ? 32 : (BN % 64 == 0 ? 64 : 32);
   static constexpr int NDW = 4 * (BN / DCOLS);
   // epilogue staging: per drain warp a 32-row x 32-float tile (rows padded to
   // 36 floats), so that global loads and stores run along rows; and the Omega
@@ -203,10 +205,11 @@ __global__ void __launch_bounds__(TcxCfg<BN, OMG>::THREADS, 1) k_tcx(const __gri
       for (int s = 0; s < STAGES; ++s) issued[s] = 0;
       bool ok = true;
       int kb_global = 0;
-      // the next item is claimed while the last K blocks of the current one
-      // are issued, so that the atomic's round trip overlaps the loads in
-      // flight but no CTA holds an item it is far from starting
-      int idx = atomicAdd(batch.claim, 1);
+      // CTA c starts with item c; each further item is claimed while the last
+      // K blocks of the current one are issued, so that the atomic's round
+      // trip overlaps the loads in flight but no CTA holds an item it is far
+      // from starting (claim[0] counts the claims past the first gridDim.x)
+      int idx = blockIdx.x;
       for (int seq = 0; ok; ++seq) {
         // pass the claimed item on once the queue has room (-1: none left)
         const int slot = seq % C::QLEN;
@@ -225,7 +228,7 @@ __global__ void __launch_bounds__(TcxCfg<BN, OMG>::THREADS, 1) k_tcx(const __gri
           const uint32_t ph = (uint32_t)(kb_global / STAGES) & 1u;
           ok = mbar_wait(bar_empty + 8 * s, ph ^ 1u, err, 11);
           if (!ok) break;
-          if (q == max(0, nkb - 2)) idx = atomicAdd(batch.claim, 1);
+          if (q == max(0, nkb - 3)) idx = (int)gridDim.x + atomicAdd(batch.claim, 1);
           const uint32_t st = sbase + s * C::STAGE_BYTES;
           const uint32_t fb = bar_full + 8 * s;
           const int kx = (kb0 + q) * 32;  // K float offset inside the problem

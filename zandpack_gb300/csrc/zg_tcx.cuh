@@ -49,10 +49,10 @@ struct TcxBatch {
   CUtensorMap maps[ZG_TCX_MAPS];
   TcxProb p[ZG_TCX_PROBS];
   // work items in the order CTAs claim them (most expensive first, ordered on
-  // the host; item w is decoded against p[].item_begin).  A CTA claims its
-  // next item when it is ready to load it: claim[0] counts the claims and
-  // claim[1] the CTAs that are done; the last CTA zeroes both, so they are
-  // zero between launches
+  // the host; item w is decoded against p[].item_begin).  CTA c starts with
+  // item c and claims each further item when it is nearly ready to load it:
+  // claim[0] counts those claims and claim[1] the CTAs that are done; the
+  // last CTA zeroes both, so they are zero between launches
   unsigned short items[ZG_TCX_ITEMS];
   int* claim;
   int nprob, nitems, bn;
@@ -69,8 +69,9 @@ struct TcxBatch {
 // BN of the kernel for products with `ncols` real output columns per tile
 // (0 when none fits)
 int tcx_bn_for(int ncols);
-// number of drain warps of the BN kernel (counters per tile)
-inline int tcx_ndw(int bn) { return 4 * (bn / (bn % 64 == 0 ? 64 : 32)); }
+// drain warps per tile of the BN kernels, the larger of the two kinds (split-K
+// counters per tile)
+inline int tcx_ndw(int bn) { return bn == 64 ? 8 : 4 * (bn / (bn % 64 == 0 ? 64 : 32)); }
 // whether the BN kernel prefetches Omega tiles into shared memory (it fits)
 bool tcx_has_omega_tile(int bn);
 int tcx_launch(const TcxBatch& b, int grid, cudaStream_t s);
