@@ -835,6 +835,8 @@ static int build_tcx(zg_traj* t, const zg_layout* Lo, const std::vector<double2>
     for (int i = 0; i < items; ++i) Bt.items[i] = (unsigned short)order[i];
     Bt.claim = claim;
     *grid_used = std::min(grid, items);
+    // many items per CTA (the Omega tiles are short): claim two items ahead
+    Bt.ahead2 = items >= 6 * *grid_used ? 1 : 0;
     return tcx_validate(Bt);
   };
   std::unique_ptr<TcxBatch> Bm;

@@ -104,8 +104,15 @@ struct TcxItem {
 };
 
 __device__ __forceinline__ TcxItem tcx_item(const TcxBatch& b, int w) {
-  int p = 0;
-  while (p + 1 < b.nprob && w >= b.p[p + 1].item_begin) ++p;
+  // the last problem whose first item is <= w (binary search: each probe is
+  // a dependent load from the parameter space)
+  int lo = 0, hi = b.nprob - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (b.p[mid].item_begin <= w) lo = mid;
+    else hi = mid - 1;
+  }
+  const int p = lo;
   const TcxProb& P = b.p[p];
   int r = w - P.item_begin;
   TcxItem it;
@@ -188,34 +195,47 @@ __global__ void __launch_bounds__(TcxCfg<BN, OMG>::THREADS, 1) k_tcx(const __gri
   const uint32_t tmem = *tmem_slot;
 
   if (warp == 0) {
+    // the descriptors of every map the problems read, into the descriptor
+    // cache (one problem per lane, so that the reads of the problem table
+    // from the parameter space overlap)
+    for (int i = lane; i < batch.nprob; i += 32) {
+      const TcxProb& P = batch.p[i];
+      const int ids[5] = {P.mapA, P.mapB, P.kseg < P.K ? P.mapA2 : -1, P.kseg < P.K ? P.mapB2 : -1, P.om_map};
+#pragma unroll
+      for (int j = 0; j < 5; ++j) {
+        if (ids[j] < 0 || ids[j] >= ZG_TCX_MAPS) continue;
+        asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&batch.maps[ids[j]]) : "memory");
+        if (j < 4 && ids[j] + 1 < ZG_TCX_MAPS)
+          asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&batch.maps[ids[j] + 1]) : "memory");
+      }
+    }
+    __syncwarp();
     if (lane == 0) {
       // ---------------- TMA producer
-      // the descriptors of every map the problems read, into the descriptor cache
-      for (int i = 0; i < batch.nprob; ++i) {
-        const TcxProb& P = batch.p[i];
-        const int ids[7] = {P.mapA, P.mapB, P.kseg < P.K ? P.mapA2 : -1, P.kseg < P.K ? P.mapB2 : -1, P.om_map, -1, -1};
-        for (int j = 0; j < 5; ++j) {
-          if (ids[j] < 0 || ids[j] + 1 >= ZG_TCX_MAPS + 1) continue;
-          asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&batch.maps[ids[j]]) : "memory");
-          if (j < 4 && ids[j] + 1 < ZG_TCX_MAPS)
-            asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&batch.maps[ids[j] + 1]) : "memory");
-        }
-      }
       int issued[STAGES];
       for (int s = 0; s < STAGES; ++s) issued[s] = 0;
       bool ok = true;
       int kb_global = 0;
-      // CTA c starts with item c; each further item is claimed while the last
-      // K blocks of the current one are issued, so that the atomic's round
-      // trip overlaps the loads in flight but no CTA holds an item it is far
-      // from starting (claim[0] counts the claims past the first gridDim.x)
-      int idx = blockIdx.x;
+      // CTA c starts with item c.  With many short items per CTA (ahead2) it
+      // also starts with item gridDim.x + c and claims each further item when
+      // it starts on the item two places before it, so that the atomic's
+      // round trip is hidden even behind short items; otherwise it claims the
+      // next item three K blocks before the current one ends, so that no CTA
+      // holds a long item it is far from starting.  claim[0] counts the
+      // claims past the first (1 + ahead2) gridDim.x items
+      const int G = (int)gridDim.x;
+      const int base = batch.ahead2 ? 2 * G : G;
+      int idx = blockIdx.x, idx_next = G + blockIdx.x;
       for (int seq = 0; ok; ++seq) {
         // pass the claimed item on once the queue has room (-1: none left)
         const int slot = seq % C::QLEN;
         ok = mbar_wait(bar_qempty + 8 * slot, ((uint32_t)(seq / C::QLEN) & 1u) ^ 1u, err, 22);
         if (!ok) break;
         const int w = idx < batch.nitems ? (int)batch.items[idx] : -1;
+        if (batch.ahead2) {
+          idx = idx_next;
+          if (w >= 0) idx_next = base + atomicAdd(batch.claim, 1);
+        }
         q_ids[slot] = w;
         mbar_arrive(bar_qfull + 8 * slot);
         if (w < 0) break;
@@ -228,7 +248,7 @@ __global__ void __launch_bounds__(TcxCfg<BN, OMG>::THREADS, 1) k_tcx(const __gri
           const uint32_t ph = (uint32_t)(kb_global / STAGES) & 1u;
           ok = mbar_wait(bar_empty + 8 * s, ph ^ 1u, err, 11);
           if (!ok) break;
-          if (q == max(0, nkb - 3)) idx = (int)gridDim.x + atomicAdd(batch.claim, 1);
+          if (!batch.ahead2 && q == max(0, nkb - 3)) idx = base + atomicAdd(batch.claim, 1);
           const uint32_t st = sbase + s * C::STAGE_BYTES;
           const uint32_t fb = bar_full + 8 * s;
           const int kx = (kb0 + q) * 32;  // K float offset inside the problem

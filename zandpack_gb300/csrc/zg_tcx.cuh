@@ -50,12 +50,13 @@ struct TcxBatch {
   TcxProb p[ZG_TCX_PROBS];
   // work items in the order CTAs claim them (most expensive first, ordered on
   // the host; item w is decoded against p[].item_begin).  CTA c starts with
-  // item c and claims each further item when it is nearly ready to load it:
-  // claim[0] counts those claims and claim[1] the CTAs that are done; the
-  // last CTA zeroes both, so they are zero between launches
+  // item c (and c + gridDim.x when ahead2) and claims each further one near
+  // the end of the previous one (two items ahead when ahead2): claim[0]
+  // counts those claims and claim[1] the CTAs that are done; the last CTA
+  // zeroes both, so they are zero between launches
   unsigned short items[ZG_TCX_ITEMS];
   int* claim;
-  int nprob, nitems, bn;
+  int nprob, nitems, bn, ahead2;
   int* err;
   // epilogue 1: stage parameters, X+ and X- of the modes (complex64), output base
   const StageParams* params;
