@@ -166,17 +166,17 @@ __global__ void __launch_bounds__(TcxCfg<BN, OMG>::THREADS, 1) k_tcx(const __gri
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
       mbar_init(bar_full + 8 * s, 1);
-      mbar_init(bar_conv + 8 * s, 32 * C::NCONV);
+      mbar_init(bar_conv + 8 * s, C::NCONV);  // lane 0 of each converter warp
       mbar_init(bar_empty + 8 * s, 1);
     }
     for (int b = 0; b < NACC; ++b) {
       mbar_init(bar_tfull + 8 * b, 1);
-      mbar_init(bar_tempty + 8 * b, 32 * NDW);
+      mbar_init(bar_tempty + 8 * b, NDW);  // lane 0 of each drain warp
     }
     mbar_init(bar_done, 1);
     mbar_init(bar_omt_full, 1);
-    mbar_init(bar_omt_empty, 32 * NDW);
-    mbar_init(bar_cread, 32 * C::NCONV);
+    mbar_init(bar_omt_empty, NDW);
+    mbar_init(bar_cread, C::NCONV);
     for (int q = 0; q < C::QLEN; ++q) {
       mbar_init(bar_qfull + 8 * q, 1);
       mbar_init(bar_qempty + 8 * q, 1 + C::NCONV + NDW);  // MMA thread, lane 0 of each warp
@@ -309,8 +309,9 @@ __global__ void __launch_bounds__(TcxCfg<BN, OMG>::THREADS, 1) k_tcx(const __gri
         mbar_arrive(bar_qempty + 8 * slot);
         if (w < 0) break;
         const TcxItem it = tcx_item(batch, w);
+        const TcxProb& P = batch.p[it.prob];
         int kb0, nkb;
-        tcx_kblocks(batch.p[it.prob], it.split, kb0, nkb);
+        tcx_kblocks(P, it.split, kb0, nkb);
         for (int q = 0; q < nkb; ++q, ++kb_global) {
           const int b = kb_global % NACC;
           if (!mbar_wait(bar_tempty + 8 * b, ((uint32_t)(kb_global / NACC) & 1u) ^ 1u, err, 15)) {
@@ -397,7 +398,8 @@ __global__ void __launch_bounds__(TcxCfg<BN, OMG>::THREADS, 1) k_tcx(const __gri
               v[part][c] = make_float4(re[(2 * c) * 128 + ct], im[(2 * c) * 128 + ct], re[(2 * c + 1) * 128 + ct],
                                        im[(2 * c + 1) * 128 + ct]);
           }
-          mbar_arrive(bar_cread);
+          __syncwarp();
+          if (lane == 0) mbar_arrive(bar_cread);
           ok = __all_sync(0xffffffffu, mbar_wait(bar_cread, (uint32_t)nform2 & 1u, err, 21));
           ++nform2;
           if (!ok) break;
@@ -410,7 +412,8 @@ __global__ void __launch_bounds__(TcxCfg<BN, OMG>::THREADS, 1) k_tcx(const __gri
         }
         // generic-proxy writes to shared memory, read next by the tensor core
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        mbar_arrive(bar_conv + 8 * s);
+        __syncwarp();
+        if (lane == 0) mbar_arrive(bar_conv + 8 * s);
       }
     }
   } else {
@@ -465,7 +468,8 @@ __global__ void __launch_bounds__(TcxCfg<BN, OMG>::THREADS, 1) k_tcx(const __gri
           for (int i = 0; i < 32; ++i) acc[c + i] += __uint_as_float(r0[i]);
         }
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-        mbar_arrive(bar_tempty + 8 * b);
+        __syncwarp();
+        if (lane == 0) mbar_arrive(bar_tempty + 8 * b);
       }
       if (!ok) break;
       // ---- epilogue of the item
@@ -547,7 +551,8 @@ __global__ void __launch_bounds__(TcxCfg<BN, OMG>::THREADS, 1) k_tcx(const __gri
             __syncwarp();
           }
           if (omt) {
-            mbar_arrive(bar_omt_empty);
+            __syncwarp();
+            if (lane == 0) mbar_arrive(bar_omt_empty);
             ++nom;
           }
           if (part_out) {
