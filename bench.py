@@ -48,6 +48,9 @@ OUT_DIR = os.environ.get("ZG_BENCH_OUT", os.path.join(HERE, "bench_out"))
 # ncu capture of that launch (ncu cannot run inside the timed region); reported
 # with its source, never as a measurement of this run
 NCU_TRAFFIC = {("c3", "real"): 83.8e6 + 8.6e6}
+# the same for one launch of the complex-product kernel k_tcx per (workload,
+# implementation): products and dOmega/dt in one launch at n=1024
+NCU_TRAFFIC_TCX = {("c3", "tc_all"): 166.9e6 + 22.7e6}
 
 METRIC = "simulated fs/s at n=1024"
 WORKLOAD_DESC = {
@@ -344,10 +347,11 @@ def mixed_roofline(args, w, L, reg, stages, peaks, tf32, impl):
                  % ("real" if h_real else "complex"), 8.0 * N * n * n, bf16, "TFLOP/s",
                  "MEASURED_PEAKS.json bf16_tflops (burst)"),
         # the small products read psi's hi/lo planes and the Omega blocks and write PI, Omega xi, xi sigma^T
+        # (with dOmega/dt: the Omega blocks once more written, their second read not counted)
         "small": ("hbm", "k_tcx (PI partials, Omega xi, xi sigma^T%s on tcgen05)" % (
                   " and dOmega/dt" if impl == "tc_all" else "") if impl != "simt" else "k_zgemm<float> SIMT batch",
                   16.0 * N * np_ + 8.0 * om + 8.0 * (2 * NL * n * nc + NL * N * nc + NL * Ns * nc + Ns * n)
-                  + (16.0 * om if impl == "tc_all" else 0.0), hbm, "GB/s", "MEASURED_PEAKS.json hbm_gbs"),
+                  + (8.0 * om if impl == "tc_all" else 0.0), hbm, "GB/s", "MEASURED_PEAKS.json hbm_gbs"),
         "omega": ("hbm", "k_omega<float> (dOmega/dt, SIMT)", 16.0 * om, hbm, "GB/s", "MEASURED_PEAKS.json hbm_gbs"),
         "final": ("hbm", "k_final_all_mixed (k_sigma and k_psi finalisation)",
                   8.0 * (4 * N * n + Ns * n) + 8.0 * 3 * n * n, hbm, "GB/s", "MEASURED_PEAKS.json hbm_gbs"),
@@ -378,6 +382,11 @@ def mixed_roofline(args, w, L, reg, stages, peaks, tf32, impl):
             if name == "gemm":
                 roof["traffic"] = traffic
                 roof["traffic_source"] = roof["psi_HT"]["traffic_source"]
+    if name == "small" and NCU_TRAFFIC_TCX.get((args.config, impl)) is not None:
+        roof["traffic"] = NCU_TRAFFIC_TCX[(args.config, impl)]
+        roof["traffic_source"] = ("dram__bytes_read.sum + dram__bytes_write.sum of one launch, separate ncu "
+                                  "capture at this workload (not this run); writes still in L2 at kernel end "
+                                  "are not counted")
     return roof
 
 
@@ -417,8 +426,9 @@ def kernel_roofs(L, reg, stages, peaks, tf32, impl="simt"):
         put("small", 8.0 * (n * N * nc + Ns * nc * n + N * Ns * nc + Ns * Nf * nc), "TFLOP/s", fp32, live)
     else:  # on the tensor cores: bytes of psi's planes, the Omega blocks and the products
         put("small", 16.0 * N * np_ + 8.0 * om + 8.0 * (2 * L.NL * n * nc + L.NL * N * nc + L.NL * Ns * nc + Ns * n)
-            + (16.0 * om if impl == "tc_all" else 0.0), "GB/s", hbm, mp)
-    put("omega", 16.0 * om, "GB/s", hbm, mp)
+            + (8.0 * om if impl == "tc_all" else 0.0), "GB/s", hbm, mp)
+    if impl != "tc_all":  # else dOmega/dt is part of the products' launch
+        put("omega", 16.0 * om, "GB/s", hbm, mp)
     # executed tensor flops of H sigma with a real H(t) (the workloads' Hamiltonians and Hubbard term)
     put("gemm2", 3 * 2.0 * ((n + 31) // 32 * 32) * 2 * np_ * np_, "TFLOP/s", tf32, "live cuBLAS TF32")
     return out
