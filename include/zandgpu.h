@@ -220,7 +220,10 @@ int zg_graph_run(zg_traj* t, int count, zg_attempt_rec* recs, int* nrec, double*
  *                        trajectory's second stream);
  *   ZG_IMPL_TC_PRODUCTS  the products on the tensor cores, dOmega/dt SIMT on
  *                        the second stream;
- *   ZG_IMPL_TC_ALL       both in one tensor-core launch.
+ *   ZG_IMPL_TC_ALL       both in one tensor-core launch;
+ *   ZG_IMPL_TC_SPLIT     the products on the tensor cores, dOmega/dt as a
+ *                        second tensor-core launch (tiles of 32 complex
+ *                        columns whatever n_c) on the second stream.
  * zg_set_impl selects one (ZG_EINVAL when the trajectory's shapes do not
  * allow it; the FP64 path ignores it); zg_get_impl reads the current choice
  * and, in *avail, a bit mask of the implementations the trajectory supports.
@@ -237,7 +240,7 @@ int zg_graph_run(zg_traj* t, int count, zg_attempt_rec* recs, int* nrec, double*
  * These replace no reference interface: they choose among this library's
  * kernels for the reference's Q_np / Omega stage terms
  * (Zandpack/mpi/zand:91-110,770-809). */
-enum { ZG_IMPL_SIMT = 0, ZG_IMPL_TC_PRODUCTS = 1, ZG_IMPL_TC_ALL = 2, ZG_IMPL_COUNT = 3 };
+enum { ZG_IMPL_SIMT = 0, ZG_IMPL_TC_PRODUCTS = 1, ZG_IMPL_TC_ALL = 2, ZG_IMPL_TC_SPLIT = 3, ZG_IMPL_COUNT = 4 };
 enum { ZG_SCHED_LATE = 0, ZG_SCHED_EARLY = 1, ZG_SCHED_COUNT = 2 };
 int zg_set_impl(zg_traj* t, int impl);
 int zg_get_impl(const zg_traj* t, int* impl, int* avail);

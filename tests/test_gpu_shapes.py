@@ -1,7 +1,8 @@
 """The larger workloads on the device: the n=256 ribbon (c2) and the n=2048,
 4-lead, n_c=72 device (c5).  One right-hand side on a random dense state in
-both precisions; the mixed result must agree with the FP64 one to 2e-5 of
-the magnitude of the products (the per-RHS tolerance of the mixed path)."""
+both precisions; the mixed result, in every kernel form the trajectory
+supports, must agree with the FP64 one to 2e-5 of the magnitude of the
+products (the per-RHS tolerance of the mixed path)."""
 import numpy as np
 import pytest
 
@@ -23,21 +24,29 @@ def test_mixed_vs_f64_rhs_large(case):
     sig, psi, _, _ = L.views(y)
     sig[...] = (sig + sig.conj().T) / 2 + np.asarray(w.arrays["DM_Ortho"][0])
     delta = [w.bias_fn()(3.0, a) for a in range(L.NL)]
-    out = {}
-    for prec in ("f64", "mixed"):
-        tr = Trajectory(w.arrays, w.hbar, precision=prec, layout=L)
-        tr.set_slot(tr.stages, y)
-        tr.stage_input(0)
-        J = tr.rhs(0, 3.0, 0.02, delta, currents=True)
-        out[prec] = (tr.get_slot(0), J)
-        tr.close()
-    kf, Jf = out["f64"]
-    km, Jm = out["mixed"]
-    a, b = L.views(kf), L.views(km)
+    tr = Trajectory(w.arrays, w.hbar, precision="f64", layout=L)
+    tr.set_slot(tr.stages, y)
+    tr.stage_input(0)
+    Jf = tr.rhs(0, 3.0, 0.02, delta, currents=True)
+    kf = tr.get_slot(0)
+    tr.close()
+    a = L.views(kf)
     H = np.asarray(w.arrays["H_Ortho"][0])
     scale_sig = np.abs(H @ sig).max() * 0.02 / w.hbar
     scale_psi = np.abs(psi @ H.T).max() * 0.02 / w.hbar
-    for name, x, r, sc in zip(("sig", "psi", "omA", "omB"), b, a, (scale_sig, scale_psi, 0.0, 0.0)):
-        err = np.abs(x - r).max() / max(np.abs(r).max(), sc, 1e-300)
-        assert err < 2e-5, (case, name, err)
-    np.testing.assert_allclose(Jm, Jf, rtol=1e-11, atol=1e-14)
+    # every kernel form of the mixed path the trajectory supports
+    tr = Trajectory(w.arrays, w.hbar, precision="mixed", layout=L)
+    tr.set_slot(tr.stages, y)
+    _, avail = tr.get_impl()
+    assert _lib.ZG_IMPL_TC_PRODUCTS in avail
+    for impl in avail:
+        tr.set_impl(impl)
+        tr.stage_input(0)
+        Jm = tr.rhs(0, 3.0, 0.02, delta, currents=True)
+        b = L.views(tr.get_slot(0))
+        for name, x, r, sc in zip(("sig", "psi", "omA", "omB"), b, a, (scale_sig, scale_psi, 0.0, 0.0)):
+            err = np.abs(x - r).max() / max(np.abs(r).max(), sc, 1e-300)
+            print("\n%s %s %s: %.2e" % (case, _lib.IMPL_NAMES[impl], name, err))
+            assert err < 2e-5, (case, _lib.IMPL_NAMES[impl], name, err)
+        np.testing.assert_allclose(Jm, Jf, rtol=1e-11, atol=1e-14)
+    tr.close()

@@ -1,6 +1,8 @@
-"""The three implementations of the mixed path's small products and dOmega/dt
-(FP32 SIMT; products on the tensor cores; products and dOmega/dt on the
-tensor cores) against the oracle on one right-hand side, and the measured
+"""The implementations of the mixed path's small products and dOmega/dt
+(FP32 SIMT; products on the tensor cores; products and dOmega/dt in one
+tensor-core launch; products and dOmega/dt in two tensor-core launches, the
+second on the second stream) against the oracle on one right-hand side, and
+the measured
 choice (zg_tune).  Tolerance: the mixed path's per-RHS bar, 2e-5 of the
 magnitude of the products each array is made of."""
 import numpy as np

@@ -16,8 +16,8 @@ ZG_PREC_F64, ZG_PREC_MIXED = 0, 1
 ZG_DH_NONE, ZG_DH_MATRIX, ZG_DH_HUBBARD = 0, 1, 2
 ZG_MAX_LEADS = 16
 ZG_MAX_STAGES = 13
-ZG_IMPL_SIMT, ZG_IMPL_TC_PRODUCTS, ZG_IMPL_TC_ALL, ZG_IMPL_COUNT = 0, 1, 2, 3
-IMPL_NAMES = ["simt", "tc_products", "tc_all"]
+ZG_IMPL_SIMT, ZG_IMPL_TC_PRODUCTS, ZG_IMPL_TC_ALL, ZG_IMPL_TC_SPLIT, ZG_IMPL_COUNT = 0, 1, 2, 3, 4
+IMPL_NAMES = ["simt", "tc_products", "tc_all", "tc_split"]
 ZG_SCHED_LATE, ZG_SCHED_EARLY, ZG_SCHED_COUNT = 0, 1, 2
 SCHED_NAMES = ["late", "early"]
 PROF_REGIONS = ["gemm", "omega", "final", "combine", "error", "update", "rhs", "prep", "small", "gemm2"]

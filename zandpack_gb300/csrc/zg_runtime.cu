@@ -224,8 +224,9 @@ struct zg_traj {
   bool tcx_on = false;
   TcxBatch* tcx = nullptr;      // the products alone
   TcxBatch* tcx_all = nullptr;  // the products and the Omega derivative
-  int* tcx_claim = nullptr;     // item claim counters of the two batches
-  int tcx_grid_all = 0;
+  TcxBatch* tcx_om = nullptr;   // the Omega derivative alone, 64-column tiles
+  int* tcx_claim = nullptr;     // item claim counters of the three batches
+  int tcx_grid_all = 0, tcx_grid_om = 0;
   int prod_impl = 0;            // ZG_IMPL_*: which kernels compute the products and dOmega/dt
   int sched = 0;                // ZG_SCHED_*: where the second stream forks off
   TcxOperands tcx_ops;
@@ -412,6 +413,7 @@ static void free_traj(zg_traj* t) {
   for (void* p : ptrs) dfree(t, p);
   delete t->tcx;
   delete t->tcx_all;
+  delete t->tcx_om;
   if (t->stream2) {
     cudaStreamSynchronize(t->stream2);
     cudaStreamDestroy(t->stream2);
@@ -659,6 +661,7 @@ static int build_tcx(zg_traj* t, const zg_layout* Lo, const std::vector<double2>
   // (A rows Gt[b][m] and V[m]; B' rows the embeddings of U and of conj psi),
   // the diagonal term in the kernel's epilogue.
   bool omega_tc = (int)probs.size() + 3 * L * L <= ZG_TCX_PROBS;
+  std::vector<int> om_tile_map;  // per Omega problem: its tile map when tiles are prefetched
   if (omega_tc) {
     std::vector<float> Vf((size_t)N * ldx, 0.f), Uf((size_t)2 * N * ldx, 0.f);
     for (int64_t m = 0; m < N; ++m)
@@ -736,7 +739,8 @@ static int build_tcx(zg_traj* t, const zg_layout* Lo, const std::vector<double2>
           P.la = a;
           P.lb = b;
           // TMA needs the block's first float column on a 16-byte boundary
-          P.om_map = tiles_ok && lc0 % 2 == 0 ? (kind == 2 ? 19 : 18) : -1;
+          om_tile_map.push_back(lc0 % 2 == 0 ? (kind == 2 ? 19 : 18) : -1);
+          P.om_map = tiles_ok ? om_tile_map.back() : -1;
           P.om_x0 = (int)(2 * lc0);
           P.om_y0 = (int)r0;
           probs.push_back(P);
@@ -814,8 +818,8 @@ static int build_tcx(zg_traj* t, const zg_layout* Lo, const std::vector<double2>
     return nkb * ((P.amode == 1 ? 16 : 32) + bn / 4) + tile * (1 + (P.nsplit > 1) + (P.epi == 1));
   };
   // two claim counters per batch, zero between launches
-  ZG_TRY(dalloc(t, &t->tcx_claim, 4));
-  ZG_CHECK_CUDA(cudaMemsetAsync(t->tcx_claim, 0, 4 * sizeof(int), s));
+  ZG_TRY(dalloc(t, &t->tcx_claim, 6));
+  ZG_CHECK_CUDA(cudaMemsetAsync(t->tcx_claim, 0, 6 * sizeof(int), s));
   auto finish = [&](TcxBatch& Bt, bool with_omega, int* claim, int* grid_used) -> int {
     int np_ = 0, items = 0;
     std::vector<int64_t> cost;
@@ -839,14 +843,79 @@ static int build_tcx(zg_traj* t, const zg_layout* Lo, const std::vector<double2>
     Bt.ahead2 = items >= 6 * *grid_used ? 1 : 0;
     return tcx_validate(Bt);
   };
-  std::unique_ptr<TcxBatch> Bm;
+  std::unique_ptr<TcxBatch> Bm, Bo;
   if (omega_tc) {
     Bm.reset(new TcxBatch(*B));
     ZG_TRY(finish(*Bm, true, t->tcx_claim + 2, &t->tcx_grid_all));
+    // dOmega/dt alone in tiles of 128 rows x 32 complex columns, whatever
+    // the products' width, for the second stream (ZG_IMPL_TC_SPLIT): the
+    // Omega blocks' tile width does not depend on n_c.  Wider tiles (64 or
+    // 96 complex columns) when the narrow ones overflow the item table
+    int bo = 0;
+    for (int cand : {64, 128, 192}) {
+      int64_t it = 0;
+      for (const TcxProb& P0 : probs)
+        if (P0.epi == 1) it += (int64_t)P0.tiles_m * ((P0.Nv + cand - 1) / cand);
+      if (it <= ZG_TCX_ITEMS) {
+        bo = cand;
+        break;
+      }
+    }
+    if (bo == 0) bo = 192;  // no width fits: the batch is not built below
+    Bo.reset(new TcxBatch());
+    memset(Bo.get(), 0, sizeof(TcxBatch));
+    const float2* oA = t->stage32 + ml.st_om;
+    const float2* oB = oA + N * Ns;
+    ZG_TRY(tcx_map(*Bo, 10, t->Gth, L * N, 2 * nc, ldx, 128, 32, true));
+    ZG_TRY(tcx_map(*Bo, 11, t->Gtl, L * N, 2 * nc, ldx, 128, 32, true));
+    ZG_TRY(tcx_map(*Bo, 12, t->Uh, 2 * N, 2 * nc, ldx, bo, 32, true));
+    ZG_TRY(tcx_map(*Bo, 13, t->Ul, 2 * N, 2 * nc, ldx, bo, 32, true));
+    ZG_TRY(tcx_map(*Bo, 14, t->Vh, N, 2 * nc, ldx, 128, 32, true));
+    ZG_TRY(tcx_map(*Bo, 15, t->Vl, N, 2 * nc, ldx, 128, 32, true));
+    ZG_TRY(tcx_map(*Bo, 16, t->Gch, L * 2 * N, 2 * nc, ldx, bo, 32, true));
+    ZG_TRY(tcx_map(*Bo, 17, t->Gcl, L * 2 * N, 2 * nc, ldx, bo, 32, true));
+    const bool bo_tiles = tcx_has_omega_tile(bo);
+    if (bo_tiles) {
+      ZG_TRY(tcx_map(*Bo, 18, oA, N, 2 * Ns, 2 * Ns, 128, bo, false));
+      if (Nf > 0) ZG_TRY(tcx_map(*Bo, 19, oB, Ns, 2 * Nf, 2 * Nf, 128, bo, false));
+    }
+    int np_ = 0, items = 0, om_i = 0;
+    std::vector<int64_t> cost;
+    for (const TcxProb& P0 : probs) {
+      if (P0.epi != 1) continue;
+      TcxProb P = P0;
+      P.tiles_n = (P.Nv + bo - 1) / bo;
+      P.om_map = bo_tiles ? om_tile_map[om_i] : -1;
+      ++om_i;
+      P.item_begin = items;
+      items += P.tiles_m * P.tiles_n;
+      for (int w = 0; w < P.tiles_m * P.tiles_n; ++w) cost.push_back((P.K / 32) * (32 + bo / 4) + bo);
+      Bo->p[np_++] = P;
+    }
+    if (items > 0 && items <= ZG_TCX_ITEMS) {
+      Bo->nprob = np_;
+      Bo->nitems = items;
+      Bo->bn = bo;
+      Bo->err = t->tc_err;
+      Bo->params = t->d_params;
+      Bo->Xp = t->Xp32;
+      Bo->Xm = t->Xm32;
+      std::vector<int> order(items);
+      for (int i = 0; i < items; ++i) order[i] = i;
+      std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cost[x] > cost[y]; });
+      for (int i = 0; i < items; ++i) Bo->items[i] = (unsigned short)order[i];
+      Bo->claim = t->tcx_claim + 4;
+      t->tcx_grid_om = std::min(grid, items);
+      Bo->ahead2 = items >= 6 * t->tcx_grid_om ? 1 : 0;
+      ZG_TRY(tcx_validate(*Bo));
+    } else {
+      Bo.reset();
+    }
   }
   ZG_TRY(finish(*B, false, t->tcx_claim, &t->tcx_grid));
   t->tcx = B.release();
   t->tcx_all = Bm.release();
+  t->tcx_om = Bo.release();
   t->tcx_on = true;
   t->prod_impl = ZG_IMPL_TC_PRODUCTS;
   t->tcx_ops.sigEh = t->sigEh;
@@ -1441,7 +1510,7 @@ static int rhs_mixed(zg_traj* t, int stage, const StageParams* p, int dH_mode, d
       ops.sigEl = t->tcx_ops.sigEl;
       ops.ldx = t->tcx_ops.ldx;
     }
-    if (impl == ZG_IMPL_TC_ALL) {
+    if (impl == ZG_IMPL_TC_ALL || impl == ZG_IMPL_TC_SPLIT) {
       ops.Gth = t->Gth; ops.Gtl = t->Gtl; ops.Gch = t->Gch; ops.Gcl = t->Gcl;
     }
     ZG_TRY(launch_prep_mixed((int)n, (int)np, t->nonorth ? t->Hn0 : t->H0, sig, t->nonorth ? t->dHn : t->dH, dH_mode,
@@ -1468,9 +1537,15 @@ static int rhs_mixed(zg_traj* t, int stage, const StageParams* p, int dH_mode, d
     ZG_TRY(tc_gemm_launch(gT, s2));
     prof_end(t, ZG_PROF_GEMM2, s2);
     prof_begin(t, ZG_PROF_OMEGA, s2);
-    if (impl != ZG_IMPL_TC_ALL)  // else the Omega derivative runs in the tensor-core batch below
+    if (impl == ZG_IMPL_TC_SPLIT) {  // its own tensor-core launch
+      TcxBatch* bo = t->tcx_om;
+      bo->om_out_base = out;
+      bo->params = p;
+      ZG_TRY(tcx_launch(*bo, t->tcx_grid_om, s2));
+    } else if (impl != ZG_IMPL_TC_ALL) {  // else it runs in the tensor-core batch below
       ZG_TRY(launch_omega<float>(d, p, t->tiles, t->ntiles, t->G32, omA, omB, out + t->off_omA, out + t->off_omB,
                                  s2));
+    }
     prof_end(t, ZG_PROF_OMEGA, s2);
     ZG_CHECK_CUDA(cudaEventRecord(t->ev_join, s2));
   }
@@ -2037,7 +2112,8 @@ int zg_stationary_precond(zg_traj* t, const double* r_dev, double* out_dev) {
 
 static int impl_mask(const zg_traj* t) {
   if (t->precision != ZG_PREC_MIXED) return 1 << ZG_IMPL_SIMT;
-  return (1 << ZG_IMPL_SIMT) | (t->tcx_on ? 1 << ZG_IMPL_TC_PRODUCTS : 0) | (t->tcx_all ? 1 << ZG_IMPL_TC_ALL : 0);
+  return (1 << ZG_IMPL_SIMT) | (t->tcx_on ? 1 << ZG_IMPL_TC_PRODUCTS : 0) | (t->tcx_all ? 1 << ZG_IMPL_TC_ALL : 0) |
+         (t->tcx_on && t->tcx_om ? 1 << ZG_IMPL_TC_SPLIT : 0);
 }
 
 int zg_set_impl(zg_traj* t, int impl) {

@@ -18,7 +18,7 @@ def main():
     ap.add_argument("--attempts", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=1)
     ap.add_argument("--regions", action="store_true", help="print CUDA-event times per region of the timed attempts")
-    ap.add_argument("--impl", default=None, choices=["simt", "tc_products", "tc_all"],
+    ap.add_argument("--impl", default=None, choices=["simt", "tc_products", "tc_all", "tc_split"],
                     help="kernels of the small products and dOmega/dt (default: the trajectory's)")
     ap.add_argument("--nonorth", action="store_true",
                     help="the workload posed in a non-orthogonal basis, propagated as nozand does")
