@@ -228,8 +228,9 @@ int zg_graph_run(zg_traj* t, int count, zg_attempt_rec* recs, int* nrec, double*
  * allow it; the FP64 path ignores it); zg_get_impl reads the current choice
  * and, in *avail, a bit mask of the implementations the trajectory supports.
  * The second stream (H(t) sigma, and dOmega/dt unless ZG_IMPL_TC_ALL) forks
- * off before psi H(t)^T (ZG_SCHED_EARLY) or after it (ZG_SCHED_LATE, the
- * default): zg_set_schedule / zg_get_schedule.
+ * off before psi H(t)^T (ZG_SCHED_EARLY, the default: faster on every
+ * workload measured) or after it (ZG_SCHED_LATE): zg_set_schedule /
+ * zg_get_schedule.
  * zg_tune times one right-hand side of every supported implementation under
  * both schedules (CUDA events, `reps` evaluations each, after one untimed
  * evaluation) on the current state, keeps the fastest and returns it as

@@ -12,6 +12,10 @@ GOLDEN = os.path.join(ROOT, "tests", "golden")
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300) and the built libzandgpu.so")
+    # kernel choices measured during the tests stay in a file of this session
+    if "ZG_TUNE_CACHE" not in os.environ:
+        import tempfile
+        os.environ["ZG_TUNE_CACHE"] = os.path.join(tempfile.mkdtemp(prefix="zg_tune_"), "tune.json")
 
 
 def load_golden(case):

@@ -2,8 +2,8 @@
 
 The mixed-precision path can compute its small complex products (the PI
 partials, Omega xi, xi sigma^T) and dOmega/dt with FP32 SIMT kernels, with the
-products on the tensor cores, or with both on the tensor cores in one launch
-(``zg_set_impl``), and fork its second stream before or after psi H^T
+products on the tensor cores, or with both on the tensor cores in one or two
+launches (``zg_set_impl``), and fork its second stream before or after psi H^T
 (``zg_set_schedule``).  Which is fastest depends on the shapes (orbitals n, modes
 N, sourced modes Ns, coupling width n_c, leads) and on the GPU, so it is
 measured: ``zg_tune`` times one right-hand side of each, and the winner is
@@ -18,10 +18,14 @@ from __future__ import annotations
 import json
 import os
 import tempfile
+import threading
 
 from . import _lib
 
 _MEM = {}
+# one measurement at a time in this process (the serving loop tunes from its
+# worker threads): a class is measured once, and the file is rewritten whole
+_LOCK = threading.Lock()
 
 
 def cache_path():
@@ -80,22 +84,23 @@ def choose(traj, device=0, reps=5, path=None, retune=False):
     path = path or cache_path()
     key = class_key(traj.layout, traj.precision, device_name(device))
     _, avail = traj.get_impl()
-    entry = None if retune else (_MEM.get(key) or _load(path).get(key))
-    if entry is not None:
+    with _LOCK:
+        entry = None if retune else (_MEM.get(key) or _load(path).get(key))
+        if entry is not None:
+            try:
+                impl, sched = _parse(entry["impl"])
+            except (ValueError, KeyError):
+                impl = -1
+            if impl in avail:
+                traj.set_impl(impl)
+                traj.set_schedule(sched)
+                _MEM[key] = entry
+                return dict(entry, measured=False)
+        (impl, sched), times = traj.tune(reps)
+        entry = {"impl": _name(impl, sched), "ms": {_name(i, s): m for (i, s), m in sorted(times.items())}}
+        _MEM[key] = entry
         try:
-            impl, sched = _parse(entry["impl"])
-        except (ValueError, KeyError):
-            impl = -1
-        if impl in avail:
-            traj.set_impl(impl)
-            traj.set_schedule(sched)
-            _MEM[key] = entry
-            return dict(entry, measured=False)
-    (impl, sched), times = traj.tune(reps)
-    entry = {"impl": _name(impl, sched), "ms": {_name(i, s): m for (i, s), m in sorted(times.items())}}
-    _MEM[key] = entry
-    try:
-        _store(path, key, entry)
-    except OSError:
-        pass  # a read-only home: the choice still holds for this process
+            _store(path, key, entry)
+        except OSError:
+            pass  # a read-only home: the choice still holds for this process
     return dict(entry, measured=True)

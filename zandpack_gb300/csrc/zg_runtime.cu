@@ -228,7 +228,7 @@ struct zg_traj {
   int* tcx_claim = nullptr;     // item claim counters of the three batches
   int tcx_grid_all = 0, tcx_grid_om = 0;
   int prod_impl = 0;            // ZG_IMPL_*: which kernels compute the products and dOmega/dt
-  int sched = 0;                // ZG_SCHED_*: where the second stream forks off
+  int sched = ZG_SCHED_EARLY;   // ZG_SCHED_*: where the second stream forks off
   TcxOperands tcx_ops;
   // the Omega derivative in the same batch (epilogue 1 of zg_tcx.cu): the
   // constant operands U' (embedded) and V (TF32 hi/lo), and the per-stage psi

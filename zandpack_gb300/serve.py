@@ -33,6 +33,7 @@ from typing import Callable, List, Optional
 
 import numpy as np
 
+from . import autotune
 from .engine import Trajectory, native_bias
 from .layout import CompactLayout
 
@@ -76,8 +77,14 @@ class Result:
 
 class Server:
     def __init__(self, build: Callable, estimate: Callable, device=0, max_slots=16, hbm_budget=None,
-                 precision="mixed", keep_sigma=True, attempt_mode="graph", max_batch=32, prep_workers=0):
+                 precision="mixed", keep_sigma=True, attempt_mode="graph", max_batch=32, prep_workers=0,
+                 tune=False):
         self.build, self.estimate = build, estimate
+        # tune: the kernels of each trajectory chosen by measurement, once per
+        # class of shapes (zandpack_gb300.autotune keeps the choice).  Off by
+        # default: a class is keyed by every shape (n, N, Ns, n_c, leads), so
+        # a stream of distinct requests measures each one, serialised
+        self.tune = tune
         self.device, self.max_slots = device, max_slots
         self.precision = precision
         self.keep_sigma = keep_sigma
@@ -105,6 +112,8 @@ class Server:
             res.modes = L.N
             tr = Trajectory(None, w.hbar, precision=self.precision, device=self.device, layout=L)
             tr.set_y(w.arrays["DM_Ortho"])
+            if self.tune:
+                autotune.choose(tr, self.device)
             b = native_bias(w.bias, L.NL)
             t, h = w.t0, w.stepsize
             J = None
