@@ -1,6 +1,8 @@
 // Complex products of the mixed-precision right-hand side on the tcgen05
 // tensor cores: the PI partials psi^T IXI (Zandpack/mpi/zand:91-110,363-366),
-// the Omega xi products (:770-778) and the xi sigma^T rows (:760-768).
+// the Omega xi products (:770-778), the xi sigma^T rows (:760-768) and,
+// optionally, the Omega derivative (:782-809: its two rank-n_c source terms
+// as products, the diagonal term in the epilogue).
 //
 // Every product is C = A B^T with complex A (M x K) and B (Nc x K).  On the
 // tensor core it is the real GEMM
@@ -31,15 +33,18 @@
 // that the CTAs finish together whatever the items cost; the producer claims
 // and passes each item to the other roles through a small queue in shared
 // memory.  Warp roles:
-//   warp 0      one thread: TMA loads into a 2-stage ring;
-//   warp 1      one thread: tcgen05.mma issue, owns the TMEM allocation;
+//   warp 0      one thread: claims items, TMA loads into a ring of 2 to 4
+//               stages (as many as shared memory holds);
+//   warp 1      one thread: tcgen05.mma issue, owns the TMEM allocation (up
+//               to 8 accumulators of BN columns);
 //   warps 2-5   converters (forms 1 and 2; form 0 passes through);
 //   warps 6..   drain: TMEM -> registers, per-item sums, epilogue.
 // Split-K items write FP32 partial tiles; the last drain warp to finish a
 // 32-row slice of a tile (an atomic counter per slice) adds the partials in a
-// fixed order and writes the result, so results are deterministic.  Waits on mbarriers are bounded like
-// those of the 3xTF32 GEMM (zg_tc.cu): on timeout the error code is recorded,
-// in-flight copies and MMAs are waited for (bounded) and TMEM is freed.
+// fixed order and writes the result, so results are deterministic whichever
+// CTA computed which item.  Waits on mbarriers are bounded like those of the
+// 3xTF32 GEMM (zg_tc.cu): on timeout the error code is recorded, in-flight
+// copies and MMAs are waited for (bounded) and TMEM is freed.
 #include <vector>
 
 #include "zg_tc_ptx.cuh"
