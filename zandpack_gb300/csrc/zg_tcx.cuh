@@ -66,6 +66,8 @@ struct TcxBatch {
   // box of each tensor map (columns x rows; 0: map not set), for tcx_validate
   int box_cols[ZG_TCX_MAPS], box_rows[ZG_TCX_MAPS];
 };
+// the batch is the kernel's __grid_constant__ parameter
+static_assert(sizeof(TcxBatch) <= 32764, "kernel parameter space");
 
 // BN of the kernel for products with `ncols` real output columns per tile
 // (0 when none fits)
