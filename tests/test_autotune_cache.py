@@ -59,3 +59,22 @@ def test_fp64_is_not_measured(tmp_path):
     t = _FakeTraj([0], best=0, precision="f64")
     e = autotune.choose(t, path=str(tmp_path / "t.json"))
     assert t.tuned == 0 and not e["measured"]
+
+
+def test_coarse_classes_share_one_measurement(tmp_path, monkeypatch):
+    """Requests that differ only in their mode counts share a coarse class
+    (the serving loop's default) and are measured apart in the full one."""
+    monkeypatch.setattr(autotune, "device_name", lambda device=0: "GB300")
+    monkeypatch.setattr(autotune, "_MEM", {})
+    path = str(tmp_path / "tune.json")
+    a = _FakeTraj([0, 1, 2], best=1)
+    b = _FakeTraj([0, 1, 2], best=2)
+    b.layout = types.SimpleNamespace(n=64, N=420, Ns=56, nc=8, NL=2)
+    assert autotune.choose(a, path=path, coarse=True)["measured"]
+    e = autotune.choose(b, path=path, coarse=True)
+    assert not e["measured"] and b.tuned == 0 and b.impl == 1
+    e = autotune.choose(b, path=path)
+    assert e["measured"] and b.impl == 2
+    keys = set(json.load(open(path)))
+    assert keys == {autotune.class_key(a.layout, "mixed", "GB300", coarse=True),
+                    autotune.class_key(b.layout, "mixed", "GB300")}

@@ -35,9 +35,14 @@ def cache_path():
     return os.path.join(os.path.expanduser("~"), ".cache", "zandpack_gb300", "tune.json")
 
 
-def class_key(layout, precision, device_name):
-    """Key of a trajectory class: the shapes that decide the kernels' work."""
+def class_key(layout, precision, device_name, coarse=False):
+    """Key of a trajectory class: the shapes that decide the kernels' work.
+    ``coarse``: orbitals, coupling width and leads only (the mode counts N and
+    Ns left out), so that requests that differ only in their pole counts
+    share one measurement."""
     L = layout
+    if coarse:
+        return "%s|%s|n=%d|nc=%d|L=%d|coarse" % (device_name, precision, L.n, L.nc, L.NL)
     return "%s|%s|n=%d|N=%d|Ns=%d|nc=%d|L=%d" % (device_name, precision, L.n, L.N, L.Ns, L.nc, L.NL)
 
 
@@ -74,15 +79,16 @@ def _parse(name):
     return _lib.IMPL_NAMES.index(impl), _lib.SCHED_NAMES.index(sched)
 
 
-def choose(traj, device=0, reps=5, path=None, retune=False):
+def choose(traj, device=0, reps=5, path=None, retune=False, coarse=False):
     """Set the trajectory's kernels and stream schedule from the cache,
     measuring (and storing) the class's choice first when it is not there.
+    ``coarse`` keys the class by orbitals, coupling width and leads only.
     Returns the entry: {"impl": "<kernels>/<schedule>", "ms": {name: ms per
     RHS}, "measured": bool}."""
     if traj.precision != "mixed":
         return {"impl": _name(_lib.ZG_IMPL_SIMT, _lib.ZG_SCHED_LATE), "ms": {}, "measured": False}
     path = path or cache_path()
-    key = class_key(traj.layout, traj.precision, device_name(device))
+    key = class_key(traj.layout, traj.precision, device_name(device), coarse)
     _, avail = traj.get_impl()
     with _LOCK:
         entry = None if retune else (_MEM.get(key) or _load(path).get(key))

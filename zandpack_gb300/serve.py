@@ -78,12 +78,17 @@ class Result:
 class Server:
     def __init__(self, build: Callable, estimate: Callable, device=0, max_slots=16, hbm_budget=None,
                  precision="mixed", keep_sigma=True, attempt_mode="graph", max_batch=32, prep_workers=0,
-                 tune=False):
+                 tune=None):
         self.build, self.estimate = build, estimate
         # tune: the kernels of each trajectory chosen by measurement, once per
-        # class of shapes (zandpack_gb300.autotune keeps the choice).  Off by
-        # default: a class is keyed by every shape (n, N, Ns, n_c, leads), so
-        # a stream of distinct requests measures each one, serialised
+        # class (zandpack_gb300.autotune keeps the choice): "coarse" keys a
+        # class by orbitals, coupling width and leads, so that requests that
+        # differ in their pole counts share one measurement; "full" by every
+        # shape (each distinct request is then measured, one at a time); None
+        # (the default; both measured slower on the 512-request ensemble) or
+        # False: the library's defaults
+        if tune not in (None, False, "coarse", "full"):
+            raise ValueError("tune must be 'coarse', 'full' or None")
         self.tune = tune
         self.device, self.max_slots = device, max_slots
         self.precision = precision
@@ -113,7 +118,7 @@ class Server:
             tr = Trajectory(None, w.hbar, precision=self.precision, device=self.device, layout=L)
             tr.set_y(w.arrays["DM_Ortho"])
             if self.tune:
-                autotune.choose(tr, self.device)
+                autotune.choose(tr, self.device, coarse=self.tune == "coarse")
             b = native_bias(w.bias, L.NL)
             t, h = w.t0, w.stepsize
             J = None
