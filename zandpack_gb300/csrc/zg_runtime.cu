@@ -749,15 +749,16 @@ static int build_tcx(zg_traj* t, const zg_layout* Lo, const std::vector<double2>
   int sms = 0;
   ZG_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, t->dev));
   const int grid = std::max(1, std::min(sms, ZG_TCX_GRID));
-  // K chunks: at most about half the average work of a CTA over the products,
-  // so that the CTAs, claiming the items most expensive first, end close
-  // together, while split-K partials stay few; each problem's K is cut into
-  // equal chunks (the same chunks in both batches below, so that they share
-  // the split-K scratch)
+  // K chunks: at most about the average work of a CTA over the products
+  // (measured at n=1024 against half and a third of it: the fewer split-K
+  // partials outweigh the coarser balance, which the CTAs' run-time claims
+  // of the items, most expensive first, keep close); each problem's K is cut
+  // into equal chunks (the same chunks in both batches below, so that they
+  // share the split-K scratch)
   int64_t total_kb = 0;
   for (const TcxProb& P : probs)
     if (P.epi == 0) total_kb += (int64_t)P.tiles_m * P.tiles_n * (P.K / 32);
-  const int chunk_kb0 = (int)std::min<int64_t>(64, std::max<int64_t>(8, (total_kb + 2 * grid - 1) / (2 * grid)));
+  const int chunk_kb0 = (int)std::min<int64_t>(64, std::max<int64_t>(8, (total_kb + grid - 1) / grid));
   int chunk_kb = chunk_kb0;
   for (;;) {
     int items = 0;
